@@ -1,0 +1,168 @@
+/*
+ * ithaca_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the spectral/hp
+ * Helmholtz + conjugate-gradient + POD hot path of ITHACA-SEM (Nektar++ 5.0.0).
+ *
+ * Plain C: opaque handles, raw pointers and sizes, int status codes, no exceptions
+ * and no C++ or torch types across the boundary. Every call returns ITHACA_GPU_OK (0)
+ * or a positive ITHACA_GPU_ERR_* code; ithaca_gpu_last_error() gives the message
+ * (thread-local). Pointers flagged by `on_device` are device pointers when it is 1
+ * and host pointers when it is 0 (the library then stages them through device
+ * buffers itself). All arrays use the reference's element-contiguous layouts:
+ *
+ *   coefficients  quad e*n^2 + q*n + p          hex e*n^3 + (r*n + q)*n + p
+ *   physical      quad e*Q^2 + j*Q + i          hex e*Q^3 + (k*Q + j)*Q + i
+ *   jac           deformed: e*Q^d + pt          regular: e
+ *   df            deformed: dir*E*Q^d + e*Q^d + pt   regular: dir*E + e,
+ *                 dir = k*d + j holding dxi_j/dx_k
+ *                 (Collections/CoalescedGeomData.cpp:53-313 GetJac/GetDerivFactors)
+ *
+ * Threading: a context owns one CUDA stream; calls on one context are not
+ * re-entrant (like the reference operators, which keep mutable work buffers).
+ */
+#ifndef ITHACA_GPU_H
+#define ITHACA_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference raises NekError; the adapter maps these back) ---- */
+enum {
+  ITHACA_GPU_OK = 0,
+  ITHACA_GPU_ERR_ARG = 1,           /* invalid argument (null pointer, bad size)        */
+  ITHACA_GPU_ERR_UNSUPPORTED = 2,   /* shape / (modes, points) combination not built    */
+  ITHACA_GPU_ERR_CUDA = 3,          /* CUDA runtime error (message has the detail)      */
+  ITHACA_GPU_ERR_NOMEM = 4,         /* device allocation failed                          */
+  ITHACA_GPU_ERR_NOT_CONVERGED = 5, /* iterative solve hit max_iter (reference: efatal)  */
+  ITHACA_GPU_ERR_GEOMETRY = 6,      /* non-positive Jacobian (GeomFactors.cpp:610-676)   */
+  ITHACA_GPU_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up                */
+  ITHACA_GPU_ERR_NUMERIC = 8        /* NaN / Inf met in a reduction                      */
+};
+
+/* LibUtilities::ShapeType values of the two supported shapes. */
+enum { ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_HEX = 8 };
+
+/* Arithmetic of an element operator. */
+enum { ITHACA_GPU_FP64 = 0, ITHACA_GPU_FP32 = 1 };
+
+/* Solver precision modes for ithaca_gpu_cg_solve. */
+enum {
+  ITHACA_GPU_SOLVE_FP64 = 0,        /* reference recurrence, FP64 throughout             */
+  ITHACA_GPU_SOLVE_MIXED_FP32 = 1   /* FP32 inner PCG inside FP64 iterative refinement   */
+};
+
+typedef struct ithaca_gpu_ctx ithaca_gpu_ctx;
+typedef struct ithaca_gpu_op ithaca_gpu_op;
+typedef struct ithaca_gpu_cg ithaca_gpu_cg;
+
+/* ---- errors / context ---- */
+
+/* Copies the last error message of this thread into buf (NUL-terminated). */
+int ithaca_gpu_last_error(char* buf, size_t len);
+int ithaca_gpu_version(void);
+
+/* Creates a context on `device` with its own non-blocking stream. */
+int ithaca_gpu_ctx_create(int device, ithaca_gpu_ctx** ctx);
+int ithaca_gpu_ctx_destroy(ithaca_gpu_ctx* ctx);
+/* Blocks until all work queued on the context's stream has finished. */
+int ithaca_gpu_ctx_synchronize(ithaca_gpu_ctx* ctx);
+/* The context's cudaStream_t, returned as void* (for event timing by callers). */
+int ithaca_gpu_ctx_stream(ithaca_gpu_ctx* ctx, void** stream);
+/* Number of library kernels launched on this context so far. */
+int ithaca_gpu_ctx_launch_count(ithaca_gpu_ctx* ctx, long long* count);
+
+/* ---- 1-D tables (LibUtilities/Polylib/Polylib.cpp:195,690 zwglj/Dglj;
+ *      LibUtilities/Foundations/Basis.cpp:392-421 eModified_A) ----
+ * z, w: Q; D: Q*Q with D[k*Q+i] = l_k'(z_i); B, DB: n*Q with B[p*Q+i]. Host arrays. */
+int ithaca_gpu_basis_modA(int nmodes, int npoints, double* z, double* w, double* D, double* B, double* DB);
+
+/* ---- geometry (SpatialDomains/GeomFactors.cpp:168-475 ComputeDeriv/ComputeJac/
+ *      ComputeDerivFactors) ----
+ * coords: d arrays of E*Q^d physical coordinates at the GLL quadrature points,
+ * stored one after another (coordinate k at coords[k*E*Q^d]). Writes jac (E*Q^d)
+ * and df (d*d*E*Q^d) in the deformed layout above. Returns ITHACA_GPU_ERR_GEOMETRY
+ * if any Jacobian is not positive. */
+int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
+                            double* jac, double* df, int on_device);
+
+/* ---- element operators: one Collection of same-shape elements ----
+ * Replaces Collections::Operator (Collections/Operator.h:113-165) implementations
+ * BwdTrans/IProductWRTBase/PhysDeriv/Helmholtz for ImplementationType "GPU", and
+ * MatrixFree::Operator (MatrixFreeOps/Operator.hpp:21-201) with its SetJac/SetDF.
+ * Basis: ModifiedA with `nmodes` modes on `npoints` GLL points in every direction
+ * (the homogeneous case MatrixFreeOps/Helmholtz.h:42-44 requires). Supported:
+ * npoints == nmodes + 1, 2 <= nmodes <= 10. `precision` selects the arithmetic. */
+int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
+                         const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op);
+int ithaca_gpu_op_destroy(ithaca_gpu_op* op);
+/* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282). */
+int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof);
+
+/* BwdTrans (Collections/BwdTrans.cpp:143-240): coefficients -> physical values. */
+int ithaca_gpu_bwdtrans(ithaca_gpu_op* op, const void* in, void* out, int on_device);
+/* IProductWRTBase (Collections/IProductWRTBase.cpp:168-262): physical -> coefficients. */
+int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_device);
+/* PhysDeriv (Collections/PhysDeriv.cpp:270-415): physical -> d physical derivatives.
+ * d2 may be NULL for quads. */
+int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, void* d2, int on_device);
+/* Helmholtz (Collections/Helmholtz.cpp:391-430): out = lambda M in + L in, with
+ * lambda = factors[eFactorLambda]. Arrays are double for FP64 ops and float for FP32. */
+int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device);
+/* Diagonals of the element Helmholtz matrices (E*n^d), the per-element input of
+ * PreconditionerDiagonal::DiagonalPreconditionerSum (PreconditionerDiagonal.cpp:98-161). */
+int ithaca_gpu_helmholtz_diag(ithaca_gpu_op* op, double lambda, double* out, int on_device);
+
+/* ---- global C0 system + conjugate gradient ----
+ * Replaces GlobalLinSysIterativeFull (MultiRegions/GlobalLinSysIterativeFull.cpp:110-257)
+ * with NekLinSysIterCG (LibUtilities/LinearAlgebra/NekLinSysIterCG.cpp:104-263) and
+ * PreconditionerDiagonal. l2g/sign: the local-to-global map and signs of
+ * AssemblyMapCG (one entry per local coefficient, E*n^d), global ids < nglobal with
+ * the ndir Dirichlet ids numbered first. The operator `op` must be FP64. */
+int ithaca_gpu_cg_create(ithaca_gpu_op* op, const int* l2g, const double* sign, int nglobal, int ndir,
+                         ithaca_gpu_cg** cg);
+int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg);
+
+typedef struct {
+  double tol;          /* IterativeSolverTolerance (default 1e-9); stop when ||r||^2 < tol^2 ||b||^2 */
+  int max_iter;        /* NekLinSysMaxIterations (default 5000)                                      */
+  int mode;            /* ITHACA_GPU_SOLVE_*                                                         */
+  double inner_tol;    /* mixed mode: relative reduction asked of each inner FP32 solve (default 1e-4) */
+  int max_outer;       /* mixed mode: maximum refinement steps (default 50)                          */
+  int check_every;     /* iterations per device-side convergence check (default 8)                   */
+} ithaca_gpu_cg_opts;
+
+typedef struct {
+  int iterations;         /* total CG iterations (inner iterations in mixed mode) */
+  int outer_iterations;   /* refinement steps (0 in FP64 mode)                    */
+  double rel_residual;    /* ||b - A x||_2 / ||b||_2 over non-Dirichlet dofs, FP64  */
+  double eps;             /* last reference-style residual r.r of the FP64 recurrence */
+  double rhs_magnitude;   /* ||b||^2 with the 1e-6 -> 1 floor of NekLinSysIter.cpp:142 */
+} ithaca_gpu_cg_result;
+
+void ithaca_gpu_cg_default_opts(ithaca_gpu_cg_opts* opts);
+
+/* Solves A(lambda) x = rhs for the non-Dirichlet global dofs (rhs, x: nglobal
+ * doubles; x[0..ndir) is left untouched, the solve starts from x = 0 elsewhere as
+ * the reference does). Returns ITHACA_GPU_ERR_NOT_CONVERGED past max_iter. */
+int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, double* x,
+                        const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
+
+/* Global operator y = Assemble(Helmholtz(GlobalToLocal(x))) in FP64 (nglobal entries;
+ * Dirichlet entries of x are used as given). GlobalLinSysIterativeFull::v_DoMatrixMultiply. */
+int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, double* y, int on_device);
+/* Assembled Jacobi diagonal over the non-Dirichlet dofs (nglobal - ndir entries). */
+int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int on_device);
+
+/* ContField::v_HelmSolve (MultiRegions/ContField.cpp:878-945) for homogeneous
+ * Dirichlet data: forcing f at quadrature points (E*Q^d) -> solution in local
+ * coefficient space (E*n^d): rhs = Assemble(-IProductWRTBase(f)), CG, GlobalToLocal. */
+int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
+                         const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ITHACA_GPU_H */

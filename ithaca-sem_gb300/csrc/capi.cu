@@ -1,0 +1,397 @@
+// C-ABI layer: contexts, element operators, geometry. No exception crosses the
+// boundary; each entry point returns a status code (include/ithaca_gpu.h).
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "ithaca_internal.h"
+
+namespace ithaca {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear sticky-free errors so the context stays usable
+    fail(e == cudaErrorMemoryAllocation ? ITHACA_GPU_ERR_NOMEM : ITHACA_GPU_ERR_CUDA,
+         std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+void* Ctx::stage_ptr(int slot, size_t bytes) {
+  if (bytes > stage_bytes[slot]) {
+    if (stage[slot]) ITHACA_CUDA(cudaFree(stage[slot]));
+    stage[slot] = nullptr;
+    stage_bytes[slot] = 0;
+    ITHACA_CUDA(cudaMalloc(&stage[slot], bytes));
+    stage_bytes[slot] = bytes;
+  }
+  return stage[slot];
+}
+
+Ctx::~Ctx() {
+  for (auto& p : stage)
+    if (p) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+Op::~Op() {
+  cudaFree(t64.base);
+  cudaFree(t32.base);
+  cudaFree(jg64);
+  cudaFree(df64);
+  cudaFree(jg32);
+  cudaFree(df32);
+}
+
+template <typename F>
+static int guarded(F f) {
+  try {
+    f();
+    return ITHACA_GPU_OK;
+  } catch (const Error& e) {
+    set_last_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return ITHACA_GPU_ERR_NOMEM;
+  } catch (...) {
+    set_last_error("unknown error");
+    return ITHACA_GPU_ERR_ARG;
+  }
+}
+
+static int shape_dim(int shape) {
+  if (shape == ITHACA_GPU_SHAPE_QUAD) return 2;
+  if (shape == ITHACA_GPU_SHAPE_HEX) return 3;
+  fail(ITHACA_GPU_ERR_UNSUPPORTED, "shape must be quadrilateral (4) or hexahedron (8)");
+}
+
+template <typename T>
+static void upload_tables(DevTables<T>& dt, const BasisTables& b) {
+  const int n = b.n, Q = b.Q;
+  dt.n = n;
+  dt.Q = Q;
+  std::vector<T> h(dt.size());
+  for (int p = 0; p < n; ++p)
+    for (int i = 0; i < Q; ++i) {
+      h[off_B(n, Q) + p * Q + i] = (T)b.B[p * Q + i];
+      h[off_Bt(n, Q) + i * n + p] = (T)b.B[p * Q + i];
+      h[off_DB(n, Q) + p * Q + i] = (T)b.DB[p * Q + i];
+      h[off_DBt(n, Q) + i * n + p] = (T)b.DB[p * Q + i];
+    }
+  for (int k = 0; k < Q; ++k)
+    for (int i = 0; i < Q; ++i) {
+      h[off_D(n, Q) + k * Q + i] = (T)b.D[k * Q + i];
+      h[off_Dt(n, Q) + i * Q + k] = (T)b.D[k * Q + i];
+    }
+  for (int i = 0; i < Q; ++i) h[off_w(n, Q) + i] = (T)b.w[i];
+  ITHACA_CUDA(cudaMalloc(&dt.base, h.size() * sizeof(T)));
+  ITHACA_CUDA(cudaMemcpy(dt.base, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// Copies `bytes` from a host or device pointer into a device buffer (returned).
+static const void* to_device(Ctx* c, int slot, const void* p, size_t bytes, int on_device) {
+  if (on_device) return p;
+  void* d = c->stage_ptr(slot, bytes);
+  ITHACA_CUDA(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, c->stream));
+  return d;
+}
+
+static void* out_buffer(Ctx* c, int slot, void* p, size_t bytes, int on_device) {
+  return on_device ? p : c->stage_ptr(slot, bytes);
+}
+
+static void from_device(Ctx* c, void* host, const void* dev, size_t bytes, int on_device) {
+  if (on_device) return;
+  ITHACA_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+}
+
+static void finish(Ctx* c, int on_device) {
+  ITHACA_CUDA(cudaGetLastError());
+  if (!on_device) ITHACA_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+static void require(bool ok, const char* msg) {
+  if (!ok) fail(ITHACA_GPU_ERR_ARG, msg);
+}
+
+static size_t elt(const Op* op) { return op->precision == ITHACA_GPU_FP64 ? sizeof(double) : sizeof(float); }
+
+}  // namespace ithaca
+
+using namespace ithaca;
+
+struct ithaca_gpu_ctx : public Ctx {};
+struct ithaca_gpu_op : public Op {};
+
+extern "C" {
+
+int ithaca_gpu_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return ITHACA_GPU_ERR_ARG;
+  std::snprintf(buf, len, "%s", g_last_error.c_str());
+  return ITHACA_GPU_OK;
+}
+
+int ithaca_gpu_version(void) { return 100; }
+
+int ithaca_gpu_ctx_create(int device, ithaca_gpu_ctx** ctx) {
+  return guarded([&] {
+    require(ctx != nullptr, "ctx is null");
+    int ndev = 0;
+    ITHACA_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) fail(ITHACA_GPU_ERR_ARG, "no such CUDA device");
+    ITHACA_CUDA(cudaSetDevice(device));
+    auto c = std::make_unique<ithaca_gpu_ctx>();
+    c->device = device;
+    ITHACA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    *ctx = c.release();
+  });
+}
+
+int ithaca_gpu_ctx_destroy(ithaca_gpu_ctx* ctx) {
+  return guarded([&] {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+  });
+}
+
+int ithaca_gpu_ctx_synchronize(ithaca_gpu_ctx* ctx) {
+  return guarded([&] {
+    require(ctx, "ctx is null");
+    ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int ithaca_gpu_ctx_stream(ithaca_gpu_ctx* ctx, void** stream) {
+  return guarded([&] {
+    require(ctx && stream, "null argument");
+    *stream = (void*)ctx->stream;
+  });
+}
+
+int ithaca_gpu_ctx_launch_count(ithaca_gpu_ctx* ctx, long long* count) {
+  return guarded([&] {
+    require(ctx && count, "null argument");
+    *count = ctx->launches;
+  });
+}
+
+int ithaca_gpu_basis_modA(int nmodes, int npoints, double* z, double* w, double* D, double* B, double* DB) {
+  return guarded([&] {
+    require(nmodes >= 1 && npoints >= 2, "need nmodes >= 1 and npoints >= 2");
+    BasisTables t = make_basis(nmodes, npoints);
+    if (z) std::memcpy(z, t.z.data(), sizeof(double) * npoints);
+    if (w) std::memcpy(w, t.w.data(), sizeof(double) * npoints);
+    if (D) std::memcpy(D, t.D.data(), sizeof(double) * npoints * npoints);
+    if (B) std::memcpy(B, t.B.data(), sizeof(double) * nmodes * npoints);
+    if (DB) std::memcpy(DB, t.DB.data(), sizeof(double) * nmodes * npoints);
+  });
+}
+
+int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
+                            double* jac, double* df, int on_device) {
+  return guarded([&] {
+    require(ctx && coords && jac && df, "null argument");
+    require(nelmt > 0 && npoints >= 2 && npoints <= 16, "bad sizes");
+    const int dim = shape_dim(shape);
+    const int Q = npoints;
+    const size_t nq = dim == 2 ? (size_t)Q * Q : (size_t)Q * Q * Q;
+    const size_t tot = (size_t)nelmt * nq;
+    BasisTables b = make_basis(2, Q);
+    double* dD = nullptr;
+    int* dbad = nullptr;
+    ITHACA_CUDA(cudaMalloc(&dD, sizeof(double) * Q * Q));
+    ITHACA_CUDA(cudaMalloc(&dbad, sizeof(int)));
+    std::unique_ptr<double, decltype(&cudaFree)> g1(dD, cudaFree);
+    std::unique_ptr<int, decltype(&cudaFree)> g2(dbad, cudaFree);
+    ITHACA_CUDA(cudaMemcpyAsync(dD, b.D.data(), sizeof(double) * Q * Q, cudaMemcpyHostToDevice, ctx->stream));
+    ITHACA_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+    const double* X = (const double*)to_device(ctx, 0, coords, sizeof(double) * dim * tot, on_device);
+    double* J = (double*)out_buffer(ctx, 1, jac, sizeof(double) * tot, on_device);
+    double* F = (double*)out_buffer(ctx, 2, df, sizeof(double) * dim * dim * tot, on_device);
+    launch_geom_factors(dim, Q, nelmt, dD, X, J, F, dbad, ctx->stream);
+    ctx->launches++;
+    from_device(ctx, jac, J, sizeof(double) * tot, on_device);
+    from_device(ctx, df, F, sizeof(double) * dim * dim * tot, on_device);
+    int hbad = 0;
+    ITHACA_CUDA(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hbad) fail(ITHACA_GPU_ERR_GEOMETRY, "non-positive Jacobian at a quadrature point");
+  });
+}
+
+int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
+                         const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op) {
+  return guarded([&] {
+    require(ctx && jac && df && op, "null argument");
+    require(nelmt > 0, "nelmt must be positive");
+    require(precision == ITHACA_GPU_FP64 || precision == ITHACA_GPU_FP32, "unknown precision");
+    const int dim = shape_dim(shape);
+    if (!(npoints == nmodes + 1 && nmodes >= 2 && nmodes <= 10))
+      fail(ITHACA_GPU_ERR_UNSUPPORTED,
+           "GPU operators are built for npoints == nmodes + 1, 2 <= nmodes <= 10 (got nmodes=" +
+               std::to_string(nmodes) + ", npoints=" + std::to_string(npoints) + ")");
+    auto o = std::make_unique<ithaca_gpu_op>();
+    o->ctx = ctx;
+    o->shape = shape;
+    o->dim = dim;
+    o->n = nmodes;
+    o->Q = npoints;
+    o->E = nelmt;
+    o->deformed = deformed ? 1 : 0;
+    o->precision = precision;
+    o->nm = dim == 2 ? nmodes * nmodes : nmodes * nmodes * nmodes;
+    o->nq = dim == 2 ? npoints * npoints : npoints * npoints * npoints;
+    BasisTables b = make_basis(nmodes, npoints);
+    upload_tables(o->t64, b);
+    upload_tables(o->t32, b);
+    const size_t npt = o->deformed ? (size_t)o->nq : 1;
+    const size_t njg = (size_t)nelmt * n_jg(dim) * npt, ndf = (size_t)nelmt * dim * dim * npt;
+    const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * npt, on_device);
+    const double* F = (const double*)to_device(ctx, 1, df, sizeof(double) * dim * dim * nelmt * npt, on_device);
+    double* dw = nullptr;
+    ITHACA_CUDA(cudaMalloc(&dw, sizeof(double) * npoints));
+    std::unique_ptr<double, decltype(&cudaFree)> gw(dw, cudaFree);
+    ITHACA_CUDA(cudaMemcpyAsync(dw, b.w.data(), sizeof(double) * npoints, cudaMemcpyHostToDevice, ctx->stream));
+    ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
+    ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * ndf));
+    launch_build_jg<double>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg64, o->df64, ctx->stream);
+    ctx->launches++;
+    if (precision == ITHACA_GPU_FP32) {
+      ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
+      launch_build_jg<float>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg32, o->df32, ctx->stream);
+      ctx->launches++;
+    }
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+    *op = o.release();
+  });
+}
+
+int ithaca_gpu_op_destroy(ithaca_gpu_op* op) {
+  return guarded([&] {
+    if (!op) return;
+    cudaStreamSynchronize(op->ctx->stream);
+    delete op;
+  });
+}
+
+int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof) {
+  return guarded([&] {
+    require(op && ndof, "null argument");
+    *ndof = (long long)op->E * op->nm;
+  });
+}
+
+int ithaca_gpu_bwdtrans(ithaca_gpu_op* op, const void* in, void* out, int on_device) {
+  return guarded([&] {
+    require(op && in && out, "null argument");
+    Ctx* c = op->ctx;
+    const size_t es = elt(op), nin = (size_t)op->E * op->nm, nout = (size_t)op->E * op->nq;
+    const void* din = to_device(c, 0, in, es * nin, on_device);
+    void* dout = out_buffer(c, 1, out, es * nout, on_device);
+    bool ok;
+    if (op->precision == ITHACA_GPU_FP64)
+      ok = launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, (const double*)din, (double*)dout,
+                                   c->stream);
+    else
+      ok = launch_bwdtrans<float>(op->dim, op->n, op->Q, op->E, op->t32.base, (const float*)din, (float*)dout,
+                                  c->stream);
+    if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "BwdTrans: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, out, dout, es * nout, on_device);
+    finish(c, on_device);
+  });
+}
+
+int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_device) {
+  return guarded([&] {
+    require(op && in && out, "null argument");
+    Ctx* c = op->ctx;
+    const size_t es = elt(op), nin = (size_t)op->E * op->nq, nout = (size_t)op->E * op->nm;
+    const void* din = to_device(c, 0, in, es * nin, on_device);
+    void* dout = out_buffer(c, 1, out, es * nout, on_device);
+    bool ok;
+    if (op->precision == ITHACA_GPU_FP64)
+      ok = launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
+                                   (const double*)din, (double*)dout, c->stream);
+    else
+      ok = launch_iproduct<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+                                  (const float*)din, (float*)dout, c->stream);
+    if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, out, dout, es * nout, on_device);
+    finish(c, on_device);
+  });
+}
+
+int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, void* d2, int on_device) {
+  return guarded([&] {
+    require(op && in && d0 && d1, "null argument");
+    require(op->dim == 2 || d2, "d2 is required for hexahedra");
+    Ctx* c = op->ctx;
+    const size_t es = elt(op), nq = (size_t)op->E * op->nq;
+    const void* din = to_device(c, 0, in, es * nq, on_device);
+    void* o[3] = {out_buffer(c, 1, d0, es * nq, on_device), out_buffer(c, 2, d1, es * nq, on_device),
+                  op->dim == 3 ? out_buffer(c, 3, d2, es * nq, on_device) : nullptr};
+    bool ok;
+    if (op->precision == ITHACA_GPU_FP64)
+      ok = launch_physderiv<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->df64,
+                                    (const double*)din, (double*)o[0], (double*)o[1], (double*)o[2], c->stream);
+    else
+      ok = launch_physderiv<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->df32,
+                                   (const float*)din, (float*)o[0], (float*)o[1], (float*)o[2], c->stream);
+    if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "PhysDeriv: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, d0, o[0], es * nq, on_device);
+    from_device(c, d1, o[1], es * nq, on_device);
+    if (op->dim == 3) from_device(c, d2, o[2], es * nq, on_device);
+    finish(c, on_device);
+  });
+}
+
+int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device) {
+  return guarded([&] {
+    require(op && in && out, "null argument");
+    Ctx* c = op->ctx;
+    const size_t es = elt(op), nm = (size_t)op->E * op->nm;
+    const void* din = to_device(c, 0, in, es * nm, on_device);
+    void* dout = out_buffer(c, 1, out, es * nm, on_device);
+    bool ok;
+    if (op->precision == ITHACA_GPU_FP64)
+      ok = launch_helmholtz<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
+                                    (const double*)din, (double*)dout, nullptr, 0, c->stream);
+    else
+      ok = launch_helmholtz<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+                                   (float)lambda, (const float*)din, (float*)dout, nullptr, 0, c->stream);
+    if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, out, dout, es * nm, on_device);
+    finish(c, on_device);
+  });
+}
+
+int ithaca_gpu_helmholtz_diag(ithaca_gpu_op* op, double lambda, double* out, int on_device) {
+  return guarded([&] {
+    require(op && out, "null argument");
+    Ctx* c = op->ctx;
+    const size_t nm = (size_t)op->E * op->nm;
+    double* dout = (double*)out_buffer(c, 1, out, sizeof(double) * nm, on_device);
+    if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda, dout,
+                                  c->stream))
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, out, dout, sizeof(double) * nm, on_device);
+    finish(c, on_device);
+  });
+}
+
+}  // extern "C"

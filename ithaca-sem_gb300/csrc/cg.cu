@@ -1,0 +1,730 @@
+// Global C0 Helmholtz system and its conjugate-gradient solvers.
+//
+//  * Assembly (AssemblyMapCG::v_Assemble, MultiRegions/AssemblyMap/AssemblyMapCG.cpp:2885-2910)
+//    is an owner-computes CSR sum over the local dofs of each global dof, in a fixed
+//    order: no atomics, so results and iteration counts are bit-reproducible.
+//  * GlobalToLocal (:2853-2876) is fused into the element Helmholtz kernel (gather).
+//  * PCG follows the single-reduction recurrence of NekLinSysIterCG::DoConjugateGradient
+//    (LibUtilities/LinearAlgebra/NekLinSysIterCG.cpp:104-263) with the Jacobi
+//    preconditioner of PreconditionerDiagonal (MultiRegions/PreconditionerDiagonal.cpp:98-206)
+//    and the ||b||^2 <= 1e-6 -> 1 floor of NekLinSysIter::Set_Rhs_Magnitude (NekLinSysIter.cpp:128-152).
+//    Per iteration: update(p, q, x, r, w = M^-1 r; r.w, r.r) -> gather + element apply
+//    -> assemble(s; s.w) -> scalars. Partial sums go through fixed-size per-CTA slots
+//    and a one-CTA reduction in fixed order. Chunks of iterations run as one CUDA graph;
+//    a device flag stops the remaining kernels of a chunk once the solve has converged.
+//  * Mixed precision: FP64 residuals r = b - A x (FP64 operator), FP32 inner PCG on
+//    the FP32 copy of the operator, x += ||r|| d, until ||r|| <= tol ||b||.
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "ithaca_internal.h"
+
+namespace ithaca {
+
+constexpr int RB = 608;      // reduction CTAs (4 per SM)
+constexpr int RT = 256;      // threads per reduction CTA
+constexpr int NSLOT = 4;     // partial-sum slots: 0 r.w, 1 r.r, 2 b.b, 3 s.w
+
+struct CgScalars {
+  double alpha, beta, rho, mu, eps, rhs_mag, tol2, mag_override;
+  double lambda;
+  float lambda32, pad0;
+  int iters, k, done, status, max_iter, pad1;
+};
+
+// ---- reductions -------------------------------------------------------------
+template <int NC>
+__device__ __forceinline__ void block_partials(double (&v)[NC], double* partials, const int* slots) {
+  __shared__ double sm[NC][RT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    if (lane == 0) sm[c][warp] = v[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double s = 0;
+#pragma unroll
+    for (int w = 0; w < RT / 32; ++w) s += sm[threadIdx.x][w];
+    partials[slots[threadIdx.x] * RB + blockIdx.x] = s;
+  }
+}
+
+__device__ __forceinline__ double reduce_slot(const double* partials, int slot) {
+  __shared__ double sm[RT];
+  double s = 0;
+  for (int i = threadIdx.x; i < RB; i += RT) s += partials[slot * RB + i];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = RT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
+}
+
+// ---- PCG vector kernels (T = double or float; reductions in double) ----------
+template <typename T>
+__global__ void __launch_bounds__(RT) pcg_init_kernel(int N, int ndir, const T* __restrict__ b, T* __restrict__ x,
+                                                      T* __restrict__ r, T* __restrict__ w,
+                                                      const T* __restrict__ dinv, double* partials) {
+  double v[3] = {0, 0, 0};
+  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+    const double bg = (double)b[g];
+    v[2] += bg * bg;
+    if (g >= ndir) {
+      const T rg = b[g];
+      const T wg = dinv[g] * rg;
+      r[g] = rg;
+      x[g] = T(0);
+      w[g] = wg;
+      v[0] += (double)rg * (double)wg;
+      v[1] += (double)rg * (double)rg;
+    } else {
+      w[g] = T(0);
+    }
+  }
+  const int slots[3] = {0, 1, 2};
+  block_partials<3>(v, partials, slots);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RT) pcg_update_kernel(int N, int ndir, const CgScalars* sc, T* __restrict__ x,
+                                                        T* __restrict__ r, T* __restrict__ w,
+                                                        const T* __restrict__ s, T* __restrict__ p,
+                                                        T* __restrict__ q, const T* __restrict__ dinv,
+                                                        double* partials) {
+  if (sc->done) return;
+  const T alpha = (T)sc->alpha, beta = (T)sc->beta;
+  double v[2] = {0, 0};
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+    const T pg = beta * p[g] + w[g];
+    const T qg = beta * q[g] + s[g];
+    p[g] = pg;
+    q[g] = qg;
+    x[g] += alpha * pg;
+    const T rg = r[g] - alpha * qg;
+    r[g] = rg;
+    const T wg = dinv[g] * rg;
+    w[g] = wg;
+    v[0] += (double)rg * (double)wg;
+    v[1] += (double)rg * (double)rg;
+  }
+  const int slots[2] = {0, 1};
+  block_partials<2>(v, partials, slots);
+}
+
+// s[g] = sum_{local l of g} sign_l * yloc[l] for g in [g0, N); partial s.w in slot 3.
+template <typename T, bool SIGNED = true>
+__global__ void __launch_bounds__(RT) assemble_dot_kernel(int N, int g0, const int* __restrict__ rowptr,
+                                                          const int* __restrict__ cols, const T* __restrict__ yloc,
+                                                          T* __restrict__ s, const T* __restrict__ w,
+                                                          const int* skip, double* partials) {
+  if (skip != nullptr && *skip) return;
+  double v[1] = {0};
+  for (int g = g0 + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+    T acc = 0;
+    for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+      const int c = cols[j];
+      if (SIGNED)
+        acc += c >= 0 ? yloc[c] : -yloc[~c];
+      else
+        acc += yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
+    }
+    s[g] = acc;
+    if (w) v[0] += (double)acc * (double)w[g];
+  }
+  if (partials) {
+    const int slots[1] = {3};
+    block_partials<1>(v, partials, slots);
+  }
+}
+
+// Reference initial step (NekLinSysIterCG.cpp:147-190).
+__global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc) {
+  const double rw = reduce_slot(partials, 0), rr = reduce_slot(partials, 1);
+  const double bb = reduce_slot(partials, 2), sw = reduce_slot(partials, 3);
+  if (threadIdx.x == 0) {
+    sc->rhs_mag = sc->mag_override > 0 ? sc->mag_override : (bb > 1e-6 ? bb : 1.0);
+    sc->eps = rr;
+    sc->iters = 0;
+    sc->k = 0;
+    sc->status = ITHACA_GPU_OK;
+    sc->done = 0;
+    if (!isfinite(rr) || !isfinite(rw) || !isfinite(sw)) {
+      sc->status = ITHACA_GPU_ERR_NUMERIC;
+      sc->done = 1;
+    } else if (rr < sc->tol2 * sc->rhs_mag) {
+      sc->done = 1;
+    } else {
+      sc->rho = rw;
+      sc->mu = sw;
+      sc->beta = 0.0;
+      sc->alpha = rw / sw;
+      sc->iters = 1;
+      if (sc->max_iter <= 0) {
+        sc->status = ITHACA_GPU_ERR_NOT_CONVERGED;
+        sc->done = 1;
+      }
+    }
+  }
+}
+
+// Reference loop tail (NekLinSysIterCG.cpp:219-261).
+__global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials, CgScalars* sc) {
+  if (sc->done) return;
+  const double rho_new = reduce_slot(partials, 0), eps = reduce_slot(partials, 1);
+  const double mu = reduce_slot(partials, 3);
+  if (threadIdx.x == 0) {
+    sc->eps = eps;
+    sc->mu = mu;
+    sc->iters += 1;
+    if (!isfinite(eps) || !isfinite(rho_new) || !isfinite(mu)) {
+      sc->status = ITHACA_GPU_ERR_NUMERIC;
+      sc->done = 1;
+    } else if (eps < sc->tol2 * sc->rhs_mag) {
+      sc->done = 1;
+    } else {
+      const double beta = rho_new / sc->rho;
+      sc->alpha = rho_new / (mu - rho_new * beta / sc->alpha);
+      sc->beta = beta;
+      sc->rho = rho_new;
+      sc->k += 1;
+      if (sc->k >= sc->max_iter) {
+        sc->status = ITHACA_GPU_ERR_NOT_CONVERGED;
+        sc->done = 1;
+      }
+    }
+  }
+}
+
+// ---- FP64 outer-step kernels ----------------------------------------------------
+// r[g] = b[g] - sum yloc (g >= ndir), partial r.r -> slot 1; b.b -> slot 2.
+__global__ void __launch_bounds__(RT) residual_kernel(int N, int ndir, const int* __restrict__ rowptr,
+                                                      const int* __restrict__ cols, const double* __restrict__ yloc,
+                                                      const double* __restrict__ b, double* __restrict__ r,
+                                                      double* partials) {
+  double v[2] = {0, 0};
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+    double acc = 0;
+    for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+      const int c = cols[j];
+      acc += c >= 0 ? yloc[c] : -yloc[~c];
+    }
+    const double rg = b[g] - acc;
+    r[g] = rg;
+    v[0] += rg * rg;
+    v[1] += b[g] * b[g];
+  }
+  const int slots[2] = {1, 2};
+  block_partials<2>(v, partials, slots);
+}
+
+__global__ void reduce_to_kernel(const double* partials, int slot, double* out) {
+  const double v = reduce_slot(partials, slot);
+  if (threadIdx.x == 0) *out = v;
+}
+
+// r32 = r64 * scale on g >= ndir, zero below.
+__global__ void __launch_bounds__(RT) scale_to_f32_kernel(int N, int ndir, const double* __restrict__ r,
+                                                          const double* __restrict__ scale_src, float* __restrict__ r32) {
+  const double sc = 1.0 / sqrt(*scale_src);
+  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) r32[g] = g >= ndir ? (float)(r[g] * sc) : 0.f;
+}
+
+// x64 += sqrt(*scale_src) * d32 on g >= ndir.
+__global__ void __launch_bounds__(RT) axpy_f32_kernel(int N, int ndir, const double* __restrict__ scale_src,
+                                                      const float* __restrict__ d32, double* __restrict__ x) {
+  const double sc = sqrt(*scale_src);
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) x[g] += sc * (double)d32[g];
+}
+
+__global__ void __launch_bounds__(RT) inv_kernel(int n, const double* __restrict__ d, double* __restrict__ dinv,
+                                                 float* __restrict__ dinv32, int ndir) {
+  for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += RB * RT) {
+    const double v = g >= ndir ? 1.0 / d[g] : 0.0;
+    dinv[g] = v;
+    if (dinv32) dinv32[g] = (float)v;
+  }
+}
+
+// local[l] = sign * x[g] (AssemblyMapCG::GlobalToLocal), l2g signed-encoded.
+__global__ void __launch_bounds__(RT) g2l_kernel(size_t nloc, const int* __restrict__ l2g,
+                                                 const double* __restrict__ x, double* __restrict__ loc) {
+  for (size_t l = (size_t)blockIdx.x * RT + threadIdx.x; l < nloc; l += (size_t)RB * RT) {
+    const int c = l2g[l];
+    loc[l] = c >= 0 ? x[c] : -x[~c];
+  }
+}
+
+__global__ void __launch_bounds__(RT) neg_kernel(size_t n, double* __restrict__ a) {
+  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)RB * RT) a[i] = -a[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RT) cast_kernel(size_t n, const double* __restrict__ a, T* __restrict__ b) {
+  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)RB * RT) b[i] = (T)a[i];
+}
+
+// ---- solver object --------------------------------------------------------------
+template <typename T>
+struct Vecs {
+  T *x = nullptr, *r = nullptr, *w = nullptr, *s = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr,
+    *yloc = nullptr, *b = nullptr;
+  void alloc(size_t N, size_t nloc) {
+    T** v[] = {&x, &r, &w, &s, &p, &q, &dinv, &b};
+    for (auto pp : v) {
+      ITHACA_CUDA(cudaMalloc(pp, sizeof(T) * N));
+      ITHACA_CUDA(cudaMemset(*pp, 0, sizeof(T) * N));
+    }
+    ITHACA_CUDA(cudaMalloc(&yloc, sizeof(T) * nloc));
+  }
+  void release() {
+    for (T* p0 : {x, r, w, s, p, q, dinv, yloc, b}) cudaFree(p0);
+  }
+};
+
+struct Cg {
+  Op* op = nullptr;
+  int N = 0, ndir = 0;
+  size_t nloc = 0;
+  int* l2g = nullptr;     // signed-encoded
+  int* rowptr = nullptr;  // N + 1
+  int* cols = nullptr;    // nloc, signed-encoded local index
+  Vecs<double> v64;
+  Vecs<float> v32;
+  bool have32 = false;
+  float* jg32 = nullptr;  // FP32 copy of the operator geometry
+  double* partials = nullptr;
+  double* dscal = nullptr;  // scratch doubles (norms)
+  CgScalars* sc = nullptr;
+  CgScalars* sc_host = nullptr;  // pinned
+  double diag_lambda = NAN;
+  cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
+  int graph64_len = 0, graph32_len = 0;
+  ~Cg();
+};
+
+Cg::~Cg() {
+  if (graph64) cudaGraphExecDestroy(graph64);
+  if (graph32) cudaGraphExecDestroy(graph32);
+  cudaFree(l2g);
+  cudaFree(rowptr);
+  cudaFree(cols);
+  v64.release();
+  if (have32) v32.release();
+  cudaFree(jg32);
+  cudaFree(partials);
+  cudaFree(dscal);
+  cudaFree(sc);
+  if (sc_host) cudaFreeHost(sc_host);
+}
+
+static const int* skip_ptr(Cg* cg) { return &cg->sc->done; }
+
+// Gather (signed l2g; ids < ndir read as zero when zero_dir) + element Helmholtz into v.yloc.
+template <typename T>
+static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda, const T* lam_ptr, const T* xin,
+                         cudaStream_t s, bool zero_dir, const int* skip) {
+  Op* op = cg->op;
+  if (!launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+                           zero_dir ? cg->ndir : 0, s, skip, lam_ptr))
+    fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
+  op->ctx->launches++;
+}
+
+template <typename T>
+static const T* lam_dev(Cg* cg);
+template <>
+const double* lam_dev<double>(Cg* cg) { return &cg->sc->lambda; }
+template <>
+const float* lam_dev<float>(Cg* cg) { return &cg->sc->lambda32; }
+
+// One PCG iteration: update -> gather+apply -> assemble(+s.w) -> scalars.
+template <typename T>
+static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cudaStream_t s) {
+  pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv, cg->partials);
+  launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg));
+  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, v.yloc, v.s, v.w, skip_ptr(cg),
+                                           cg->partials);
+  scalars_iter_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
+  cg->op->ctx->launches += 3;
+}
+
+template <typename T>
+static cudaGraphExec_t capture_chunk(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, int iters) {
+  cudaStream_t s = cg->op->ctx->stream;
+  cudaGraph_t g;
+  ITHACA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const long long before = cg->op->ctx->launches;
+  for (int i = 0; i < iters; ++i) enqueue_iteration<T>(cg, v, tab, jg, s);
+  cg->op->ctx->launches = before;  // captured, not launched
+  ITHACA_CUDA(cudaStreamEndCapture(s, &g));
+  cudaGraphExec_t ex;
+  ITHACA_CUDA(cudaGraphInstantiate(&ex, g, 0));
+  cudaGraphDestroy(g);
+  return ex;
+}
+
+// Runs the reference PCG recurrence on vectors of type T with right-hand side v.b;
+// the final scalars are left in sc_host. lambda is read from the device scalars.
+template <typename T>
+static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda, double tol2, double mag_override,
+                    int max_iter, int chunk) {
+  Ctx* c = cg->op->ctx;
+  cudaStream_t s = c->stream;
+  CgScalars init{};
+  init.tol2 = tol2;
+  init.mag_override = mag_override;
+  init.max_iter = max_iter;
+  init.lambda = lambda;
+  init.lambda32 = (float)lambda;
+  *cg->sc_host = init;
+  ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
+  pcg_init_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
+  launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
+  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
+                                           cg->partials);
+  scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
+  c->launches += 3;
+  ITHACA_CUDA(cudaGetLastError());
+  cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
+  int& len = sizeof(T) == 8 ? cg->graph64_len : cg->graph32_len;
+  if (!ex || len != chunk) {
+    if (ex) cudaGraphExecDestroy(ex);
+    ex = nullptr;
+    ex = capture_chunk<T>(cg, v, tab, jg, chunk);
+    len = chunk;
+  }
+  // Bounded host loop: at most max_iter / chunk + 2 graph launches.
+  const long long max_launches = (long long)max_iter / chunk + 2;
+  for (long long it = 0;; ++it) {
+    ITHACA_CUDA(cudaMemcpyAsync(cg->sc_host, cg->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    if (cg->sc_host->done) break;
+    if (it >= max_launches) fail(ITHACA_GPU_ERR_TIMEOUT, "CG did not flag completion within its iteration bound");
+    ITHACA_CUDA(cudaGraphLaunch(ex, s));
+    c->launches += 4LL * chunk;
+  }
+}
+
+static void ensure_fp32(Cg* cg) {
+  if (cg->have32) return;
+  Op* op = cg->op;
+  cg->v32.alloc(cg->N, cg->nloc);
+  const size_t njg = (size_t)op->E * n_jg(op->dim) * (op->deformed ? op->nq : 1);
+  ITHACA_CUDA(cudaMalloc(&cg->jg32, sizeof(float) * njg));
+  cast_kernel<float><<<RB, RT, 0, op->ctx->stream>>>(njg, op->jg64, cg->jg32);
+  op->ctx->launches++;
+  cg->have32 = true;
+  cg->diag_lambda = NAN;  // rebuild so that the FP32 inverse diagonal is filled too
+}
+
+// Assembled Jacobi diagonal (sum of element diagonals, sign^2 = 1) and its inverse.
+static void ensure_diag(Cg* cg, double lambda) {
+  if (cg->diag_lambda == lambda) return;
+  Op* op = cg->op;
+  cudaStream_t s = op->ctx->stream;
+  if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
+                                cg->v64.yloc, s))
+    fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
+  assemble_dot_kernel<double, false><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
+                                                       nullptr, nullptr, nullptr);
+  inv_kernel<<<RB, RT, 0, s>>>(cg->N, cg->v64.s, cg->v64.dinv, cg->have32 ? cg->v32.dinv : nullptr, cg->ndir);
+  op->ctx->launches += 3;
+  ITHACA_CUDA(cudaGetLastError());
+  cg->diag_lambda = lambda;
+}
+
+// FP64 residual r = b - A x over the non-Dirichlet dofs; ||r||^2 -> dscal[0], ||b||^2 -> dscal[1].
+static void fp64_residual(Cg* cg, double lambda, const double* x, const double* b, double* r) {
+  cudaStream_t s = cg->op->ctx->stream;
+  launch_apply<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, nullptr, x, s, true, nullptr);
+  residual_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, cg->v64.yloc, b, r, cg->partials);
+  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 1, cg->dscal);
+  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 2, cg->dscal + 1);
+  cg->op->ctx->launches += 3;
+}
+
+static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithaca_gpu_cg_result* res) {
+  Ctx* c = cg->op->ctx;
+  cudaStream_t s = c->stream;
+  if (o.mode == ITHACA_GPU_SOLVE_MIXED_FP32) ensure_fp32(cg);
+  ensure_diag(cg, lambda);
+  const int chunk = std::max(1, std::min(o.check_every, 64));
+  const double tol = std::max(o.tol, 1e-16);  // tolerance floor of NekLinSysIter.cpp:83
+  ithaca_gpu_cg_result out{};
+  int status = ITHACA_GPU_OK;
+  if (o.mode == ITHACA_GPU_SOLVE_FP64) {
+    run_pcg<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, tol * tol, 0.0, o.max_iter, chunk);
+    out.iterations = cg->sc_host->iters;
+    out.eps = cg->sc_host->eps;
+    out.rhs_magnitude = cg->sc_host->rhs_mag;
+    status = cg->sc_host->status;
+  } else if (o.mode == ITHACA_GPU_SOLVE_MIXED_FP32) {
+    double hs[2];
+    // x64 = 0; r64 = b
+    ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->N, s));
+    fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.r);
+    ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    const double bnorm2 = hs[1];
+    double rnorm2 = hs[0];
+    int total_inner = 0, outer = 0;
+    const double inner2 = o.inner_tol * o.inner_tol;
+    while (rnorm2 > tol * tol * bnorm2 && bnorm2 > 0) {
+      if (outer >= o.max_outer || total_inner >= o.max_iter) {
+        status = ITHACA_GPU_ERR_NOT_CONVERGED;
+        break;
+      }
+      if (!std::isfinite(rnorm2)) {
+        status = ITHACA_GPU_ERR_NUMERIC;
+        break;
+      }
+      // r32 = r64 / ||r64||, inner FP32 PCG from zero to relative inner_tol
+      scale_to_f32_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.r, cg->dscal, cg->v32.b);
+      c->launches++;
+      run_pcg<float>(cg, cg->v32, cg->op->t32.base, cg->jg32, lambda, inner2, 1.0, o.max_iter - total_inner, chunk);
+      total_inner += cg->sc_host->iters;
+      const int st = cg->sc_host->status;
+      if (st == ITHACA_GPU_ERR_NUMERIC) {
+        status = st;
+        break;
+      }
+      // x64 += ||r|| d32 ; r64 = b - A x64
+      axpy_f32_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->dscal, cg->v32.x, cg->v64.x);
+      c->launches++;
+      fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.r);
+      ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+      ITHACA_CUDA(cudaStreamSynchronize(s));
+      rnorm2 = hs[0];
+      ++outer;
+    }
+    out.iterations = total_inner;
+    out.outer_iterations = outer;
+    out.eps = rnorm2;
+    out.rhs_magnitude = bnorm2 > 1e-6 ? bnorm2 : 1.0;
+  } else {
+    fail(ITHACA_GPU_ERR_ARG, "unknown solve mode");
+  }
+  // final FP64 relative residual ||b - A x|| / ||b|| (reported in both modes)
+  {
+    double hs[2];
+    fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.w);
+    ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    out.rel_residual = hs[1] > 0 ? std::sqrt(hs[0] / hs[1]) : 0.0;
+  }
+  if (res) *res = out;
+  if (status == ITHACA_GPU_ERR_NOT_CONVERGED)
+    fail(status, "Exceeded maximum number of iterations (" + std::to_string(out.iterations) + ")");
+  if (status != ITHACA_GPU_OK) fail(status, "NaN or Inf in the CG recurrence");
+}
+
+}  // namespace ithaca
+
+using namespace ithaca;
+
+struct ithaca_gpu_cg : public Cg {};
+
+template <typename F>
+static int cg_guarded(F f) {
+  try {
+    f();
+    return ITHACA_GPU_OK;
+  } catch (const Error& e) {
+    set_last_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return ITHACA_GPU_ERR_NOMEM;
+  }
+}
+
+static void req(bool ok, const char* msg) {
+  if (!ok) fail(ITHACA_GPU_ERR_ARG, msg);
+}
+
+static ithaca_gpu_cg_opts opts_or_default(const ithaca_gpu_cg_opts* o);
+
+extern "C" {
+
+void ithaca_gpu_cg_default_opts(ithaca_gpu_cg_opts* o) {
+  if (!o) return;
+  o->tol = 1e-9;
+  o->max_iter = 5000;
+  o->mode = ITHACA_GPU_SOLVE_FP64;
+  o->inner_tol = 1e-4;
+  o->max_outer = 50;
+  o->check_every = 8;
+}
+
+int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign, int nglobal, int ndir,
+                         ithaca_gpu_cg** out) {
+  return cg_guarded([&] {
+    Op* op = reinterpret_cast<Op*>(opp);
+    req(op && l2g && sign && out, "null argument");
+    req(op->precision == ITHACA_GPU_FP64, "the global system needs an FP64 operator");
+    req(nglobal > 0 && ndir >= 0 && ndir <= nglobal, "bad nglobal / ndir");
+    const size_t nloc = (size_t)op->E * op->nm;
+    req(nloc < (size_t)0x7fffffff, "too many local dofs for 32-bit indices");
+    std::vector<int> code(nloc), cnt(nglobal + 1, 0);
+    for (size_t l = 0; l < nloc; ++l) {
+      const int g = l2g[l];
+      if (g < 0 || g >= nglobal) fail(ITHACA_GPU_ERR_ARG, "l2g entry out of range");
+      if (!(sign[l] == 1.0 || sign[l] == -1.0)) fail(ITHACA_GPU_ERR_ARG, "sign entries must be +1 or -1");
+      code[l] = sign[l] > 0 ? g : ~g;
+      cnt[g + 1]++;
+    }
+    for (int g = 0; g < nglobal; ++g) cnt[g + 1] += cnt[g];
+    std::vector<int> cols(nloc), fill(cnt.begin(), cnt.end() - 1);
+    for (size_t l = 0; l < nloc; ++l) {
+      const int g = l2g[l];
+      cols[fill[g]++] = sign[l] > 0 ? (int)l : ~(int)l;
+    }
+    auto cg = std::make_unique<ithaca_gpu_cg>();
+    cg->op = op;
+    cg->N = nglobal;
+    cg->ndir = ndir;
+    cg->nloc = nloc;
+    cudaStream_t s = op->ctx->stream;
+    ITHACA_CUDA(cudaMalloc(&cg->l2g, sizeof(int) * nloc));
+    ITHACA_CUDA(cudaMalloc(&cg->rowptr, sizeof(int) * (nglobal + 1)));
+    ITHACA_CUDA(cudaMalloc(&cg->cols, sizeof(int) * nloc));
+    ITHACA_CUDA(cudaMemcpyAsync(cg->l2g, code.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+    ITHACA_CUDA(cudaMemcpyAsync(cg->rowptr, cnt.data(), sizeof(int) * (nglobal + 1), cudaMemcpyHostToDevice, s));
+    ITHACA_CUDA(cudaMemcpyAsync(cg->cols, cols.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+    cg->v64.alloc(nglobal, nloc);
+    ITHACA_CUDA(cudaMalloc(&cg->partials, sizeof(double) * NSLOT * RB));
+    ITHACA_CUDA(cudaMalloc(&cg->dscal, sizeof(double) * 8));
+    ITHACA_CUDA(cudaMalloc(&cg->sc, sizeof(CgScalars)));
+    ITHACA_CUDA(cudaMallocHost(&cg->sc_host, sizeof(CgScalars)));
+    *cg->sc_host = CgScalars{};
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    *out = cg.release();
+  });
+}
+
+int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg) {
+  return cg_guarded([&] {
+    if (!cg) return;
+    cudaStreamSynchronize(cg->op->ctx->stream);
+    delete cg;
+  });
+}
+
+int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, double* y, int on_device) {
+  return cg_guarded([&] {
+    req(cg && x && y, "null argument");
+    Ctx* c = cg->op->ctx;
+    cudaStream_t s = c->stream;
+    const size_t bytes = sizeof(double) * cg->N;
+    const double* dx = x;
+    if (!on_device) {
+      ITHACA_CUDA(cudaMemcpyAsync(cg->v64.p, x, bytes, cudaMemcpyHostToDevice, s));
+      dx = cg->v64.p;
+    }
+    double* dy = on_device ? y : cg->v64.q;
+    launch_apply<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, nullptr, dx, s, false, nullptr);
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
+                                                  nullptr, nullptr);
+    c->launches++;
+    if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    if (!on_device) ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int on_device) {
+  return cg_guarded([&] {
+    req(cg && diag, "null argument");
+    cudaStream_t s = cg->op->ctx->stream;
+    cg->diag_lambda = NAN;
+    ensure_diag(cg, lambda);
+    const size_t bytes = sizeof(double) * (cg->N - cg->ndir);
+    ITHACA_CUDA(cudaMemcpyAsync(diag, cg->v64.s + cg->ndir, bytes,
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (!on_device) ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, double* x,
+                        const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device) {
+  return cg_guarded([&] {
+    req(cg && rhs && x, "null argument");
+    const ithaca_gpu_cg_opts o = opts_or_default(opts);
+    Ctx* c = cg->op->ctx;
+    cudaStream_t s = c->stream;
+    const size_t bytes = sizeof(double) * cg->N;
+    ITHACA_CUDA(cudaMemcpyAsync(cg->v64.b, rhs, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                s));
+    struct Copyback {
+      Cg* cg;
+      double* x;
+      int on_device;
+      size_t off, bytes;
+      ~Copyback() {
+        // the solution (non-Dirichlet part) goes back even when the solve failed to converge
+        cudaMemcpyAsync(x + off, cg->v64.x + off, bytes,
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, cg->op->ctx->stream);
+        cudaStreamSynchronize(cg->op->ctx->stream);
+      }
+    } cb{cg, x, on_device, (size_t)cg->ndir, sizeof(double) * (cg->N - cg->ndir)};
+    solve_impl(cg, lambda, o, res);
+  });
+}
+
+int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
+                         const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device) {
+  return cg_guarded([&] {
+    req(cg && forcing && out_local, "null argument");
+    const ithaca_gpu_cg_opts o = opts_or_default(opts);
+    Op* op = cg->op;
+    Ctx* c = op->ctx;
+    cudaStream_t s = c->stream;
+    const size_t nphys = (size_t)op->E * op->nq, nloc = cg->nloc;
+    const double* f = forcing;
+    if (!on_device) {
+      double* d = (double*)c->stage_ptr(0, sizeof(double) * nphys);
+      ITHACA_CUDA(cudaMemcpyAsync(d, forcing, sizeof(double) * nphys, cudaMemcpyHostToDevice, s));
+      f = d;
+    }
+    // wsp = -IProductWRTBase(f) (ContField.cpp:895-900); b = Assemble(wsp)
+    if (!launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, f,
+                                 cg->v64.yloc, s))
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
+    neg_kernel<<<RB, RT, 0, s>>>(nloc, cg->v64.yloc);
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
+                                                  nullptr, nullptr);
+    c->launches += 3;
+    solve_impl(cg, lambda, o, res);
+    // homogeneous Dirichlet values, then GlobalToLocal
+    ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->ndir, s));
+    double* dout = on_device ? out_local : (double*)c->stage_ptr(1, sizeof(double) * nloc);
+    g2l_kernel<<<RB, RT, 0, s>>>(nloc, cg->l2g, cg->v64.x, dout);
+    c->launches++;
+    if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(out_local, dout, sizeof(double) * nloc, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"
+
+static ithaca_gpu_cg_opts opts_or_default(const ithaca_gpu_cg_opts* o) {
+  ithaca_gpu_cg_opts d;
+  ithaca_gpu_cg_default_opts(&d);
+  if (!o) return d;
+  d = *o;
+  if (d.max_iter <= 0) d.max_iter = 5000;
+  if (d.check_every <= 0) d.check_every = 8;
+  if (d.max_outer <= 0) d.max_outer = 50;
+  if (!(d.inner_tol > 0 && d.inner_tol < 1)) d.inner_tol = 1e-4;
+  return d;
+}

@@ -1,0 +1,142 @@
+// Host-side launchers for the element kernels of one precision and dimension.
+// Each translation unit that includes this instantiates all (n, Q = n + 1),
+// 2 <= n <= 10, for one (T, DIM) pair through ITHACA_ELEM_INSTANTIATE.
+#pragma once
+
+#include "elem.cuh"
+
+namespace ithaca {
+namespace dev {
+
+template <typename T, int DIM, int N, int Q>
+struct Cfg {
+  using S = Shape<DIM, Q>;
+  static size_t smem() { return Layout<T, DIM, N, Q>::bytes(S::EB); }
+  static dim3 block() { return dim3(S::TPE, S::EB); }
+  static dim3 grid(int E) { return dim3((E + S::EB - 1) / S::EB); }
+  template <class K>
+  static void prep(K k) {
+    static bool done = false;  // attribute set once per kernel instantiation
+    if (!done) {
+      ITHACA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
+      done = true;
+    }
+  }
+};
+
+template <typename T, int DIM, int N, int Q>
+void helm_nq(int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g, int ndir,
+             const int* skip, const T* lam_ptr, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  constexpr int TPE = C::S::TPE;
+  auto k = deformed ? (l2g ? helm_kernel<T, DIM, N, Q, TPE, true, true> : helm_kernel<T, DIM, N, Q, TPE, true, false>)
+                    : (l2g ? helm_kernel<T, DIM, N, Q, TPE, false, true> : helm_kernel<T, DIM, N, Q, TPE, false, false>);
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr);
+}
+
+template <typename T, int DIM, int N, int Q>
+void bwd_nq(int E, const T* tab, const T* in, T* out, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  auto k = bwd_kernel<T, DIM, N, Q, C::S::TPE>;
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, out, tab, E);
+}
+
+template <typename T, int DIM, int N, int Q>
+void ipr_nq(int E, int deformed, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  auto k = deformed ? ipr_kernel<T, DIM, N, Q, C::S::TPE, true> : ipr_kernel<T, DIM, N, Q, C::S::TPE, false>;
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, out, tab, jg, E);
+}
+
+template <typename T, int DIM, int N, int Q>
+void deriv_nq(int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  auto k = deformed ? deriv_kernel<T, DIM, N, Q, C::S::TPE, true> : deriv_kernel<T, DIM, N, Q, C::S::TPE, false>;
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, d0, d1, d2, tab, df, E);
+}
+
+template <typename T, int DIM, int N, int Q>
+void diag_nq(int E, int deformed, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  auto k = deformed ? diag_kernel<T, DIM, N, Q, C::S::TPE, true> : diag_kernel<T, DIM, N, Q, C::S::TPE, false>;
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(out, tab, jg, lambda, E);
+}
+
+
+}  // namespace dev
+
+#define ITHACA_FOR_EACH_NQ(X) X(2, 3) X(3, 4) X(4, 5) X(5, 6) X(6, 7) X(7, 8) X(8, 9) X(9, 10) X(10, 11)
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in,
+                           T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, cudaStream_t s) {
+#define X(NN, QQ)                                                                                  \
+  if (n == NN && Q == QQ) {                                                                        \
+    dev::helm_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);             \
+    return true;                                                                                   \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
+#define X(NN, QQ)                                          \
+  if (n == NN && Q == QQ) {                                \
+    dev::bwd_nq<T, DIM, NN, QQ>(E, tab, in, out, s);       \
+    return true;                                           \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::ipr(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in, T* out,
+                          cudaStream_t s) {
+#define X(NN, QQ)                                                      \
+  if (n == NN && Q == QQ) {                                            \
+    dev::ipr_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, in, out, s);     \
+    return true;                                                       \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1,
+                            T* d2, cudaStream_t s) {
+#define X(NN, QQ)                                                                \
+  if (n == NN && Q == QQ) {                                                      \
+    dev::deriv_nq<T, DIM, NN, QQ>(E, deformed, tab, df, in, d0, d1, d2, s);      \
+    return true;                                                                 \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::diag(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, T* out,
+                           cudaStream_t s) {
+#define X(NN, QQ)                                                          \
+  if (n == NN && Q == QQ) {                                                \
+    dev::diag_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, lambda, out, s);    \
+    return true;                                                           \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+
+}  // namespace ithaca
+
+#define ITHACA_ELEM_INSTANTIATE(T, DIM) template struct ithaca::ElemApi<T, DIM>;

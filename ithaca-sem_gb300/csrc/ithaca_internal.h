@@ -1,0 +1,138 @@
+// Internal declarations shared by the C-ABI layer and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/ithaca_gpu.h"
+
+namespace ithaca {
+
+// ---------------------------------------------------------------------------
+// Errors: every C-ABI entry point catches `Error` and returns its code; the message
+// is kept per thread for ithaca_gpu_last_error().
+struct Error {
+  int code;
+  std::string msg;
+};
+void set_last_error(const std::string& msg);
+[[noreturn]] void fail(int code, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what);
+#define ITHACA_CUDA(x) ::ithaca::check_cuda((x), #x)
+
+// ---------------------------------------------------------------------------
+// Basis tables (host, FP64), see basis.cpp.
+struct BasisTables {
+  int n = 0, Q = 0;
+  std::vector<double> z, w, D, B, DB;
+};
+BasisTables make_basis(int n, int Q);
+double jacobi(int m, double a, double b, double x);
+
+// Device copy of the 1-D tables for one (n, Q), packed for the kernels:
+//   B  [p*Q + i]   Bt  [i*n + p]   DB [p*Q + i]   DBt [i*n + p]
+//   D  [k*Q + i] = l_k'(z_i)        Dt  [i*Q + k] = D[k*Q + i]       w [i]
+template <typename T>
+struct DevTables {
+  T* base = nullptr;  // one allocation, offsets below
+  int n = 0, Q = 0;
+  size_t size() const { return (size_t)4 * n * Q + 2 * Q * Q + Q; }
+};
+// Offsets (in elements) of each table inside the packed buffer.
+inline __host__ __device__ int off_B(int, int) { return 0; }
+inline __host__ __device__ int off_Bt(int n, int Q) { return n * Q; }
+inline __host__ __device__ int off_DB(int n, int Q) { return 2 * n * Q; }
+inline __host__ __device__ int off_DBt(int n, int Q) { return 3 * n * Q; }
+inline __host__ __device__ int off_D(int n, int Q) { return 4 * n * Q; }
+inline __host__ __device__ int off_Dt(int n, int Q) { return 4 * n * Q + Q * Q; }
+inline __host__ __device__ int off_w(int n, int Q) { return 4 * n * Q + 2 * Q * Q; }
+
+// Number of geometry fields per quadrature point used by the Helmholtz kernels:
+// J*w followed by the symmetric metric J*w*g^{ab} (upper triangle, row-major).
+inline __host__ __device__ constexpr int n_jg(int dim) { return 1 + dim * (dim + 1) / 2; }
+
+// ---------------------------------------------------------------------------
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  long long launches = 0;
+  // grow-only staging buffers for host-pointer calls
+  void* stage[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t stage_bytes[4] = {0, 0, 0, 0};
+  void* stage_ptr(int slot, size_t bytes);
+  ~Ctx();
+};
+
+struct Op {
+  Ctx* ctx = nullptr;
+  int shape = 0, dim = 0, n = 0, Q = 0, E = 0;
+  int deformed = 1, precision = ITHACA_GPU_FP64;
+  int nm = 0, nq = 0;  // modes / points per element
+  DevTables<double> t64;
+  DevTables<float> t32;
+  // geometry: jg[e][n_jg][nq or 1], df[e][d*d][nq or 1] (FP64 always; FP32 copies for FP32 ops)
+  double* jg64 = nullptr;
+  double* df64 = nullptr;
+  float* jg32 = nullptr;
+  float* df32 = nullptr;
+  ~Op();
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (elem_*.cu), one explicit instantiation per (T, DIM). All take
+// device pointers and launch on `s`; they return false if (n, Q) is not built.
+// helm: element Helmholtz. With l2g != nullptr the input is gathered from a global
+// vector, in_e[m] = sign * x[g] with l2g[e*nm+m] = g (sign +1) or ~g (sign -1), and
+// global ids g < ndir read as zero (homogeneous Dirichlet dofs).
+template <typename T, int DIM>
+struct ElemApi {
+  static bool helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out,
+                   const int* l2g, int ndir, const int* skip, const T* lam_ptr, cudaStream_t s);
+  static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
+  static bool ipr(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
+  static bool deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
+                    cudaStream_t s);
+  static bool diag(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+};
+
+template <typename T>
+inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
+                             const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
+                             const int* skip = nullptr, const T* lam_ptr = nullptr) {
+  return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s)
+                  : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);
+}
+template <typename T>
+inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
+  return dim == 2 ? ElemApi<T, 2>::bwd(n, Q, E, tab, in, out, s) : ElemApi<T, 3>::bwd(n, Q, E, tab, in, out, s);
+}
+template <typename T>
+inline bool launch_iproduct(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in,
+                            T* out, cudaStream_t s) {
+  return dim == 2 ? ElemApi<T, 2>::ipr(n, Q, E, deformed, tab, jg, in, out, s)
+                  : ElemApi<T, 3>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
+}
+template <typename T>
+inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in,
+                             T* d0, T* d1, T* d2, cudaStream_t s) {
+  return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
+                  : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
+}
+template <typename T>
+inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
+                             T* out, cudaStream_t s) {
+  return dim == 2 ? ElemApi<T, 2>::diag(n, Q, E, deformed, tab, jg, lambda, out, s)
+                  : ElemApi<T, 3>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
+}
+
+// Geometry kernels (geom.cu)
+void launch_geom_factors(int dim, int Q, int E, const double* D, const double* coords, double* jac, double* df,
+                         int* bad, cudaStream_t s);
+template <typename T>
+void launch_build_jg(int dim, int Q, int E, int deformed, const double* w, const double* jac, const double* df,
+                     T* jg, T* dfo, cudaStream_t s);
+
+}  // namespace ithaca

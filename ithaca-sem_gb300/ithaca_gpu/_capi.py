@@ -1,0 +1,111 @@
+"""ctypes binding of lib/libithaca_gpu.so (the C ABI declared in include/ithaca_gpu.h).
+
+The library must have been built (``python ithaca-sem_gb300/build.py``); there is no
+CPU fallback: loading fails loudly when the shared object is missing.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(_PKG)
+LIB_PATH = os.path.join(ROOT, "lib", "libithaca_gpu.so")
+
+OK = 0
+ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM = 1, 2, 3, 4
+ERR_NOT_CONVERGED, ERR_GEOMETRY, ERR_TIMEOUT, ERR_NUMERIC = 5, 6, 7, 8
+SHAPE_QUAD, SHAPE_HEX = 4, 8
+FP64, FP32 = 0, 1
+SOLVE_FP64, SOLVE_MIXED_FP32 = 0, 1
+
+_ERRNAMES = {1: "ERR_ARG", 2: "ERR_UNSUPPORTED", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_NOT_CONVERGED",
+             6: "ERR_GEOMETRY", 7: "ERR_TIMEOUT", 8: "ERR_NUMERIC"}
+
+
+class GpuError(RuntimeError):
+    """A non-zero status from the C ABI (the reference would raise NekError)."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class CgOpts(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("mode", ctypes.c_int),
+                ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int), ("check_every", ctypes.c_int)]
+
+
+class CgResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("eps", ctypes.c_double), ("rhs_magnitude", ctypes.c_double)]
+
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+_pp = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> argtypes (all return int status)
+SIGNATURES = {
+    "ithaca_gpu_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+    "ithaca_gpu_version": [],
+    "ithaca_gpu_ctx_create": [_i, _pp],
+    "ithaca_gpu_ctx_destroy": [_vp],
+    "ithaca_gpu_ctx_synchronize": [_vp],
+    "ithaca_gpu_ctx_stream": [_vp, _pp],
+    "ithaca_gpu_ctx_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "ithaca_gpu_basis_modA": [_i, _i, _vp, _vp, _vp, _vp, _vp],
+    "ithaca_gpu_geom_factors": [_vp, _i, _i, _i, _vp, _vp, _vp, _i],
+    "ithaca_gpu_op_create": [_vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _i, _pp],
+    "ithaca_gpu_op_destroy": [_vp],
+    "ithaca_gpu_op_ndof": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "ithaca_gpu_bwdtrans": [_vp, _vp, _vp, _i],
+    "ithaca_gpu_iproduct": [_vp, _vp, _vp, _i],
+    "ithaca_gpu_physderiv": [_vp, _vp, _vp, _vp, _vp, _i],
+    "ithaca_gpu_helmholtz": [_vp, _d, _vp, _vp, _i],
+    "ithaca_gpu_helmholtz_diag": [_vp, _d, _vp, _i],
+    "ithaca_gpu_cg_create": [_vp, _vp, _vp, _i, _i, _pp],
+    "ithaca_gpu_cg_destroy": [_vp],
+    "ithaca_gpu_cg_default_opts": [ctypes.POINTER(CgOpts)],
+    "ithaca_gpu_cg_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_cg_apply": [_vp, _d, _vp, _vp, _i],
+    "ithaca_gpu_cg_diagonal": [_vp, _d, _vp, _i],
+    "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+}
+
+_lib = None
+
+
+def exported_symbols():
+    """Names of every entry point the header declares (checked against the .so)."""
+    return sorted(SIGNATURES)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with python ithaca-sem_gb300/build.py "
+                               "(the GPU path has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = None if name == "ithaca_gpu_cg_default_opts" else ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().ithaca_gpu_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc):
+    if rc != OK:
+        raise GpuError(rc, last_error())
+    return rc
+
+
+def call(name, *args):
+    return check(getattr(lib(), name)(*args))

@@ -1,0 +1,238 @@
+"""Python mirror of the reference operator interfaces over the C ABI.
+
+* ``Context``           -- a device + stream (ithaca_gpu_ctx).
+* ``geom_factors``      -- GeomFactors::ComputeJac/ComputeDerivFactors on the GPU.
+* ``Collection``        -- one collection of same-shape elements with the GPU
+                           implementation of BwdTrans / IProductWRTBase / PhysDeriv /
+                           Helmholtz (Collections/Collection.h:119-171 ApplyOperator).
+* ``GlobalLinSysIterativeFullGPU`` -- the C0 global Helmholtz system solved by the
+                           reference CG recurrence (MultiRegions/GlobalLinSysIterativeFull.cpp)
+                           in FP64 or in mixed precision.
+
+Arrays are numpy arrays (host; the library copies them) or CUDA tensors exposing
+``data_ptr()`` and ``is_cuda`` (device; no copy). Element arrays use the reference
+layouts (include/ithaca_gpu.h). Errors raise ``GpuError`` as the reference raises NekError.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+
+SHAPES = {"quad": C.SHAPE_QUAD, "hex": C.SHAPE_HEX}
+PRECISIONS = {"fp64": C.FP64, "fp32": C.FP32}
+SOLVE_MODES = {"fp64": C.SOLVE_FP64, "mixed": C.SOLVE_MIXED_FP32}
+
+
+def _is_device(a):
+    return getattr(a, "is_cuda", False)
+
+
+def _ptr(a, dtype=None):
+    """(pointer, on_device) for a numpy array or a CUDA tensor."""
+    if a is None:
+        return None, 1
+    if _is_device(a):
+        if not a.is_contiguous():
+            raise ValueError("device tensors must be contiguous")
+        return ctypes.c_void_p(a.data_ptr()), 1
+    if not isinstance(a, np.ndarray) or not a.flags.c_contiguous:
+        raise ValueError("host arrays must be C-contiguous numpy arrays")
+    if dtype is not None and a.dtype != dtype:
+        raise ValueError(f"expected {np.dtype(dtype)} array, got {a.dtype}")
+    return ctypes.c_void_p(a.ctypes.data), 0
+
+
+class Context:
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        C.call("ithaca_gpu_ctx_create", device, ctypes.byref(h))
+        self.handle = h
+        self.device = device
+
+    def synchronize(self):
+        C.call("ithaca_gpu_ctx_synchronize", self.handle)
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        C.call("ithaca_gpu_ctx_stream", self.handle, ctypes.byref(s))
+        return s.value
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        C.call("ithaca_gpu_ctx_launch_count", self.handle, ctypes.byref(n))
+        return n.value
+
+    def close(self):
+        if self.handle:
+            C.call("ithaca_gpu_ctx_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def basis_modA(nmodes, npoints):
+    """(z, w, D, B, DB) host tables computed by the library (ModifiedA on GLL)."""
+    z, w = np.zeros(npoints), np.zeros(npoints)
+    D = np.zeros(npoints * npoints)
+    B, DB = np.zeros(nmodes * npoints), np.zeros(nmodes * npoints)
+    C.call("ithaca_gpu_basis_modA", nmodes, npoints, *[ctypes.c_void_p(a.ctypes.data) for a in (z, w, D, B, DB)])
+    return z, w, D, B, DB
+
+
+def geom_factors(ctx, shape, npoints, coords):
+    """coords (d, E, Q^d) -> (jac (E*Q^d,), df (d*d, E*Q^d)) computed on the GPU."""
+    dim = 2 if shape == "quad" else 3
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    E = coords.shape[1]
+    nq = npoints ** dim
+    jac = np.zeros(E * nq)
+    df = np.zeros((dim * dim, E * nq))
+    C.call("ithaca_gpu_geom_factors", ctx.handle, SHAPES[shape], npoints, E, ctypes.c_void_p(coords.ctypes.data),
+           ctypes.c_void_p(jac.ctypes.data), ctypes.c_void_p(df.ctypes.data), 0)
+    return jac, df
+
+
+class Collection:
+    """Element operators for one collection (ImplementationType "GPU")."""
+
+    def __init__(self, ctx, shape, nmodes, npoints, nelmt, jac, df, deformed=True, precision="fp64"):
+        self.ctx = ctx
+        self.shape = shape
+        self.dim = 2 if shape == "quad" else 3
+        self.n, self.Q, self.E = nmodes, npoints, nelmt
+        self.nm, self.nq = nmodes ** self.dim, npoints ** self.dim
+        self.precision = precision
+        self.dtype = np.float64 if precision == "fp64" else np.float32
+        jac = np.ascontiguousarray(jac, dtype=np.float64)
+        df = np.ascontiguousarray(df, dtype=np.float64)
+        h = ctypes.c_void_p()
+        C.call("ithaca_gpu_op_create", ctx.handle, SHAPES[shape], nmodes, npoints, nelmt,
+               ctypes.c_void_p(jac.ctypes.data), ctypes.c_void_p(df.ctypes.data), int(bool(deformed)),
+               PRECISIONS[precision], 0, ctypes.byref(h))
+        self.handle = h
+
+    def Ndof(self):
+        n = ctypes.c_longlong()
+        C.call("ithaca_gpu_op_ndof", self.handle, ctypes.byref(n))
+        return n.value
+
+    def _out(self, a, size):
+        if a is not None:
+            return a
+        return np.zeros(size, dtype=self.dtype)
+
+    def bwdtrans(self, inp, out=None):
+        out = self._out(out, self.E * self.nq)
+        pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_bwdtrans", self.handle, pi, po, d)
+        return out
+
+    def iproduct(self, inp, out=None):
+        out = self._out(out, self.E * self.nm)
+        pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_iproduct", self.handle, pi, po, d)
+        return out
+
+    def physderiv(self, inp, outs=None):
+        outs = outs or [self._out(None, self.E * self.nq) for _ in range(self.dim)]
+        pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
+        ps = [_ptr(o)[0] for o in outs] + [None] * (3 - len(outs))
+        C.call("ithaca_gpu_physderiv", self.handle, pi, ps[0], ps[1], ps[2], d)
+        return outs
+
+    def helmholtz(self, lam, inp, out=None):
+        out = self._out(out, self.E * self.nm)
+        pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_helmholtz", self.handle, ctypes.c_double(lam), pi, po, d)
+        return out
+
+    def helmholtz_diag(self, lam, out=None):
+        out = out if out is not None else np.zeros(self.E * self.nm)
+        po, d = _ptr(out)
+        C.call("ithaca_gpu_helmholtz_diag", self.handle, ctypes.c_double(lam), po, d)
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.call("ithaca_gpu_op_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GlobalLinSysIterativeFullGPU:
+    """C0 global Helmholtz system + Jacobi-preconditioned CG on the GPU."""
+
+    def __init__(self, coll, amap):
+        if coll.precision != "fp64":
+            raise ValueError("the global system needs an FP64 collection (mixed mode derives its FP32 copy)")
+        self.coll, self.amap = coll, amap
+        l2g = np.ascontiguousarray(amap.l2g, dtype=np.int32)
+        sign = np.ascontiguousarray(amap.sign, dtype=np.float64)
+        h = ctypes.c_void_p()
+        C.call("ithaca_gpu_cg_create", coll.handle, ctypes.c_void_p(l2g.ctypes.data),
+               ctypes.c_void_p(sign.ctypes.data), amap.nglobal, amap.ndir, ctypes.byref(h))
+        self.handle = h
+
+    @staticmethod
+    def options(tol=1e-9, max_iter=5000, mode="fp64", inner_tol=1e-4, max_outer=50, check_every=8):
+        o = C.CgOpts()
+        C.lib().ithaca_gpu_cg_default_opts(ctypes.byref(o))
+        o.tol, o.max_iter, o.mode = tol, max_iter, SOLVE_MODES[mode]
+        o.inner_tol, o.max_outer, o.check_every = inner_tol, max_outer, check_every
+        return o
+
+    def solve(self, lam, rhs, x=None, **kw):
+        x = x if x is not None else np.zeros(self.amap.nglobal)
+        res = C.CgResult()
+        o = self.options(**kw)
+        pr, d = _ptr(rhs, np.float64 if not _is_device(rhs) else None)
+        px, _ = _ptr(x)
+        C.call("ithaca_gpu_cg_solve", self.handle, ctypes.c_double(lam), pr, px, ctypes.byref(o), ctypes.byref(res), d)
+        return x, res
+
+    def apply(self, lam, x, y=None):
+        y = y if y is not None else np.zeros(self.amap.nglobal)
+        px, d = _ptr(x, np.float64 if not _is_device(x) else None)
+        py, _ = _ptr(y)
+        C.call("ithaca_gpu_cg_apply", self.handle, ctypes.c_double(lam), px, py, d)
+        return y
+
+    def diagonal(self, lam, out=None):
+        out = out if out is not None else np.zeros(self.amap.nglobal - self.amap.ndir)
+        po, d = _ptr(out)
+        C.call("ithaca_gpu_cg_diagonal", self.handle, ctypes.c_double(lam), po, d)
+        return out
+
+    def helmsolve(self, lam, forcing, out=None, **kw):
+        out = out if out is not None else np.zeros(self.coll.E * self.coll.nm)
+        res = C.CgResult()
+        o = self.options(**kw)
+        pf, d = _ptr(forcing, np.float64 if not _is_device(forcing) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_helmsolve", self.handle, ctypes.c_double(lam), pf, po, ctypes.byref(o), ctypes.byref(res), d)
+        return out, res
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.call("ithaca_gpu_cg_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

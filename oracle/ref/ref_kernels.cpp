@@ -1,0 +1,470 @@
+// Oracle driver around the reference's OWN arithmetic (test infrastructure only).
+//
+// Compiled by oracle/ref/Makefile against the unmodified reference sources
+//   library/LibUtilities/Polylib/Polylib.cpp            (GLL points, weights, D)
+//   library/MatrixFreeOps/{BwdTrans,IProduct,PhysDeriv}Kernels.hpp
+//   library/LibUtilities/SimdLib/*.hpp                  (tinysimd; scalar width 1)
+// into oracle/_ref/libithaca_ref.so. This file only drives those kernels the way the
+// reference operators do; every driver cites the reference routine it restates.
+// It also provides the reference-path CPU baseline (multi-threaded element loop and
+// the reference CG recurrence around it).
+
+#include <LibUtilities/BasicConst/NektarUnivTypeDefs.hpp>
+#include <LibUtilities/Polylib/Polylib.h>
+#include <boost/core/ignore_unused.hpp>
+#include <MatrixFreeOps/BwdTransKernels.hpp>
+#include <MatrixFreeOps/IProductKernels.hpp>
+#include <MatrixFreeOps/PhysDerivKernels.hpp>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+using namespace Nektar;
+using namespace Nektar::MatrixFree;
+using vvec = std::vector<vec_t, tinysimd::allocator<vec_t>>;
+static constexpr int W = vec_t::width;
+
+namespace {
+
+// ---- basis -----------------------------------------------------------------
+// GaussPoints::CalculatePoints / CalculateDerivMatrix for eGaussLobattoLegendre
+// (LibUtilities/Foundations/GaussPoints.cpp:91-92,178-179,235).
+void gll_tables(int Q, double* z, double* w, double* D) {
+  Polylib::zwglj(z, w, Q, 0.0, 0.0);
+  Polylib::Dglj(D, z, Q, 0.0, 0.0);  // raw storage copied as-is into the column-major matrix
+}
+
+// Basis::GenBasis eModified_A (LibUtilities/Foundations/Basis.cpp:392-421).
+void modA_tables(int n, int Q, const double* z, const double* D, double* B, double* DB) {
+  for (int i = 0; i < Q; ++i) {
+    B[i] = 0.5 * (1 - z[i]);
+    B[Q + i] = 0.5 * (1 + z[i]);
+  }
+  for (int p = 2; p < n; ++p) {
+    double* mode = B + p * Q;
+    Polylib::jacobfd(Q, z, mode, nullptr, p - 2, 1.0, 1.0);
+    for (int i = 0; i < Q; ++i) mode[i] *= B[i] * B[Q + i];
+  }
+  // DB = D * B with D column-major (Q x Q) and B column-major (Q x n)
+  for (int p = 0; p < n; ++p)
+    for (int i = 0; i < Q; ++i) {
+      double s = 0;
+      for (int k = 0; k < Q; ++k) s += D[k * Q + i] * B[p * Q + k];
+      DB[p * Q + i] = s;
+    }
+}
+
+struct Tables {
+  vvec b, db, D, w;
+};
+
+Tables make_tables(int n, int Q) {
+  std::vector<double> z(Q), w(Q), D(Q * Q), B(n * Q), DB(n * Q);
+  gll_tables(Q, z.data(), w.data(), D.data());
+  modA_tables(n, Q, z.data(), D.data(), B.data(), DB.data());
+  Tables t;
+  t.b.assign(B.begin(), B.end());
+  t.db.assign(DB.begin(), DB.end());
+  t.D.assign(D.begin(), D.end());
+  t.w.assign(w.begin(), w.end());
+  return t;
+}
+
+// ---- geometry interleave (Collections/CoalescedGeomData.cpp:115-198, 315-403) ----
+// Reference layouts in: jac[e*nq + q] (deformed) or jac[e]; df[dir][e*nq + q] or df[dir][e].
+struct Geo {
+  vvec jac, df;
+};
+
+Geo interleave(int dim, int nq, int E, int Epad, const double* jac, const double* df, bool deformed) {
+  const int ndf = dim * dim;
+  const int nb = Epad / W;
+  Geo g;
+  alignas(64) double tmp[16];
+  if (deformed) {
+    g.jac.resize((size_t)nb * nq);
+    g.df.resize((size_t)nb * nq * ndf);
+    for (int b = 0; b < nb; ++b)
+      for (int q = 0; q < nq; ++q) {
+        for (int j = 0; j < W; ++j) {
+          int e = b * W + j;
+          tmp[j] = e < E ? jac[(size_t)e * nq + q] : 0.0;
+        }
+        g.jac[(size_t)b * nq + q].load(tmp);
+        for (int dir = 0; dir < ndf; ++dir) {
+          for (int j = 0; j < W; ++j) {
+            int e = b * W + j;
+            tmp[j] = e < E ? df[(size_t)dir * E * nq + (size_t)e * nq + q] : 0.0;
+          }
+          g.df[((size_t)b * nq + q) * ndf + dir].load(tmp);
+        }
+      }
+  } else {
+    g.jac.resize(nb);
+    g.df.resize((size_t)nb * ndf);
+    for (int b = 0; b < nb; ++b) {
+      for (int j = 0; j < W; ++j) tmp[j] = b * W + j < E ? jac[b * W + j] : 0.0;
+      g.jac[b].load(tmp);
+      for (int dir = 0; dir < ndf; ++dir) {
+        for (int j = 0; j < W; ++j) tmp[j] = b * W + j < E ? df[(size_t)dir * E + b * W + j] : 0.0;
+        g.df[(size_t)b * ndf + dir].load(tmp);
+      }
+    }
+  }
+  return g;
+}
+
+template <class F>
+void parallel_blocks(int nb, int nthreads, F f) {
+  nthreads = std::max(1, std::min(nthreads, nb));
+  if (nthreads == 1) {
+    f(0, nb);
+    return;
+  }
+  std::vector<std::thread> th;
+  int chunk = (nb + nthreads - 1) / nthreads;
+  for (int t = 0; t < nthreads; ++t) {
+    int b0 = t * chunk, b1 = std::min(nb, b0 + chunk);
+    if (b0 >= b1) break;
+    th.emplace_back([=] { f(b0, b1); });
+  }
+  for (auto& x : th) x.join();
+}
+
+// ---- Helmholtz: HelmholtzQuadImpl (MatrixFreeOps/Helmholtz.h:137-275) ----
+template <int N, int Q, bool DEF>
+void helm_quad(const Tables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int nm = N * N, nq = Q * Q, ndf = 4;
+  constexpr int wspSize = (Q > Q * N) ? Q : Q * N;
+  vec_t wsp[wspSize];
+  vvec tmpIn(nm), tmpOut(nm), bwd(nq), d0v(nq), d1v(nq);
+  const int dfSize = DEF ? ndf * nq : ndf;
+  vec_t df0, df1, df2, df3, m00, m01, m11;
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * dfSize];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nm * W, nm, tmpIn);
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2]; df3 = df_ptr[3];
+      m00 = df0 * df0; m00.fma(df2, df2);
+      m01 = df0 * df1; m01.fma(df2, df3);
+      m11 = df1 * df1; m11.fma(df3, df3);
+    }
+    BwdTransQuadKernel<N, N, Q, Q>(tmpIn, t.b, t.b, wsp, bwd);
+    IProductQuadKernel<N, N, Q, Q, true, false, DEF>(bwd, t.b, t.b, t.w, t.w, jac_ptr, wsp, tmpOut, lambda);
+    PhysDerivTensor2DKernel<Q, Q>(bwd, t.D, t.D, d0v, d1v);
+    for (int c = 0; c < nq; ++c) {
+      if (DEF) {
+        df0 = df_ptr[c * ndf]; df1 = df_ptr[c * ndf + 1]; df2 = df_ptr[c * ndf + 2]; df3 = df_ptr[c * ndf + 3];
+        m00 = df0 * df0; m00.fma(df2, df2);
+        m01 = df0 * df1; m01.fma(df2, df3);
+        m11 = df1 * df1; m11.fma(df3, df3);
+      }
+      vec_t a = d0v[c], b = d1v[c];
+      vec_t t0 = m00 * a; t0.fma(m01, b);
+      vec_t t1 = m01 * a; t1.fma(m11, b);
+      bwd[c] = t0;
+      d0v[c] = t1;
+    }
+    IProductQuadKernel<N, N, Q, Q, false, true, DEF>(bwd, t.db, t.b, t.w, t.w, jac_ptr, wsp, tmpOut);
+    IProductQuadKernel<N, N, Q, Q, false, true, DEF>(d0v, t.b, t.db, t.w, t.w, jac_ptr, wsp, tmpOut);
+    deinterleave_store(tmpOut, nm, out + (size_t)e * nm * W);
+  }
+}
+
+// ---- Helmholtz: HelmholtzHexImpl (MatrixFreeOps/Helmholtz.h:763-993) ----
+template <int N, int Q, bool DEF>
+void helm_hex(const Tables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int nm = N * N * N, nq = Q * Q * Q, ndf = 9;
+  std::vector<vec_t> w1(nq), w2(nq);
+  vvec tmpIn(nm), tmpOut(nm), bwd(nq), d0v(nq), d1v(nq), d2v(nq);
+  const int dfSize = DEF ? ndf * nq : ndf;
+  vec_t df[9], m00, m01, m02, m11, m12, m22;
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * dfSize];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nm * W, nm, tmpIn);
+    auto metrics = [&](const vec_t* d) {
+      m00 = d[0] * d[0]; m00.fma(d[3], d[3]); m00.fma(d[6], d[6]);
+      m01 = d[0] * d[1]; m01.fma(d[3], d[4]); m01.fma(d[6], d[7]);
+      m02 = d[0] * d[2]; m02.fma(d[3], d[5]); m02.fma(d[6], d[8]);
+      m11 = d[1] * d[1]; m11.fma(d[4], d[4]); m11.fma(d[7], d[7]);
+      m12 = d[1] * d[2]; m12.fma(d[4], d[5]); m12.fma(d[7], d[8]);
+      m22 = d[2] * d[2]; m22.fma(d[5], d[5]); m22.fma(d[8], d[8]);
+    };
+    if (!DEF) {
+      for (int k = 0; k < 9; ++k) df[k] = df_ptr[k];
+      metrics(df);
+    }
+    // The reference passes the direction-0 tables for all three directions
+    // (Helmholtz.h:843-856); for homogeneous n and Q this is the same data.
+    BwdTransHexKernel<N, N, N, Q, Q, Q>(tmpIn, t.b, t.b, t.b, w1.data(), w2.data(), bwd);
+    IProductHexKernel<N, N, N, Q, Q, Q, true, false, DEF>(bwd, t.b, t.b, t.b, t.w, t.w, t.w, jac_ptr, w1.data(),
+                                                          w2.data(), tmpOut, lambda);
+    PhysDerivTensor3DKernel<Q, Q, Q>(bwd, t.D, t.D, t.D, d0v, d1v, d2v);
+    for (int c = 0; c < nq; ++c) {
+      if (DEF) {
+        for (int k = 0; k < 9; ++k) df[k] = df_ptr[c * ndf + k];
+        metrics(df);
+      }
+      vec_t a = d0v[c], b = d1v[c], cc = d2v[c];
+      vec_t t0 = m00 * a; t0.fma(m01, b); t0.fma(m02, cc);
+      vec_t t1 = m01 * a; t1.fma(m11, b); t1.fma(m12, cc);
+      vec_t t2 = m02 * a; t2.fma(m12, b); t2.fma(m22, cc);
+      d0v[c] = t0; d1v[c] = t1; d2v[c] = t2;
+    }
+    IProductHexKernel<N, N, N, Q, Q, Q, false, true, DEF>(d0v, t.db, t.b, t.b, t.w, t.w, t.w, jac_ptr, w1.data(),
+                                                          w2.data(), tmpOut);
+    IProductHexKernel<N, N, N, Q, Q, Q, false, true, DEF>(d1v, t.b, t.db, t.b, t.w, t.w, t.w, jac_ptr, w1.data(),
+                                                          w2.data(), tmpOut);
+    IProductHexKernel<N, N, N, Q, Q, Q, false, true, DEF>(d2v, t.b, t.b, t.db, t.w, t.w, t.w, jac_ptr, w1.data(),
+                                                          w2.data(), tmpOut);
+    deinterleave_store(tmpOut, nm, out + (size_t)e * nm * W);
+  }
+}
+
+// ---- BwdTrans / IProduct / PhysDeriv operators (MatrixFreeOps/BwdTrans.h:172-331,576-734;
+//      IProduct.h:178-347,604-786; PhysDeriv.h:255-380,508-644) ----
+template <int N, int Q>
+void bwd_op(int dim, const Tables& t, const double* in, double* out, int b0, int b1) {
+  const int nm = dim == 2 ? N * N : N * N * N, nq = dim == 2 ? Q * Q : Q * Q * Q;
+  vvec tin(nm), tout(nq);
+  std::vector<vec_t> w1(Q * Q * Q), w2(Q * Q * Q);
+  for (int e = b0; e < b1; ++e) {
+    load_interleave(in + (size_t)e * nm * W, nm, tin);
+    if (dim == 2)
+      BwdTransQuadKernel<N, N, Q, Q>(tin, t.b, t.b, w1.data(), tout);
+    else
+      BwdTransHexKernel<N, N, N, Q, Q, Q>(tin, t.b, t.b, t.b, w1.data(), w2.data(), tout);
+    deinterleave_store(tout, nq, out + (size_t)e * nq * W);
+  }
+}
+
+template <int N, int Q, bool DEF>
+void iprod_op(int dim, const Tables& t, const Geo& g, const double* in, double* out, int b0, int b1) {
+  const int nm = dim == 2 ? N * N : N * N * N, nq = dim == 2 ? Q * Q : Q * Q * Q;
+  vvec tin(nq), tout(nm);
+  std::vector<vec_t> w1(Q * Q * Q), w2(Q * Q * Q);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    if (dim == 2)
+      IProductQuadKernel<N, N, Q, Q, false, false, DEF>(tin, t.b, t.b, t.w, t.w, jac_ptr, w1.data(), tout);
+    else
+      IProductHexKernel<N, N, N, Q, Q, Q, false, false, DEF>(tin, t.b, t.b, t.b, t.w, t.w, t.w, jac_ptr, w1.data(),
+                                                             w2.data(), tout);
+    deinterleave_store(tout, nm, out + (size_t)e * nm * W);
+  }
+}
+
+template <int N, int Q, bool DEF>
+void deriv_op(int dim, const Tables& t, const Geo& g, const double* in, double* o0, double* o1, double* o2, int b0,
+              int b1) {
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q;
+  const int ndf = dim * dim;
+  vvec tin(nq), a(nq), b(nq), c(nq);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nq : ndf)];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    if (dim == 2) {
+      PhysDerivQuadKernel<Q, Q, DEF>(tin, t.w, t.w, t.D, t.D, df_ptr, a, b);
+    } else {
+      PhysDerivHexKernel<Q, Q, Q, DEF>(tin, t.w, t.w, t.w, t.D, t.D, t.D, df_ptr, a, b, c);
+      deinterleave_store(c, nq, o2 + (size_t)e * nq * W);
+    }
+    deinterleave_store(a, nq, o0 + (size_t)e * nq * W);
+    deinterleave_store(b, nq, o1 + (size_t)e * nq * W);
+  }
+}
+
+// Runs fn<N, Q=N+1>(args...) for N in 2..10 (P = 1..9, Q = P + 2).
+#define ORACLE_DISPATCH(n, Q, CALL)                                    \
+  switch (n) {                                                         \
+    case 2: if (Q == 3) { CALL(2, 3); return 0; } break;               \
+    case 3: if (Q == 4) { CALL(3, 4); return 0; } break;               \
+    case 4: if (Q == 5) { CALL(4, 5); return 0; } break;               \
+    case 5: if (Q == 6) { CALL(5, 6); return 0; } break;               \
+    case 6: if (Q == 7) { CALL(6, 7); return 0; } break;               \
+    case 7: if (Q == 8) { CALL(7, 8); return 0; } break;               \
+    case 8: if (Q == 9) { CALL(8, 9); return 0; } break;               \
+    case 9: if (Q == 10) { CALL(9, 10); return 0; } break;             \
+    case 10: if (Q == 11) { CALL(10, 11); return 0; } break;           \
+    default: break;                                                    \
+  }                                                                    \
+  return 1;
+
+}  // namespace
+
+extern "C" {
+
+int ref_simd_width() { return W; }
+
+int ref_gll(int Q, double* z, double* w, double* D) {
+  gll_tables(Q, z, w, D);
+  return 0;
+}
+
+int ref_modA(int n, int Q, double* B, double* DB) {
+  std::vector<double> z(Q), w(Q), D(Q * Q);
+  gll_tables(Q, z.data(), w.data(), D.data());
+  modA_tables(n, Q, z.data(), D.data(), B, DB);
+  return 0;
+}
+
+// Element-local Helmholtz apply, reference layouts; E must be a multiple of W.
+int ref_helmholtz(int dim, int n, int Q, int E, const double* jac, const double* df, int deformed, double lambda,
+                  const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q;
+  Tables t = make_tables(n, Q);
+  Geo g = interleave(dim, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define HCALL(NN, QQ)                                                                             \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                                             \
+    if (dim == 2) {                                                                               \
+      if (deformed) helm_quad<NN, QQ, true>(t, g, lambda, in, out, b0, b1);                       \
+      else helm_quad<NN, QQ, false>(t, g, lambda, in, out, b0, b1);                               \
+    } else {                                                                                      \
+      if (deformed) helm_hex<NN, QQ, true>(t, g, lambda, in, out, b0, b1);                        \
+      else helm_hex<NN, QQ, false>(t, g, lambda, in, out, b0, b1);                                \
+    }                                                                                             \
+  })
+  ORACLE_DISPATCH(n, Q, HCALL)
+#undef HCALL
+}
+
+int ref_bwdtrans(int dim, int n, int Q, int E, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  Tables t = make_tables(n, Q);
+  const int nb = E / W;
+#define BCALL(NN, QQ) parallel_blocks(nb, nthreads, [&](int b0, int b1) { bwd_op<NN, QQ>(dim, t, in, out, b0, b1); })
+  ORACLE_DISPATCH(n, Q, BCALL)
+#undef BCALL
+}
+
+int ref_iproduct(int dim, int n, int Q, int E, const double* jac, int deformed, const double* in, double* out,
+                 int nthreads) {
+  if (E % W) return 2;
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q;
+  Tables t = make_tables(n, Q);
+  std::vector<double> dfz((size_t)dim * dim * E * (deformed ? nq : 1), 0.0);
+  Geo g = interleave(dim, nq, E, E, jac, dfz.data(), deformed != 0);
+  const int nb = E / W;
+#define ICALL(NN, QQ)                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                 \
+    if (deformed) iprod_op<NN, QQ, true>(dim, t, g, in, out, b0, b1); \
+    else iprod_op<NN, QQ, false>(dim, t, g, in, out, b0, b1);         \
+  })
+  ORACLE_DISPATCH(n, Q, ICALL)
+#undef ICALL
+}
+
+int ref_physderiv(int dim, int n, int Q, int E, const double* df, int deformed, const double* in, double* o0,
+                  double* o1, double* o2, int nthreads) {
+  if (E % W) return 2;
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q;
+  Tables t = make_tables(n, Q);
+  std::vector<double> jz((size_t)E * (deformed ? nq : 1), 1.0);
+  Geo g = interleave(dim, nq, E, E, jz.data(), df, deformed != 0);
+  const int nb = E / W;
+#define DCALL(NN, QQ)                                                                  \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                                  \
+    if (deformed) deriv_op<NN, QQ, true>(dim, t, g, in, o0, o1, o2, b0, b1);           \
+    else deriv_op<NN, QQ, false>(dim, t, g, in, o0, o1, o2, b0, b1);                   \
+  })
+  ORACLE_DISPATCH(n, Q, DCALL)
+#undef DCALL
+}
+
+// Reference CG solve for the CPU baseline: the single-reduction PCG of
+// LibUtilities/LinearAlgebra/NekLinSysIterCG.cpp:104-263 with Jacobi preconditioning
+// (MultiRegions/PreconditionerDiagonal.cpp:191-206), the matrix-free operator of
+// GlobalLinSysIterativeFull::v_DoMatrixMultiply (:215-257) = GlobalToLocal, element
+// Helmholtz, Assemble (AssemblyMapCG.cpp:2853-2910). x holds the solution on return.
+// Returns the iteration count (>=0), or -1 if max_iter was reached.
+int ref_cg_solve(int dim, int n, int Q, int E, const double* jac, const double* df, int deformed, double lambda,
+                 const int* l2g, const double* sign, int nglobal, int ndir, const double* dinv, const double* rhs,
+                 double* x, double tol, int max_iter, int nthreads, double* final_eps) {
+  if (E % W) return -2;
+  const int nm = dim == 2 ? n * n : n * n * n;
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q;
+  const size_t nloc = (size_t)E * nm;
+  Tables t = make_tables(n, Q);
+  Geo g = interleave(dim, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+  const int nnd = nglobal - ndir;
+  std::vector<double> wA(nglobal, 0.0), sA(nglobal, 0.0), p(nnd, 0.0), r(nnd), q(nnd, 0.0);
+  std::vector<double> loc_in(nloc), loc_out(nloc);
+
+  auto apply = [&](const std::vector<double>& gin, std::vector<double>& gout) -> int {
+    for (size_t i = 0; i < nloc; ++i) loc_in[i] = sign[i] * gin[l2g[i]];
+    int rc = 1;
+#define CGCALL(NN, QQ)                                                                                  \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                                                   \
+    if (dim == 2) {                                                                                     \
+      if (deformed) helm_quad<NN, QQ, true>(t, g, lambda, loc_in.data(), loc_out.data(), b0, b1);       \
+      else helm_quad<NN, QQ, false>(t, g, lambda, loc_in.data(), loc_out.data(), b0, b1);               \
+    } else {                                                                                            \
+      if (deformed) helm_hex<NN, QQ, true>(t, g, lambda, loc_in.data(), loc_out.data(), b0, b1);        \
+      else helm_hex<NN, QQ, false>(t, g, lambda, loc_in.data(), loc_out.data(), b0, b1);                \
+    }                                                                                                   \
+  });                                                                                                   \
+  rc = 0;
+    [&]() -> int { ORACLE_DISPATCH(n, Q, CGCALL) }();
+#undef CGCALL
+    rc = 0;
+    std::fill(gout.begin(), gout.end(), 0.0);
+    for (size_t i = 0; i < nloc; ++i) gout[l2g[i]] += sign[i] * loc_out[i];
+    return rc;
+  };
+  auto dot = [&](const double* a, const double* b) {
+    double s = 0;
+    for (int i = 0; i < nnd; ++i) s += a[i] * b[i];
+    return s;
+  };
+  for (int i = 0; i < nnd; ++i) r[i] = rhs[ndir + i];
+  for (int i = 0; i < nnd; ++i) x[ndir + i] = 0.0;
+  double eps = dot(r.data(), r.data());
+  double rhs_mag = 0;
+  for (int i = 0; i < nglobal; ++i) rhs_mag += rhs[i] * rhs[i];
+  rhs_mag = rhs_mag > 1e-6 ? rhs_mag : 1.0;
+  if (eps < tol * tol * rhs_mag) {
+    if (final_eps) *final_eps = eps;
+    return 0;
+  }
+  for (int i = 0; i < nnd; ++i) wA[ndir + i] = r[i] * dinv[i];
+  apply(wA, sA);
+  double rho = dot(r.data(), wA.data() + ndir), mu = dot(sA.data() + ndir, wA.data() + ndir);
+  double beta = 0.0, alpha = rho / mu;
+  int iters = 1, k = 0;
+  while (true) {
+    if (k >= max_iter) {
+      if (final_eps) *final_eps = eps;
+      return -1;
+    }
+    for (int i = 0; i < nnd; ++i) {
+      p[i] = beta * p[i] + wA[ndir + i];
+      q[i] = beta * q[i] + sA[ndir + i];
+      x[ndir + i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+    }
+    for (int i = 0; i < nnd; ++i) wA[ndir + i] = r[i] * dinv[i];
+    apply(wA, sA);
+    double rho_new = dot(r.data(), wA.data() + ndir);
+    mu = dot(sA.data() + ndir, wA.data() + ndir);
+    eps = dot(r.data(), r.data());
+    iters++;
+    if (eps < tol * tol * rhs_mag) break;
+    beta = rho_new / rho;
+    alpha = rho_new / (mu - rho_new * beta / alpha);
+    rho = rho_new;
+    k++;
+  }
+  if (final_eps) *final_eps = eps;
+  return iters;
+}
+
+}  // extern "C"

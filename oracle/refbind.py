@@ -1,0 +1,106 @@
+"""ctypes binding of oracle/_ref/libithaca_ref.so (reference kernels compiled in place).
+
+The library is built by ``oracle/ref/Makefile`` from the reference's Polylib.cpp and
+MatrixFreeOps kernel headers; see oracle/ref/ref_kernels.cpp for the drivers.
+Test infrastructure only.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libithaca_ref.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not available():
+            raise RuntimeError("oracle/_ref/libithaca_ref.so is not built (make -C oracle/ref)")
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.ref_cg_solve.restype = ctypes.c_int
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags.c_contiguous
+    if a.dtype == np.int32:
+        return a.ctypes.data_as(_ip)
+    assert a.dtype == np.float64
+    return a.ctypes.data_as(_dp)
+
+
+def gll(Q):
+    z, w, D = np.zeros(Q), np.zeros(Q), np.zeros(Q * Q)
+    lib().ref_gll(Q, _p(z), _p(w), _p(D))
+    return z, w, D
+
+
+def modA(n, Q):
+    B, DB = np.zeros(n * Q), np.zeros(n * Q)
+    lib().ref_modA(n, Q, _p(B), _p(DB))
+    return B, DB
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"{what}: reference driver returned {rc}")
+
+
+def helmholtz(dim, n, Q, E, jac, df, deformed, lam, coeffs, nthreads=1):
+    out = np.zeros(E * n ** dim)
+    rc = lib().ref_helmholtz(dim, n, Q, E, _p(np.ascontiguousarray(jac, dtype=np.float64)),
+                             _p(np.ascontiguousarray(df, dtype=np.float64)), int(deformed),
+                             ctypes.c_double(lam), _p(np.ascontiguousarray(coeffs, dtype=np.float64)),
+                             _p(out), nthreads)
+    _check(rc, "ref_helmholtz")
+    return out
+
+
+def bwdtrans(dim, n, Q, E, coeffs, nthreads=1):
+    out = np.zeros(E * Q ** dim)
+    rc = lib().ref_bwdtrans(dim, n, Q, E, _p(np.ascontiguousarray(coeffs, dtype=np.float64)), _p(out), nthreads)
+    _check(rc, "ref_bwdtrans")
+    return out
+
+
+def iproduct(dim, n, Q, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n ** dim)
+    rc = lib().ref_iproduct(dim, n, Q, E, _p(np.ascontiguousarray(jac, dtype=np.float64)), int(deformed),
+                            _p(np.ascontiguousarray(phys, dtype=np.float64)), _p(out), nthreads)
+    _check(rc, "ref_iproduct")
+    return out
+
+
+def physderiv(dim, n, Q, E, df, deformed, phys, nthreads=1):
+    outs = [np.zeros(E * Q ** dim) for _ in range(3)]
+    rc = lib().ref_physderiv(dim, n, Q, E, _p(np.ascontiguousarray(df, dtype=np.float64)), int(deformed),
+                             _p(np.ascontiguousarray(phys, dtype=np.float64)), _p(outs[0]), _p(outs[1]),
+                             _p(outs[2]), nthreads)
+    _check(rc, "ref_physderiv")
+    return outs[:dim]
+
+
+def cg_solve(dim, n, Q, E, jac, df, deformed, lam, l2g, sign, nglobal, ndir, dinv, rhs, tol, max_iter,
+             nthreads=1, x0=None):
+    x = np.zeros(nglobal) if x0 is None else np.array(x0, dtype=np.float64)
+    eps = ctypes.c_double(0.0)
+    it = lib().ref_cg_solve(dim, n, Q, E, _p(np.ascontiguousarray(jac, dtype=np.float64)),
+                            _p(np.ascontiguousarray(df, dtype=np.float64)), int(deformed), ctypes.c_double(lam),
+                            _p(np.ascontiguousarray(l2g, dtype=np.int32)),
+                            _p(np.ascontiguousarray(sign, dtype=np.float64)), nglobal, ndir,
+                            _p(np.ascontiguousarray(dinv, dtype=np.float64)),
+                            _p(np.ascontiguousarray(rhs, dtype=np.float64)), _p(x), ctypes.c_double(tol),
+                            max_iter, nthreads, ctypes.byref(eps))
+    return x, it, eps.value

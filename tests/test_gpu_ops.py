@@ -1,0 +1,125 @@
+"""GPU element operators vs the FP64 oracle (quad + hex, deformed + regular, FP64 + FP32).
+
+Tolerances: FP64 kernels 1e-12 relative (max-norm of the difference over max-norm of
+the oracle), as the reference's own collection tests demand 1e-10; FP32 kernels 2e-5.
+"""
+import numpy as np
+import pytest
+
+from cases import hex_case, quad_case, rel_err
+from oracle import ops as oops
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ithaca_gpu.operators import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _coll(ctx, c, precision="fp64"):
+    from ithaca_gpu.operators import Collection
+    return Collection(ctx, c.shape, c.n, c.Q, c.E, c.jac, c.df, deformed=c.deformed, precision=precision)
+
+
+QUAD_N = list(range(2, 11))
+HEX_N = [2, 3, 4, 5, 7, 9, 10]
+
+
+def _cases():
+    out = []
+    for n in QUAD_N:
+        out.append(("quad", n, True))
+    out += [("quad", 5, False), ("quad", 7, False)]
+    for n in HEX_N:
+        out.append(("hex", n, True))
+    out += [("hex", 5, False), ("hex", 7, False)]
+    return out
+
+
+def _make(shape, n, deformed):
+    if shape == "quad":
+        return quad_case(5, 3, n, jitter=0.1 if deformed else 0.0, seed=3, deformed=deformed)
+    return hex_case(3, 2, 2, n, amp=0.05 if deformed else 0.0, deformed=deformed)
+
+
+@pytest.mark.parametrize("shape,n,deformed", _cases())
+def test_helmholtz_fp64(ctx, shape, n, deformed):
+    c = _make(shape, n, deformed)
+    coll = _coll(ctx, c)
+    rng = np.random.default_rng(1)
+    u = rng.uniform(-1, 1, c.E * c.nm)
+    for lam in (0.0, 1.0, 10.0):
+        out = coll.helmholtz(lam, u)
+        ref = oops.helmholtz(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, lam, u)
+        assert rel_err(out, ref) < TOL64, (shape, n, lam)
+
+
+@pytest.mark.parametrize("shape,n,deformed", _cases())
+def test_bwd_iprod_deriv_fp64(ctx, shape, n, deformed):
+    c = _make(shape, n, deformed)
+    coll = _coll(ctx, c)
+    rng = np.random.default_rng(2)
+    u = rng.uniform(-1, 1, c.E * c.nm)
+    phys = coll.bwdtrans(u)
+    assert rel_err(phys, oops.bwdtrans(c.basis, c.dim, u)) < TOL64
+    f = rng.uniform(-1, 1, c.E * c.nq)
+    ip = coll.iproduct(f)
+    assert rel_err(ip, oops.iproduct(c.basis, c.dim, c.jac.reshape(c.E, -1), f)) < TOL64
+    ds = coll.physderiv(f)
+    refs = oops.physderiv(c.basis, c.dim, c.df, f)
+    for d, r in zip(ds, refs):
+        assert rel_err(d, r) < TOL64
+
+
+@pytest.mark.parametrize("shape,n,deformed", [("quad", 7, True), ("quad", 9, True), ("hex", 5, True),
+                                              ("hex", 7, True), ("hex", 9, True)])
+def test_helmholtz_fp32(ctx, shape, n, deformed):
+    c = _make(shape, n, deformed)
+    coll = _coll(ctx, c, "fp32")
+    rng = np.random.default_rng(4)
+    u = rng.uniform(-1, 1, c.E * c.nm)
+    out = coll.helmholtz(1.0, u.astype(np.float32))
+    ref = oops.helmholtz(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, 1.0, u)
+    assert rel_err(out, ref) < TOL32
+
+
+@pytest.mark.parametrize("shape,n", [("quad", 3), ("quad", 7), ("hex", 3), ("hex", 5)])
+def test_helmholtz_diag(ctx, shape, n):
+    c = _make(shape, n, True)
+    coll = _coll(ctx, c)
+    d = coll.helmholtz_diag(2.0)
+    ref = oops.helmholtz_diag(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, 2.0)
+    assert rel_err(d, ref) < TOL64
+    # and it is the diagonal of the operator the apply uses
+    E1 = quad_case(1, 1, n) if shape == "quad" else hex_case(1, 1, 1, n)
+    coll1 = _coll(ctx, E1)
+    eye = np.eye(E1.nm)
+    A = np.stack([coll1.helmholtz(2.0, np.ascontiguousarray(eye[i])) for i in range(E1.nm)], axis=1)
+    assert rel_err(coll1.helmholtz_diag(2.0), np.diag(A)) < TOL64
+
+
+def test_geom_factors_gpu(ctx):
+    from ithaca_gpu.operators import geom_factors
+    from oracle import geom as ogeom
+    for c in (quad_case(4, 3, 6), hex_case(2, 2, 2, 5)):
+        jac, df = geom_factors(ctx, c.shape, c.Q, c.X)
+        rj, rdf = ogeom.geom_factors(c.X, c.basis.D2, c.dim)
+        assert rel_err(jac, rj) < TOL64
+        assert rel_err(df, rdf) < TOL64
+
+
+def test_unsupported_order_raises(ctx):
+    from ithaca_gpu._capi import GpuError
+    from ithaca_gpu.operators import Collection
+    c = quad_case(2, 2, 5)
+    with pytest.raises(GpuError):
+        Collection(ctx, "quad", 5, 7, c.E, c.jac, c.df)  # npoints != nmodes + 1
+    with pytest.raises(GpuError):
+        Collection(ctx, "quad", 12, 13, c.E, c.jac, c.df)
