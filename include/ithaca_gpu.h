@@ -152,6 +152,11 @@ int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, dou
 /* Global operator y = Assemble(Helmholtz(GlobalToLocal(x))) in FP64 (nglobal entries;
  * Dirichlet entries of x are used as given). GlobalLinSysIterativeFull::v_DoMatrixMultiply. */
 int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, double* y, int on_device);
+/* AssemblyMapCG::Assemble (MultiRegions/AssemblyMap/AssemblyMapCG.cpp:2885-2910):
+ * global[g] = sum of sign * local over the local copies of g (nglobal entries). */
+int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* global, int on_device);
+/* AssemblyMapCG::GlobalToLocal (:2853-2876): local = sign * global[map] (E*n^d entries). */
+int ithaca_gpu_cg_global_to_local(ithaca_gpu_cg* cg, const double* global, double* local, int on_device);
 /* Assembled Jacobi diagonal over the non-Dirichlet dofs (nglobal - ndir entries). */
 int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int on_device);
 
@@ -160,6 +165,13 @@ int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int o
  * coefficient space (E*n^d): rhs = Assemble(-IProductWRTBase(f)), CG, GlobalToLocal. */
 int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
+
+/* Measurement hook (no reference counterpart): runs the gather + element-Helmholtz
+ * kernel that ithaca_gpu_cg_solve launches for `mode` `reps` times on the context
+ * stream and returns its average device time in ms (CUDA events) and the algorithmic
+ * bytes of one launch (local-vector, index and geometry traffic). */
+int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int reps, double* avg_ms,
+                                double* bytes_per_launch);
 
 #ifdef __cplusplus
 }

@@ -641,6 +641,46 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
   });
 }
 
+int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* global, int on_device) {
+  return cg_guarded([&] {
+    req(cg && local && global, "null argument");
+    Ctx* c = cg->op->ctx;
+    cudaStream_t s = c->stream;
+    const double* dl = local;
+    if (!on_device) {
+      double* d = (double*)c->stage_ptr(0, sizeof(double) * cg->nloc);
+      ITHACA_CUDA(cudaMemcpyAsync(d, local, sizeof(double) * cg->nloc, cudaMemcpyHostToDevice, s));
+      dl = d;
+    }
+    double* dg = on_device ? global : (double*)c->stage_ptr(1, sizeof(double) * cg->N);
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
+    c->launches++;
+    if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(global, dg, sizeof(double) * cg->N, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    if (!on_device) ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_cg_global_to_local(ithaca_gpu_cg* cg, const double* global, double* local, int on_device) {
+  return cg_guarded([&] {
+    req(cg && local && global, "null argument");
+    Ctx* c = cg->op->ctx;
+    cudaStream_t s = c->stream;
+    const double* dg = global;
+    if (!on_device) {
+      double* d = (double*)c->stage_ptr(0, sizeof(double) * cg->N);
+      ITHACA_CUDA(cudaMemcpyAsync(d, global, sizeof(double) * cg->N, cudaMemcpyHostToDevice, s));
+      dg = d;
+    }
+    double* dl = on_device ? local : (double*)c->stage_ptr(1, sizeof(double) * cg->nloc);
+    g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, dg, dl);
+    c->launches++;
+    if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(local, dl, sizeof(double) * cg->nloc, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    if (!on_device) ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
 int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int on_device) {
   return cg_guarded([&] {
     req(cg && diag, "null argument");
@@ -712,6 +752,42 @@ int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(out_local, dout, sizeof(double) * nloc, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int reps, double* avg_ms,
+                                double* bytes_per_launch) {
+  return cg_guarded([&] {
+    req(cg && avg_ms && reps > 0, "bad argument");
+    Op* op = cg->op;
+    cudaStream_t s = op->ctx->stream;
+    const bool f32 = mode == ITHACA_GPU_SOLVE_MIXED_FP32;
+    if (f32) ensure_fp32(cg);
+    cudaEvent_t e0, e1;
+    ITHACA_CUDA(cudaEventCreate(&e0));
+    ITHACA_CUDA(cudaEventCreate(&e1));
+    auto run = [&] {
+      if (f32)
+        launch_apply<float>(cg, cg->v32, op->t32.base, cg->jg32, (float)lambda, nullptr, cg->v32.w, s, true, nullptr);
+      else
+        launch_apply<double>(cg, cg->v64, op->t64.base, op->jg64, lambda, nullptr, cg->v64.w, s, true, nullptr);
+    };
+    run();  // warm-up
+    ITHACA_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < reps; ++i) run();
+    ITHACA_CUDA(cudaEventRecord(e1, s));
+    ITHACA_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    ITHACA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *avg_ms = ms / reps;
+    if (bytes_per_launch) {
+      // per element: l2g index (4 B) + gathered input + output per local dof, geometry per point
+      const double es = f32 ? 4.0 : 8.0;
+      const double npt = op->deformed ? op->nq : 1;
+      *bytes_per_launch = (double)op->E * (op->nm * (4.0 + 2.0 * es) + n_jg(op->dim) * npt * es);
+    }
   });
 }
 

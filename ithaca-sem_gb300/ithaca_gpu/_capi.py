@@ -69,7 +69,10 @@ SIGNATURES = {
     "ithaca_gpu_cg_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_cg_apply": [_vp, _d, _vp, _vp, _i],
     "ithaca_gpu_cg_diagonal": [_vp, _d, _vp, _i],
+    "ithaca_gpu_cg_assemble": [_vp, _vp, _vp, _i],
+    "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_cg_profile_apply": [_vp, _i, _d, _i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
 }
 
 _lib = None

@@ -86,8 +86,18 @@ def basis_modA(nmodes, npoints):
 
 
 def geom_factors(ctx, shape, npoints, coords):
-    """coords (d, E, Q^d) -> (jac (E*Q^d,), df (d*d, E*Q^d)) computed on the GPU."""
+    """coords (d, E, Q^d) -> (jac (E*Q^d,), df (d*d, E*Q^d)) computed on the GPU.
+    Host numpy in -> host numpy out; CUDA tensor in -> CUDA tensors out."""
     dim = 2 if shape == "quad" else 3
+    if _is_device(coords):
+        import torch
+        E = coords.shape[1]
+        nq = npoints ** dim
+        jac = torch.empty(E * nq, dtype=torch.float64, device=coords.device)
+        df = torch.empty((dim * dim, E * nq), dtype=torch.float64, device=coords.device)
+        C.call("ithaca_gpu_geom_factors", ctx.handle, SHAPES[shape], npoints, E, ctypes.c_void_p(coords.data_ptr()),
+               ctypes.c_void_p(jac.data_ptr()), ctypes.c_void_p(df.data_ptr()), 1)
+        return jac, df
     coords = np.ascontiguousarray(coords, dtype=np.float64)
     E = coords.shape[1]
     nq = npoints ** dim
@@ -109,12 +119,14 @@ class Collection:
         self.nm, self.nq = nmodes ** self.dim, npoints ** self.dim
         self.precision = precision
         self.dtype = np.float64 if precision == "fp64" else np.float32
-        jac = np.ascontiguousarray(jac, dtype=np.float64)
-        df = np.ascontiguousarray(df, dtype=np.float64)
+        if not _is_device(jac):
+            jac = np.ascontiguousarray(jac, dtype=np.float64)
+            df = np.ascontiguousarray(df, dtype=np.float64)
+        pj, on_dev = _ptr(jac)
+        pd, _ = _ptr(df)
         h = ctypes.c_void_p()
-        C.call("ithaca_gpu_op_create", ctx.handle, SHAPES[shape], nmodes, npoints, nelmt,
-               ctypes.c_void_p(jac.ctypes.data), ctypes.c_void_p(df.ctypes.data), int(bool(deformed)),
-               PRECISIONS[precision], 0, ctypes.byref(h))
+        C.call("ithaca_gpu_op_create", ctx.handle, SHAPES[shape], nmodes, npoints, nelmt, pj, pd,
+               int(bool(deformed)), PRECISIONS[precision], on_dev, ctypes.byref(h))
         self.handle = h
 
     def Ndof(self):
@@ -210,6 +222,31 @@ class GlobalLinSysIterativeFullGPU:
         py, _ = _ptr(y)
         C.call("ithaca_gpu_cg_apply", self.handle, ctypes.c_double(lam), px, py, d)
         return y
+
+    def assemble(self, loc, out=None):
+        """AssemblyMapCG::Assemble on the GPU (local E*n^d -> global nglobal)."""
+        out = out if out is not None else np.zeros(self.amap.nglobal)
+        pl, d = _ptr(loc, np.float64 if not _is_device(loc) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_cg_assemble", self.handle, pl, po, d)
+        return out
+
+    def global_to_local(self, glob, out=None):
+        """AssemblyMapCG::GlobalToLocal on the GPU (global -> local E*n^d)."""
+        out = out if out is not None else np.zeros(self.coll.E * self.coll.nm)
+        pg, d = _ptr(glob, np.float64 if not _is_device(glob) else None)
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_cg_global_to_local", self.handle, pg, po, d)
+        return out
+
+    def profile_apply(self, lam, mode="mixed", reps=20):
+        """Average device time (ms) of the gather + element-apply kernel the solver
+        launches for `mode`, timed with CUDA events on the context stream, and the
+        algorithmic bytes of one launch."""
+        ms, nbytes = ctypes.c_double(), ctypes.c_double()
+        C.call("ithaca_gpu_cg_profile_apply", self.handle, SOLVE_MODES[mode], ctypes.c_double(lam), reps,
+               ctypes.byref(ms), ctypes.byref(nbytes))
+        return ms.value, nbytes.value
 
     def diagonal(self, lam, out=None):
         out = out if out is not None else np.zeros(self.amap.nglobal - self.amap.ndir)

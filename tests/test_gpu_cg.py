@@ -1,0 +1,136 @@
+"""GPU global system + CG vs the oracle's restatement of the reference recurrence.
+
+FP64 mode must reproduce the reference iteration count (within one iteration: the
+reductions are summed in a different order) and the solution to 1e-10 relative;
+the mixed mode must reach the requested FP64 relative residual.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cases import hex_case, quad_case, rel_err
+from oracle import ops as oops
+from oracle import solve as osolve
+
+pytestmark = pytest.mark.gpu
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ithaca_gpu.operators import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _system(ctx, c):
+    from ithaca_gpu.operators import Collection, GlobalLinSysIterativeFullGPU
+    coll = Collection(ctx, c.shape, c.n, c.Q, c.E, c.jac, c.df, deformed=c.deformed)
+    amap = c.mesh.assembly(c.n)
+    return coll, amap, GlobalLinSysIterativeFullGPU(coll, amap)
+
+
+def _forcing(c):
+    f = np.sin(np.pi * c.X[0]) * np.sin(np.pi * c.X[1])
+    if c.dim == 3:
+        f = f * np.sin(np.pi * c.X[2])
+    return f.reshape(-1)
+
+
+def test_golden_reference_cg(ctx):
+    """The reference CG recurrence on tests/golden/cg_quad.npz (4x4 quads, 5 modes)."""
+    from ithaca_gpu.operators import Collection, GlobalLinSysIterativeFullGPU
+    from ithaca_gpu.mesh import AssemblyMap
+    g = np.load(os.path.join(G, "cg_quad.npz"))
+    n, Q = 5, 6
+    E = g["l2g"].size // (n * n)
+    coll = Collection(ctx, "quad", n, Q, E, g["jac"], g["df"])
+    amap = AssemblyMap(g["l2g"], g["sign"], int(g["nglobal"]), int(g["ndir"]))
+    sys_ = GlobalLinSysIterativeFullGPU(coll, amap)
+    diag = sys_.diagonal(1.0)
+    assert rel_err(1.0 / diag, g["dinv"]) < 1e-12
+    x, res = sys_.solve(1.0, g["rhs"], tol=1e-12)
+    assert abs(res.iterations - int(g["iterations"])) <= 1
+    assert rel_err(x[amap.ndir:], g["x"][amap.ndir:]) < 1e-10
+
+
+@pytest.mark.parametrize("kind", ["quad_p6", "quad_rot_p4", "hex_p4", "quad_regular_p6"])
+def test_fp64_cg_matches_oracle(ctx, kind):
+    if kind == "quad_p6":
+        c = quad_case(6, 5, 7)
+    elif kind == "quad_rot_p4":
+        c = quad_case(5, 4, 5, rotate=np.random.default_rng(9).integers(0, 4, 20))
+    elif kind == "quad_regular_p6":
+        c = quad_case(4, 4, 7, jitter=0.0, deformed=False)
+    else:
+        c = hex_case(3, 2, 2, 5)
+    coll, amap, sys_ = _system(ctx, c)
+    lam = 1.0
+    rhs = -osolve.Map.of(amap).assemble(oops.iproduct(c.basis, c.dim, c.jac.reshape(c.E, -1), _forcing(c)))
+    # global operator
+    xr = np.random.default_rng(3).uniform(-1, 1, amap.nglobal)
+    y = sys_.apply(lam, xr)
+    yo = osolve.global_apply(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, lam, amap, xr, zero_dir=False)
+    assert rel_err(y, yo) < 1e-12
+    x, res = sys_.solve(lam, rhs, tol=1e-11)
+    xo, it_o, _, _ = osolve.solve(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, lam, amap, rhs, tol=1e-11)
+    assert abs(res.iterations - it_o) <= 1, (res.iterations, it_o)
+    assert rel_err(x[amap.ndir:], xo[amap.ndir:]) < 1e-9
+    assert res.rel_residual < 1e-10
+
+
+@pytest.mark.parametrize("lam", [0.1, 1.0, 10.0])
+def test_mixed_reaches_fp64_residual(ctx, lam):
+    c = quad_case(8, 8, 7)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = -osolve.Map.of(amap).assemble(oops.iproduct(c.basis, 2, c.jac.reshape(c.E, -1), _forcing(c)))
+    x, res = sys_.solve(lam, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+    assert res.outer_iterations >= 1
+    xo, _, _, _ = osolve.solve(c.basis, 2, c.jac.reshape(c.E, -1), c.df, lam, amap, rhs, tol=1e-13)
+    assert rel_err(x[amap.ndir:], xo[amap.ndir:]) < 1e-8
+
+
+def test_helmsolve_matches_analytic(ctx):
+    c = quad_case(8, 8, 7, jitter=0.1, seed=0)
+    coll, amap, sys_ = _system(ctx, c)
+    out, res = sys_.helmsolve(1.0, _forcing(c), tol=1e-12)
+    phys = oops.bwdtrans(c.basis, 2, out).reshape(-1)
+    exact = -_forcing(c) / (2 * np.pi ** 2 + 1.0)
+    assert np.max(np.abs(phys - exact)) < 1e-10
+
+
+def test_deterministic_iterations(ctx):
+    c = hex_case(2, 2, 2, 4)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(0).uniform(-1, 1, amap.nglobal)
+    x1, r1 = sys_.solve(1.0, rhs, tol=1e-12)
+    x2, r2 = sys_.solve(1.0, rhs, tol=1e-12)
+    assert r1.iterations == r2.iterations
+    assert np.array_equal(x1, x2)
+
+
+def test_max_iter_reports_not_converged(ctx):
+    from ithaca_gpu._capi import ERR_NOT_CONVERGED, GpuError
+    c = quad_case(4, 4, 5)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(1).uniform(-1, 1, amap.nglobal)
+    with pytest.raises(GpuError) as ei:
+        sys_.solve(1.0, rhs, tol=1e-14, max_iter=3)
+    assert ei.value.code == ERR_NOT_CONVERGED
+    # the context stays usable
+    x, res = sys_.solve(1.0, rhs, tol=1e-10)
+    assert res.rel_residual < 1e-9
+
+
+def test_nan_rhs_reports_numeric(ctx):
+    from ithaca_gpu._capi import ERR_NUMERIC, GpuError
+    c = quad_case(3, 3, 4)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.ones(amap.nglobal)
+    rhs[amap.ndir + 2] = np.nan
+    with pytest.raises(GpuError) as ei:
+        sys_.solve(1.0, rhs)
+    assert ei.value.code == ERR_NUMERIC
