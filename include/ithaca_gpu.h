@@ -166,6 +166,46 @@ int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int o
 int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
 
+/* ---- variable coefficient and adjoint gradient ----
+ * Isotropic diffusion coefficient kappa at the quadrature points (E*Q^d) of a deformed
+ * collection: the solver's operator becomes lambda M + L_kappa, the reference's
+ * LaplacianMatrixOp_MatFree with eVarCoeffD00 = eVarCoeffD11 [= D22] = kappa
+ * (StdRegions/StdExpansion.cpp:664-717). kappa == NULL restores kappa = 1. */
+int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_device);
+/* Misfit J = sum_q Jw_q (u(x_q) - u_target_q)^2 of the global vector x (Dirichlet
+ * values taken as zero) and, if dJdx != NULL, its gradient w.r.t. x (nglobal entries,
+ * zero on Dirichlet dofs). No reference counterpart (the reference has no adjoint). */
+int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target, double* J, double* dJdx,
+                      int on_device);
+/* dJ/dkappa_q = -Jw_q grad psi(x_q) . grad u(x_q) for the forward solution x and the
+ * adjoint solution psi of A(kappa) psi = dJ/dx (E*Q^d entries). No reference counterpart. */
+int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* psi, double* grad, int on_device);
+
+/* ---- POD reduced basis (solvers/IncNavierStokesSolver/EquationSystems/CoupledLinearNS_ROM.cpp) ----
+ * Column-major FP64 matrices throughout. */
+
+/* Gram matrix C = S^T S (ns x ns) of the snapshot matrix S (N x ns). */
+int ithaca_gpu_pod_gram(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, double* C, int on_device);
+/* ROM_offline_phase (:3916-4001) by the method of snapshots: the leading `nmodes`
+ * orthonormal POD modes V (N x nmodes) and all ns singular values sigma (descending).
+ * *nmodes_out < nmodes when trailing modes are not resolved in FP64. */
+int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, int nmodes, double* V,
+                           double* sigma, int* nmodes_out, int on_device);
+/* Reduced-basis size from the cumulative singular-value fraction (:3935-3944). Host only. */
+int ithaca_gpu_pod_rb_size(int ns, const double* sigma, double pod_tolerance, int* size);
+/* Affine reduced operators A_L = V^T L V, A_M = V^T M V (nmodes x nmodes) for the
+ * Helmholtz system of `cg`; V holds nmodes columns over the nglobal - ndir free dofs
+ * (gen_reference_matrices :3904-3911, gen_affine_mat_proj :4694-4703). */
+int ithaca_gpu_pod_project(ithaca_gpu_cg* cg, int nmodes, const double* V, double* A_L, double* A_M,
+                           int on_device);
+/* ROM_online_phase (:4003-4100): x_r[k] solves (A_L + lambdas[k] A_M) x = f_r for each of
+ * nlambda parameters (r <= 64), FP64 LU with partial pivoting; x_r is r x nlambda. */
+int ithaca_gpu_pod_online(ithaca_gpu_ctx* ctx, int r, const double* A_L, const double* A_M, const double* f_r,
+                          int nlambda, const double* lambdas, double* x_r, int on_device);
+/* Reconstruction u = V x_r (:4054), N x nsol. */
+int ithaca_gpu_pod_reconstruct(ithaca_gpu_ctx* ctx, int N, int r, const double* V, int nsol, const double* x_r,
+                               double* u, int on_device);
+
 /* Measurement hook (no reference counterpart): runs the gather + element-Helmholtz
  * kernel that ithaca_gpu_cg_solve launches for `mode` `reps` times on the context
  * stream and returns its average device time in ms (CUDA events) and the algorithmic

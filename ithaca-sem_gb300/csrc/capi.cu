@@ -37,6 +37,8 @@ void* Ctx::stage_ptr(int slot, size_t bytes) {
 Ctx::~Ctx() {
   for (auto& p : stage)
     if (p) cudaFree(p);
+  if (ev_in) cudaEventDestroy(ev_in);
+  if (ev_out) cudaEventDestroy(ev_out);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -130,6 +132,20 @@ using namespace ithaca;
 struct ithaca_gpu_ctx : public Ctx {};
 struct ithaca_gpu_op : public Op {};
 
+namespace ithaca {
+void retain_op(Op* op) { op->refs++; }
+void release_op(Op* op) {
+  if (--op->refs == 0) {
+    Ctx* c = op->ctx;
+    delete static_cast<ithaca_gpu_op*>(op);
+    release_ctx(c);
+  }
+}
+void release_ctx(Ctx* c) {
+  if (c && --c->refs == 0) delete static_cast<ithaca_gpu_ctx*>(c);
+}
+}  // namespace ithaca
+
 extern "C" {
 
 int ithaca_gpu_last_error(char* buf, size_t len) {
@@ -150,6 +166,8 @@ int ithaca_gpu_ctx_create(int device, ithaca_gpu_ctx** ctx) {
     auto c = std::make_unique<ithaca_gpu_ctx>();
     c->device = device;
     ITHACA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    ITHACA_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
+    ITHACA_CUDA(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming));
     *ctx = c.release();
   });
 }
@@ -158,7 +176,7 @@ int ithaca_gpu_ctx_destroy(ithaca_gpu_ctx* ctx) {
   return guarded([&] {
     if (!ctx) return;
     cudaStreamSynchronize(ctx->stream);
-    delete ctx;
+    release_ctx(ctx);
   });
 }
 
@@ -199,6 +217,7 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
                             double* jac, double* df, int on_device) {
   return guarded([&] {
     require(ctx && coords && jac && df, "null argument");
+    StreamOrder order_(ctx);
     require(nelmt > 0 && npoints >= 2 && npoints <= 16, "bad sizes");
     const int dim = shape_dim(shape);
     const int Q = npoints;
@@ -231,6 +250,7 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
                          const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op) {
   return guarded([&] {
     require(ctx && jac && df && op, "null argument");
+    StreamOrder order_(ctx);
     require(nelmt > 0, "nelmt must be positive");
     require(precision == ITHACA_GPU_FP64 || precision == ITHACA_GPU_FP32, "unknown precision");
     const int dim = shape_dim(shape);
@@ -272,6 +292,7 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     }
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->refs++;  // the operator holds its context
     *op = o.release();
   });
 }
@@ -280,7 +301,7 @@ int ithaca_gpu_op_destroy(ithaca_gpu_op* op) {
   return guarded([&] {
     if (!op) return;
     cudaStreamSynchronize(op->ctx->stream);
-    delete op;
+    release_op(op);
   });
 }
 
@@ -294,6 +315,7 @@ int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof) {
 int ithaca_gpu_bwdtrans(ithaca_gpu_op* op, const void* in, void* out, int on_device) {
   return guarded([&] {
     require(op && in && out, "null argument");
+    StreamOrder order_(op->ctx);
     Ctx* c = op->ctx;
     const size_t es = elt(op), nin = (size_t)op->E * op->nm, nout = (size_t)op->E * op->nq;
     const void* din = to_device(c, 0, in, es * nin, on_device);
@@ -315,6 +337,7 @@ int ithaca_gpu_bwdtrans(ithaca_gpu_op* op, const void* in, void* out, int on_dev
 int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_device) {
   return guarded([&] {
     require(op && in && out, "null argument");
+    StreamOrder order_(op->ctx);
     Ctx* c = op->ctx;
     const size_t es = elt(op), nin = (size_t)op->E * op->nq, nout = (size_t)op->E * op->nm;
     const void* din = to_device(c, 0, in, es * nin, on_device);
@@ -336,6 +359,7 @@ int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_dev
 int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, void* d2, int on_device) {
   return guarded([&] {
     require(op && in && d0 && d1, "null argument");
+    StreamOrder order_(op->ctx);
     require(op->dim == 2 || d2, "d2 is required for hexahedra");
     Ctx* c = op->ctx;
     const size_t es = elt(op), nq = (size_t)op->E * op->nq;
@@ -361,6 +385,7 @@ int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, 
 int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device) {
   return guarded([&] {
     require(op && in && out, "null argument");
+    StreamOrder order_(op->ctx);
     Ctx* c = op->ctx;
     const size_t es = elt(op), nm = (size_t)op->E * op->nm;
     const void* din = to_device(c, 0, in, es * nm, on_device);
@@ -382,6 +407,7 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
 int ithaca_gpu_helmholtz_diag(ithaca_gpu_op* op, double lambda, double* out, int on_device) {
   return guarded([&] {
     require(op && out, "null argument");
+    StreamOrder order_(op->ctx);
     Ctx* c = op->ctx;
     const size_t nm = (size_t)op->E * op->nm;
     double* dout = (double*)out_buffer(c, 1, out, sizeof(double) * nm, on_device);

@@ -300,7 +300,9 @@ struct Cg {
   Vecs<double> v64;
   Vecs<float> v32;
   bool have32 = false;
-  float* jg32 = nullptr;  // FP32 copy of the operator geometry
+  float* jg32 = nullptr;   // FP32 copy of the geometry the solver uses
+  double* jgk64 = nullptr; // geometry with the metric scaled by a variable coefficient (else op->jg64)
+  double* adj_scratch = nullptr;
   double* partials = nullptr;
   double* dscal = nullptr;  // scratch doubles (norms)
   CgScalars* sc = nullptr;
@@ -320,6 +322,8 @@ Cg::~Cg() {
   v64.release();
   if (have32) v32.release();
   cudaFree(jg32);
+  cudaFree(jgk64);
+  cudaFree(adj_scratch);
   cudaFree(partials);
   cudaFree(dscal);
   cudaFree(sc);
@@ -327,6 +331,9 @@ Cg::~Cg() {
 }
 
 static const int* skip_ptr(Cg* cg) { return &cg->sc->done; }
+
+// FP64 geometry of the system: the operator's, or its variable-coefficient copy.
+static const double* geo64(Cg* cg) { return cg->jgk64 ? cg->jgk64 : cg->op->jg64; }
 
 // Gather (signed l2g; ids < ndir read as zero when zero_dir) + element Helmholtz into v.yloc.
 template <typename T>
@@ -420,7 +427,7 @@ static void ensure_fp32(Cg* cg) {
   cg->v32.alloc(cg->N, cg->nloc);
   const size_t njg = (size_t)op->E * n_jg(op->dim) * (op->deformed ? op->nq : 1);
   ITHACA_CUDA(cudaMalloc(&cg->jg32, sizeof(float) * njg));
-  cast_kernel<float><<<RB, RT, 0, op->ctx->stream>>>(njg, op->jg64, cg->jg32);
+  cast_kernel<float><<<RB, RT, 0, op->ctx->stream>>>(njg, geo64(cg), cg->jg32);
   op->ctx->launches++;
   cg->have32 = true;
   cg->diag_lambda = NAN;  // rebuild so that the FP32 inverse diagonal is filled too
@@ -431,7 +438,7 @@ static void ensure_diag(Cg* cg, double lambda) {
   if (cg->diag_lambda == lambda) return;
   Op* op = cg->op;
   cudaStream_t s = op->ctx->stream;
-  if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
+  if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
                                 cg->v64.yloc, s))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
   assemble_dot_kernel<double, false><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
@@ -445,7 +452,7 @@ static void ensure_diag(Cg* cg, double lambda) {
 // FP64 residual r = b - A x over the non-Dirichlet dofs; ||r||^2 -> dscal[0], ||b||^2 -> dscal[1].
 static void fp64_residual(Cg* cg, double lambda, const double* x, const double* b, double* r) {
   cudaStream_t s = cg->op->ctx->stream;
-  launch_apply<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, nullptr, x, s, true, nullptr);
+  launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, x, s, true, nullptr);
   residual_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, cg->v64.yloc, b, r, cg->partials);
   reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 1, cg->dscal);
   reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 2, cg->dscal + 1);
@@ -462,7 +469,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
   ithaca_gpu_cg_result out{};
   int status = ITHACA_GPU_OK;
   if (o.mode == ITHACA_GPU_SOLVE_FP64) {
-    run_pcg<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, tol * tol, 0.0, o.max_iter, chunk);
+    run_pcg<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, tol * tol, 0.0, o.max_iter, chunk);
     out.iterations = cg->sc_host->iters;
     out.eps = cg->sc_host->eps;
     out.rhs_magnitude = cg->sc_host->rhs_mag;
@@ -607,6 +614,7 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     ITHACA_CUDA(cudaMallocHost(&cg->sc_host, sizeof(CgScalars)));
     *cg->sc_host = CgScalars{};
     ITHACA_CUDA(cudaStreamSynchronize(s));
+    retain_op(op);  // the solver holds its operator (and through it the context)
     *out = cg.release();
   });
 }
@@ -615,13 +623,16 @@ int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg) {
   return cg_guarded([&] {
     if (!cg) return;
     cudaStreamSynchronize(cg->op->ctx->stream);
+    Op* op = cg->op;
     delete cg;
+    release_op(op);  // the solver held its operator
   });
 }
 
 int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, double* y, int on_device) {
   return cg_guarded([&] {
     req(cg && x && y, "null argument");
+    StreamOrder order_(cg->op->ctx);
     Ctx* c = cg->op->ctx;
     cudaStream_t s = c->stream;
     const size_t bytes = sizeof(double) * cg->N;
@@ -631,7 +642,7 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
       dx = cg->v64.p;
     }
     double* dy = on_device ? y : cg->v64.q;
-    launch_apply<double>(cg, cg->v64, cg->op->t64.base, cg->op->jg64, lambda, nullptr, dx, s, false, nullptr);
+    launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, dx, s, false, nullptr);
     assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
                                                   nullptr, nullptr);
     c->launches++;
@@ -644,6 +655,7 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
 int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* global, int on_device) {
   return cg_guarded([&] {
     req(cg && local && global, "null argument");
+    StreamOrder order_(cg->op->ctx);
     Ctx* c = cg->op->ctx;
     cudaStream_t s = c->stream;
     const double* dl = local;
@@ -664,6 +676,7 @@ int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* globa
 int ithaca_gpu_cg_global_to_local(ithaca_gpu_cg* cg, const double* global, double* local, int on_device) {
   return cg_guarded([&] {
     req(cg && local && global, "null argument");
+    StreamOrder order_(cg->op->ctx);
     Ctx* c = cg->op->ctx;
     cudaStream_t s = c->stream;
     const double* dg = global;
@@ -684,6 +697,7 @@ int ithaca_gpu_cg_global_to_local(ithaca_gpu_cg* cg, const double* global, doubl
 int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int on_device) {
   return cg_guarded([&] {
     req(cg && diag, "null argument");
+    StreamOrder order_(cg->op->ctx);
     cudaStream_t s = cg->op->ctx->stream;
     cg->diag_lambda = NAN;
     ensure_diag(cg, lambda);
@@ -698,6 +712,7 @@ int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, dou
                         const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device) {
   return cg_guarded([&] {
     req(cg && rhs && x, "null argument");
+    StreamOrder order_(cg->op->ctx);
     const ithaca_gpu_cg_opts o = opts_or_default(opts);
     Ctx* c = cg->op->ctx;
     cudaStream_t s = c->stream;
@@ -724,6 +739,7 @@ int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device) {
   return cg_guarded([&] {
     req(cg && forcing && out_local, "null argument");
+    StreamOrder order_(cg->op->ctx);
     const ithaca_gpu_cg_opts o = opts_or_default(opts);
     Op* op = cg->op;
     Ctx* c = op->ctx;
@@ -759,6 +775,7 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
                                 double* bytes_per_launch) {
   return cg_guarded([&] {
     req(cg && avg_ms && reps > 0, "bad argument");
+    StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     cudaStream_t s = op->ctx->stream;
     const bool f32 = mode == ITHACA_GPU_SOLVE_MIXED_FP32;
@@ -770,7 +787,7 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
       if (f32)
         launch_apply<float>(cg, cg->v32, op->t32.base, cg->jg32, (float)lambda, nullptr, cg->v32.w, s, true, nullptr);
       else
-        launch_apply<double>(cg, cg->v64, op->t64.base, op->jg64, lambda, nullptr, cg->v64.w, s, true, nullptr);
+        launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, cg->v64.w, s, true, nullptr);
     };
     run();  // warm-up
     ITHACA_CUDA(cudaEventRecord(e0, s));
@@ -804,3 +821,170 @@ static ithaca_gpu_cg_opts opts_or_default(const ithaca_gpu_cg_opts* o) {
   if (!(d.inner_tol > 0 && d.inner_tol < 1)) d.inner_tol = 1e-4;
   return d;
 }
+
+namespace ithaca {
+
+int cg_sizes(ithaca_gpu_cg* cg, int* nglobal, int* ndir, Ctx** ctx) {
+  *nglobal = cg->N;
+  *ndir = cg->ndir;
+  *ctx = cg->op->ctx;
+  return 0;
+}
+
+// Columns of X (nglobal rows each): LX = Assemble(Laplacian(GlobalToLocal x)) and
+// MX = Assemble(IProduct(BwdTrans(GlobalToLocal x))), the lambda-free pieces of the
+// affine operator A(lambda) = L + lambda M (Dirichlet entries of x read as zero).
+void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, double* MX) {
+  Op* op = cg->op;
+  Ctx* c = op->ctx;
+  cudaStream_t s = c->stream;
+  double* phys = (double*)c->stage_ptr(2, sizeof(double) * op->E * op->nq);
+  double* loc = (double*)c->stage_ptr(3, sizeof(double) * cg->nloc);
+  for (int j = 0; j < ncols; ++j) {
+    const double* x = X + (size_t)j * cg->N;
+    launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), 0.0, nullptr, x, s, true, nullptr);
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc,
+                                                  LX + (size_t)j * cg->N, nullptr, nullptr, nullptr);
+    g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, x, loc);
+    if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
+        !launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "mass operator: (modes, points) combination not built");
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
+                                                  nullptr, nullptr, nullptr);
+    c->launches += 5;
+  }
+  ITHACA_CUDA(cudaGetLastError());
+}
+
+// adjoint.cu
+void launch_scale_metric(int E, int ng, int nq, const double* src, const double* kappa, double* dst, cudaStream_t s);
+void launch_misfit(int E, int ng, int nq, const double* jg, double* u, const double* t, double* partial, double* out,
+                   cudaStream_t s);
+void launch_kappa_grad(int E, int ng, int nq, int dim, const double* jg, const double* du, const double* dp,
+                       double* grad, cudaStream_t s);
+void launch_zero_head(int n, double* a, cudaStream_t s);
+
+// (2 dim + 2) physical-size FP64 arrays for the misfit / gradient pipelines.
+static double* adj_buffers(Cg* cg) {
+  if (!cg->adj_scratch) {
+    const size_t nphys = (size_t)cg->op->E * cg->op->nq;
+    ITHACA_CUDA(cudaMalloc(&cg->adj_scratch, sizeof(double) * nphys * (2 * cg->op->dim + 2)));
+  }
+  return cg->adj_scratch;
+}
+
+}  // namespace ithaca
+
+extern "C" {
+
+int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_device) {
+  return cg_guarded([&] {
+    req(cg != nullptr, "null argument");
+    StreamOrder order_(cg->op->ctx);
+    Op* op = cg->op;
+    cudaStream_t s = op->ctx->stream;
+    const size_t njg = (size_t)op->E * n_jg(op->dim) * op->nq;
+    if (kappa == nullptr) {  // back to kappa = 1
+      cudaFree(cg->jgk64);
+      cg->jgk64 = nullptr;
+    } else {
+      req(op->deformed != 0, "a quadrature-point coefficient needs a deformed (per-point) collection");
+      const double* dk = kappa;
+      if (!on_device) {
+        double* d = (double*)op->ctx->stage_ptr(0, sizeof(double) * op->E * op->nq);
+        ITHACA_CUDA(cudaMemcpyAsync(d, kappa, sizeof(double) * op->E * op->nq, cudaMemcpyHostToDevice, s));
+        dk = d;
+      }
+      if (!cg->jgk64) ITHACA_CUDA(cudaMalloc(&cg->jgk64, sizeof(double) * njg));
+      launch_scale_metric(op->E, n_jg(op->dim), op->nq, op->jg64, dk, cg->jgk64, s);
+      op->ctx->launches++;
+    }
+    if (cg->have32) {
+      cast_kernel<float><<<RB, RT, 0, s>>>(njg / (op->deformed ? 1 : op->nq), geo64(cg), cg->jg32);
+      op->ctx->launches++;
+    }
+    cg->diag_lambda = NAN;
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target, double* J, double* dJdx,
+                      int on_device) {
+  return cg_guarded([&] {
+    req(cg && x && u_target && J, "null argument");
+    StreamOrder order_(cg->op->ctx);
+    Op* op = cg->op;
+    Ctx* c = op->ctx;
+    cudaStream_t s = c->stream;
+    const size_t nphys = (size_t)op->E * op->nq;
+    double* buf = adj_buffers(cg);
+    double *phys = buf, *tgt = buf + nphys;
+    const double* dx = x;
+    if (!on_device) {
+      ITHACA_CUDA(cudaMemcpyAsync(cg->v64.p, x, sizeof(double) * cg->N, cudaMemcpyHostToDevice, s));
+      dx = cg->v64.p;
+    }
+    ITHACA_CUDA(cudaMemcpyAsync(tgt, u_target, sizeof(double) * nphys,
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    // u at the points from the non-Dirichlet part of x (Dirichlet values are zero)
+    ITHACA_CUDA(cudaMemcpyAsync(cg->v64.q, dx, sizeof(double) * cg->N, cudaMemcpyDeviceToDevice, s));
+    launch_zero_head(cg->ndir, cg->v64.q, s);
+    g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, cg->v64.q, cg->v64.yloc);
+    if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, cg->v64.yloc, phys, s))
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "BwdTrans: (modes, points) combination not built");
+    launch_misfit(op->E, n_jg(op->dim), op->nq, op->jg64, phys, tgt, cg->partials, cg->dscal + 2, s);
+    c->launches += 5;
+    if (dJdx) {
+      // dJ/dx = Assemble(IProduct(2 (u - t))), zero on Dirichlet dofs
+      if (!launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys,
+                                   cg->v64.yloc, s))
+        fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
+      double* dg = on_device ? dJdx : cg->v64.q;
+      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
+                                                    nullptr, nullptr);
+      launch_zero_head(cg->ndir, dg, s);
+      c->launches += 3;
+      if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(dJdx, dg, sizeof(double) * cg->N, cudaMemcpyDeviceToHost, s));
+    }
+    ITHACA_CUDA(cudaMemcpyAsync(J, cg->dscal + 2, sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* psi, double* grad, int on_device) {
+  return cg_guarded([&] {
+    req(cg && x && psi && grad, "null argument");
+    StreamOrder order_(cg->op->ctx);
+    Op* op = cg->op;
+    Ctx* c = op->ctx;
+    cudaStream_t s = c->stream;
+    const int dim = op->dim;
+    const size_t nphys = (size_t)op->E * op->nq;
+    double* buf = adj_buffers(cg);
+    double *du = buf, *dp = buf + dim * nphys, *phys = buf + 2 * dim * nphys;
+    const double* src[2] = {x, psi};
+    double* outs[2] = {du, dp};
+    for (int k = 0; k < 2; ++k) {
+      ITHACA_CUDA(cudaMemcpyAsync(cg->v64.q, src[k], sizeof(double) * cg->N,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+      launch_zero_head(cg->ndir, cg->v64.q, s);
+      g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, cg->v64.q, cg->v64.yloc);
+      if (!launch_bwdtrans<double>(dim, op->n, op->Q, op->E, op->t64.base, cg->v64.yloc, phys, s) ||
+          !launch_physderiv<double>(dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->df64, phys, outs[k],
+                                    outs[k] + nphys, dim == 3 ? outs[k] + 2 * nphys : nullptr, s))
+        fail(ITHACA_GPU_ERR_UNSUPPORTED, "BwdTrans/PhysDeriv: (modes, points) combination not built");
+      c->launches += 4;
+    }
+    double* dgrad = on_device ? grad : phys;
+    launch_kappa_grad(op->E, n_jg(dim), op->nq, dim, op->jg64, du, dp, dgrad, s);
+    c->launches++;
+    if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(grad, dgrad, sizeof(double) * nphys, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"

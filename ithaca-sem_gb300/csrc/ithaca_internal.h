@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -55,7 +56,11 @@ inline __host__ __device__ int off_w(int n, int Q) { return 4 * n * Q + 2 * Q * 
 inline __host__ __device__ constexpr int n_jg(int dim) { return 1 + dim * (dim + 1) / 2; }
 
 // ---------------------------------------------------------------------------
+// Contexts and operators are reference counted: an operator holds its context and a
+// solver holds its operator, so handles may be destroyed in any order (the reference
+// shares these objects through std::shared_ptr).
 struct Ctx {
+  std::atomic<int> refs{1};
   int device = 0;
   cudaStream_t stream = nullptr;
   long long launches = 0;
@@ -63,10 +68,31 @@ struct Ctx {
   void* stage[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t stage_bytes[4] = {0, 0, 0, 0};
   void* stage_ptr(int slot, size_t bytes);
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the legacy default stream
   ~Ctx();
 };
 
+// Orders a call's work after everything already queued on the legacy default stream
+// (where callers such as torch produce device inputs) and makes that stream wait for
+// the call's work before it continues; no host synchronisation.
+struct StreamOrder {
+  Ctx* c;
+  explicit StreamOrder(Ctx* ctx) : c(ctx) {
+    if (c && c->ev_in) {
+      cudaEventRecord(c->ev_in, cudaStreamLegacy);
+      cudaStreamWaitEvent(c->stream, c->ev_in, 0);
+    }
+  }
+  ~StreamOrder() {
+    if (c && c->ev_out) {
+      cudaEventRecord(c->ev_out, c->stream);
+      cudaStreamWaitEvent(cudaStreamLegacy, c->ev_out, 0);
+    }
+  }
+};
+
 struct Op {
+  std::atomic<int> refs{1};
   Ctx* ctx = nullptr;
   int shape = 0, dim = 0, n = 0, Q = 0, E = 0;
   int deformed = 1, precision = ITHACA_GPU_FP64;
@@ -80,6 +106,10 @@ struct Op {
   float* df32 = nullptr;
   ~Op();
 };
+
+void retain_op(Op* op);
+void release_op(Op* op);    // frees the operator (and releases its context) at zero
+void release_ctx(Ctx* ctx);  // frees the context at zero
 
 // ---------------------------------------------------------------------------
 // Kernel launchers (elem_*.cu), one explicit instantiation per (T, DIM). All take

@@ -1,0 +1,478 @@
+// POD offline / online on the GPU (FP64 throughout).
+//
+// Offline (CoupledLinearNS_ROM::ROM_offline_phase, solvers/IncNavierStokesSolver/
+// EquationSystems/CoupledLinearNS_ROM.cpp:3916-4001): the reference takes a thin SVD of
+// the snapshot matrix S with Eigen's BDCSVD. Here the method of snapshots gives the same
+// subspace: C = S^T S (FP64 split-K GEMM with a fixed-order reduction), C = W L W^T
+// (cyclic Jacobi eigen-solver on the host, ns x ns), V = S W_r L_r^{-1/2}, then two
+// Cholesky-QR passes restore orthonormality (the modes are re-orthogonalised as
+// VelocityCorrectionScheme_iROM.cpp:830-852 does with Gram-Schmidt).
+// Projection (:3661-3663, :3904-3911): A_L = V^T L V and A_M = V^T M V with L and M
+// applied matrix-free to the modes (the affine split of gen_affine_mat_proj :4694-4703).
+// Online (ROM_online_phase :4003-4100): for each lambda, (A_L + lambda A_M) x = V^T b by
+// LU with partial pivoting, one CTA per system (the reference uses colPivHouseholderQr
+// at :4053; both are direct dense solves of the same system).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "ithaca_internal.h"
+
+namespace ithaca {
+
+// ---- FP64 GEMM: C[m + n*ldc] = sum_k op(A)(m,k) op(B)(k,n), column-major operands ----
+// TRANS_A: A stored K x M (A[k + m*lda]); otherwise M x K (A[m + k*lda]). B is K x N.
+// Split-K: blockIdx.z takes rows [z*kchunk, (z+1)*kchunk) and writes its own partial.
+constexpr int GT = 64, GK = 16;
+
+template <bool TRANS_A>
+__global__ void __launch_bounds__(256) dgemm_kernel(int M, int Nn, int K, int kchunk, const double* __restrict__ A,
+                                                    int lda, const double* __restrict__ B, int ldb,
+                                                    double* __restrict__ C, size_t part_stride, int ldc) {
+  __shared__ double As[GK][GT + 1];
+  __shared__ double Bs[GK][GT + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.x * GT, n0 = blockIdx.y * GT;
+  const int k0 = blockIdx.z * kchunk, k1 = min(K, k0 + kchunk);
+  double acc[4][4] = {};
+  for (int kb = k0; kb < k1; kb += GK) {
+    for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
+      int kk, mm;
+      if (TRANS_A) {  // consecutive threads walk k (contiguous in A)
+        kk = idx % GK;
+        mm = idx / GK;
+      } else {  // consecutive threads walk m (contiguous in A)
+        mm = idx % GT;
+        kk = idx / GT;
+      }
+      const int k = kb + kk, m = m0 + mm;
+      double v = 0;
+      if (k < k1 && m < M) v = TRANS_A ? A[(size_t)m * lda + k] : A[(size_t)k * lda + m];
+      As[kk][mm] = v;
+      const int kk2 = idx % GK, nn = idx / GK;
+      const int k2 = kb + kk2, n = n0 + nn;
+      Bs[kk2][nn] = (k2 < k1 && n < Nn) ? B[(size_t)n * ldb + k2] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  double* Cp = C + blockIdx.z * part_stride;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
+      if (m < M && n < Nn) Cp[(size_t)n * ldc + m] = acc[i][j];
+    }
+}
+
+// C[i] = sum_z part[z][i] in order z = 0, 1, ... (deterministic split-K reduction).
+__global__ void sum_parts_kernel(size_t n, int nparts, const double* __restrict__ part, size_t stride,
+                                 double* __restrict__ C) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int z = 0; z < nparts; ++z) s += part[z * stride + i];
+    C[i] = s;
+  }
+}
+
+// Split count and chunk for a K-long reduction.
+static void split_k(int K, int tiles, int* nsplit, int* kchunk) {
+  const int target = std::max(1, (152 * 4) / std::max(1, tiles));
+  int ns = std::max(1, std::min(target, (K + 255) / 256));
+  int kc = (K + ns - 1) / ns;
+  kc = (kc + GK - 1) / GK * GK;
+  ns = (K + kc - 1) / kc;
+  *nsplit = ns;
+  *kchunk = kc;
+}
+
+// C (M x Nn, ldc = M) = A^T B with A: K x M, B: K x Nn (column-major, lda = ldb = K).
+// `scratch` must hold nsplit * M * Nn doubles (see tn_scratch_doubles).
+size_t tn_scratch_doubles(int M, int Nn, int K) {
+  int ns, kc;
+  split_k(K, ((M + GT - 1) / GT) * ((Nn + GT - 1) / GT), &ns, &kc);
+  return (size_t)ns * M * Nn;
+}
+
+void dgemm_tn(int M, int Nn, int K, const double* A, const double* B, double* C, double* scratch, cudaStream_t s,
+              long long* launches) {
+  int ns, kc;
+  const dim3 grid((M + GT - 1) / GT, (Nn + GT - 1) / GT, 1);
+  split_k(K, grid.x * grid.y, &ns, &kc);
+  const size_t stride = (size_t)M * Nn;
+  dgemm_kernel<true><<<dim3(grid.x, grid.y, ns), 256, 0, s>>>(M, Nn, K, kc, A, K, B, K, scratch, stride, M);
+  sum_parts_kernel<<<std::min<size_t>((stride + 255) / 256, 1024), 256, 0, s>>>(stride, ns, scratch, stride, C);
+  if (launches) *launches += 2;
+}
+
+// C (M x Nn) = A (M x K, lda = M) * B (K x Nn, ldb = K); no split (K is small).
+void dgemm_nn(int M, int Nn, int K, const double* A, const double* B, double* C, cudaStream_t s,
+              long long* launches) {
+  const dim3 grid((M + GT - 1) / GT, (Nn + GT - 1) / GT, 1);
+  dgemm_kernel<false><<<grid, 256, 0, s>>>(M, Nn, K, K, A, M, B, K, C, 0, M);
+  if (launches) *launches += 1;
+}
+
+// ---- host dense helpers (ns x ns, column-major) ----
+// Cyclic Jacobi eigen-decomposition of a symmetric matrix (Golub & Van Loan, Alg. 8.5.3).
+static void jacobi_eigen(int n, std::vector<double>& A, std::vector<double>& V, std::vector<double>& ev) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+  auto a = [&](int i, int j) -> double& { return A[(size_t)j * n + i]; };
+  double fro = 0;
+  for (double x : A) fro += x * x;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < j; ++i) off += 2 * a(i, j) * a(i, j);
+    if (off <= 1e-30 * fro) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a(p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (a(q, q) - a(p, p)) / (2 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+        const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = a(k, p), akq = a(k, q);
+          a(k, p) = c * akp - s * akq;
+          a(k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = a(p, k), aqk = a(q, k);
+          a(p, k) = c * apk - s * aqk;
+          a(q, k) = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double& vkp = V[(size_t)p * n + k];
+          double& vkq = V[(size_t)q * n + k];
+          const double x = vkp, y = vkq;
+          vkp = c * x - s * y;
+          vkq = s * x + c * y;
+        }
+      }
+  }
+  ev.resize(n);
+  for (int i = 0; i < n; ++i) ev[i] = a(i, i);
+}
+
+// Cholesky of an SPD r x r (column-major, lower); returns false if not SPD.
+static bool cholesky(int r, std::vector<double>& G) {
+  for (int j = 0; j < r; ++j) {
+    double d = G[(size_t)j * r + j];
+    for (int k = 0; k < j; ++k) d -= G[(size_t)k * r + j] * G[(size_t)k * r + j];
+    if (!(d > 0)) return false;
+    d = std::sqrt(d);
+    G[(size_t)j * r + j] = d;
+    for (int i = j + 1; i < r; ++i) {
+      double s = G[(size_t)j * r + i];
+      for (int k = 0; k < j; ++k) s -= G[(size_t)k * r + i] * G[(size_t)k * r + j];
+      G[(size_t)j * r + i] = s / d;
+    }
+  }
+  return true;
+}
+
+// ---- batched LU with partial pivoting: one CTA per system ----
+constexpr int LU_MAX = 64;
+
+__global__ void __launch_bounds__(256) batched_lu_kernel(int r, const double* __restrict__ AL,
+                                                         const double* __restrict__ AM, const double* __restrict__ f,
+                                                         const double* __restrict__ lambdas, double* __restrict__ x,
+                                                         int* __restrict__ singular) {
+  __shared__ double A[LU_MAX][LU_MAX + 1];
+  __shared__ double b[LU_MAX];
+  __shared__ int piv;
+  const int sys = blockIdx.x;
+  const double lam = lambdas[sys];
+  for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
+    const int i = idx % r, j = idx / r;  // column-major input
+    A[i][j] = AL[idx] + lam * AM[idx];
+  }
+  for (int i = threadIdx.x; i < r; i += blockDim.x) b[i] = f[i];
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (threadIdx.x == 0) {  // pivot search (r <= 64, serial is fine)
+      int p = k;
+      double best = fabs(A[k][k]);
+      for (int i = k + 1; i < r; ++i)
+        if (fabs(A[i][k]) > best) {
+          best = fabs(A[i][k]);
+          p = i;
+        }
+      piv = p;
+      if (!(best > 0)) atomicOr(singular, 1);
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < r; j += blockDim.x) {
+        const double t = A[k][j];
+        A[k][j] = A[p][j];
+        A[p][j] = t;
+      }
+      if (threadIdx.x == 0) {
+        const double t = b[k];
+        b[k] = b[p];
+        b[p] = t;
+      }
+    }
+    __syncthreads();
+    const double inv = 1.0 / A[k][k];
+    const int rows = r - k - 1;
+    for (int idx = threadIdx.x; idx < rows * (r - k); idx += blockDim.x) {
+      const int i = k + 1 + idx / (r - k), j = k + idx % (r - k);
+      const double l = A[i][k] * inv;
+      if (j > k) A[i][j] -= l * A[k][j];
+    }
+    for (int i = k + 1 + threadIdx.x; i < r; i += blockDim.x) b[i] -= A[i][k] * inv * b[k];
+    __syncthreads();
+    for (int i = k + 1 + threadIdx.x; i < r; i += blockDim.x) A[i][k] = 0.0;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {  // back substitution
+    for (int i = r - 1; i >= 0; --i) {
+      double s = b[i];
+      for (int j = i + 1; j < r; ++j) s -= A[i][j] * b[j];
+      b[i] = s / A[i][i];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < r; i += blockDim.x) x[(size_t)sys * r + i] = b[i];
+}
+
+struct DevBuf {
+  double* p = nullptr;
+  explicit DevBuf(size_t n) { ITHACA_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
+  ~DevBuf() { cudaFree(p); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+}  // namespace ithaca
+
+using namespace ithaca;
+
+struct ithaca_gpu_ctx : public Ctx {};
+struct ithaca_gpu_cg;  // defined in cg.cu
+
+namespace ithaca {
+// implemented in cg.cu: L (lambda = 0) and M applications of the global operator to
+// `ncols` global vectors (columns of X, nglobal rows), results assembled into Y.
+void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, double* MX);
+int cg_sizes(ithaca_gpu_cg* cg, int* nglobal, int* ndir, Ctx** ctx);
+}  // namespace ithaca
+
+template <typename F>
+static int pod_guarded(F f) {
+  try {
+    f();
+    return ITHACA_GPU_OK;
+  } catch (const Error& e) {
+    set_last_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return ITHACA_GPU_ERR_NOMEM;
+  }
+}
+
+static void preq(bool ok, const char* msg) {
+  if (!ok) fail(ITHACA_GPU_ERR_ARG, msg);
+}
+
+// Copies n doubles from a host or device source into a fresh device buffer.
+static std::unique_ptr<DevBuf> upload(const double* src, size_t n, int on_device, cudaStream_t s) {
+  auto b = std::make_unique<DevBuf>(n);
+  ITHACA_CUDA(cudaMemcpyAsync(b->p, src, sizeof(double) * n, on_device ? cudaMemcpyDeviceToDevice
+                                                                       : cudaMemcpyHostToDevice, s));
+  return b;
+}
+
+static void download(double* dst, const double* src, size_t n, int on_device, cudaStream_t s) {
+  ITHACA_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, on_device ? cudaMemcpyDeviceToDevice
+                                                                      : cudaMemcpyDeviceToHost, s));
+}
+
+extern "C" {
+
+int ithaca_gpu_pod_gram(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, double* C, int on_device) {
+  return pod_guarded([&] {
+    preq(ctx && S && C && N > 0 && ns > 0, "bad argument");
+    StreamOrder order_(ctx);
+    cudaStream_t s = ctx->stream;
+    auto dS = upload(S, (size_t)N * ns, on_device, s);
+    DevBuf dC((size_t)ns * ns), scratch(tn_scratch_doubles(ns, ns, N));
+    dgemm_tn(ns, ns, N, dS->p, dS->p, dC.p, scratch.p, s, &ctx->launches);
+    download(C, dC.p, (size_t)ns * ns, on_device, s);
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, int nmodes, double* V,
+                           double* sigma, int* nmodes_out, int on_device) {
+  return pod_guarded([&] {
+    preq(ctx && S && V && N > 0 && ns > 0 && nmodes > 0 && nmodes <= ns, "bad argument");
+    StreamOrder order_(ctx);
+    cudaStream_t s = ctx->stream;
+    auto dS = upload(S, (size_t)N * ns, on_device, s);
+    DevBuf dC((size_t)ns * ns), scratch(std::max(tn_scratch_doubles(ns, ns, N), tn_scratch_doubles(nmodes, nmodes, N)));
+    dgemm_tn(ns, ns, N, dS->p, dS->p, dC.p, scratch.p, s, &ctx->launches);
+    std::vector<double> C((size_t)ns * ns), W, ev;
+    ITHACA_CUDA(cudaMemcpyAsync(C.data(), dC.p, sizeof(double) * C.size(), cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    jacobi_eigen(ns, C, W, ev);
+    std::vector<int> order(ns);
+    for (int i = 0; i < ns; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return ev[a] > ev[b]; });
+    if (sigma)
+      for (int i = 0; i < ns; ++i) sigma[i] = std::sqrt(std::max(ev[order[i]], 0.0));
+    // keep modes whose eigenvalue is resolved in FP64 relative to the largest
+    const double lmax = std::max(ev[order[0]], 0.0);
+    int r = 0;
+    std::vector<double> Wr;
+    for (int j = 0; j < nmodes; ++j) {
+      const double l = ev[order[j]];
+      if (!(l > lmax * 1e-15 * ns)) break;
+      const double sc = 1.0 / std::sqrt(l);
+      for (int i = 0; i < ns; ++i) Wr.push_back(W[(size_t)order[j] * ns + i] * sc);
+      ++r;
+    }
+    preq(r > 0, "snapshot matrix is zero");
+    DevBuf dW((size_t)ns * r), dV((size_t)N * r), dG((size_t)r * r), dR((size_t)r * r), dT((size_t)N * r);
+    ITHACA_CUDA(cudaMemcpyAsync(dW.p, Wr.data(), sizeof(double) * Wr.size(), cudaMemcpyHostToDevice, s));
+    dgemm_nn(N, r, ns, dS->p, dW.p, dV.p, s, &ctx->launches);
+    // two Cholesky-QR passes: G = V^T V = R^T R, V <- V R^{-1}
+    for (int pass = 0; pass < 2; ++pass) {
+      dgemm_tn(r, r, N, dV.p, dV.p, dG.p, scratch.p, s, &ctx->launches);
+      std::vector<double> G((size_t)r * r);
+      ITHACA_CUDA(cudaMemcpyAsync(G.data(), dG.p, sizeof(double) * G.size(), cudaMemcpyDeviceToHost, s));
+      ITHACA_CUDA(cudaStreamSynchronize(s));
+      if (!cholesky(r, G)) fail(ITHACA_GPU_ERR_NUMERIC, "POD modes are numerically dependent (Cholesky-QR failed)");
+      // Rinv (upper triangular): L = G lower, R = L^T; invert R by back substitution
+      std::vector<double> Rinv((size_t)r * r, 0.0);
+      for (int j = 0; j < r; ++j) {
+        Rinv[(size_t)j * r + j] = 1.0 / G[(size_t)j * r + j];
+        for (int i = j - 1; i >= 0; --i) {
+          double sum = 0;
+          for (int k = i + 1; k <= j; ++k) sum += G[(size_t)i * r + k] * Rinv[(size_t)j * r + k];  // R(i,k)=L(k,i)
+          Rinv[(size_t)j * r + i] = -sum / G[(size_t)i * r + i];
+        }
+      }
+      ITHACA_CUDA(cudaMemcpyAsync(dR.p, Rinv.data(), sizeof(double) * Rinv.size(), cudaMemcpyHostToDevice, s));
+      dgemm_nn(N, r, r, dV.p, dR.p, dT.p, s, &ctx->launches);
+      std::swap(dV.p, dT.p);
+    }
+    download(V, dV.p, (size_t)N * r, on_device, s);
+    if (nmodes_out) *nmodes_out = r;
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_pod_project(ithaca_gpu_cg* cg, int nmodes, const double* V, double* A_L, double* A_M,
+                           int on_device) {
+  return pod_guarded([&] {
+    preq(cg && V && A_L && A_M && nmodes > 0, "bad argument");
+    int N = 0, ndir = 0;
+    Ctx* ctx = nullptr;
+    cg_sizes(cg, &N, &ndir, &ctx);
+    StreamOrder order_(ctx);
+    cudaStream_t s = ctx->stream;
+    const int nnd = N - ndir;
+    auto dV = upload(V, (size_t)nnd * nmodes, on_device, s);
+    DevBuf X((size_t)N * nmodes), LX((size_t)N * nmodes), MX((size_t)N * nmodes);
+    ITHACA_CUDA(cudaMemsetAsync(X.p, 0, sizeof(double) * N * nmodes, s));
+    ITHACA_CUDA(cudaMemcpy2DAsync(X.p + ndir, sizeof(double) * N, dV->p, sizeof(double) * nnd, sizeof(double) * nnd,
+                                  nmodes, cudaMemcpyDeviceToDevice, s));
+    cg_apply_LM(cg, nmodes, X.p, LX.p, MX.p);
+    // compact the non-Dirichlet rows, then A_X = V^T X
+    DevBuf cL((size_t)nnd * nmodes), cM((size_t)nnd * nmodes), dAL((size_t)nmodes * nmodes),
+        dAM((size_t)nmodes * nmodes), scratch(tn_scratch_doubles(nmodes, nmodes, nnd));
+    ITHACA_CUDA(cudaMemcpy2DAsync(cL.p, sizeof(double) * nnd, LX.p + ndir, sizeof(double) * N, sizeof(double) * nnd,
+                                  nmodes, cudaMemcpyDeviceToDevice, s));
+    ITHACA_CUDA(cudaMemcpy2DAsync(cM.p, sizeof(double) * nnd, MX.p + ndir, sizeof(double) * N, sizeof(double) * nnd,
+                                  nmodes, cudaMemcpyDeviceToDevice, s));
+    dgemm_tn(nmodes, nmodes, nnd, dV->p, cL.p, dAL.p, scratch.p, s, &ctx->launches);
+    dgemm_tn(nmodes, nmodes, nnd, dV->p, cM.p, dAM.p, scratch.p, s, &ctx->launches);
+    download(A_L, dAL.p, (size_t)nmodes * nmodes, on_device, s);
+    download(A_M, dAM.p, (size_t)nmodes * nmodes, on_device, s);
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_pod_online(ithaca_gpu_ctx* ctx, int r, const double* A_L, const double* A_M, const double* f_r,
+                          int nlambda, const double* lambdas, double* x_r, int on_device) {
+  return pod_guarded([&] {
+    preq(ctx && A_L && A_M && f_r && lambdas && x_r, "null argument");
+    StreamOrder order_(ctx);
+    preq(r > 0 && r <= LU_MAX && nlambda > 0, "need 0 < r <= 64 and nlambda > 0");
+    cudaStream_t s = ctx->stream;
+    auto dL = upload(A_L, (size_t)r * r, on_device, s);
+    auto dM = upload(A_M, (size_t)r * r, on_device, s);
+    auto df = upload(f_r, r, on_device, s);
+    auto dl = upload(lambdas, nlambda, on_device, s);
+    DevBuf dx((size_t)r * nlambda);
+    int* dsing = nullptr;
+    ITHACA_CUDA(cudaMalloc(&dsing, sizeof(int)));
+    std::unique_ptr<int, decltype(&cudaFree)> g(dsing, cudaFree);
+    ITHACA_CUDA(cudaMemsetAsync(dsing, 0, sizeof(int), s));
+    batched_lu_kernel<<<nlambda, 128, 0, s>>>(r, dL->p, dM->p, df->p, dl->p, dx.p, dsing);
+    ctx->launches++;
+    download(x_r, dx.p, (size_t)r * nlambda, on_device, s);
+    int hs = 0;
+    ITHACA_CUDA(cudaMemcpyAsync(&hs, dsing, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    if (hs) fail(ITHACA_GPU_ERR_NUMERIC, "a reduced system is singular");
+  });
+}
+
+int ithaca_gpu_pod_reconstruct(ithaca_gpu_ctx* ctx, int N, int r, const double* V, int nsol, const double* x_r,
+                               double* u, int on_device) {
+  return pod_guarded([&] {
+    preq(ctx && V && x_r && u && N > 0 && r > 0 && nsol > 0, "bad argument");
+    StreamOrder order_(ctx);
+    cudaStream_t s = ctx->stream;
+    auto dV = upload(V, (size_t)N * r, on_device, s);
+    auto dx = upload(x_r, (size_t)r * nsol, on_device, s);
+    DevBuf du((size_t)N * nsol);
+    dgemm_nn(N, nsol, r, dV->p, dx->p, du.p, s, &ctx->launches);
+    download(u, du.p, (size_t)N * nsol, on_device, s);
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_pod_rb_size(int ns, const double* sigma, double pod_tolerance, int* size) {
+  return pod_guarded([&] {
+    preq(sigma && size && ns > 0, "bad argument");
+    double total = 0;
+    for (int i = 0; i < ns; ++i) total += sigma[i];
+    int rb = 1;
+    double cum = 0;
+    for (int i = 0; i < ns; ++i) {
+      cum += sigma[i];
+      if (cum / total < pod_tolerance) rb = i + 2;
+    }
+    *size = rb;
+  });
+}
+
+}  // extern "C"

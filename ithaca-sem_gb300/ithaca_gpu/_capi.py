@@ -72,6 +72,15 @@ SIGNATURES = {
     "ithaca_gpu_cg_assemble": [_vp, _vp, _vp, _i],
     "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_cg_set_varcoeff": [_vp, _vp, _i],
+    "ithaca_gpu_misfit": [_vp, _vp, _vp, _vp, _vp, _i],
+    "ithaca_gpu_kappa_gradient": [_vp, _vp, _vp, _vp, _i],
+    "ithaca_gpu_pod_gram": [_vp, _i, _i, _vp, _vp, _i],
+    "ithaca_gpu_pod_offline": [_vp, _i, _i, _vp, _i, _vp, _vp, ctypes.POINTER(ctypes.c_int), _i],
+    "ithaca_gpu_pod_rb_size": [_i, _vp, _d, ctypes.POINTER(ctypes.c_int)],
+    "ithaca_gpu_pod_project": [_vp, _i, _vp, _vp, _vp, _i],
+    "ithaca_gpu_pod_online": [_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _i],
+    "ithaca_gpu_pod_reconstruct": [_vp, _i, _i, _vp, _i, _vp, _vp, _i],
     "ithaca_gpu_cg_profile_apply": [_vp, _i, _d, _i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
 }
 

@@ -239,6 +239,34 @@ class GlobalLinSysIterativeFullGPU:
         C.call("ithaca_gpu_cg_global_to_local", self.handle, pg, po, d)
         return out
 
+    def set_varcoeff(self, kappa):
+        """Isotropic diffusion coefficient at the quadrature points (None restores 1)."""
+        if kappa is None:
+            C.call("ithaca_gpu_cg_set_varcoeff", self.handle, None, 1)
+            return
+        pk, d = _ptr(kappa, np.float64 if not _is_device(kappa) else None)
+        C.call("ithaca_gpu_cg_set_varcoeff", self.handle, pk, d)
+
+    def misfit(self, x, u_target, J=None, dJdx=None):
+        """J = sum Jw (u - u_target)^2 at the points and dJ/dx (global)."""
+        dev = _is_device(x)
+        if J is None:
+            J = np.zeros(1)
+        px, d = _ptr(x, None if dev else np.float64)
+        pt, _ = _ptr(u_target)
+        pj, _ = _ptr(J)
+        pg = _ptr(dJdx)[0] if dJdx is not None else None
+        C.call("ithaca_gpu_misfit", self.handle, px, pt, pj, pg, d)
+        return J, dJdx
+
+    def kappa_gradient(self, x, psi, grad=None):
+        grad = grad if grad is not None else np.zeros(self.coll.E * self.coll.nq)
+        px, d = _ptr(x, None if _is_device(x) else np.float64)
+        pp, _ = _ptr(psi)
+        pg, _ = _ptr(grad)
+        C.call("ithaca_gpu_kappa_gradient", self.handle, px, pp, pg, d)
+        return grad
+
     def profile_apply(self, lam, mode="mixed", reps=20):
         """Average device time (ms) of the gather + element-apply kernel the solver
         launches for `mode`, timed with CUDA events on the context stream, and the
