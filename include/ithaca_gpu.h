@@ -110,6 +110,16 @@ int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, 
 /* Helmholtz (Collections/Helmholtz.cpp:391-430): out = lambda M in + L in, with
  * lambda = factors[eFactorLambda]. Arrays are double for FP64 ops and float for FP32. */
 int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device);
+/* Kernel choice for FP32 hexahedral Helmholtz applies (also used by the FP32 inner
+ * solves of a system built on this operator): 0 = shared-memory sum-factorisation
+ * kernel, 2 or 4 = register-pencil kernel with a TMA-staged geometry slab and that
+ * many elements per CTA (default 4). */
+int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
+/* Times every variant on the operator's own data and keeps the fastest, like
+ * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)
+ * picks an implementation type. times_ms (3 entries, may be NULL) receives the average
+ * FP32 apply time of variants 0, 2, 4. */
+int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* times_ms);
 /* Diagonals of the element Helmholtz matrices (E*n^d), the per-element input of
  * PreconditionerDiagonal::DiagonalPreconditionerSum (PreconditionerDiagonal.cpp:98-161). */
 int ithaca_gpu_helmholtz_diag(ithaca_gpu_op* op, double lambda, double* out, int on_device);

@@ -34,11 +34,25 @@ void* Ctx::stage_ptr(int slot, size_t bytes) {
   return stage[slot];
 }
 
+// Reads and clears the device error word; raises the recorded status (e.g. a
+// bounded wait that gave up). Synchronises the context stream.
+void Ctx::check_device_error() {
+  if (!derr) return;
+  int h = 0;
+  ITHACA_CUDA(cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  ITHACA_CUDA(cudaStreamSynchronize(stream));
+  if (h != 0) {
+    ITHACA_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), stream));
+    fail(h, "a device-side bounded wait gave up (status " + std::to_string(h) + ")");
+  }
+}
+
 Ctx::~Ctx() {
   for (auto& p : stage)
     if (p) cudaFree(p);
   if (ev_in) cudaEventDestroy(ev_in);
   if (ev_out) cudaEventDestroy(ev_out);
+  if (derr) cudaFree(derr);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -168,6 +182,8 @@ int ithaca_gpu_ctx_create(int device, ithaca_gpu_ctx** ctx) {
     ITHACA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     ITHACA_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
     ITHACA_CUDA(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming));
+    ITHACA_CUDA(cudaMalloc(&c->derr, sizeof(int)));
+    ITHACA_CUDA(cudaMemset(c->derr, 0, sizeof(int)));
     *ctx = c.release();
   });
 }
@@ -272,6 +288,8 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     BasisTables b = make_basis(nmodes, npoints);
     upload_tables(o->t64, b);
     upload_tables(o->t32, b);
+    o->hB = b.B;
+    o->hD = b.D;
     const size_t npt = o->deformed ? (size_t)o->nq : 1;
     const size_t njg = (size_t)nelmt * n_jg(dim) * npt, ndf = (size_t)nelmt * dim * dim * npt;
     const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * npt, on_device);
@@ -285,7 +303,7 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     launch_build_jg<double>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg64, o->df64, ctx->stream);
     ctx->launches++;
     if (precision == ITHACA_GPU_FP32) {
-      ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
       ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
       launch_build_jg<float>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg32, o->df32, ctx->stream);
       ctx->launches++;
@@ -394,6 +412,10 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
     if (op->precision == ITHACA_GPU_FP64)
       ok = launch_helmholtz<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
                                     (const double*)din, (double*)dout, nullptr, 0, c->stream);
+    else if (op->dim == 3 && op->deformed && op->variant32 > 0)
+      ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), op->jg32,
+                                     (float)lambda, (const float*)din, (float*)dout, nullptr, 0, nullptr, nullptr,
+                                     c->derr, c->stream);
     else
       ok = launch_helmholtz<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
                                    (float)lambda, (const float*)din, (float*)dout, nullptr, 0, c->stream);
@@ -401,6 +423,85 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
     c->launches++;
     from_device(c, out, dout, es * nm, on_device);
     finish(c, on_device);
+    if (!on_device) c->check_device_error();
+  });
+}
+
+int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant) {
+  return guarded([&] {
+    require(op != nullptr, "null argument");
+    require(variant == 0 || variant == 2 || variant == 4, "variant must be 0, 2 or 4");
+    op->variant32 = variant;
+  });
+}
+
+int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* times_ms) {
+  return guarded([&] {
+    require(op && reps > 0, "bad argument");
+    StreamOrder order_(op->ctx);
+    Ctx* c = op->ctx;
+    cudaStream_t s = c->stream;
+    const size_t nm = (size_t)op->E * op->nm;
+    const size_t njg = (size_t)op->E * n_jg(op->dim) * (op->deformed ? op->nq : 1);
+    float* jg = op->jg32;
+    float* tmp_jg = nullptr;
+    float *x = nullptr, *y = nullptr;
+    cudaEvent_t e0, e1;
+    ITHACA_CUDA(cudaEventCreate(&e0));
+    ITHACA_CUDA(cudaEventCreate(&e1));
+    struct Cleanup {
+      float** p[3];
+      cudaEvent_t a, b;
+      ~Cleanup() {
+        for (auto q : p) cudaFree(*q);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+      }
+    } cleanup{{&tmp_jg, &x, &y}, e0, e1};
+    if (!jg) {  // FP64 operator: time on an FP32 copy of its geometry
+      ITHACA_CUDA(cudaMalloc(&tmp_jg, sizeof(float) * njg + kGeoPad));
+      std::vector<double> h(njg);
+      ITHACA_CUDA(cudaMemcpy(h.data(), op->jg64, sizeof(double) * njg, cudaMemcpyDeviceToHost));
+      std::vector<float> hf(h.begin(), h.end());
+      ITHACA_CUDA(cudaMemcpy(tmp_jg, hf.data(), sizeof(float) * njg, cudaMemcpyHostToDevice));
+      jg = tmp_jg;
+    }
+    ITHACA_CUDA(cudaMalloc(&x, sizeof(float) * nm));
+    ITHACA_CUDA(cudaMalloc(&y, sizeof(float) * nm));
+    ITHACA_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * nm, s));
+    const int variants[3] = {0, 2, 4};
+    double best = 1e300;
+    int best_v = 0;
+    for (int vi = 0; vi < 3; ++vi) {
+      const int v = variants[vi];
+      double ms_avg = -1;
+      if (v == 0 || (op->dim == 3 && op->deformed)) {
+        auto run = [&] {
+          bool ok = v == 0 ? launch_helmholtz<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, jg,
+                                                     1.0f, x, y, nullptr, 0, s)
+                           : launch_helm_pencil<float>(op->n, op->Q, op->E, v, op->hB.data(), op->hD.data(), jg,
+                                                       1.0f, x, y, nullptr, 0, nullptr, nullptr, c->derr, s);
+          if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
+          c->launches++;
+        };
+        run();
+        ITHACA_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) run();
+        ITHACA_CUDA(cudaEventRecord(e1, s));
+        ITHACA_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        ITHACA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms_avg = ms / reps;
+        if (ms_avg < best) {
+          best = ms_avg;
+          best_v = v;
+        }
+      }
+      if (times_ms) times_ms[vi] = ms_avg;
+    }
+    c->check_device_error();
+    op->variant32 = best_v;
+    if (chosen) *chosen = best_v;
   });
 }
 

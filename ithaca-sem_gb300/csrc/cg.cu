@@ -340,9 +340,19 @@ template <typename T>
 static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda, const T* lam_ptr, const T* xin,
                          cudaStream_t s, bool zero_dir, const int* skip) {
   Op* op = cg->op;
-  if (!launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
-                           zero_dir ? cg->ndir : 0, s, skip, lam_ptr))
-    fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
+  bool ok;
+  if constexpr (sizeof(T) == 4) {
+    if (op->dim == 3 && op->deformed && op->variant32 > 0)
+      ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,
+                                     xin, v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
+    else
+      ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+                               zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
+  } else {
+    ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+                             zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
+  }
+  if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
   op->ctx->launches++;
 }
 
@@ -426,7 +436,7 @@ static void ensure_fp32(Cg* cg) {
   Op* op = cg->op;
   cg->v32.alloc(cg->N, cg->nloc);
   const size_t njg = (size_t)op->E * n_jg(op->dim) * (op->deformed ? op->nq : 1);
-  ITHACA_CUDA(cudaMalloc(&cg->jg32, sizeof(float) * njg));
+  ITHACA_CUDA(cudaMalloc(&cg->jg32, sizeof(float) * njg + kGeoPad));
   cast_kernel<float><<<RB, RT, 0, op->ctx->stream>>>(njg, geo64(cg), cg->jg32);
   op->ctx->launches++;
   cg->have32 = true;
@@ -529,6 +539,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
     out.rel_residual = hs[1] > 0 ? std::sqrt(hs[0] / hs[1]) : 0.0;
   }
   if (res) *res = out;
+  c->check_device_error();
   if (status == ITHACA_GPU_ERR_NOT_CONVERGED)
     fail(status, "Exceeded maximum number of iterations (" + std::to_string(out.iterations) + ")");
   if (status != ITHACA_GPU_OK) fail(status, "NaN or Inf in the CG recurrence");

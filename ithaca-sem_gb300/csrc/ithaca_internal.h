@@ -69,6 +69,8 @@ struct Ctx {
   size_t stage_bytes[4] = {0, 0, 0, 0};
   void* stage_ptr(int slot, size_t bytes);
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the legacy default stream
+  int* derr = nullptr;  // device error word set by bounded waits in kernels (0 = ok)
+  void check_device_error();
   ~Ctx();
 };
 
@@ -104,8 +106,21 @@ struct Op {
   double* df64 = nullptr;
   float* jg32 = nullptr;
   float* df32 = nullptr;
+  std::vector<double> hB, hD;  // host copies of B[p*Q+i] and D[k*Q+i] (kernel-parameter tables)
+  // Helmholtz kernel variant for FP32 hexahedra: 0 = shared-memory kernel (elem.cuh),
+  // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA.
+  int variant32 = 4;
   ~Op();
 };
+
+// Padding (bytes) after geometry buffers, so a CTA's 16-byte-rounded TMA window never
+// leaves the allocation.
+constexpr size_t kGeoPad = 64;
+
+template <typename T>
+bool launch_helm_pencil(int n, int Q, int E, int eb, const double* hB, const double* hD, const T* jg, T lambda,
+                        const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
+                        cudaStream_t s);
 
 void retain_op(Op* op);
 void release_op(Op* op);    // frees the operator (and releases its context) at zero

@@ -6,7 +6,9 @@
 // subspace: C = S^T S (FP64 split-K GEMM with a fixed-order reduction), C = W L W^T
 // (cyclic Jacobi eigen-solver on the host, ns x ns), V = S W_r L_r^{-1/2}, then two
 // Cholesky-QR passes restore orthonormality (the modes are re-orthogonalised as
-// VelocityCorrectionScheme_iROM.cpp:830-852 does with Gram-Schmidt).
+// VelocityCorrectionScheme_iROM.cpp:830-852 does with Gram-Schmidt). Eigenvalues of
+// S^T S below ~1e-13 of the largest are not resolved in FP64, so further passes repeat
+// the procedure on the deflated snapshots S - V (V^T S) to reach the smaller modes.
 // Projection (:3661-3663, :3904-3911): A_L = V^T L V and A_M = V^T M V with L and M
 // applied matrix-free to the modes (the affine split of gen_affine_mat_proj :4694-4703).
 // Online (ROM_online_phase :4003-4100): for each lambda, (A_L + lambda A_M) x = V^T b by
@@ -255,6 +257,12 @@ __global__ void __launch_bounds__(256) batched_lu_kernel(int r, const double* __
   for (int i = threadIdx.x; i < r; i += blockDim.x) x[(size_t)sys * r + i] = b[i];
 }
 
+// r = s - r elementwise (deflation of the snapshot matrix).
+__global__ void sub_from_kernel(size_t n, const double* __restrict__ s, double* __restrict__ r) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    r[i] = s[i] - r[i];
+}
+
 struct DevBuf {
   double* p = nullptr;
   explicit DevBuf(size_t n) { ITHACA_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
@@ -331,54 +339,72 @@ int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, 
     StreamOrder order_(ctx);
     cudaStream_t s = ctx->stream;
     auto dS = upload(S, (size_t)N * ns, on_device, s);
-    DevBuf dC((size_t)ns * ns), scratch(std::max(tn_scratch_doubles(ns, ns, N), tn_scratch_doubles(nmodes, nmodes, N)));
-    dgemm_tn(ns, ns, N, dS->p, dS->p, dC.p, scratch.p, s, &ctx->launches);
-    std::vector<double> C((size_t)ns * ns), W, ev;
-    ITHACA_CUDA(cudaMemcpyAsync(C.data(), dC.p, sizeof(double) * C.size(), cudaMemcpyDeviceToHost, s));
-    ITHACA_CUDA(cudaStreamSynchronize(s));
-    jacobi_eigen(ns, C, W, ev);
-    std::vector<int> order(ns);
-    for (int i = 0; i < ns; ++i) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return ev[a] > ev[b]; });
-    if (sigma)
-      for (int i = 0; i < ns; ++i) sigma[i] = std::sqrt(std::max(ev[order[i]], 0.0));
-    // keep modes whose eigenvalue is resolved in FP64 relative to the largest
-    const double lmax = std::max(ev[order[0]], 0.0);
+    DevBuf dR((size_t)N * ns), dC((size_t)ns * ns), dV((size_t)N * nmodes), dT((size_t)N * nmodes),
+        dG((size_t)nmodes * nmodes), dRinv((size_t)nmodes * nmodes), dP((size_t)nmodes * ns), dW((size_t)ns * nmodes),
+        scratch(std::max(tn_scratch_doubles(ns, ns, N), tn_scratch_doubles(nmodes, ns, N)));
+    ITHACA_CUDA(cudaMemcpyAsync(dR.p, dS->p, sizeof(double) * N * ns, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> sig(ns, 0.0);
     int r = 0;
-    std::vector<double> Wr;
-    for (int j = 0; j < nmodes; ++j) {
-      const double l = ev[order[j]];
-      if (!(l > lmax * 1e-15 * ns)) break;
-      const double sc = 1.0 / std::sqrt(l);
-      for (int i = 0; i < ns; ++i) Wr.push_back(W[(size_t)order[j] * ns + i] * sc);
-      ++r;
+    double l1 = 0;
+    // Method of snapshots with deflation: each pass takes the eigenpairs of R^T R that
+    // FP64 resolves (eigenvalue > 1e-13 of the pass maximum), appends R W L^{-1/2} to V,
+    // re-orthonormalises V (two Cholesky-QR passes) and deflates R = S - V (V^T S).
+    for (int pass = 0; pass < 4 && r < nmodes; ++pass) {
+      dgemm_tn(ns, ns, N, dR.p, dR.p, dC.p, scratch.p, s, &ctx->launches);
+      std::vector<double> C((size_t)ns * ns), W, ev;
+      ITHACA_CUDA(cudaMemcpyAsync(C.data(), dC.p, sizeof(double) * C.size(), cudaMemcpyDeviceToHost, s));
+      ITHACA_CUDA(cudaStreamSynchronize(s));
+      jacobi_eigen(ns, C, W, ev);
+      std::vector<int> order(ns);
+      for (int i = 0; i < ns; ++i) order[i] = i;
+      std::sort(order.begin(), order.end(), [&](int a, int b) { return ev[a] > ev[b]; });
+      const double lmax = std::max(ev[order[0]], 0.0);
+      if (pass == 0) l1 = lmax;
+      if (!(lmax > 1e-28 * l1) || lmax <= 0) break;  // the rest is below FP64 noise of S
+      std::vector<double> Wr;
+      int taken = 0;
+      for (int j = 0; j < ns && r + taken < nmodes; ++j) {
+        const double l = ev[order[j]];
+        if (!(l > 1e-13 * lmax)) break;
+        const double sc = 1.0 / std::sqrt(l);
+        for (int i = 0; i < ns; ++i) Wr.push_back(W[(size_t)order[j] * ns + i] * sc);
+        sig[r + taken] = std::sqrt(l);
+        ++taken;
+      }
+      for (int j = taken; j < ns && r + j < ns; ++j) sig[r + j] = std::sqrt(std::max(ev[order[j]], 0.0));
+      if (taken == 0) break;
+      ITHACA_CUDA(cudaMemcpyAsync(dW.p, Wr.data(), sizeof(double) * Wr.size(), cudaMemcpyHostToDevice, s));
+      dgemm_nn(N, taken, ns, dR.p, dW.p, dV.p + (size_t)r * N, s, &ctx->launches);
+      r += taken;
+      for (int q = 0; q < 2; ++q) {  // Cholesky-QR: G = V^T V = L L^T, V <- V L^{-T}
+        dgemm_tn(r, r, N, dV.p, dV.p, dG.p, scratch.p, s, &ctx->launches);
+        std::vector<double> G((size_t)r * r);
+        ITHACA_CUDA(cudaMemcpyAsync(G.data(), dG.p, sizeof(double) * G.size(), cudaMemcpyDeviceToHost, s));
+        ITHACA_CUDA(cudaStreamSynchronize(s));
+        if (!cholesky(r, G)) fail(ITHACA_GPU_ERR_NUMERIC, "POD modes are numerically dependent (Cholesky-QR failed)");
+        std::vector<double> Rinv((size_t)r * r, 0.0);  // inverse of R = L^T (upper triangular)
+        for (int j = 0; j < r; ++j) {
+          Rinv[(size_t)j * r + j] = 1.0 / G[(size_t)j * r + j];
+          for (int i = j - 1; i >= 0; --i) {
+            double sum = 0;
+            for (int k = i + 1; k <= j; ++k) sum += G[(size_t)i * r + k] * Rinv[(size_t)j * r + k];
+            Rinv[(size_t)j * r + i] = -sum / G[(size_t)i * r + i];
+          }
+        }
+        ITHACA_CUDA(cudaMemcpyAsync(dRinv.p, Rinv.data(), sizeof(double) * Rinv.size(), cudaMemcpyHostToDevice, s));
+        dgemm_nn(N, r, r, dV.p, dRinv.p, dT.p, s, &ctx->launches);
+        ITHACA_CUDA(cudaMemcpyAsync(dV.p, dT.p, sizeof(double) * N * r, cudaMemcpyDeviceToDevice, s));
+      }
+      if (r >= nmodes) break;
+      // R = S - V (V^T S)
+      dgemm_tn(r, ns, N, dV.p, dS->p, dP.p, scratch.p, s, &ctx->launches);
+      dgemm_nn(N, ns, r, dV.p, dP.p, dR.p, s, &ctx->launches);
+      sub_from_kernel<<<1024, 256, 0, s>>>((size_t)N * ns, dS->p, dR.p);
+      ctx->launches++;
     }
     preq(r > 0, "snapshot matrix is zero");
-    DevBuf dW((size_t)ns * r), dV((size_t)N * r), dG((size_t)r * r), dR((size_t)r * r), dT((size_t)N * r);
-    ITHACA_CUDA(cudaMemcpyAsync(dW.p, Wr.data(), sizeof(double) * Wr.size(), cudaMemcpyHostToDevice, s));
-    dgemm_nn(N, r, ns, dS->p, dW.p, dV.p, s, &ctx->launches);
-    // two Cholesky-QR passes: G = V^T V = R^T R, V <- V R^{-1}
-    for (int pass = 0; pass < 2; ++pass) {
-      dgemm_tn(r, r, N, dV.p, dV.p, dG.p, scratch.p, s, &ctx->launches);
-      std::vector<double> G((size_t)r * r);
-      ITHACA_CUDA(cudaMemcpyAsync(G.data(), dG.p, sizeof(double) * G.size(), cudaMemcpyDeviceToHost, s));
-      ITHACA_CUDA(cudaStreamSynchronize(s));
-      if (!cholesky(r, G)) fail(ITHACA_GPU_ERR_NUMERIC, "POD modes are numerically dependent (Cholesky-QR failed)");
-      // Rinv (upper triangular): L = G lower, R = L^T; invert R by back substitution
-      std::vector<double> Rinv((size_t)r * r, 0.0);
-      for (int j = 0; j < r; ++j) {
-        Rinv[(size_t)j * r + j] = 1.0 / G[(size_t)j * r + j];
-        for (int i = j - 1; i >= 0; --i) {
-          double sum = 0;
-          for (int k = i + 1; k <= j; ++k) sum += G[(size_t)i * r + k] * Rinv[(size_t)j * r + k];  // R(i,k)=L(k,i)
-          Rinv[(size_t)j * r + i] = -sum / G[(size_t)i * r + i];
-        }
-      }
-      ITHACA_CUDA(cudaMemcpyAsync(dR.p, Rinv.data(), sizeof(double) * Rinv.size(), cudaMemcpyHostToDevice, s));
-      dgemm_nn(N, r, r, dV.p, dR.p, dT.p, s, &ctx->launches);
-      std::swap(dV.p, dT.p);
-    }
     download(V, dV.p, (size_t)N * r, on_device, s);
+    if (sigma) std::copy(sig.begin(), sig.end(), sigma);
     if (nmodes_out) *nmodes_out = r;
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));

@@ -167,6 +167,18 @@ class Collection:
         C.call("ithaca_gpu_helmholtz", self.handle, ctypes.c_double(lam), pi, po, d)
         return out
 
+    def set_variant(self, variant):
+        """FP32 hex Helmholtz kernel: 0 shared-memory, 2/4 register-pencil (elements per CTA)."""
+        C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
+
+    def autotune(self, reps=10):
+        """Times each kernel variant on this collection and keeps the fastest."""
+        chosen = ctypes.c_int()
+        times = np.zeros(3)
+        C.call("ithaca_gpu_op_autotune", self.handle, int(reps), ctypes.byref(chosen),
+               ctypes.c_void_p(times.ctypes.data))
+        return chosen.value, {0: times[0], 2: times[1], 4: times[2]}
+
     def helmholtz_diag(self, lam, out=None):
         out = out if out is not None else np.zeros(self.E * self.nm)
         po, d = _ptr(out)

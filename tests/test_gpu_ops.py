@@ -123,3 +123,30 @@ def test_unsupported_order_raises(ctx):
         Collection(ctx, "quad", 5, 7, c.E, c.jac, c.df)  # npoints != nmodes + 1
     with pytest.raises(GpuError):
         Collection(ctx, "quad", 12, 13, c.E, c.jac, c.df)
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 7, 8, 9, 10])
+@pytest.mark.parametrize("variant", [0, 2, 4])
+def test_hex_fp32_kernel_variants(ctx, n, variant):
+    """Every FP32 hex Helmholtz kernel variant (shared-memory, register-pencil with
+    TMA-staged geometry, 2 or 4 elements per CTA) against the FP64 oracle; E = 7 leaves
+    a partial last CTA."""
+    c = hex_case(7, 1, 1, n)
+    coll = _coll(ctx, c, "fp32")
+    coll.set_variant(variant)
+    rng = np.random.default_rng(40 + n)
+    u = rng.uniform(-1, 1, c.E * c.nm)
+    out = coll.helmholtz(0.7, u.astype(np.float32))
+    ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 0.7, u)
+    assert rel_err(out, ref) < TOL32
+
+
+def test_autotune_picks_a_working_variant(ctx):
+    c = hex_case(4, 4, 2, 7)
+    coll = _coll(ctx, c, "fp32")
+    chosen, times = coll.autotune(reps=3)
+    assert chosen in (0, 2, 4) and all(t > 0 for t in times.values())
+    u = np.random.default_rng(3).uniform(-1, 1, c.E * c.nm)
+    out = coll.helmholtz(1.0, u.astype(np.float32))
+    ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, u)
+    assert rel_err(out, ref) < TOL32
