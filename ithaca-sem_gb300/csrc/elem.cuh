@@ -113,11 +113,12 @@ template <typename T, int DIM, int N, int Q, int TPE, bool DEF, bool GATHER>
 __global__ void __launch_bounds__(256) helm_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                     const T* __restrict__ tab, const T* __restrict__ jg, T lambda,
                                                     int E, const int* __restrict__ l2g, int ndir,
-                                                    const int* __restrict__ skip, const T* __restrict__ lam_ptr) {
+                                                    const int* __restrict__ skip, const T* __restrict__ lam_ptr,
+                                                    const int* __restrict__ esolve, int skip_stride) {
   using L = Layout<T, DIM, N, Q>;
   constexpr int NM = L::NM, NQ = L::NQ, NG = n_jg(DIM);
   constexpr int PPT = cdiv(NQ, TPE);
-  if (skip != nullptr && *skip) return;  // a converged solve: the whole CTA leaves together
+  if (esolve == nullptr && skip != nullptr && *skip) return;  // a converged solve: the whole CTA leaves together
   if (lam_ptr != nullptr) lambda = *lam_ptr;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);
@@ -132,8 +133,10 @@ __global__ void __launch_bounds__(256) helm_kernel(const T* __restrict__ in, T* 
   T* F2 = F1 + NQ;  // DIM 3 only
   T* C = DIM == 2 ? F1 : F2;
   const int e = blockIdx.x * blockDim.y + threadIdx.y;
-  const bool active = e < E;
-  const int ee = active ? e : E - 1;
+  const int ee = e < E ? e : E - 1;
+  // batched solves: elements of converged solves (skip[esolve[e] * skip_stride] != 0) do no I/O
+  const bool active = e < E && !(esolve != nullptr && skip[(size_t)esolve[ee] * skip_stride] != 0);
+
   const int t = threadIdx.x;
 
   for (int m = t; m < NM; m += TPE) {

@@ -7,8 +7,9 @@
 // (cyclic Jacobi eigen-solver on the host, ns x ns), V = S W_r L_r^{-1/2}, then two
 // Cholesky-QR passes restore orthonormality (the modes are re-orthogonalised as
 // VelocityCorrectionScheme_iROM.cpp:830-852 does with Gram-Schmidt). Eigenvalues of
-// S^T S below ~1e-13 of the largest are not resolved in FP64, so further passes repeat
-// the procedure on the deflated snapshots S - V (V^T S) to reach the smaller modes.
+// S^T S far below the largest are not resolved in FP64 (a pass keeps those above 1e-10
+// of its largest), so further passes repeat the procedure on the deflated snapshots
+// S - V (V^T S) to reach the smaller modes.
 // Projection (:3661-3663, :3904-3911): A_L = V^T L V and A_M = V^T M V with L and M
 // applied matrix-free to the modes (the affine split of gen_affine_mat_proj :4694-4703).
 // Online (ROM_online_phase :4003-4100): for each lambda, (A_L + lambda A_M) x = V^T b by
@@ -347,9 +348,9 @@ int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, 
     int r = 0;
     double l1 = 0;
     // Method of snapshots with deflation: each pass takes the eigenpairs of R^T R that
-    // FP64 resolves (eigenvalue > 1e-13 of the pass maximum), appends R W L^{-1/2} to V,
+    // FP64 resolves (eigenvalue > 1e-10 of the pass maximum, so that sigma has ~6 digits), appends R W L^{-1/2} to V,
     // re-orthonormalises V (two Cholesky-QR passes) and deflates R = S - V (V^T S).
-    for (int pass = 0; pass < 4 && r < nmodes; ++pass) {
+    for (int pass = 0; pass < 8 && r < nmodes; ++pass) {
       dgemm_tn(ns, ns, N, dR.p, dR.p, dC.p, scratch.p, s, &ctx->launches);
       std::vector<double> C((size_t)ns * ns), W, ev;
       ITHACA_CUDA(cudaMemcpyAsync(C.data(), dC.p, sizeof(double) * C.size(), cudaMemcpyDeviceToHost, s));
@@ -365,7 +366,7 @@ int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, 
       int taken = 0;
       for (int j = 0; j < ns && r + taken < nmodes; ++j) {
         const double l = ev[order[j]];
-        if (!(l > 1e-13 * lmax)) break;
+        if (!(l > 1e-10 * lmax)) break;
         const double sc = 1.0 / std::sqrt(l);
         for (int i = 0; i < ns; ++i) Wr.push_back(W[(size_t)order[j] * ns + i] * sc);
         sig[r + taken] = std::sqrt(l);

@@ -50,7 +50,7 @@ def test_offline_subspace_matches_svd(setup):
     U, s = opod.pod_svd(S, nmodes=8)
     # singular values resolved well above the FP64 floor of S agree closely
     big = s[:8] > 1e-8 * s[0]
-    assert np.max(np.abs(sigma[:8][big] - s[:8][big]) / s[:8][big]) < 1e-6
+    assert np.max(np.abs(sigma[:8][big] - s[:8][big]) / s[:8][big]) < 1e-5
     cos = opod.principal_angle_cos(U, V)
     assert np.min(cos[:int(big.sum())]) > 1 - 1e-8
     # the method of snapshots and the oracle's snapshot variant span the same space
