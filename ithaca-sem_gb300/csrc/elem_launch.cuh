@@ -26,13 +26,14 @@ struct Cfg {
 
 template <typename T, int DIM, int N, int Q>
 void helm_nq(int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g, int ndir,
-             const int* skip, const T* lam_ptr, cudaStream_t s) {
+             const int* skip, const T* lam_ptr, const int* esolve, int skip_stride, cudaStream_t s) {
   using C = Cfg<T, DIM, N, Q>;
   constexpr int TPE = C::S::TPE;
   auto k = deformed ? (l2g ? helm_kernel<T, DIM, N, Q, TPE, true, true> : helm_kernel<T, DIM, N, Q, TPE, true, false>)
                     : (l2g ? helm_kernel<T, DIM, N, Q, TPE, false, true> : helm_kernel<T, DIM, N, Q, TPE, false, false>);
   C::prep(k);
-  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, esolve,
+                                               skip_stride);
 }
 
 template <typename T, int DIM, int N, int Q>
@@ -74,10 +75,12 @@ void diag_nq(int E, int deformed, const T* tab, const T* jg, T lambda, T* out, c
 
 template <typename T, int DIM>
 bool ElemApi<T, DIM>::helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in,
-                           T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, cudaStream_t s) {
+                           T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, const int* esolve,
+                           int skip_stride, cudaStream_t s) {
 #define X(NN, QQ)                                                                                  \
   if (n == NN && Q == QQ) {                                                                        \
-    dev::helm_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);             \
+    dev::helm_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve,           \
+                                 skip_stride, s);                                                                  \
     return true;                                                                                   \
   }
   ITHACA_FOR_EACH_NQ(X)

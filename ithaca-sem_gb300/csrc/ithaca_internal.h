@@ -135,7 +135,8 @@ void release_ctx(Ctx* ctx);  // frees the context at zero
 template <typename T, int DIM>
 struct ElemApi {
   static bool helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out,
-                   const int* l2g, int ndir, const int* skip, const T* lam_ptr, cudaStream_t s);
+                   const int* l2g, int ndir, const int* skip, const T* lam_ptr, const int* esolve, int skip_stride,
+                   cudaStream_t s);
   static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
   static bool ipr(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
   static bool deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
@@ -146,9 +147,12 @@ struct ElemApi {
 template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
-                             const int* skip = nullptr, const T* lam_ptr = nullptr) {
-  return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s)
-                  : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);
+                             const int* skip = nullptr, const T* lam_ptr = nullptr, const int* esolve = nullptr,
+                             int skip_stride = 0) {
+  return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
+                                        esolve, skip_stride, s)
+                  : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
+                                        esolve, skip_stride, s);
 }
 template <typename T>
 inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
