@@ -176,6 +176,33 @@ int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int o
 int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
 
+/* ---- batched parametric solves ----
+ * Many independent C0 Helmholtz systems (own mesh, order, lambda, rhs; homogeneous
+ * Dirichlet data) solved together: the parameter loop that produces the snapshots of
+ * the ITHACA offline phase (CoupledLinearNS_ROM.cpp:1208-1283, one FOM HelmSolve per
+ * parameter) as one graph-captured batch. Every solve follows the reference CG
+ * recurrence with its own scalars. Host arrays, layouts as ithaca_gpu_cg_create. */
+typedef struct ithaca_gpu_batch ithaca_gpu_batch;
+typedef struct {
+  int nmodes, npoints, nelmt;
+  const double* jac;   /* E*Q^d   (deformed layout) */
+  const double* df;    /* d*d*E*Q^d                 */
+  int deformed;        /* must be 1                 */
+  const int* l2g;      /* E*n^d local -> global ids, Dirichlet ids first */
+  const double* sign;  /* E*n^d, +1 / -1            */
+  int nglobal, ndir;
+  double lambda;
+  const double* rhs;   /* nglobal assembled right-hand side */
+} ithaca_gpu_solve_desc;
+int ithaca_gpu_batch_create(ithaca_gpu_ctx* ctx, int shape, int nsolve, const ithaca_gpu_solve_desc* descs,
+                            ithaca_gpu_batch** batch);
+int ithaca_gpu_batch_destroy(ithaca_gpu_batch* batch);
+/* Solves every system (opts->mode FP64 or mixed). x: nsolve host pointers of nglobal
+ * doubles each (or NULL); iterations / outer / rel_res: nsolve entries (or NULL);
+ * elapsed_ms: device time of the whole batch (CUDA events on the context stream). */
+int ithaca_gpu_batch_solve(ithaca_gpu_batch* batch, const ithaca_gpu_cg_opts* opts, double* const* x,
+                           int* iterations, int* outer, double* rel_res, double* elapsed_ms);
+
 /* ---- variable coefficient and adjoint gradient ----
  * Isotropic diffusion coefficient kappa at the quadrature points (E*Q^d) of a deformed
  * collection: the solver's operator becomes lambda M + L_kappa, the reference's

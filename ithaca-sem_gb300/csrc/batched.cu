@@ -1,0 +1,427 @@
+// Batched parametric Helmholtz solves: many independent C0 systems (different meshes,
+// orders and lambdas) solved together.
+//
+// In the reference each parameter sample is a separate FOM solve (the snapshot loop
+// of the ITHACA offline phase, CoupledLinearNS_ROM.cpp:1208-1283 loads one solution per
+// parameter; each comes from ContField::HelmSolve -> NekLinSysIterCG). Here the solves
+// are grouped by polynomial order; a group is one block-diagonal system:
+//  * elements of all its solves concatenated, lambda_s folded into J w of solve s;
+//  * global ids renumbered: every solve's Dirichlet dofs first, then the free dofs of
+//    solve 0, 1, ... as contiguous segments;
+//  * per-solve CG scalars (the recurrence of NekLinSysIterCG.cpp:104-263 per segment),
+//    reductions over fixed chunks of a segment, summed in order by one CTA per solve;
+//  * elements of converged solves skip their I/O in the element kernel.
+// One CUDA graph holds `check_every` iterations of every group, one parallel branch per
+// group, and is launched until all solves flag convergence. Mixed mode wraps the FP32
+// inner batch in per-solve FP64 iterative refinement.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "ithaca_internal.h"
+
+namespace ithaca {
+namespace batch {
+
+constexpr int BT = 256;        // threads per CTA
+constexpr int CH = 4096;       // dofs per reduction chunk
+constexpr int GRID = 152 * 4;  // CTAs of the chunk kernels
+
+struct Scal {
+  double alpha, beta, rho, mu, eps, rhs_mag, tol2, mag_override, bb_dir;
+  double rn2, bn2, scale;  // mixed mode: outer residual, rhs norm, inner scaling
+  int iters, k, done, status, max_iter, outer_done;
+};
+constexpr int kDoneStride = sizeof(Scal) / sizeof(int);
+static_assert(sizeof(Scal) % sizeof(int) == 0, "Scal must be int-aligned");
+
+struct Chunk {
+  int solve, begin, end;
+};
+
+template <int NC>
+__device__ __forceinline__ void block_sum(double (&v)[NC], double* out /* NC values */) {
+  __shared__ double sm[NC][BT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    if (lane == 0) sm[c][warp] = v[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double s = 0;
+#pragma unroll
+    for (int w = 0; w < BT / 32; ++w) s += sm[threadIdx.x][w];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// part layout: part[slot * nchunks + chunk]; slots 0 r.w, 1 r.r, 2 b.b, 3 s.w
+template <typename T>
+__global__ void __launch_bounds__(BT) binit_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                   const Scal* __restrict__ sc, const T* __restrict__ b,
+                                                   T* __restrict__ x, T* __restrict__ r, T* __restrict__ w,
+                                                   const T* __restrict__ dinv, double* __restrict__ part) {
+  __shared__ double res[3];
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    double v[3] = {0, 0, 0};
+    if (!sc[ch.solve].done) {
+      for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
+        const T rg = b[g];
+        const T wg = dinv[g] * rg;
+        r[g] = rg;
+        x[g] = T(0);
+        w[g] = wg;
+        v[0] += (double)rg * (double)wg;
+        v[1] += (double)rg * (double)rg;
+        v[2] += (double)rg * (double)rg;
+      }
+    }
+    block_sum<3>(v, res);
+    if (threadIdx.x < 3) part[threadIdx.x * nchunks + c] = res[threadIdx.x];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BT) bupdate_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                     const Scal* __restrict__ sc, T* __restrict__ x,
+                                                     T* __restrict__ r, T* __restrict__ w, const T* __restrict__ s,
+                                                     T* __restrict__ p, T* __restrict__ q,
+                                                     const T* __restrict__ dinv, double* __restrict__ part) {
+  __shared__ double res[2];
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const Scal& S = sc[ch.solve];
+    double v[2] = {0, 0};
+    if (!S.done) {
+      const T alpha = (T)S.alpha, beta = (T)S.beta;
+      for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
+        const T pg = beta * p[g] + w[g];
+        const T qg = beta * q[g] + s[g];
+        p[g] = pg;
+        q[g] = qg;
+        x[g] += alpha * pg;
+        const T rg = r[g] - alpha * qg;
+        r[g] = rg;
+        const T wg = dinv[g] * rg;
+        w[g] = wg;
+        v[0] += (double)rg * (double)wg;
+        v[1] += (double)rg * (double)rg;
+      }
+    }
+    block_sum<2>(v, res);
+    if (threadIdx.x < 2) part[threadIdx.x * nchunks + c] = res[threadIdx.x];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                       const Scal* __restrict__ sc, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ cols, const T* __restrict__ yloc,
+                                                       T* __restrict__ s, const T* __restrict__ w,
+                                                       double* __restrict__ part) {
+  __shared__ double res[1];
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    double v[1] = {0};
+    if (!sc[ch.solve].done) {
+      for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
+        T acc = 0;
+        for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+          const int cc = cols[j];
+          acc += cc >= 0 ? yloc[cc] : -yloc[~cc];
+        }
+        s[g] = acc;
+        v[0] += (double)acc * (double)w[g];
+      }
+    }
+    block_sum<1>(v, res);
+    if (threadIdx.x == 0) part[3 * nchunks + c] = res[0];
+  }
+}
+
+__device__ __forceinline__ double sum_range(const double* part, int nchunks, int slot, int c0, int c1) {
+  __shared__ double sm[BT];
+  double s = 0;
+  for (int c = c0 + threadIdx.x; c < c1; c += BT) s += part[slot * nchunks + c];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int wdt = BT / 2; wdt > 0; wdt >>= 1) {
+    if (threadIdx.x < wdt) sm[threadIdx.x] += sm[threadIdx.x + wdt];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
+}
+
+// One CTA per solve: the reference's initial step (NekLinSysIterCG.cpp:147-190).
+__global__ void __launch_bounds__(BT) bscalars_init_kernel(Scal* __restrict__ sc, const double* __restrict__ part,
+                                                           int nchunks, const int* __restrict__ cstart) {
+  const int sv = blockIdx.x;
+  Scal& S = sc[sv];
+  if (S.done) return;  // solves that need no (more) work were flagged on entry
+  const int c0 = cstart[sv], c1 = cstart[sv + 1];
+  const double rw = sum_range(part, nchunks, 0, c0, c1), rr = sum_range(part, nchunks, 1, c0, c1);
+  const double bb = sum_range(part, nchunks, 2, c0, c1) + S.bb_dir, sw = sum_range(part, nchunks, 3, c0, c1);
+  if (threadIdx.x == 0) {
+    S.rhs_mag = S.mag_override > 0 ? S.mag_override : (bb > 1e-6 ? bb : 1.0);
+    S.eps = rr;
+    S.iters = 0;
+    S.k = 0;
+    S.status = ITHACA_GPU_OK;
+    if (!isfinite(rr) || !isfinite(rw) || !isfinite(sw)) {
+      S.status = ITHACA_GPU_ERR_NUMERIC;
+      S.done = 1;
+    } else if (rr < S.tol2 * S.rhs_mag) {
+      S.done = 1;
+    } else {
+      S.rho = rw;
+      S.mu = sw;
+      S.beta = 0.0;
+      S.alpha = rw / sw;
+      S.iters = 1;
+      if (S.max_iter <= 0) {
+        S.status = ITHACA_GPU_ERR_NOT_CONVERGED;
+        S.done = 1;
+      }
+    }
+  }
+}
+
+// One CTA per solve: the reference loop tail (NekLinSysIterCG.cpp:219-261).
+__global__ void __launch_bounds__(BT) bscalars_iter_kernel(Scal* __restrict__ sc, const double* __restrict__ part,
+                                                           int nchunks, const int* __restrict__ cstart) {
+  const int sv = blockIdx.x;
+  Scal& S = sc[sv];
+  if (S.done) return;
+  const int c0 = cstart[sv], c1 = cstart[sv + 1];
+  const double rho_new = sum_range(part, nchunks, 0, c0, c1), eps = sum_range(part, nchunks, 1, c0, c1);
+  const double mu = sum_range(part, nchunks, 3, c0, c1);
+  if (threadIdx.x == 0) {
+    S.eps = eps;
+    S.mu = mu;
+    S.iters += 1;
+    if (!isfinite(eps) || !isfinite(rho_new) || !isfinite(mu)) {
+      S.status = ITHACA_GPU_ERR_NUMERIC;
+      S.done = 1;
+    } else if (eps < S.tol2 * S.rhs_mag) {
+      S.done = 1;
+    } else {
+      const double beta = rho_new / S.rho;
+      S.alpha = rho_new / (mu - rho_new * beta / S.alpha);
+      S.beta = beta;
+      S.rho = rho_new;
+      S.k += 1;
+      if (S.k >= S.max_iter) {
+        S.status = ITHACA_GPU_ERR_NOT_CONVERGED;
+        S.done = 1;
+      }
+    }
+  }
+}
+
+// ---- mixed-precision outer step kernels (FP64) ----
+// r = b - sum yloc on the free dofs of solves not yet converged; partial r.r (slot 1), b.b (slot 2)
+__global__ void __launch_bounds__(BT) bresidual_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                       const Scal* __restrict__ sc, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ cols, const double* __restrict__ yloc,
+                                                       const double* __restrict__ b, double* __restrict__ r,
+                                                       double* __restrict__ part) {
+  __shared__ double res[2];
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    double v[2] = {0, 0};
+    for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
+      double acc = 0;
+      for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+        const int cc = cols[j];
+        acc += cc >= 0 ? yloc[cc] : -yloc[~cc];
+      }
+      const double rg = b[g] - acc;
+      r[g] = rg;
+      v[0] += rg * rg;
+      v[1] += b[g] * b[g];
+    }
+    block_sum<2>(v, res);
+    if (threadIdx.x < 2) part[(1 + threadIdx.x) * nchunks + c] = res[threadIdx.x];
+  }
+}
+
+// One CTA per solve: outer convergence test; arms the inner solve of the others.
+__global__ void __launch_bounds__(BT) bouter_kernel(Scal* __restrict__ outer, Scal* __restrict__ inner,
+                                                    const double* __restrict__ part, int nchunks,
+                                                    const int* __restrict__ cstart, double tol2, double inner_tol2,
+                                                    int max_iter_inner) {
+  const int sv = blockIdx.x;
+  const int c0 = cstart[sv], c1 = cstart[sv + 1];
+  const double rr = sum_range(part, nchunks, 1, c0, c1), bb = sum_range(part, nchunks, 2, c0, c1);
+  if (threadIdx.x == 0) {
+    Scal& O = outer[sv];
+    O.rn2 = rr;
+    O.bn2 = bb;
+    if (!isfinite(rr)) O.status = ITHACA_GPU_ERR_NUMERIC;
+    O.outer_done = (O.outer_done || !(rr > tol2 * bb) || bb == 0 || O.status != ITHACA_GPU_OK) ? 1 : 0;
+    Scal I = Scal{};
+    I.tol2 = inner_tol2;
+    I.mag_override = 1.0;
+    I.max_iter = max_iter_inner;
+    I.done = O.outer_done;
+    I.scale = O.outer_done ? 0.0 : 1.0 / sqrt(rr);
+    inner[sv] = I;
+  }
+}
+
+// r32 = r64 * scale_s (solves still refining), x64 += d32 / scale_s after the inner solve
+__global__ void __launch_bounds__(BT) bscale_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                    const Scal* __restrict__ inner, const double* __restrict__ r,
+                                                    float* __restrict__ r32) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const double sc = inner[ch.solve].done ? 0.0 : inner[ch.solve].scale;
+    for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) r32[g] = (float)(r[g] * sc);
+  }
+}
+
+__global__ void __launch_bounds__(BT) baxpy_kernel(const Chunk* __restrict__ chunks, int nchunks,
+                                                   const Scal* __restrict__ outer, const float* __restrict__ d32,
+                                                   double* __restrict__ x) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const Scal& O = outer[ch.solve];
+    if (O.outer_done) continue;
+    const double sc = sqrt(O.rn2);
+    for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) x[g] += sc * (double)d32[g];
+  }
+}
+
+// ---- setup kernels ----
+__global__ void scale_jw_kernel(int E, int ng, int nq, double lambda, double* __restrict__ jg) {
+  const size_t total = (size_t)E * nq;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    jg[(i / nq) * ng * nq + i % nq] *= lambda;
+}
+
+__global__ void assemble_abs_kernel(int N, const int* __restrict__ rowptr, const int* __restrict__ cols,
+                                    const double* __restrict__ loc, double* __restrict__ out) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+      const int cc = cols[j];
+      acc += loc[cc >= 0 ? cc : ~cc];
+    }
+    out[g] = acc;
+  }
+}
+
+__global__ void inv_free_kernel(int N, int ndir, const double* __restrict__ d, double* __restrict__ dinv,
+                                float* __restrict__ dinv32) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
+    const double v = g >= ndir ? 1.0 / d[g] : 0.0;
+    dinv[g] = v;
+    dinv32[g] = (float)v;
+  }
+}
+
+__global__ void cast_f32_kernel(size_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+template <typename T>
+struct Vec {
+  T *x = nullptr, *r = nullptr, *w = nullptr, *s = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr,
+    *b = nullptr, *yloc = nullptr;
+  void alloc(size_t N, size_t nloc) {
+    for (T** pp : {&x, &r, &w, &s, &p, &q, &dinv, &b}) {
+      ITHACA_CUDA(cudaMalloc(pp, sizeof(T) * N));
+      ITHACA_CUDA(cudaMemset(*pp, 0, sizeof(T) * N));
+    }
+    ITHACA_CUDA(cudaMalloc(&yloc, sizeof(T) * nloc));
+  }
+  void release() {
+    for (T* p0 : {x, r, w, s, p, q, dinv, b, yloc}) cudaFree(p0);
+  }
+};
+
+struct Group {
+  int n = 0, Q = 0, dim = 2, E = 0, nm = 0, nq = 0;
+  int N = 0, ndir = 0, nsolve = 0, nchunks = 0;
+  std::vector<int> solves;          // batch index of each solve in this group
+  std::vector<int> dir_off, free_off, nfree, nglobal_s, ndir_s;
+  std::vector<double> bbdir_host;   // squared norm of each solve's Dirichlet rhs entries
+  double* t64 = nullptr;
+  float* t32 = nullptr;
+  double* jg64 = nullptr;
+  float* jg32 = nullptr;
+  int *l2g = nullptr, *rowptr = nullptr, *cols = nullptr, *esolve = nullptr, *cstart = nullptr;
+  Chunk* chunks = nullptr;
+  double* part = nullptr;
+  Scal *sc = nullptr, *sc_outer = nullptr;
+  Vec<double> v64;
+  Vec<float> v32;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done_ev = nullptr;
+  size_t nloc() const { return (size_t)E * nm; }
+  ~Group() {
+    cudaFree(t64);
+    cudaFree(t32);
+    cudaFree(jg64);
+    cudaFree(jg32);
+    for (void* p : {(void*)l2g, (void*)rowptr, (void*)cols, (void*)esolve, (void*)cstart, (void*)chunks,
+                    (void*)part, (void*)sc, (void*)sc_outer})
+      cudaFree(p);
+    v64.release();
+    v32.release();
+    if (stream) cudaStreamDestroy(stream);
+    if (done_ev) cudaEventDestroy(done_ev);
+  }
+};
+
+template <typename T>
+static void upload_tabs(T** dst, const BasisTables& b) {
+  const int n = b.n, Q = b.Q;
+  std::vector<T> h((size_t)4 * n * Q + 2 * Q * Q + Q);
+  for (int p = 0; p < n; ++p)
+    for (int i = 0; i < Q; ++i) {
+      h[off_B(n, Q) + p * Q + i] = (T)b.B[p * Q + i];
+      h[off_Bt(n, Q) + i * n + p] = (T)b.B[p * Q + i];
+      h[off_DB(n, Q) + p * Q + i] = (T)b.DB[p * Q + i];
+      h[off_DBt(n, Q) + i * n + p] = (T)b.DB[p * Q + i];
+    }
+  for (int k = 0; k < Q; ++k)
+    for (int i = 0; i < Q; ++i) {
+      h[off_D(n, Q) + k * Q + i] = (T)b.D[k * Q + i];
+      h[off_Dt(n, Q) + i * Q + k] = (T)b.D[k * Q + i];
+    }
+  for (int i = 0; i < Q; ++i) h[off_w(n, Q) + i] = (T)b.w[i];
+  ITHACA_CUDA(cudaMalloc(dst, h.size() * sizeof(T)));
+  ITHACA_CUDA(cudaMemcpy(*dst, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+}  // namespace batch
+
+struct Batch {
+  Ctx* ctx = nullptr;
+  int dim = 2, nsolve = 0;
+  std::vector<std::unique_ptr<batch::Group>> groups;
+  std::vector<std::pair<int, int>> where;  // batch solve -> (group, index in group)
+  cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
+  int graph64_len = 0, graph32_len = 0;
+  cudaEvent_t fork = nullptr;
+  ~Batch() {
+    if (graph64) cudaGraphExecDestroy(graph64);
+    if (graph32) cudaGraphExecDestroy(graph32);
+    if (fork) cudaEventDestroy(fork);
+  }
+};
+
+}  // namespace ithaca
+
+#include "batched_api.inc"
