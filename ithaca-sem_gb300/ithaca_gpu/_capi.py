@@ -39,6 +39,14 @@ class CgResult(ctypes.Structure):
                 ("rel_residual", ctypes.c_double), ("eps", ctypes.c_double), ("rhs_magnitude", ctypes.c_double)]
 
 
+class SolveDesc(ctypes.Structure):
+    """ithaca_gpu_solve_desc (one system of a batch)."""
+    _fields_ = [("nmodes", ctypes.c_int), ("npoints", ctypes.c_int), ("nelmt", ctypes.c_int),
+                ("jac", ctypes.c_void_p), ("df", ctypes.c_void_p), ("deformed", ctypes.c_int),
+                ("l2g", ctypes.c_void_p), ("sign", ctypes.c_void_p), ("nglobal", ctypes.c_int),
+                ("ndir", ctypes.c_int), ("lam", ctypes.c_double), ("rhs", ctypes.c_void_p)]
+
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _d = ctypes.c_double
@@ -74,6 +82,9 @@ SIGNATURES = {
     "ithaca_gpu_cg_assemble": [_vp, _vp, _vp, _i],
     "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_batch_create": [_vp, _i, _i, ctypes.POINTER(SolveDesc), _pp],
+    "ithaca_gpu_batch_destroy": [_vp],
+    "ithaca_gpu_batch_solve": [_vp, ctypes.POINTER(CgOpts), _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)],
     "ithaca_gpu_cg_set_varcoeff": [_vp, _vp, _i],
     "ithaca_gpu_misfit": [_vp, _vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_kappa_gradient": [_vp, _vp, _vp, _vp, _i],

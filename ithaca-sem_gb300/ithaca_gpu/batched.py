@@ -15,11 +15,7 @@ from .mesh import QuadMesh
 from .operators import SOLVE_MODES, SHAPES
 
 
-class SolveDesc(ctypes.Structure):
-    _fields_ = [("nmodes", ctypes.c_int), ("npoints", ctypes.c_int), ("nelmt", ctypes.c_int),
-                ("jac", ctypes.c_void_p), ("df", ctypes.c_void_p), ("deformed", ctypes.c_int),
-                ("l2g", ctypes.c_void_p), ("sign", ctypes.c_void_p), ("nglobal", ctypes.c_int),
-                ("ndir", ctypes.c_int), ("lam", ctypes.c_double), ("rhs", ctypes.c_void_p)]
+SolveDesc = C.SolveDesc
 
 
 class BatchedHelmholtz:
