@@ -1,0 +1,72 @@
+"""The benchmark's hexahedral workload (BASELINE config 2) and a small command-line driver.
+
+``hex_workload(mesh, order)`` builds the curved 32^3 (or mesh^3) hexahedral Helmholtz
+problem on the GPU: geometry factors, the FP64 collection, the C0 system and the
+assembled right-hand side of f = sin(pi x) sin(pi y) sin(pi z).
+
+    python ithaca-sem_gb300/ithaca_gpu/workload.py --mesh 24 --order 6 --mode mixed --solves 1
+
+runs that many solves and prints iterations and times; it is the command the ncu
+summaries under profiles/ were taken on.
+"""
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+if __package__ in (None, ""):
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from ithaca_gpu.mesh import HexMesh  # noqa: E402
+
+
+def hex_workload(mesh_n=32, order=6, device=0, amp=0.05):
+    import torch
+    from ithaca_gpu.operators import Collection, Context, GlobalLinSysIterativeFullGPU, geom_factors
+    cuda = f"cuda:{device}"
+    n, Q = order + 1, order + 2
+    mesh = HexMesh(mesh_n, mesh_n, mesh_n, curve_amp=amp)
+    X = mesh.coords(Q)
+    amap = mesh.assembly(n)
+    f = (np.sin(np.pi * X[0]) * np.sin(np.pi * X[1]) * np.sin(np.pi * X[2])).reshape(-1)
+    ctx = Context(device)
+    jac, df = geom_factors(ctx, "hex", Q, torch.from_numpy(X).to(cuda))
+    coll = Collection(ctx, "hex", n, Q, mesh.E, jac, df, deformed=True, precision="fp64")
+    sysg = GlobalLinSysIterativeFullGPU(coll, amap)
+    fd = torch.from_numpy(f).to(cuda)
+    loc = torch.empty(mesh.E * n ** 3, dtype=torch.float64, device=cuda)
+    coll.iproduct(fd, loc)
+    loc.neg_()
+    b = torch.empty(amap.nglobal, dtype=torch.float64, device=cuda)
+    sysg.assemble(loc, b)
+    ctx.synchronize()
+    return dict(ctx=ctx, mesh=mesh, n=n, Q=Q, X=X, amap=amap, f=f, jac=jac, df=df, coll=coll, system=sysg, b=b)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--mesh", type=int, default=24)
+    ap.add_argument("--order", type=int, default=6)
+    ap.add_argument("--mode", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--solves", type=int, default=1)
+    ap.add_argument("--variant", type=int, default=-1, help="FP32 hex kernel variant (-1: autotune)")
+    a = ap.parse_args()
+    import torch
+    w = hex_workload(a.mesh, a.order)
+    if a.variant < 0:
+        v, times = w["coll"].autotune(reps=3)
+        print("autotune", v, times)
+    else:
+        w["coll"].set_variant(a.variant)
+    x = torch.zeros_like(w["b"])
+    for _ in range(a.solves):
+        t0 = time.perf_counter()
+        _, res = w["system"].solve(1.0, w["b"], x, tol=1e-10, mode=a.mode)
+        print(f"{a.mode}: {res.iterations} iterations, {res.outer_iterations} outer, rel residual "
+              f"{res.rel_residual:.3e}, {time.perf_counter() - t0:.3f} s")
+
+
+if __name__ == "__main__":
+    main()
