@@ -243,6 +243,21 @@ int ithaca_gpu_pod_online(ithaca_gpu_ctx* ctx, int r, const double* A_L, const d
 int ithaca_gpu_pod_reconstruct(ithaca_gpu_ctx* ctx, int N, int r, const double* V, int nsol, const double* x_r,
                                double* u, int on_device);
 
+/* Allocation-free Gram matrix C = S^T S (no counterpart in the reference). For callers
+ * that cannot allocate device memory where they need it: a ROM step recorded inside a
+ * CUDA graph capture (cudaMalloc/cudaFree are not allowed while a stream is captured), or
+ * a host that reserves its device memory up front and forbids allocation in its loop.
+ * S (N x ns, column-major) and C (ns x ns) are device pointers owned by the caller; work
+ * is queued on `stream` (a cudaStream_t, NULL for the legacy default stream) and not
+ * waited for. The split-K scratch is a fixed 2 MiB device array in the library, held on
+ * every device that loads it until the process exits, so ns <= 128 (larger ns returns
+ * ITHACA_GPU_ERR_ARG). Nothing in the array needs to start at zero: every partial sum is
+ * written before it is read. The first call on a device looks that array up
+ * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
+ * array: calls whose work overlaps on the GPU race and must be serialised by the caller.
+ * It calls no cudaMalloc or cudaFree and needs no context. */
+int ithaca_gpu_pod_gram_noalloc(int N, int ns, const double* S, double* C, void* stream);
+
 /* Measurement hook (no reference counterpart): runs the gather + element-Helmholtz
  * kernel that ithaca_gpu_cg_solve launches for `mode` `reps` times on the context
  * stream and returns its average device time in ms (CUDA events) and the algorithmic

@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "ithaca_internal.h"
@@ -503,3 +505,77 @@ int ithaca_gpu_pod_rb_size(int ns, const double* sigma, double pod_tolerance, in
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Gram matrix without any device allocation.
+//
+// Some callers cannot allocate device memory at the point where they need S^T S: a
+// reduced-order model that rebuilds its Gram matrix inside a CUDA graph being captured
+// (cudaMalloc and cudaFree are not allowed during stream capture), or a host that
+// reserves all device memory up front for a fixed-budget pool and forbids further
+// allocations in its solve loop. ithaca_gpu_pod_gram allocates its split-K partial sums
+// per call; this variant keeps them in a fixed, file-scope device array instead.
+//
+// The array holds kNoAllocGramDoubles doubles (2 MiB), allocated when the library is
+// loaded on a device and held until the process exits. It bounds the problem: ns <= 128
+// snapshots (the split-K reduction is capped so that splits * ns * ns fits). Every call
+// shares the array and leaves the last call's partial sums in it; each partial is fully
+// written before it is read, so nothing needs clearing, but calls whose work overlaps on
+// the GPU (different streams, or other devices' host threads racing on one device) race
+// on the array and must be serialised by the caller.
+namespace ithaca {
+
+constexpr int kNoAllocMaxSnapshots = 128;
+constexpr int kNoAllocMaxSplits = 16;
+constexpr size_t kNoAllocGramDoubles = (size_t)kNoAllocMaxSplits * kNoAllocMaxSnapshots * kNoAllocMaxSnapshots;
+
+static __device__ __align__(256) double g_gram_scratch[kNoAllocGramDoubles];
+
+// Device address of g_gram_scratch on the current device, looked up once per device
+// (the host-side name of a __device__ array is only a stand-in, not a device address).
+static double* gram_scratch_on_current_device() {
+  constexpr int kMaxDevices = 64;
+  static double* cache[kMaxDevices] = {};
+  static std::mutex m;
+  int dev = 0;
+  ITHACA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) fail(ITHACA_GPU_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(m);
+  if (!cache[dev]) {
+    void* p = nullptr;
+    const cudaError_t rc = cudaGetSymbolAddress(&p, g_gram_scratch);
+    if (rc != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      fail(ITHACA_GPU_ERR_CUDA, std::string("cudaGetSymbolAddress(g_gram_scratch): ") + cudaGetErrorString(rc));
+    }
+    cache[dev] = static_cast<double*>(p);
+  }
+  return cache[dev];
+}
+
+}  // namespace ithaca
+
+extern "C" int ithaca_gpu_pod_gram_noalloc(int N, int ns, const double* S, double* C, void* stream) {
+  return pod_guarded([&] {
+    preq(S && C && N > 0 && ns > 0, "bad argument");
+    if (ns > kNoAllocMaxSnapshots)
+      fail(ITHACA_GPU_ERR_ARG, "ithaca_gpu_pod_gram_noalloc: ns = " + std::to_string(ns) + " exceeds the " +
+                                   std::to_string(kNoAllocMaxSnapshots) +
+                                   " snapshots its fixed scratch holds (use ithaca_gpu_pod_gram)");
+    double* scratch = gram_scratch_on_current_device();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const dim3 grid((ns + GT - 1) / GT, (ns + GT - 1) / GT, 1);
+    int nsplit, kc;
+    split_k(N, grid.x * grid.y, &nsplit, &kc);
+    if (nsplit > kNoAllocMaxSplits) {  // fewer, longer splits so that the partials fit
+      kc = (N + kNoAllocMaxSplits - 1) / kNoAllocMaxSplits;
+      kc = (kc + GK - 1) / GK * GK;
+      nsplit = (N + kc - 1) / kc;
+    }
+    const size_t stride = (size_t)ns * ns;
+    if ((size_t)nsplit * stride > kNoAllocGramDoubles) fail(ITHACA_GPU_ERR_ARG, "noalloc Gram scratch too small");
+    dgemm_kernel<true><<<dim3(grid.x, grid.y, nsplit), 256, 0, s>>>(ns, ns, N, kc, S, N, S, N, scratch, stride, ns);
+    sum_parts_kernel<<<std::min<size_t>((stride + 255) / 256, 1024), 256, 0, s>>>(stride, nsplit, scratch, stride, C);
+    ITHACA_CUDA(cudaGetLastError());
+  });
+}

@@ -89,6 +89,7 @@ SIGNATURES = {
     "ithaca_gpu_misfit": [_vp, _vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_kappa_gradient": [_vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_pod_gram": [_vp, _i, _i, _vp, _vp, _i],
+    "ithaca_gpu_pod_gram_noalloc": [_i, _i, _vp, _vp, _vp],
     "ithaca_gpu_pod_offline": [_vp, _i, _i, _vp, _i, _vp, _vp, ctypes.POINTER(ctypes.c_int), _i],
     "ithaca_gpu_pod_rb_size": [_i, _vp, _d, ctypes.POINTER(ctypes.c_int)],
     "ithaca_gpu_pod_project": [_vp, _i, _vp, _vp, _vp, _i],
