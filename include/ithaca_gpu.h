@@ -113,12 +113,14 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
 /* Kernel choice for FP32 hexahedral Helmholtz applies (also used by the FP32 inner
  * solves of a system built on this operator): 0 = shared-memory sum-factorisation
  * kernel, 2 or 4 = register-pencil kernel with a TMA-staged geometry slab and that
- * many elements per CTA (default 4). */
+ * many elements per CTA (default 4), 21 or 22 = the persistent pencil kernel that
+ * prefetches the next group of 1 or 2 elements (geometry by TMA into a double buffer,
+ * gathered coefficients into registers) while computing the current one. */
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
 /* Times every variant on the operator's own data and keeps the fastest, like
  * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)
- * picks an implementation type. times_ms (3 entries, may be NULL) receives the average
- * FP32 apply time of variants 0, 2, 4. */
+ * picks an implementation type. times_ms (5 entries, may be NULL) receives the average
+ * FP32 apply time of variants 0, 2, 4, 21, 22 (-1 where a variant does not apply). */
 int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* times_ms);
 /* Diagonals of the element Helmholtz matrices (E*n^d), the per-element input of
  * PreconditionerDiagonal::DiagonalPreconditionerSum (PreconditionerDiagonal.cpp:98-161). */
@@ -138,7 +140,7 @@ typedef struct {
   double tol;          /* IterativeSolverTolerance (default 1e-9); stop when ||r||^2 < tol^2 ||b||^2 */
   int max_iter;        /* NekLinSysMaxIterations (default 5000)                                      */
   int mode;            /* ITHACA_GPU_SOLVE_*                                                         */
-  double inner_tol;    /* mixed mode: relative reduction asked of each inner FP32 solve (default 1e-4) */
+  double inner_tol;    /* mixed mode: relative reduction asked of each inner FP32 solve (default 1e-2) */
   int max_outer;       /* mixed mode: maximum refinement steps (default 50)                          */
   int check_every;     /* iterations per device-side convergence check (default 8)                   */
 } ithaca_gpu_cg_opts;

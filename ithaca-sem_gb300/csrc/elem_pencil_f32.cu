@@ -1,5 +1,7 @@
-// FP32 instantiations and launcher of the pencil hexahedral Helmholtz kernel.
-#include "elem_pencil.cuh"
+// FP32 instantiations and launcher of the pencil hexahedral Helmholtz kernels.
+#include <algorithm>
+
+#include "elem_pencil_pipe.cuh"
 
 namespace ithaca {
 namespace dev {
@@ -21,19 +23,53 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
   k<<<grid, block, L::bytes(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, err);
 }
 
+// Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
+// occupancy calculator), never more CTAs than element groups.
+template <typename T, int N, int Q, int EB>
+static void pipe_nq(int E, const double* hB, const double* hD, const T* jg, T lambda, const T* in, T* out,
+                    const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s) {
+  PTabs<T, N, Q> tab;
+  for (int i = 0; i < N * Q; ++i) tab.B[i] = (T)hB[i];
+  for (int i = 0; i < Q * Q; ++i) tab.D[i] = (T)hD[i];
+  using L = PipeLayout<T, N, Q, EB>;
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true> : helm3_pipe_kernel<T, N, Q, EB, false>;
+  static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
+  const int gi = l2g ? 1 : 0;
+  if (slots[gi] == 0) {
+    ITHACA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes()));
+    int dev = 0, sms = 0, per_sm = 0;
+    ITHACA_CUDA(cudaGetDevice(&dev));
+    ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ITHACA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Q * Q * EB, L::bytes()));
+    slots[gi] = std::max(1, sms * std::max(1, per_sm));
+  }
+  const int ngroups = (E + EB - 1) / EB;
+  const dim3 block(Q * Q, EB), grid(std::min(ngroups, slots[gi]));
+  k<<<grid, block, L::bytes(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, err);
+}
+
 }  // namespace dev
 
+// variant: 2 or 4 = one pass per CTA with a TMA-staged geometry slab and that many
+// elements per CTA; 21 or 22 = the persistent pipelined kernel with 1 or 2 elements per
+// group.
 template <typename T>
-bool launch_helm_pencil(int n, int Q, int E, int eb, const double* hB, const double* hD, const T* jg, T lambda,
+bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s) {
-#define X(NN, QQ)                                                                                        \
-  if (n == NN && Q == QQ) {                                                                              \
-    if (eb >= 4)                                                                                         \
-      dev::pencil_nq<T, NN, QQ, 4>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);    \
-    else                                                                                                 \
-      dev::pencil_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);    \
-    return true;                                                                                         \
+#define X(NN, QQ)                                                                                          \
+  if (n == NN && Q == QQ) {                                                                                \
+    if (variant == 4)                                                                                      \
+      dev::pencil_nq<T, NN, QQ, 4>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);      \
+    else if (variant == 2)                                                                                 \
+      dev::pencil_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);      \
+    else if (variant == 21)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);        \
+    else if (variant == 22)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);        \
+    else                                                                                                   \
+      return false;                                                                                        \
+    return true;                                                                                           \
   }
   X(2, 3) X(3, 4) X(4, 5) X(5, 6) X(6, 7) X(7, 8) X(8, 9) X(9, 10) X(10, 11)
 #undef X

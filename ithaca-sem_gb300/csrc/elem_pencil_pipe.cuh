@@ -1,0 +1,343 @@
+// Persistent, software-pipelined version of the register-pencil hexahedral Helmholtz
+// kernel (elem_pencil.cuh holds the single-pass version and the shared helpers).
+//
+// One CTA per resident slot loops over groups of EB elements (group, group + gridDim.x,
+// ...). While it computes group i it already has in flight
+//   * the TMA copy of group i+1's geometry slab into the other half of a double buffer
+//     (issued at the top of iteration i, waited for at the metric stage of i+1), and
+//   * the gather of group i+1's input coefficients into registers: the signed l2g codes
+//     are loaded right after stage 1 of group i and the dependent x loads are issued
+//     after stage 5, so both latencies hide behind group i's arithmetic; the values are
+//     written to shared memory at stage 1 of iteration i+1, where the sign is applied.
+// The arithmetic per element is exactly that of helm3_pencil_kernel (same stages, same
+// tables, same summation order), so both kernels give bit-identical results.
+#pragma once
+
+#include "elem_pencil.cuh"
+
+namespace ithaca {
+namespace dev {
+
+template <typename T, int N, int Q, int EB>
+struct PipeLayout {
+  static constexpr int NQ = Q * Q * Q, GEO = 7 * NQ;
+  static constexpr int PJ = Q, PK = pk_stride(Q), FS = PK * Q;
+  static constexpr size_t GEO_BYTES = ((size_t)EB * GEO * sizeof(T) + 32 + 15) / 16 * 16;  // + window slack
+  static constexpr size_t bytes() { return 16 + 2 * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
+};
+
+template <typename T, int N, int Q, int EB, bool GATHER>
+__global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
+                                                               const PTabs<T, N, Q> tab, const T* __restrict__ jg,
+                                                               T lambda, int E, const int* __restrict__ l2g,
+                                                               int ndir, const int* __restrict__ skip,
+                                                               const T* __restrict__ lam_ptr, int* __restrict__ err) {
+  using L = PipeLayout<T, N, Q, EB>;
+  constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
+  constexpr int PJ = L::PJ, PK = L::PK, FS = L::FS;
+  constexpr int NPT = (NM + TPE - 1) / TPE;  // coefficients gathered per thread
+  if (skip != nullptr && *skip) return;  // converged solve: the whole CTA leaves together
+  if (lam_ptr != nullptr) lambda = *lam_ptr;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // bar[0], bar[1]
+  unsigned char* geo_base = smem + 16;
+  T* work = reinterpret_cast<T*>(smem + 16 + 2 * L::GEO_BYTES);
+
+  const int t = threadIdx.x, el = threadIdx.y;
+  const int tid = t + el * TPE;
+  const int ngroups = (E + EB - 1) / EB;
+  T* SU = work + el * 3 * FS;
+  T* S0 = SU + FS;
+  T* S1 = S0 + FS;
+
+  // TMA window of group `grp` into buffer `b`; returns the byte shift of its first element.
+  auto issue_geometry = [&](int grp, int b) {
+    const int e0 = grp * EB, ne = min(EB, E - e0);
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(jg + (size_t)e0 * GEO);
+    const uintptr_t lo = a0 & ~uintptr_t(15);
+    const uintptr_t hi = (a0 + (size_t)ne * GEO * sizeof(T) + 15) & ~uintptr_t(15);
+    mbar_arrive_expect_tx(bar + b, static_cast<uint32_t>(hi - lo));
+    tma_bulk_load(geo_base + b * L::GEO_BYTES, reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo),
+                  bar + b);
+  };
+  auto geometry_of = [&](int grp, int b) -> const T* {
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(jg + (size_t)grp * EB * GEO);
+    const int shift = static_cast<int>(a0 & uintptr_t(15));
+    return reinterpret_cast<const T*>(geo_base + b * L::GEO_BYTES + shift) + el * GEO;
+  };
+
+  // prefetch registers: raw gathered values and a sign mask for the next group
+  T xv[NPT];
+  int code[NPT];
+  unsigned neg = 0;
+  auto load_codes = [&](int grp) {
+    const int e = grp * EB + el;
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+      const int m = t + j * TPE;
+      code[j] = 0;
+      if (e < E && m < NM) {
+        if constexpr (GATHER) code[j] = __ldg(l2g + (size_t)e * NM + m);
+      }
+    }
+  };
+  auto load_values = [&](int grp) {
+    const int e = grp * EB + el;
+    neg = 0;
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+      const int m = t + j * TPE;
+      xv[j] = T(0);
+      if (e < E && m < NM) {
+        if constexpr (GATHER) {
+          const int c = code[j];
+          const int g = c >= 0 ? c : ~c;
+          if (g >= ndir) xv[j] = in[g];
+          neg |= (c < 0 ? 1u : 0u) << j;
+        } else {
+          xv[j] = in[(size_t)e * NM + m];
+        }
+      }
+    }
+  };
+
+  int grp = blockIdx.x;
+  if (grp >= ngroups) return;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (tid == 0) issue_geometry(grp, 0);
+  load_codes(grp);
+  load_values(grp);
+
+  for (int it = 0; grp < ngroups; ++it, grp += gridDim.x) {
+    const int b = it & 1;
+    const uint32_t parity = (it >> 1) & 1;
+    const int nxt = grp + gridDim.x;
+    const bool has_next = nxt < ngroups;
+    const int e = grp * EB + el;
+    const bool active = e < E;
+    // the other buffer was last read in the previous iteration, which ended in a barrier
+    if (tid == 0 && has_next) issue_geometry(nxt, b ^ 1);
+
+    // ---- 1: prefetched coefficients -> S0 as (p, q, r); then the next group's codes ----
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+      const int m = t + j * TPE;
+      if (m < NM) {
+        const int p = m % N, q = (m / N) % N, r = m / (N * N);
+        S0[p + PJ * q + PK * r] = (neg >> j) & 1u ? -xv[j] : xv[j];
+      }
+    }
+    if (has_next) load_codes(nxt);
+    __syncthreads();
+    // ---- 2: BwdTrans along p: pencils (q, r) ----
+    if (t < N * N) {
+      const int q = t % N, r = t / N;
+      T c[N];
+#pragma unroll
+      for (int p = 0; p < N; ++p) c[p] = S0[p + PJ * q + PK * r];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        T acc = tab.B[i] * c[0];
+#pragma unroll
+        for (int p = 1; p < N; ++p) acc = fma(tab.B[p * Q + i], c[p], acc);
+        S1[i + PJ * q + PK * r] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- 3: along q: pencils (i, r) ----
+    if (t < Q * N) {
+      const int i = t % Q, r = t / Q;
+      T c[N];
+#pragma unroll
+      for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) {
+        T acc = tab.B[j] * c[0];
+#pragma unroll
+        for (int q = 1; q < N; ++q) acc = fma(tab.B[q * Q + j], c[q], acc);
+        S0[i + PJ * j + PK * r] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- 4: along r: columns (i, j) -> u in registers; d/dxi_2 in registers ----
+    const int ci = t % Q, cj = t / Q;
+    T u[Q], g2[Q];
+    {
+      T c[N];
+#pragma unroll
+      for (int r = 0; r < N; ++r) c[r] = S0[ci + PJ * cj + PK * r];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        T acc = tab.B[k] * c[0];
+#pragma unroll
+        for (int r = 1; r < N; ++r) acc = fma(tab.B[r * Q + k], c[r], acc);
+        u[k] = acc;
+      }
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        T acc = tab.D[k] * u[0];
+#pragma unroll
+        for (int c2 = 1; c2 < Q; ++c2) acc = fma(tab.D[c2 * Q + k], u[c2], acc);
+        g2[k] = acc;
+      }
+#pragma unroll
+      for (int k = 0; k < Q; ++k) SU[ci + PJ * cj + PK * k] = u[k];
+    }
+    __syncthreads();
+    // ---- 5: d/dxi_0 on pencils (j, k) -> S0 ; d/dxi_1 on pencils (i, k) -> S1 ----
+    {
+      const int pj = t % Q, pk = t / Q;
+      T c[Q];
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = SU[a + PJ * pj + PK * pk];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        T acc = tab.D[i] * c[0];
+#pragma unroll
+        for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + i], c[a], acc);
+        S0[i + PJ * pj + PK * pk] = acc;
+      }
+      const int pi = t % Q;
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) {
+        T acc = tab.D[j] * c[0];
+#pragma unroll
+        for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + j], c[a], acc);
+        S1[pi + PJ * j + PK * pk] = acc;
+      }
+    }
+    // the next group's gather: its codes have had stages 2-5 to arrive
+    if (has_next) load_values(nxt);
+    // geometry of this group must have landed before the point-wise stage
+    const bool ok = mbar_wait_bounded(bar + b, parity, kWaitCycles);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0 && err != nullptr) atomicExch(err, ITHACA_GPU_ERR_TIMEOUT);
+      // give the copies in flight time to finish before the CTA's shared memory goes away
+      mbar_wait_bounded(bar + b, parity, kWaitCycles);
+      if (has_next) mbar_wait_bounded(bar + (b ^ 1), ((it + 1) >> 1) & 1, kWaitCycles);
+      return;
+    }
+    const T* G = geometry_of(grp, b);
+    // ---- 6: point-wise metric on columns (i, j) ----
+    T v[Q];
+    {
+      T f2[Q];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        const int s = ci + PJ * cj + PK * k;
+        const int pt = ci + Q * cj + Q * Q * k;
+        const T g0 = S0[s], g1 = S1[s];
+        const T jw = G[pt];
+        const T m00 = G[NQ + pt], m01 = G[2 * NQ + pt], m02 = G[3 * NQ + pt];
+        const T m11 = G[4 * NQ + pt], m12 = G[5 * NQ + pt], m22 = G[6 * NQ + pt];
+        S0[s] = fma(m00, g0, fma(m01, g1, m02 * g2[k]));
+        S1[s] = fma(m01, g0, fma(m11, g1, m12 * g2[k]));
+        f2[k] = fma(m02, g0, fma(m12, g1, m22 * g2[k]));
+        v[k] = lambda * jw * u[k];
+      }
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        T acc = v[k];
+#pragma unroll
+        for (int c2 = 0; c2 < Q; ++c2) acc = fma(tab.D[k * Q + c2], f2[c2], acc);
+        v[k] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- 7: D^T along i on pencils (j, k) in S0, along j on pencils (i, k) in S1 ----
+    {
+      const int pj = t % Q, pk = t / Q;
+      T c[Q], o[Q];
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = S0[a + PJ * pj + PK * pk];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        T acc = tab.D[i * Q] * c[0];
+#pragma unroll
+        for (int a = 1; a < Q; ++a) acc = fma(tab.D[i * Q + a], c[a], acc);
+        o[i] = acc;
+      }
+#pragma unroll
+      for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
+      const int pi = t % Q;
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = S1[pi + PJ * a + PK * pk];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) {
+        T acc = tab.D[j * Q] * c[0];
+#pragma unroll
+        for (int a = 1; a < Q; ++a) acc = fma(tab.D[j * Q + a], c[a], acc);
+        o[j] = acc;
+      }
+#pragma unroll
+      for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pk] = o[j];
+    }
+    __syncthreads();
+    // ---- 8: sum the three directions on columns, IProduct along k -> SU as (i, j, r) ----
+    {
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        const int s = ci + PJ * cj + PK * k;
+        v[k] += S0[s] + S1[s];
+      }
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        T acc = tab.B[r * Q] * v[0];
+#pragma unroll
+        for (int k = 1; k < Q; ++k) acc = fma(tab.B[r * Q + k], v[k], acc);
+        SU[ci + PJ * cj + PK * r] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- 9: along j: pencils (i, r) -> S0 as (i, q, r) ----
+    if (t < Q * N) {
+      const int i = t % Q, r = t / Q;
+      T c[Q];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        T acc = tab.B[q * Q] * c[0];
+#pragma unroll
+        for (int j = 1; j < Q; ++j) acc = fma(tab.B[q * Q + j], c[j], acc);
+        S0[i + PJ * q + PK * r] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- 10: along i: pencils (q, r) -> S1 as (p, q, r) ----
+    if (t < N * N) {
+      const int q = t % N, r = t / N;
+      T c[Q];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) c[i] = S0[i + PJ * q + PK * r];
+#pragma unroll
+      for (int p = 0; p < N; ++p) {
+        T acc = tab.B[p * Q] * c[0];
+#pragma unroll
+        for (int i = 1; i < Q; ++i) acc = fma(tab.B[p * Q + i], c[i], acc);
+        S1[p + PJ * q + PK * r] = acc;
+      }
+    }
+    __syncthreads();
+    if (active) {
+      for (int m = t; m < NM; m += TPE) {
+        const int p = m % N, q = (m / N) % N, r = m / (N * N);
+        out[(size_t)e * NM + m] = S1[p + PJ * q + PK * r];
+      }
+    }
+    // S0 and S1 are rewritten by the next group's stages 1-2, and the geometry buffer
+    // read here is refilled by the copy issued at the top of the iteration after next
+    __syncthreads();
+  }
+}
+
+}  // namespace dev
+}  // namespace ithaca

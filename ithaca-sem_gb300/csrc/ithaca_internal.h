@@ -108,7 +108,8 @@ struct Op {
   float* df32 = nullptr;
   std::vector<double> hB, hD;  // host copies of B[p*Q+i] and D[k*Q+i] (kernel-parameter tables)
   // Helmholtz kernel variant for FP32 hexahedra: 0 = shared-memory kernel (elem.cuh),
-  // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA.
+  // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA and a
+  // TMA-staged geometry slab, 21 or 22 = persistent pipelined pencil kernel (elem_pencil_pipe.cuh).
   int variant32 = 4;
   ~Op();
 };
@@ -118,7 +119,7 @@ struct Op {
 constexpr size_t kGeoPad = 64;
 
 template <typename T>
-bool launch_helm_pencil(int n, int Q, int E, int eb, const double* hB, const double* hD, const T* jg, T lambda,
+bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s);
 

@@ -168,16 +168,18 @@ class Collection:
         return out
 
     def set_variant(self, variant):
-        """FP32 hex Helmholtz kernel: 0 shared-memory, 2/4 register-pencil (elements per CTA)."""
+        """FP32 hex Helmholtz kernel: 0 shared-memory, 2/4 register-pencil with TMA-staged
+        geometry (elements per CTA), 21/22 persistent pipelined pencil (1/2 elements per group)."""
         C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
 
     def autotune(self, reps=10):
         """Times each kernel variant on this collection and keeps the fastest."""
         chosen = ctypes.c_int()
-        times = np.zeros(3)
+        variants = (0, 2, 4, 21, 22)
+        times = np.zeros(len(variants))
         C.call("ithaca_gpu_op_autotune", self.handle, int(reps), ctypes.byref(chosen),
                ctypes.c_void_p(times.ctypes.data))
-        return chosen.value, {0: times[0], 2: times[1], 4: times[2]}
+        return chosen.value, dict(zip(variants, times.tolist()))
 
     def helmholtz_diag(self, lam, out=None):
         out = out if out is not None else np.zeros(self.E * self.nm)
@@ -212,7 +214,7 @@ class GlobalLinSysIterativeFullGPU:
         self.handle = h
 
     @staticmethod
-    def options(tol=1e-9, max_iter=5000, mode="fp64", inner_tol=1e-4, max_outer=50, check_every=8):
+    def options(tol=1e-9, max_iter=5000, mode="fp64", inner_tol=1e-2, max_outer=50, check_every=8):
         o = C.CgOpts()
         C.lib().ithaca_gpu_cg_default_opts(ctypes.byref(o))
         o.tol, o.max_iter, o.mode = tol, max_iter, SOLVE_MODES[mode]
