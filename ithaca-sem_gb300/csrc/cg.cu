@@ -57,7 +57,8 @@ __device__ __forceinline__ void block_partials(double (&v)[NC], double* partials
 __device__ __forceinline__ double reduce_slot(const double* partials, int slot) {
   __shared__ double sm[RT];
   double s = 0;
-  for (int i = threadIdx.x; i < RB; i += RT) s += partials[slot * RB + i];
+  // L2 loads: the partials may have been written by other CTAs of the same launch
+  for (int i = threadIdx.x; i < RB; i += RT) s += __ldcg(partials + slot * RB + i);
   sm[threadIdx.x] = s;
   __syncthreads();
   for (int w = RT / 2; w > 0; w >>= 1) {
@@ -120,29 +121,138 @@ __global__ void __launch_bounds__(RT) pcg_update_kernel(int N, int ndir, const C
   block_partials<2>(v, partials, slots);
 }
 
+// FP32 update on four dofs per step (16-byte loads and stores; the vectors are padded
+// to a multiple of four entries). Lanes outside [ndir, N) are stored back unchanged.
+// The per-thread sums r.w and r.r are accumulated in FP32 (a few dozen terms per
+// thread) and only the CTA reduction is in FP64: FP64 throughput on this GPU is ~1/60
+// of FP32, and per-dof FP64 products and conversions would dominate the kernel.
+__global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, const CgScalars* sc,
+                                                              float* __restrict__ x, float* __restrict__ r,
+                                                              float* __restrict__ w, const float* __restrict__ s,
+                                                              float* __restrict__ p, float* __restrict__ q,
+                                                              const float* __restrict__ dinv, double* partials) {
+  if (sc->done) return;
+  const float alpha = (float)sc->alpha, beta = (float)sc->beta;
+  float rw = 0.f, rr = 0.f;
+  const int c0 = ndir >> 2, c1 = (N + 3) >> 2;
+  for (int c = c0 + blockIdx.x * RT + threadIdx.x; c < c1; c += RB * RT) {
+    float4 P = reinterpret_cast<const float4*>(p)[c], W = reinterpret_cast<const float4*>(w)[c];
+    float4 Qv = reinterpret_cast<const float4*>(q)[c];
+    const float4 S = reinterpret_cast<const float4*>(s)[c];
+    float4 X = reinterpret_cast<const float4*>(x)[c], R = reinterpret_cast<const float4*>(r)[c];
+    const float4 Dv = reinterpret_cast<const float4*>(dinv)[c];
+    float* pa = &P.x;
+    float* wa = &W.x;
+    float* qa = &Qv.x;
+    const float* sa = &S.x;
+    float* xa = &X.x;
+    float* ra = &R.x;
+    const float* da = &Dv.x;
+    const int g0 = 4 * c;
+    const bool full = g0 >= ndir && g0 + 4 <= N;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (full || (g0 + j >= ndir && g0 + j < N)) {
+        const float pg = fmaf(beta, pa[j], wa[j]);
+        const float qg = fmaf(beta, qa[j], sa[j]);
+        pa[j] = pg;
+        qa[j] = qg;
+        xa[j] = fmaf(alpha, pg, xa[j]);
+        const float rg = fmaf(-alpha, qg, ra[j]);
+        ra[j] = rg;
+        const float wg = da[j] * rg;
+        wa[j] = wg;
+        rw = fmaf(rg, wg, rw);
+        rr = fmaf(rg, rg, rr);
+      }
+    }
+    reinterpret_cast<float4*>(p)[c] = P;
+    reinterpret_cast<float4*>(q)[c] = Qv;
+    reinterpret_cast<float4*>(x)[c] = X;
+    reinterpret_cast<float4*>(r)[c] = R;
+    reinterpret_cast<float4*>(w)[c] = W;
+  }
+  double v[2] = {(double)rw, (double)rr};
+  const int slots[2] = {0, 1};
+  block_partials<2>(v, partials, slots);
+}
+
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc);
+
 // s[g] = sum_{local l of g} sign_l * yloc[l] for g in [g0, N); partial s.w in slot 3.
+// With fuse_sc != nullptr the last CTA to finish (ticket on `counter`) also runs the
+// loop-tail scalar update, saving one launch per CG iteration; the reduction order of
+// the partial sums does not depend on which CTA that is.
 template <typename T, bool SIGNED = true>
 __global__ void __launch_bounds__(RT) assemble_dot_kernel(int N, int g0, const int* __restrict__ rowptr,
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
                                                           T* __restrict__ s, const T* __restrict__ w,
-                                                          const int* skip, double* partials) {
+                                                          const int* skip, double* partials,
+                                                          CgScalars* fuse_sc = nullptr,
+                                                          unsigned int* counter = nullptr) {
   if (skip != nullptr && *skip) return;
-  double v[1] = {0};
-  for (int g = g0 + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
-    T acc = 0;
-    for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
-      const int c = cols[j];
-      if (SIGNED)
-        acc += c >= 0 ? yloc[c] : -yloc[~c];
-      else
-        acc += yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
+  // Four rows per thread step, their loads issued together: a row is a chain of three
+  // dependent loads (row pointer -> local index -> local value), so independent rows
+  // in flight are what keeps the memory system busy. Within a row the entries are
+  // summed in CSR order.
+  constexpr int U = 4;
+  constexpr int STRIDE = RB * RT;
+  T sw = 0;  // per-thread s.w in T (FP32 sums stay off the slow FP64 pipe); CTA sum in FP64
+  for (int g = g0 + blockIdx.x * RT + threadIdx.x; g < N; g += U * STRIDE) {
+    int a[U], b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int gg = g + u * STRIDE;
+      a[u] = gg < N ? rowptr[gg] : 0;
+      b[u] = gg < N ? rowptr[gg + 1] : 0;
     }
-    s[g] = acc;
-    if (w) v[0] += (double)acc * (double)w[g];
+    T acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      acc[u] = 0;
+      if (a[u] < b[u]) {  // first entry (every free row has one)
+        const int c = cols[a[u]];
+        if (SIGNED)
+          acc[u] = c >= 0 ? yloc[c] : -yloc[~c];
+        else
+          acc[u] = yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      for (int j = a[u] + 1; j < b[u]; ++j) {
+        const int c = cols[j];
+        if (SIGNED)
+          acc[u] += c >= 0 ? yloc[c] : -yloc[~c];
+        else
+          acc[u] += yloc[c >= 0 ? c : ~c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int gg = g + u * STRIDE;
+      if (gg < N) {
+        s[gg] = acc[u];
+        if (w) sw = fma(acc[u], w[gg], sw);
+      }
+    }
   }
+  double v[1] = {(double)sw};
   if (partials) {
     const int slots[1] = {3};
     block_partials<1>(v, partials, slots);
+  }
+  if (fuse_sc != nullptr) {
+    __shared__ unsigned int ticket;
+    __threadfence();  // this CTA's partial is visible before it takes a ticket
+    __syncthreads();
+    if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+    __syncthreads();
+    if (ticket == gridDim.x - 1) {
+      __threadfence();
+      scalars_iter_body(partials, fuse_sc);
+      if (threadIdx.x == 0) *counter = 0u;  // re-armed for the next iteration
+    }
   }
 }
 
@@ -178,6 +288,10 @@ __global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials
 
 // Reference loop tail (NekLinSysIterCG.cpp:219-261).
 __global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials, CgScalars* sc) {
+  scalars_iter_body(partials, sc);
+}
+
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc) {
   if (sc->done) return;
   const double rho_new = reduce_slot(partials, 0), eps = reduce_slot(partials, 1);
   const double mu = reduce_slot(partials, 3);
@@ -279,9 +393,10 @@ struct Vecs {
     *yloc = nullptr, *b = nullptr;
   void alloc(size_t N, size_t nloc) {
     T** v[] = {&x, &r, &w, &s, &p, &q, &dinv, &b};
+    const size_t N4 = (N + 3) / 4 * 4;  // padded for the four-wide FP32 update
     for (auto pp : v) {
-      ITHACA_CUDA(cudaMalloc(pp, sizeof(T) * N));
-      ITHACA_CUDA(cudaMemset(*pp, 0, sizeof(T) * N));
+      ITHACA_CUDA(cudaMalloc(pp, sizeof(T) * N4));
+      ITHACA_CUDA(cudaMemset(*pp, 0, sizeof(T) * N4));
     }
     ITHACA_CUDA(cudaMalloc(&yloc, sizeof(T) * nloc));
   }
@@ -305,6 +420,7 @@ struct Cg {
   double* adj_scratch = nullptr;
   double* partials = nullptr;
   double* dscal = nullptr;  // scratch doubles (norms)
+  unsigned int* counter = nullptr;  // CTA ticket of the fused assembly + scalar update
   CgScalars* sc = nullptr;
   CgScalars* sc_host = nullptr;  // pinned
   double diag_lambda = NAN;
@@ -326,6 +442,7 @@ Cg::~Cg() {
   cudaFree(adj_scratch);
   cudaFree(partials);
   cudaFree(dscal);
+  cudaFree(counter);
   cudaFree(sc);
   if (sc_host) cudaFreeHost(sc_host);
 }
@@ -363,15 +480,19 @@ const double* lam_dev<double>(Cg* cg) { return &cg->sc->lambda; }
 template <>
 const float* lam_dev<float>(Cg* cg) { return &cg->sc->lambda32; }
 
-// One PCG iteration: update -> gather+apply -> assemble(+s.w) -> scalars.
+// One PCG iteration: update -> gather+apply -> assemble(+s.w, + scalars in the last CTA).
 template <typename T>
 static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cudaStream_t s) {
-  pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv, cg->partials);
+  if constexpr (sizeof(T) == 4)
+    pcg_update_f32x4_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
+                                              cg->partials);
+  else
+    pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
+                                           cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg));
   assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, v.yloc, v.s, v.w, skip_ptr(cg),
-                                           cg->partials);
-  scalars_iter_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
-  cg->op->ctx->launches += 3;
+                                           cg->partials, cg->sc, cg->counter);
+  cg->op->ctx->launches += 2;
 }
 
 template <typename T>
@@ -427,7 +548,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
     if (cg->sc_host->done) break;
     if (it >= max_launches) fail(ITHACA_GPU_ERR_TIMEOUT, "CG did not flag completion within its iteration bound");
     ITHACA_CUDA(cudaGraphLaunch(ex, s));
-    c->launches += 4LL * chunk;
+    c->launches += 3LL * chunk;
   }
 }
 
@@ -578,7 +699,7 @@ void ithaca_gpu_cg_default_opts(ithaca_gpu_cg_opts* o) {
   o->tol = 1e-9;
   o->max_iter = 5000;
   o->mode = ITHACA_GPU_SOLVE_FP64;
-  o->inner_tol = 1e-4;
+  o->inner_tol = 1e-2;
   o->max_outer = 50;
   o->check_every = 8;
 }
@@ -621,6 +742,8 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     cg->v64.alloc(nglobal, nloc);
     ITHACA_CUDA(cudaMalloc(&cg->partials, sizeof(double) * NSLOT * RB));
     ITHACA_CUDA(cudaMalloc(&cg->dscal, sizeof(double) * 8));
+    ITHACA_CUDA(cudaMalloc(&cg->counter, sizeof(unsigned int)));
+    ITHACA_CUDA(cudaMemset(cg->counter, 0, sizeof(unsigned int)));
     ITHACA_CUDA(cudaMalloc(&cg->sc, sizeof(CgScalars)));
     ITHACA_CUDA(cudaMallocHost(&cg->sc_host, sizeof(CgScalars)));
     *cg->sc_host = CgScalars{};
@@ -829,7 +952,7 @@ static ithaca_gpu_cg_opts opts_or_default(const ithaca_gpu_cg_opts* o) {
   if (d.max_iter <= 0) d.max_iter = 5000;
   if (d.check_every <= 0) d.check_every = 8;
   if (d.max_outer <= 0) d.max_outer = 50;
-  if (!(d.inner_tol > 0 && d.inner_tol < 1)) d.inner_tol = 1e-4;
+  if (!(d.inner_tol > 0 && d.inner_tol < 1)) d.inner_tol = 1e-2;
   return d;
 }
 

@@ -38,7 +38,7 @@ class BatchedHelmholtz:
         C.call("ithaca_gpu_batch_create", ctx.handle, SHAPES[shape], len(problems), descs, ctypes.byref(h))
         self.handle = h
 
-    def solve(self, mode="fp64", tol=1e-10, max_iter=5000, inner_tol=1e-4, max_outer=50, check_every=8,
+    def solve(self, mode="fp64", tol=1e-10, max_iter=5000, inner_tol=1e-2, max_outer=50, check_every=8,
               want_x=True):
         from .operators import GlobalLinSysIterativeFullGPU
         o = GlobalLinSysIterativeFullGPU.options(tol=tol, max_iter=max_iter, mode=mode, inner_tol=inner_tol,

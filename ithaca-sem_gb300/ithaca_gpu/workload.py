@@ -49,10 +49,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--mesh", type=int, default=24)
     ap.add_argument("--order", type=int, default=6)
-    ap.add_argument("--mode", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--mode", choices=["fp64", "mixed"], nargs="*", default=["mixed"])
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--variant", type=int, default=-1, help="FP32 hex kernel variant (-1: autotune)")
-    ap.add_argument("--inner-tol", type=float, nargs="*", default=[1e-4],
+    ap.add_argument("--inner-tol", type=float, nargs="*", default=[1e-2],
                     help="relative reduction asked of each inner FP32 solve (mixed mode)")
     a = ap.parse_args()
     import torch
@@ -63,12 +63,13 @@ def main():
     else:
         w["coll"].set_variant(a.variant)
     x = torch.zeros_like(w["b"])
-    for itol in a.inner_tol:
-        for _ in range(a.solves):
-            t0 = time.perf_counter()
-            _, res = w["system"].solve(1.0, w["b"], x, tol=1e-10, mode=a.mode, inner_tol=itol)
-            print(f"{a.mode} inner_tol {itol:g}: {res.iterations} iterations, {res.outer_iterations} outer, "
-                  f"rel residual {res.rel_residual:.3e}, {time.perf_counter() - t0:.3f} s")
+    for mode in a.mode:
+        for itol in a.inner_tol if mode != "fp64" else [0.0]:
+            for _ in range(a.solves):
+                t0 = time.perf_counter()
+                _, res = w["system"].solve(1.0, w["b"], x, tol=1e-10, mode=mode, inner_tol=itol or 1e-2)
+                print(f"{mode} inner_tol {itol:g}: {res.iterations} iterations, {res.outer_iterations} outer, "
+                      f"rel residual {res.rel_residual:.3e}, {time.perf_counter() - t0:.3f} s")
 
 
 if __name__ == "__main__":

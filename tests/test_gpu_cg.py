@@ -93,6 +93,20 @@ def test_mixed_reaches_fp64_residual(ctx, lam):
     assert rel_err(x[amap.ndir:], xo[amap.ndir:]) < 1e-8
 
 
+@pytest.mark.parametrize("inner_tol", [1e-1, 1e-2, 1e-4])
+def test_mixed_curved_hex_inner_tolerances(ctx, inner_tol):
+    """Mixed refinement on a curved hex mesh for loose and tight inner tolerances: the
+    FP64 residual is reached and the solution agrees with the FP64 solve."""
+    c = hex_case(4, 4, 3, 5)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(5).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, r64 = sys_.solve(1.0, rhs, tol=1e-12)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed", inner_tol=inner_tol)
+    assert res.rel_residual < 1e-10
+    assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
+
+
 def test_helmsolve_matches_analytic(ctx):
     c = quad_case(8, 8, 7, jitter=0.1, seed=0)
     coll, amap, sys_ = _system(ctx, c)
