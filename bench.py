@@ -9,6 +9,7 @@ Jacobi-preconditioned CG solve of the assembled C0 system to an FP64 relative re
 Inputs are synthetic and seeded; no dataset is involved.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--order P] [--mesh M]
+  python bench.py --config quad2d|mixed2d|batched|pod|adjoint|all   (secondary workloads)
 
 `--impl reference` times the reference path's CPU implementation on the host cores
 (the compiled C++ port of the reference kernels and CG recurrence, oracle/cport).
@@ -106,6 +107,21 @@ def build_workload(mesh_n, order):
     return mesh, n, Q, X, amap, f
 
 
+def fp32_kernel_name(variant, n, Q):
+    """Name of the FP32 hex Helmholtz kernel an autotuner variant launches."""
+    if variant == 0:
+        return f"helm_kernel<float,3,{n},{Q}>"
+    if variant in (2, 4):
+        return f"helm3_pencil_kernel<float,{n},{Q},{variant}>"
+    return f"helm3_pipe_kernel<float,{n},{Q},{variant % 10},gather,{2 if variant // 10 == 2 else 1}>"
+
+
+# DRAM bytes (read + write) per element of one gathered FP32 apply, from the ncu capture
+# of the same kernel on 24^3 hexes (profiles/helm3_pipe_fp32_hex_p6_mesh24.md); the
+# traffic of a launch grows with the number of elements, so the bench scales it by E.
+TRAFFIC_PER_ELEMENT = {}
+
+
 def workload_config(args, n, Q, E, N, ndir):
     return {"workload": f"3-D Helmholtz, {args.mesh}^3 curved hexes, P={args.order} (n={n}, Q={Q}), "
                         f"lambda={LAMBDA}, Jacobi PCG to {TOL:g} rel. residual",
@@ -161,8 +177,9 @@ def run_gpu(args, rank, world):
     coll32 = Collection(ctx, "hex", n, Q, E, jac, df, deformed=True, precision="fp32")
     sysg = GlobalLinSysIterativeFullGPU(coll, amap)
     stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
-    # pick the FP32 element-kernel variant by timing (CollectionOptimisation analogue)
-    variant, variant_ms = coll.autotune(reps=5)
+    # pick the FP32 element-kernel variant by timing the solver's own gathered inner
+    # apply (CollectionOptimisation analogue)
+    variant, variant_ms = sysg.autotune_inner(LAMBDA, reps=10)
     coll32.set_variant(variant)
 
     # b = Assemble(-IProductWRTBase(f)) on the device (ContField::v_HelmSolve)
@@ -270,7 +287,9 @@ def run_gpu(args, rank, world):
         "helmholtz_gdofs": {"fp64": gdofs64, "fp32": gdofs32},
         "solver_gdofs": {"mixed": value / world * (N - ndir) / 1e9, "fp64": fp64_solves * (N - ndir) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": ("helm3_pencil_kernel<float,7,8>" if variant else "helm_kernel<float,3,7,8>") + " gather (inner FP32 apply)",
+                     "traffic": (TRAFFIC_PER_ELEMENT[(variant, n, Q)] * E
+                                 if (variant, n, Q) in TRAFFIC_PER_ELEMENT else None),
+                     "kernel": fp32_kernel_name(variant, n, Q) + " gather (inner FP32 apply)",
                      "kernel_ms": k_ms, "bytes_per_launch": k_bytes, "peak_source": peak_kind},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_host.nbytes),
                 "d2h_bytes_per_step": int(out_host.nbytes), "rel_residual": rese.rel_residual},
@@ -357,6 +376,233 @@ def run_reference(args, rank, world):
 REF_ITERATIONS = {(32, 6): 961}
 
 
+# ---------------------------------------------------------------------------------
+# Secondary workloads (--config): one JSON line each, same timing rules (warm-up, CUDA
+# events on the library stream, host-side timing where the call includes host copies).
+# ---------------------------------------------------------------------------------
+def _events(torch, stream):
+    a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    return a, z
+
+
+def _time_device(torch, stream, fn, reps, warmup=3):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, z = _events(torch, stream)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    z.record(stream)
+    z.synchronize()
+    return a.elapsed_time(z) / reps  # ms
+
+
+def _time_host(fn, reps, warmup=1):
+    for _ in range(warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = fn()
+    return (time.perf_counter() - t0) / reps * 1e3, out  # ms
+
+
+def _line(metric, value, unit, args, cfg, higher=True, **extra):
+    d = {"metric": metric, "value": value, "unit": unit, "impl": "gpu", "n_gpus": 1, "steps": args.steps,
+         "warmup": args.warmup, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None,
+         "data": "synthetic (seeded)", "config": cfg}
+    d.update(extra)
+    print(json.dumps(d))
+
+
+def suite_quad2d(args):
+    """32 x 32 jittered quads, P = 6: the four operators (GDOF/s, FP64) and Jacobi PCG
+    to 1e-12 (FP64 and mixed)."""
+    import torch
+    from ithaca_gpu.workload import quad_workload
+    w = quad_workload(32, 6)
+    ctx, coll, sysg, amap = w["ctx"], w["coll"], w["system"], w["amap"]
+    E, n, Q, N, ndir = w["mesh"].E, w["n"], w["Q"], amap.nglobal, amap.ndir
+    stream = torch.cuda.ExternalStream(ctx.stream, device="cuda:0")
+    u = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, E * n * n)).cuda()
+    phys = torch.empty(E * Q * Q, dtype=torch.float64, device="cuda")
+    coef = torch.empty_like(u)
+    d0, d1 = torch.empty_like(phys), torch.empty_like(phys)
+    coll.bwdtrans(u, phys)
+    reps = 200
+    ops = {"bwdtrans": lambda: coll.bwdtrans(u, phys), "iproduct": lambda: coll.iproduct(phys, coef),
+           "physderiv": lambda: coll.physderiv(phys, [d0, d1]),
+           "helmholtz": lambda: coll.helmholtz(1.0, u, coef)}
+    gdofs = {k: E * n * n / (_time_device(torch, stream, f, reps) / 1e3) / 1e9 for k, f in ops.items()}
+    b = torch.from_numpy(w["b"]).cuda()
+    x = torch.zeros_like(b)
+    out = {}
+    for mode in ("fp64", "mixed"):
+        _, res = sysg.solve(1.0, b, x, tol=1e-12, mode=mode)
+        ms = _time_device(torch, stream, lambda: sysg.solve(1.0, b, x, tol=1e-12, mode=mode), args.steps, 1)
+        _, res = sysg.solve(1.0, b, x, tol=1e-12, mode=mode)
+        out[mode] = {"solves_per_s": 1e3 / ms, "ms": ms, "iterations": res.iterations,
+                     "rel_residual": res.rel_residual}
+    cfg = {"workload": "2-D Helmholtz, 32x32 jittered quads (0.1 h), P=6 (n=7, Q=8), lambda=1, Jacobi PCG to 1e-12",
+           "elements": E, "global_dofs": N, "solve_dofs": N - ndir,
+           "l2": "working set (~3 MB) is L2-resident: latency-bound, not an HBM roofline case"}
+    cpu = None
+    try:
+        from oracle import cportbind
+        if cportbind.available():
+            diag = sysg.diagonal(1.0)
+            nth = os.cpu_count() or 1
+            run = lambda: cportbind.cg_solve(2, n, Q, E, w["jac"], w["df"], True, 1.0, amap.l2g, amap.sign, N, ndir,
+                                             1.0 / diag, w["b"], 1e-12, 5000, nth)
+            ms_c, res_c = _time_host(run, 3)
+            cpu = {"value": 1e3 / ms_c, "unit": "solves/s", "cores": nth, "kind": "port",
+                   "sample": f"3 full FP64 solves ({res_c[1]} iterations)"}
+    except Exception as ex:
+        cpu = {"value": None, "error": str(ex)[:200]}
+    _line("config 1: 2-D Helmholtz CG solves/s (FP64, 1e-12) and operator GDOF/s", out["fp64"]["solves_per_s"],
+          "solves/s", args, cfg, dtype="f64", helmholtz_gdofs_fp64=gdofs, solve=out, cpu_baseline=cpu)
+
+
+def suite_mixed2d(args):
+    """Config-1 mesh at P = 6 and 8, lambda in {0.1, 1, 10}: FP64 vs mixed (FP32 inner)
+    solves to 1e-10."""
+    import torch
+    from ithaca_gpu.workload import quad_workload
+    rows = []
+    for P in (6, 8):
+        w = quad_workload(32, P)
+        sysg, ctx = w["system"], w["ctx"]
+        stream = torch.cuda.ExternalStream(ctx.stream, device="cuda:0")
+        b = torch.from_numpy(w["b"]).cuda()
+        x = torch.zeros_like(b)
+        for lam in (0.1, 1.0, 10.0):
+            row = {"P": P, "lambda": lam}
+            for mode in ("fp64", "mixed"):
+                ms = _time_device(torch, stream, lambda: sysg.solve(lam, b, x, tol=1e-10, mode=mode), args.steps, 1)
+                _, res = sysg.solve(lam, b, x, tol=1e-10, mode=mode)
+                row[mode] = {"solves_per_s": 1e3 / ms, "iterations": res.iterations,
+                             "outer": res.outer_iterations, "rel_residual": res.rel_residual}
+            row["speedup"] = row["mixed"]["solves_per_s"] / row["fp64"]["solves_per_s"]
+            rows.append(row)
+    head = [r for r in rows if r["P"] == 6 and r["lambda"] == 1.0][0]
+    cfg = {"workload": "2-D Helmholtz, 32x32 jittered quads, P in {6, 8}, lambda in {0.1, 1, 10}, "
+                       "FP32 inner PCG in FP64 refinement to 1e-10", "l2": "L2-resident (latency-bound)"}
+    _line("config 3: mixed-precision solves/s (P=6, lambda=1; all cases in 'cases')",
+          head["mixed"]["solves_per_s"], "solves/s", args, cfg, dtype="f64 (outer) / f32 (inner)", cases=rows)
+
+
+def suite_batched(args):
+    """256 parametric solves (lambda log-uniform, E ~ U{500..8000}, P ~ U{3..9}) in one
+    batch, FP64 and mixed."""
+    from ithaca_gpu.batched import BatchedHelmholtz, parametric_quad_problems
+    from ithaca_gpu.operators import Context
+    ctx = Context(0)
+    t0 = time.perf_counter()
+    probs = parametric_quad_problems(ctx, nsolve=256)
+    setup_s = time.perf_counter() - t0
+    bt = BatchedHelmholtz(ctx, "quad", probs)
+    out = {}
+    for mode in ("fp64", "mixed"):
+        bt.solve(mode=mode, tol=1e-10, want_x=False)  # warm-up (graph capture)
+        ms, res = _time_host(lambda: bt.solve(mode=mode, tol=1e-10, want_x=False), 1, 0)
+        it = res["iterations"]
+        out[mode] = {"solves_per_s": 256 / (ms / 1e3), "batch_ms": ms, "device_ms": res["elapsed_ms"],
+                     "iterations": {"min": int(it.min()), "median": float(np.median(it)), "max": int(it.max())},
+                     "max_rel_residual": float(res["rel_residual"].max())}
+    ndof = int(sum(p["amap"].nglobal - p["amap"].ndir for p in probs))
+    cfg = {"workload": "256 2-D Helmholtz solves, lambda = 10^U(-2,2), E ~ U{500..8000} jittered quads, "
+                       "P ~ U{3..9}, Q = P+2, tol 1e-10, one graph-captured batch",
+           "solve_dofs_total": ndof, "host_setup_s": setup_s}
+    _line("config 4: batched parametric solves/s (256 solves, mixed)", out["mixed"]["solves_per_s"], "solves/s", args,
+          cfg, dtype="f64 (outer) / f32 (inner)", batch=out,
+          speedup_mixed_vs_fp64=out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"])
+
+
+def suite_pod(args):
+    """POD on the config-1 FOM (32x32 quads, P=6): 256 lambda snapshots (one batch), 50
+    modes by the method of snapshots, reduced operators, 4096 online FP64 LU solves."""
+    import torch
+    from ithaca_gpu import pod
+    from ithaca_gpu.batched import BatchedHelmholtz
+    from ithaca_gpu.workload import quad_workload
+    w = quad_workload(32, 6)
+    ctx, sysg, amap = w["ctx"], w["system"], w["amap"]
+    ndir = amap.ndir
+    lams = 10 ** np.random.default_rng(4).uniform(-2, 2, 256)
+    probs = [dict(nmodes=w["n"], npoints=w["Q"], jac=w["jac"], df=w["df"], amap=amap, lam=float(l), rhs=w["b"])
+             for l in lams]
+    bt = BatchedHelmholtz(ctx, "quad", probs)
+    snap_ms, res = _time_host(lambda: bt.solve(mode="fp64", tol=1e-10), 1, 1)
+    S = np.stack([x[ndir:] for x in res["x"]], axis=1)
+    off_ms, (V, sigma, r) = _time_host(lambda: pod.offline(ctx, S, 50), args.steps)
+    proj_ms, (A_L, A_M) = _time_host(lambda: pod.project(sysg, V), args.steps)
+    f_r = V.T @ w["b"][ndir:]
+    new = 10 ** np.random.default_rng(5).uniform(-2, 2, 4096)
+    on_ms, X = _time_host(lambda: pod.online(ctx, A_L, A_M, f_r, new), args.steps)
+    rec_ms, U = _time_host(lambda: pod.reconstruct(ctx, V, X[:256]), args.steps)
+    errs = []
+    for j in range(8):
+        xf, _ = sysg.solve(float(new[j]), w["b"], tol=1e-12)
+        errs.append(float(np.max(np.abs(U[j] - xf[ndir:])) / np.max(np.abs(xf))))
+    cpu = None
+    try:
+        from oracle import pod as opod
+        t0 = time.perf_counter()
+        opod.pod_svd(S, nmodes=50)
+        svd_ms = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        opod.online_lu(A_L, A_M, f_r, new[:512])
+        lu_ms = (time.perf_counter() - t0) * 1e3 * 4096 / 512
+        cpu = {"value": 4096 / (lu_ms / 1e3), "unit": "online solves/s", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": f"numpy LU on 512 of the 4096 lambdas (scaled); thin SVD of S took "
+                                         f"{svd_ms:.0f} ms"}
+    except Exception as ex:
+        cpu = {"value": None, "error": str(ex)[:200]}
+    cfg = {"workload": "POD of 256 FP64 snapshots (lambda = 10^U(-2,2)) of 32x32 quads P=6, 50 modes, "
+                       "4096 online lambdas, 50x50 FP64 LU", "snapshot_rows": int(S.shape[0]), "modes": r}
+    _line("POD: online reduced solves/s (4096 lambdas, 50 modes)", 4096 / (on_ms / 1e3), "online solves/s", args,
+          cfg, dtype="f64", ms={"snapshots_batch": snap_ms, "offline": off_ms, "project": proj_ms,
+                                "online_4096": on_ms, "reconstruct_256": rec_ms},
+          rom_vs_fom_max_rel_err=max(errs), sigma_ratio_50=float(sigma[49] / sigma[0]) if r >= 50 else None,
+          cpu_baseline=cpu)
+
+
+def suite_adjoint(args):
+    """64 x 64 quads, P = 6, FP64: J(kappa) and dJ/dkappa by the adjoint (forward solve,
+    adjoint solve, gradient kernel) through torch.autograd."""
+    import torch
+    from ithaca_gpu.adjoint import misfit
+    from ithaca_gpu.workload import quad_workload, smooth_field
+    w = quad_workload(64, 6)
+    ctx, sysg, coll, amap = w["ctx"], w["system"], w["coll"], w["amap"]
+    X = w["X"]
+    kappa = torch.from_numpy((1 + 0.5 * smooth_field(X, 6)).reshape(-1)).cuda()
+    kt = torch.from_numpy((1 + 0.5 * smooth_field(X, 7)).reshape(-1)).cuda()
+    b = torch.from_numpy(w["b"]).cuda()
+    sysg.set_varcoeff(kt)
+    xt = torch.zeros_like(b)
+    sysg.solve(1.0, b, xt, tol=1e-13)
+    xt[:amap.ndir] = 0
+    ut = coll.bwdtrans(sysg.global_to_local(xt))
+
+    def grad():
+        k = kappa.clone().requires_grad_(True)
+        J = misfit(k, sysg, 1.0, b, ut, 1e-12)
+        J.backward()
+        return J.item(), k.grad
+
+    ms, (J, g) = _time_host(grad, args.steps, 1)
+    cfg = {"workload": "variable-coefficient Helmholtz, 64x64 jittered quads, P=6, kappa = 1 + 0.5 g (8 seeded "
+                       "Fourier modes), J = sum Jw (u - u_t)^2, adjoint gradient, FP64 CG to 1e-12",
+           "quadrature_points": int(kappa.numel())}
+    _line("config 5: adjoint gradients/s (forward + adjoint solve + dJ/dkappa)", 1e3 / ms, "gradients/s", args, cfg,
+          dtype="f64", J=J, grad_max=float(g.abs().max()))
+
+
+SUITES = {"quad2d": suite_quad2d, "mixed2d": suite_mixed2d, "batched": suite_batched, "pod": suite_pod,
+          "adjoint": suite_adjoint}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,9 +611,17 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--order", type=int, default=6)
     ap.add_argument("--mesh", type=int, default=32)
+    ap.add_argument("--config", choices=["hex"] + list(SUITES) + ["all"], default="hex",
+                    help="hex: the headline workload (default); the others: secondary workloads, one line each")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.config != "hex" and args.impl == "gpu":
+        sys.path.insert(0, os.path.join(ROOT, "ithaca-sem_gb300"))
+        for name, fn in SUITES.items():
+            if args.config in (name, "all") and rank == 0:
+                fn(args)
+        return None
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_gpu(args, rank, world)

@@ -430,8 +430,9 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant) {
   return guarded([&] {
     require(op != nullptr, "null argument");
-    require(variant == 0 || variant == 2 || variant == 4 || variant == 21 || variant == 22,
-            "variant must be 0, 2, 4, 21 or 22");
+    require(variant == 0 || variant == 2 || variant == 4 || variant == 21 || variant == 22 || variant == 31 ||
+                variant == 32,
+            "variant must be 0, 2, 4, 21, 22, 31 or 32");
     op->variant32 = variant;
   });
 }
@@ -470,10 +471,10 @@ int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* tim
     ITHACA_CUDA(cudaMalloc(&x, sizeof(float) * nm));
     ITHACA_CUDA(cudaMalloc(&y, sizeof(float) * nm));
     ITHACA_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * nm, s));
-    const int variants[5] = {0, 2, 4, 21, 22};
+    const int variants[7] = {0, 2, 4, 21, 22, 31, 32};
     double best = 1e300;
     int best_v = 0;
-    for (int vi = 0; vi < 5; ++vi) {
+    for (int vi = 0; vi < 7; ++vi) {
       const int v = variants[vi];
       double ms_avg = -1;
       if (v == 0 || (op->dim == 3 && op->deformed)) {

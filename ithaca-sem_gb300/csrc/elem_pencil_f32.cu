@@ -25,14 +25,14 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 
 // Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
 // occupancy calculator), never more CTAs than element groups.
-template <typename T, int N, int Q, int EB>
+template <typename T, int N, int Q, int EB, int NB>
 static void pipe_nq(int E, const double* hB, const double* hD, const T* jg, T lambda, const T* in, T* out,
                     const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s) {
   PTabs<T, N, Q> tab;
   for (int i = 0; i < N * Q; ++i) tab.B[i] = (T)hB[i];
   for (int i = 0; i < Q * Q; ++i) tab.D[i] = (T)hD[i];
-  using L = PipeLayout<T, N, Q, EB>;
-  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true> : helm3_pipe_kernel<T, N, Q, EB, false>;
+  using L = PipeLayout<T, N, Q, EB, NB>;
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB> : helm3_pipe_kernel<T, N, Q, EB, false, NB>;
   static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
   const int gi = l2g ? 1 : 0;
   if (slots[gi] == 0) {
@@ -52,7 +52,7 @@ static void pipe_nq(int E, const double* hB, const double* hD, const T* jg, T la
 
 // variant: 2 or 4 = one pass per CTA with a TMA-staged geometry slab and that many
 // elements per CTA; 21 or 22 = the persistent pipelined kernel with 1 or 2 elements per
-// group.
+// group and a double geometry buffer; 31 or 32 = the same with a single buffer.
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
@@ -64,9 +64,13 @@ bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, cons
     else if (variant == 2)                                                                                 \
       dev::pencil_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);      \
     else if (variant == 21)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);        \
+      dev::pipe_nq<T, NN, QQ, 1, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
     else if (variant == 22)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);        \
+      dev::pipe_nq<T, NN, QQ, 2, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+    else if (variant == 31)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 1, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+    else if (variant == 32)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 2, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
     else                                                                                                   \
       return false;                                                                                        \
     return true;                                                                                           \

@@ -3,8 +3,10 @@
 //
 // One CTA per resident slot loops over groups of EB elements (group, group + gridDim.x,
 // ...). While it computes group i it already has in flight
-//   * the TMA copy of group i+1's geometry slab into the other half of a double buffer
-//     (issued at the top of iteration i, waited for at the metric stage of i+1), and
+//   * the TMA copy of group i+1's geometry slab: with NB = 2 into the other half of a
+//     double buffer (issued at the top of iteration i); with NB = 1 into the single
+//     buffer as soon as group i's metric stage has read it (half the shared memory, so
+//     about twice the resident CTAs, for a shorter lead); and
 //   * the gather of group i+1's input coefficients into registers: the signed l2g codes
 //     are loaded right after stage 1 of group i and the dependent x loads are issued
 //     after stage 5, so both latencies hide behind group i's arithmetic; the values are
@@ -18,21 +20,22 @@
 namespace ithaca {
 namespace dev {
 
-template <typename T, int N, int Q, int EB>
+template <typename T, int N, int Q, int EB, int NB>
 struct PipeLayout {
   static constexpr int NQ = Q * Q * Q, GEO = 7 * NQ;
   static constexpr int PJ = Q, PK = pk_stride(Q), FS = PK * Q;
   static constexpr size_t GEO_BYTES = ((size_t)EB * GEO * sizeof(T) + 32 + 15) / 16 * 16;  // + window slack
-  static constexpr size_t bytes() { return 16 + 2 * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
+  static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
-template <typename T, int N, int Q, int EB, bool GATHER>
+template <typename T, int N, int Q, int EB, bool GATHER, int NB>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                                const PTabs<T, N, Q> tab, const T* __restrict__ jg,
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
                                                                const T* __restrict__ lam_ptr, int* __restrict__ err) {
-  using L = PipeLayout<T, N, Q, EB>;
+  static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
+  using L = PipeLayout<T, N, Q, EB, NB>;
   constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
   constexpr int PJ = L::PJ, PK = L::PK, FS = L::FS;
   constexpr int NPT = (NM + TPE - 1) / TPE;  // coefficients gathered per thread
@@ -40,9 +43,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   if (lam_ptr != nullptr) lambda = *lam_ptr;
 
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // bar[0], bar[1]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // bar[0] (and bar[1] with NB = 2)
   unsigned char* geo_base = smem + 16;
-  T* work = reinterpret_cast<T*>(smem + 16 + 2 * L::GEO_BYTES);
+  T* work = reinterpret_cast<T*>(smem + 16 + NB * L::GEO_BYTES);
 
   const int t = threadIdx.x, el = threadIdx.y;
   const int tid = t + el * TPE;
@@ -106,7 +109,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   if (grp >= ngroups) return;
   if (tid == 0) {
     mbar_init(bar, 1);
-    mbar_init(bar + 1, 1);
+    if (NB == 2) mbar_init(bar + 1, 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -115,14 +118,14 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   load_values(grp);
 
   for (int it = 0; grp < ngroups; ++it, grp += gridDim.x) {
-    const int b = it & 1;
-    const uint32_t parity = (it >> 1) & 1;
+    const int b = NB == 2 ? (it & 1) : 0;
+    const uint32_t parity = NB == 2 ? ((it >> 1) & 1) : (it & 1);
     const int nxt = grp + gridDim.x;
     const bool has_next = nxt < ngroups;
     const int e = grp * EB + el;
     const bool active = e < E;
     // the other buffer was last read in the previous iteration, which ended in a barrier
-    if (tid == 0 && has_next) issue_geometry(nxt, b ^ 1);
+    if (NB == 2 && tid == 0 && has_next) issue_geometry(nxt, b ^ 1);
 
     // ---- 1: prefetched coefficients -> S0 as (p, q, r); then the next group's codes ----
 #pragma unroll
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       if (tid == 0 && err != nullptr) atomicExch(err, ITHACA_GPU_ERR_TIMEOUT);
       // give the copies in flight time to finish before the CTA's shared memory goes away
       mbar_wait_bounded(bar + b, parity, kWaitCycles);
-      if (has_next) mbar_wait_bounded(bar + (b ^ 1), ((it + 1) >> 1) & 1, kWaitCycles);
+      if (NB == 2 && has_next) mbar_wait_bounded(bar + (b ^ 1), ((it + 1) >> 1) & 1, kWaitCycles);
       return;
     }
     const T* G = geometry_of(grp, b);
@@ -252,6 +255,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       }
     }
     __syncthreads();
+    // single buffer: stage 6 has read it, so the next group's copy can start now
+    if (NB == 1 && tid == 0 && has_next) issue_geometry(nxt, 0);
     // ---- 7: D^T along i on pencils (j, k) in S0, along j on pencils (i, k) in S1 ----
     {
       const int pj = t % Q, pk = t / Q;
@@ -333,8 +338,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         out[(size_t)e * NM + m] = S1[p + PJ * q + PK * r];
       }
     }
-    // S0 and S1 are rewritten by the next group's stages 1-2, and the geometry buffer
-    // read here is refilled by the copy issued at the top of the iteration after next
+    // S0 and S1 are rewritten by the next group's stages 1-2; with NB = 2 the geometry
+    // buffer read here is refilled by the copy issued at the top of the iteration after next
     __syncthreads();
   }
 }

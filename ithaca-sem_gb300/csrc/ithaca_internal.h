@@ -109,7 +109,8 @@ struct Op {
   std::vector<double> hB, hD;  // host copies of B[p*Q+i] and D[k*Q+i] (kernel-parameter tables)
   // Helmholtz kernel variant for FP32 hexahedra: 0 = shared-memory kernel (elem.cuh),
   // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA and a
-  // TMA-staged geometry slab, 21 or 22 = persistent pipelined pencil kernel (elem_pencil_pipe.cuh).
+  // TMA-staged geometry slab, 21/22 (31/32) = persistent pipelined pencil kernel with a
+  // double (single) geometry buffer (elem_pencil_pipe.cuh).
   int variant32 = 4;
   ~Op();
 };

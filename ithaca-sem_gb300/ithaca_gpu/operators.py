@@ -43,6 +43,24 @@ def _ptr(a, dtype=None):
     return ctypes.c_void_p(a.ctypes.data), 0
 
 
+def _like(ref, size, dtype=np.float64):
+    """A zeroed output buffer on the same side as `ref`: a CUDA tensor (same device)
+    for a CUDA input, else a numpy array. One call passes one on_device flag for all
+    its pointers, so outputs must live where the inputs live."""
+    if _is_device(ref):
+        import torch
+        tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+        return torch.zeros(size, dtype=tdt, device=ref.device)
+    return np.zeros(size, dtype=dtype)
+
+
+def _same_side(*arrays):
+    """Rejects a call that mixes host arrays and CUDA tensors."""
+    kinds = {_is_device(a) for a in arrays if a is not None}
+    if len(kinds) > 1:
+        raise ValueError("the arrays of one call must be all host numpy arrays or all CUDA tensors")
+
+
 class Context:
     def __init__(self, device=0):
         h = ctypes.c_void_p()
@@ -134,34 +152,36 @@ class Collection:
         C.call("ithaca_gpu_op_ndof", self.handle, ctypes.byref(n))
         return n.value
 
-    def _out(self, a, size):
+    def _out(self, a, size, ref=None):
         if a is not None:
+            _same_side(a, ref)
             return a
-        return np.zeros(size, dtype=self.dtype)
+        return _like(ref, size, self.dtype)
 
     def bwdtrans(self, inp, out=None):
-        out = self._out(out, self.E * self.nq)
+        out = self._out(out, self.E * self.nq, inp)
         pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
         po, _ = _ptr(out)
         C.call("ithaca_gpu_bwdtrans", self.handle, pi, po, d)
         return out
 
     def iproduct(self, inp, out=None):
-        out = self._out(out, self.E * self.nm)
+        out = self._out(out, self.E * self.nm, inp)
         pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
         po, _ = _ptr(out)
         C.call("ithaca_gpu_iproduct", self.handle, pi, po, d)
         return out
 
     def physderiv(self, inp, outs=None):
-        outs = outs or [self._out(None, self.E * self.nq) for _ in range(self.dim)]
+        outs = outs or [self._out(None, self.E * self.nq, inp) for _ in range(self.dim)]
+        _same_side(inp, *outs)
         pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
         ps = [_ptr(o)[0] for o in outs] + [None] * (3 - len(outs))
         C.call("ithaca_gpu_physderiv", self.handle, pi, ps[0], ps[1], ps[2], d)
         return outs
 
     def helmholtz(self, lam, inp, out=None):
-        out = self._out(out, self.E * self.nm)
+        out = self._out(out, self.E * self.nm, inp)
         pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
         po, _ = _ptr(out)
         C.call("ithaca_gpu_helmholtz", self.handle, ctypes.c_double(lam), pi, po, d)
@@ -169,13 +189,14 @@ class Collection:
 
     def set_variant(self, variant):
         """FP32 hex Helmholtz kernel: 0 shared-memory, 2/4 register-pencil with TMA-staged
-        geometry (elements per CTA), 21/22 persistent pipelined pencil (1/2 elements per group)."""
+        geometry (elements per CTA), 21/22 persistent pipelined pencil (1/2 elements per group,
+        double geometry buffer), 31/32 the same with a single geometry buffer."""
         C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
 
     def autotune(self, reps=10):
         """Times each kernel variant on this collection and keeps the fastest."""
         chosen = ctypes.c_int()
-        variants = (0, 2, 4, 21, 22)
+        variants = (0, 2, 4, 21, 22, 31, 32)
         times = np.zeros(len(variants))
         C.call("ithaca_gpu_op_autotune", self.handle, int(reps), ctypes.byref(chosen),
                ctypes.c_void_p(times.ctypes.data))
@@ -222,7 +243,8 @@ class GlobalLinSysIterativeFullGPU:
         return o
 
     def solve(self, lam, rhs, x=None, **kw):
-        x = x if x is not None else np.zeros(self.amap.nglobal)
+        x = x if x is not None else _like(rhs, self.amap.nglobal)
+        _same_side(rhs, x)
         res = C.CgResult()
         o = self.options(**kw)
         pr, d = _ptr(rhs, np.float64 if not _is_device(rhs) else None)
@@ -231,7 +253,8 @@ class GlobalLinSysIterativeFullGPU:
         return x, res
 
     def apply(self, lam, x, y=None):
-        y = y if y is not None else np.zeros(self.amap.nglobal)
+        y = y if y is not None else _like(x, self.amap.nglobal)
+        _same_side(x, y)
         px, d = _ptr(x, np.float64 if not _is_device(x) else None)
         py, _ = _ptr(y)
         C.call("ithaca_gpu_cg_apply", self.handle, ctypes.c_double(lam), px, py, d)
@@ -239,7 +262,8 @@ class GlobalLinSysIterativeFullGPU:
 
     def assemble(self, loc, out=None):
         """AssemblyMapCG::Assemble on the GPU (local E*n^d -> global nglobal)."""
-        out = out if out is not None else np.zeros(self.amap.nglobal)
+        out = out if out is not None else _like(loc, self.amap.nglobal)
+        _same_side(loc, out)
         pl, d = _ptr(loc, np.float64 if not _is_device(loc) else None)
         po, _ = _ptr(out)
         C.call("ithaca_gpu_cg_assemble", self.handle, pl, po, d)
@@ -247,7 +271,8 @@ class GlobalLinSysIterativeFullGPU:
 
     def global_to_local(self, glob, out=None):
         """AssemblyMapCG::GlobalToLocal on the GPU (global -> local E*n^d)."""
-        out = out if out is not None else np.zeros(self.coll.E * self.coll.nm)
+        out = out if out is not None else _like(glob, self.coll.E * self.coll.nm)
+        _same_side(glob, out)
         pg, d = _ptr(glob, np.float64 if not _is_device(glob) else None)
         po, _ = _ptr(out)
         C.call("ithaca_gpu_cg_global_to_local", self.handle, pg, po, d)
@@ -265,7 +290,8 @@ class GlobalLinSysIterativeFullGPU:
         """J = sum Jw (u - u_target)^2 at the points and dJ/dx (global)."""
         dev = _is_device(x)
         if J is None:
-            J = np.zeros(1)
+            J = _like(x, 1)
+        _same_side(x, u_target, J, dJdx)
         px, d = _ptr(x, None if dev else np.float64)
         pt, _ = _ptr(u_target)
         pj, _ = _ptr(J)
@@ -274,7 +300,8 @@ class GlobalLinSysIterativeFullGPU:
         return J, dJdx
 
     def kappa_gradient(self, x, psi, grad=None):
-        grad = grad if grad is not None else np.zeros(self.coll.E * self.coll.nq)
+        grad = grad if grad is not None else _like(x, self.coll.E * self.coll.nq)
+        _same_side(x, psi, grad)
         px, d = _ptr(x, None if _is_device(x) else np.float64)
         pp, _ = _ptr(psi)
         pg, _ = _ptr(grad)
@@ -290,6 +317,19 @@ class GlobalLinSysIterativeFullGPU:
                ctypes.byref(ms), ctypes.byref(nbytes))
         return ms.value, nbytes.value
 
+    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32), reps=10):
+        """Times the gathered FP32 apply of the mixed solver's inner iteration with each
+        FP32 kernel variant of the collection and keeps the fastest (the solver-side
+        counterpart of Collection.autotune, which times the ungathered apply).
+        Returns (chosen variant, {variant: ms})."""
+        times = {}
+        for v in variants:
+            self.coll.set_variant(v)
+            times[v] = self.profile_apply(lam, mode="mixed", reps=reps)[0]
+        best = min(times, key=times.get)
+        self.coll.set_variant(best)
+        return best, times
+
     def diagonal(self, lam, out=None):
         out = out if out is not None else np.zeros(self.amap.nglobal - self.amap.ndir)
         po, d = _ptr(out)
@@ -297,7 +337,8 @@ class GlobalLinSysIterativeFullGPU:
         return out
 
     def helmsolve(self, lam, forcing, out=None, **kw):
-        out = out if out is not None else np.zeros(self.coll.E * self.coll.nm)
+        out = out if out is not None else _like(forcing, self.coll.E * self.coll.nm)
+        _same_side(forcing, out)
         res = C.CgResult()
         o = self.options(**kw)
         pf, d = _ptr(forcing, np.float64 if not _is_device(forcing) else None)

@@ -126,12 +126,12 @@ def test_unsupported_order_raises(ctx):
 
 
 @pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 7, 8, 9, 10])
-@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22])
+@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22, 31, 32])
 def test_hex_fp32_kernel_variants(ctx, n, variant):
     """Every FP32 hex Helmholtz kernel variant (shared-memory; register-pencil with a
     TMA-staged geometry slab, one pass with 2 or 4 elements per CTA or persistent and
-    pipelined with 1 or 2 elements per group) against the FP64 oracle; E = 7 leaves a
-    partial last group."""
+    pipelined with 1 or 2 elements per group and one or two geometry buffers) against the
+    FP64 oracle; E = 7 leaves a partial last group."""
     c = hex_case(7, 1, 1, n)
     coll = _coll(ctx, c, "fp32")
     coll.set_variant(variant)
@@ -146,7 +146,7 @@ def test_autotune_picks_a_working_variant(ctx):
     c = hex_case(4, 4, 2, 7)
     coll = _coll(ctx, c, "fp32")
     chosen, times = coll.autotune(reps=3)
-    assert chosen in (0, 2, 4, 21, 22) and all(t > 0 for t in times.values())
+    assert chosen in (0, 2, 4, 21, 22, 31, 32) and all(t > 0 for t in times.values())
     u = np.random.default_rng(3).uniform(-1, 1, c.E * c.nm)
     out = coll.helmholtz(1.0, u.astype(np.float32))
     ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, u)
