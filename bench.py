@@ -199,8 +199,9 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
 
     # ---- headline: mixed-precision solves, inputs resident in HBM ----
+    mode = args.mixed_mode
     for _ in range(args.warmup):
-        _, res = sysg.solve(LAMBDA, b, x, tol=TOL, mode="mixed")
+        _, res = sysg.solve(LAMBDA, b, x, tol=TOL, mode=mode)
     barrier()
     l0 = ctx.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -208,7 +209,7 @@ def run_gpu(args, rank, world):
         ev0.record(stream)
         results = []
         for _ in range(args.steps):
-            _, res = sysg.solve(LAMBDA, b, x, tol=TOL, mode="mixed")
+            _, res = sysg.solve(LAMBDA, b, x, tol=TOL, mode=mode)
             results.append((res.iterations, res.outer_iterations, res.rel_residual))
         ev1.record(stream)
         ev1.synchronize()
@@ -222,8 +223,19 @@ def run_gpu(args, rank, world):
     value = world * args.steps / (ms / 1e3)
     x_mixed = x.clone()
 
+    # the other inner-solve variant, for comparison (not the headline)
+    other = "mixed" if mode == "mixed_geo16" else "mixed_geo16"
+    _, res_o = sysg.solve(LAMBDA, b, x, tol=TOL, mode=other)
+    eo0, eo1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eo0.record(stream)
+    for _ in range(2):
+        _, res_o = sysg.solve(LAMBDA, b, x, tol=TOL, mode=other)
+    eo1.record(stream)
+    eo1.synchronize()
+    other_solves = 2 / (eo0.elapsed_time(eo1) / 1e3)
+
     # ---- dominant kernel: the FP32 gather + element Helmholtz of the inner solve ----
-    k_ms, k_bytes = sysg.profile_apply(LAMBDA, mode="mixed", reps=20)
+    k_ms, k_bytes = sysg.profile_apply(LAMBDA, mode=mode, reps=20)
     peak, peak_kind = load_peaks()
     achieved = k_bytes / (k_ms / 1e3) / 1e9
 
@@ -261,11 +273,11 @@ def run_gpu(args, rank, world):
     # ---- end to end through the public HelmSolve call with host buffers ----
     f_host = np.ascontiguousarray(f)
     out_host = np.zeros(E * n ** 3)
-    sysg.helmsolve(LAMBDA, f_host, out_host, tol=TOL, mode="mixed")
+    sysg.helmsolve(LAMBDA, f_host, out_host, tol=TOL, mode=mode)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, rese = sysg.helmsolve(LAMBDA, f_host, out_host, tol=TOL, mode="mixed")
+        _, rese = sysg.helmsolve(LAMBDA, f_host, out_host, tol=TOL, mode=mode)
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e = world * args.steps / e2e_s
@@ -273,23 +285,28 @@ def run_gpu(args, rank, world):
     if rank != 0:
         return
     cfg = workload_config(args, n, Q, E, N, ndir)
+    tkey = ("geo16" if mode == "mixed_geo16" else variant, n, Q)
     cfg["fp32_kernel_variant"] = variant
     cfg["autotune_ms"] = {str(k): round(v, 4) for k, v in variant_ms.items()}
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (outer) / f32 (inner)", "data": "synthetic (seeded mesh and forcing)",
+        "vs_baseline": None, "dtype": "f64 (outer) / f32 (inner)" + (", 16-bit geometry storage" if mode == "mixed_geo16" else ""),
+        "data": "synthetic (seeded mesh and forcing)",
         "config": cfg,
         "iterations": {"inner": results[-1][0], "outer": results[-1][1], "rel_residual": results[-1][2]},
+        "mixed_mode": mode,
+        "other_mixed_mode": {"mode": other, "solves_per_s": other_solves, "iterations": res_o.iterations,
+                             "outer": res_o.outer_iterations, "rel_residual": res_o.rel_residual},
         "fp64": {"solves_per_s": fp64_solves, "iterations": res64.iterations, "rel_residual": res64.rel_residual,
                  "speedup_mixed_vs_fp64": value / world / fp64_solves, "max_rel_diff_vs_mixed": sol_diff,
                  "apply_ms": k64_ms, "apply_fp64_tflops": None},
         "helmholtz_gdofs": {"fp64": gdofs64, "fp32": gdofs32},
         "solver_gdofs": {"mixed": value / world * (N - ndir) / 1e9, "fp64": fp64_solves * (N - ndir) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (TRAFFIC_PER_ELEMENT[(variant, n, Q)] * E
-                                 if (variant, n, Q) in TRAFFIC_PER_ELEMENT else None),
-                     "kernel": fp32_kernel_name(variant, n, Q) + " gather (inner FP32 apply)",
+                     "traffic": (TRAFFIC_PER_ELEMENT[tkey] * E if tkey in TRAFFIC_PER_ELEMENT else None),
+                     "kernel": (f"helm3_pipe_kernel<float,{n},{Q},1,gather,1,half>" if mode == "mixed_geo16"
+                                else fp32_kernel_name(variant, n, Q)) + " gather (inner FP32 apply)",
                      "kernel_ms": k_ms, "bytes_per_launch": k_bytes, "peak_source": peak_kind},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_host.nbytes),
                 "d2h_bytes_per_step": int(out_host.nbytes), "rel_residual": rese.rel_residual},
@@ -611,6 +628,8 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--order", type=int, default=6)
     ap.add_argument("--mesh", type=int, default=32)
+    ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed_geo16",
+                    help="inner solve of the headline: FP32 on FP32 geometry, or FP32 on 16-bit geometry")
     ap.add_argument("--config", choices=["hex"] + list(SUITES) + ["all"], default="hex",
                     help="hex: the headline workload (default); the others: secondary workloads, one line each")
     args = ap.parse_args()

@@ -50,7 +50,10 @@ enum { ITHACA_GPU_FP64 = 0, ITHACA_GPU_FP32 = 1 };
 /* Solver precision modes for ithaca_gpu_cg_solve. */
 enum {
   ITHACA_GPU_SOLVE_FP64 = 0,        /* reference recurrence, FP64 throughout             */
-  ITHACA_GPU_SOLVE_MIXED_FP32 = 1   /* FP32 inner PCG inside FP64 iterative refinement   */
+  ITHACA_GPU_SOLVE_MIXED_FP32 = 1,  /* FP32 inner PCG inside FP64 iterative refinement   */
+  ITHACA_GPU_SOLVE_MIXED_FP32_GEO16 = 2 /* as MIXED_FP32, with the inner applies reading
+                                         * 16-bit geometry (per-element scaled halves);
+                                         * curved hexahedra only (else ERR_UNSUPPORTED) */
 };
 
 typedef struct ithaca_gpu_ctx ithaca_gpu_ctx;

@@ -75,7 +75,7 @@ def build(force=False, jobs=None, verbose=False, extra=None):
         raise RuntimeError("\n".join(errors))
     objs = [o for o, _ in results]
     if force or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcusolver"]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + p.stdout + p.stderr)

@@ -48,6 +48,7 @@ void Ctx::check_device_error() {
 }
 
 Ctx::~Ctx() {
+  if (solver && solver_free) solver_free(solver);
   for (auto& p : stage)
     if (p) cudaFree(p);
   if (ev_in) cudaEventDestroy(ev_in);

@@ -19,11 +19,13 @@
 #include <memory>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "ithaca_internal.h"
 
 namespace ithaca {
 
-constexpr int RB = 608;      // reduction CTAs (4 per SM)
+constexpr int RB = 760;      // reduction CTAs: 5 per SM of 152 (one wave at <= 51 registers per thread)
 constexpr int RT = 256;      // threads per reduction CTA
 constexpr int NSLOT = 4;     // partial-sum slots: 0 r.w, 1 r.r, 2 b.b, 3 s.w
 
@@ -68,6 +70,30 @@ __device__ __forceinline__ double reduce_slot(const double* partials, int slot) 
   const double r = sm[0];
   __syncthreads();
   return r;
+}
+
+// Several slots at once (same summation order as reduce_slot for each): the loads of
+// all slots are in flight together and the tree steps are shared.
+template <int NS>
+__device__ __forceinline__ void reduce_slots(const double* partials, const int (&slots)[NS], double (&out)[NS]) {
+  __shared__ double sm[NS][RT];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    double s = 0;
+    for (int i = threadIdx.x; i < RB; i += RT) s += __ldcg(partials + slots[k] * RB + i);
+    sm[k][threadIdx.x] = s;
+  }
+  __syncthreads();
+  for (int w = RT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) sm[k][threadIdx.x] += sm[k][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < NS; ++k) out[k] = sm[k][0];
+  __syncthreads();
 }
 
 // ---- PCG vector kernels (T = double or float; reductions in double) ----------
@@ -179,61 +205,105 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
 
 __device__ void scalars_iter_body(const double* partials, CgScalars* sc);
 
-// s[g] = sum_{local l of g} sign_l * yloc[l] for g in [g0, N); partial s.w in slot 3.
-// With fuse_sc != nullptr the last CTA to finish (ticket on `counter`) also runs the
-// loop-tail scalar update, saving one launch per CG iteration; the reduction order of
-// the partial sums does not depend on which CTA that is.
+// ---- assembly plan: rows grouped by their number of local entries ----------------
+// Class c < kAsmK holds the rows with exactly c + 1 local entries, stored ELL-style
+// (entry j of row slot i at cols[col_off + j * n + i], entries in increasing local
+// index, as the reference's scatter-add visits them); class kAsmK holds the rows with
+// more entries, which are read through the CSR arrays. Inside a class the rows are in
+// increasing global order, so the Dirichlet rows (numbered first) lead each class.
+// The CTAs of a launch are split among the classes in proportion to their entries, so
+// every CTA (and warp) handles rows of one length: no divergence, and each thread keeps
+// up to kAsmK independent entry loads in flight.
+constexpr int kAsmK = 8;
+struct AsmPlan {
+  int n[kAsmK + 1];          // rows per class
+  int ndir[kAsmK + 1];       // leading Dirichlet rows per class
+  int rows_off[kAsmK + 1];   // first slot of the class in the row list
+  long long col_off[kAsmK];  // first ELL entry of the class
+  int cta0[kAsmK + 2];       // CTAs [cta0[c], cta0[c + 1]) work on class c
+};
+
+template <typename T, bool SIGNED>
+__device__ __forceinline__ T asm_value(const T* __restrict__ yloc, int c) {
+  if (SIGNED) return c >= 0 ? yloc[c] : -yloc[~c];
+  return yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
+}
+
+template <int K, typename T, bool SIGNED>
+__device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int ncta, bool skip_dir,
+                                          const int* __restrict__ rows, const int* __restrict__ ecols,
+                                          const T* __restrict__ yloc, T* __restrict__ s, const T* __restrict__ w,
+                                          T& sw) {
+  constexpr int U = K >= 8 ? 1 : 8 / K;  // rows per thread step
+  const int n = P.n[c];
+  const int* R = rows + P.rows_off[c];
+  const int* C = ecols + P.col_off[c];
+  const int stride = ncta * RT;
+  for (int i = (skip_dir ? P.ndir[c] : 0) + cta * RT + threadIdx.x; i < n; i += U * stride) {
+    int g[U], idx[U][K];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int ii = i + u * stride;
+      const bool in = ii < n;
+      g[u] = in ? R[ii] : -1;
+#pragma unroll
+      for (int j = 0; j < K; ++j) idx[u][j] = in ? C[(size_t)j * n + ii] : 0;
+    }
+    // second level: every local value and w[g] of the U rows, all loads in flight
+    T val[U][K], wg[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) val[u][j] = g[u] >= 0 ? asm_value<T, SIGNED>(yloc, idx[u][j]) : T(0);
+      wg[u] = (w != nullptr && g[u] >= 0) ? w[g[u]] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (g[u] >= 0) {
+        T acc = val[u][0];
+#pragma unroll
+        for (int j = 1; j < K; ++j) acc += val[u][j];
+        s[g[u]] = acc;
+        sw = fma(acc, wg[u], sw);
+      }
+    }
+  }
+}
+
+// s[g] = sum_{local l of g} sign_l * yloc[l] over all rows (skip_dir: free rows only);
+// partial s.w in slot 3. With fuse_sc != nullptr the last CTA to finish (ticket on
+// `counter`) also runs the loop-tail scalar update, saving one launch per CG iteration;
+// the reduction order of the partial sums does not depend on which CTA that is.
 template <typename T, bool SIGNED = true>
-__global__ void __launch_bounds__(RT) assemble_dot_kernel(int N, int g0, const int* __restrict__ rowptr,
+__global__ void __launch_bounds__(RT, RB / 152) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
+                                                          const int* __restrict__ ecols, const int* __restrict__ rowptr,
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
-                                                          T* __restrict__ s, const T* __restrict__ w,
-                                                          const int* skip, double* partials,
-                                                          CgScalars* fuse_sc = nullptr,
+                                                          T* __restrict__ s, const T* __restrict__ w, const int* skip,
+                                                          double* partials, CgScalars* fuse_sc = nullptr,
                                                           unsigned int* counter = nullptr) {
   if (skip != nullptr && *skip) return;
-  // Four rows per thread step, their loads issued together: a row is a chain of three
-  // dependent loads (row pointer -> local index -> local value), so independent rows
-  // in flight are what keeps the memory system busy. Within a row the entries are
-  // summed in CSR order.
-  constexpr int U = 4;
-  constexpr int STRIDE = RB * RT;
+  int c = 0;
+  while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
+  const int cta = blockIdx.x - P.cta0[c], ncta = P.cta0[c + 1] - P.cta0[c];
   T sw = 0;  // per-thread s.w in T (FP32 sums stay off the slow FP64 pipe); CTA sum in FP64
-  for (int g = g0 + blockIdx.x * RT + threadIdx.x; g < N; g += U * STRIDE) {
-    int a[U], b[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int gg = g + u * STRIDE;
-      a[u] = gg < N ? rowptr[gg] : 0;
-      b[u] = gg < N ? rowptr[gg + 1] : 0;
-    }
-    T acc[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      acc[u] = 0;
-      if (a[u] < b[u]) {  // first entry (every free row has one)
-        const int c = cols[a[u]];
-        if (SIGNED)
-          acc[u] = c >= 0 ? yloc[c] : -yloc[~c];
-        else
-          acc[u] = yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      for (int j = a[u] + 1; j < b[u]; ++j) {
-        const int c = cols[j];
-        if (SIGNED)
-          acc[u] += c >= 0 ? yloc[c] : -yloc[~c];
-        else
-          acc[u] += yloc[c >= 0 ? c : ~c];
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int gg = g + u * STRIDE;
-      if (gg < N) {
-        s[gg] = acc[u];
-        if (w) sw = fma(acc[u], w[gg], sw);
+  switch (c) {
+    case 0: asm_class<1, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 1: asm_class<2, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 2: asm_class<3, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 3: asm_class<4, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 4: asm_class<5, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 5: asm_class<6, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 6: asm_class<7, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 7: asm_class<8, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    default: {  // longer rows: CSR
+      const int n = P.n[kAsmK];
+      const int* R = rows + P.rows_off[kAsmK];
+      for (int i = (skip_dir ? P.ndir[kAsmK] : 0) + cta * RT + threadIdx.x; i < n; i += ncta * RT) {
+        const int g = R[i];
+        T acc = 0;
+        for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) acc += asm_value<T, SIGNED>(yloc, cols[j]);
+        s[g] = acc;
+        if (w) sw = fma(acc, w[g], sw);
       }
     }
   }
@@ -258,8 +328,10 @@ __global__ void __launch_bounds__(RT) assemble_dot_kernel(int N, int g0, const i
 
 // Reference initial step (NekLinSysIterCG.cpp:147-190).
 __global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc) {
-  const double rw = reduce_slot(partials, 0), rr = reduce_slot(partials, 1);
-  const double bb = reduce_slot(partials, 2), sw = reduce_slot(partials, 3);
+  const int slots[4] = {0, 1, 2, 3};
+  double red[4];
+  reduce_slots<4>(partials, slots, red);
+  const double rw = red[0], rr = red[1], bb = red[2], sw = red[3];
   if (threadIdx.x == 0) {
     sc->rhs_mag = sc->mag_override > 0 ? sc->mag_override : (bb > 1e-6 ? bb : 1.0);
     sc->eps = rr;
@@ -293,8 +365,10 @@ __global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials
 
 __device__ void scalars_iter_body(const double* partials, CgScalars* sc) {
   if (sc->done) return;
-  const double rho_new = reduce_slot(partials, 0), eps = reduce_slot(partials, 1);
-  const double mu = reduce_slot(partials, 3);
+  const int slots[3] = {0, 1, 3};
+  double red[3];
+  reduce_slots<3>(partials, slots, red);
+  const double rho_new = red[0], eps = red[1], mu = red[2];
   if (threadIdx.x == 0) {
     sc->eps = eps;
     sc->mu = mu;
@@ -411,11 +485,19 @@ struct Cg {
   size_t nloc = 0;
   int* l2g = nullptr;     // signed-encoded
   int* rowptr = nullptr;  // N + 1
+  AsmPlan plan{};           // assembly by row classes (see AsmPlan)
+  int* asm_rows = nullptr;  // N: global rows, grouped by class
+  int* asm_cols = nullptr;  // ELL entries of the classes with at most kAsmK entries
   int* cols = nullptr;    // nloc, signed-encoded local index
   Vecs<double> v64;
   Vecs<float> v32;
   bool have32 = false;
   float* jg32 = nullptr;   // FP32 copy of the geometry the solver uses
+  // half-precision geometry with per-element, per-field scales (mixed mode with 16-bit
+  // geometry, curved hexahedra); geo16 selects it for the FP32 applies of the solve
+  void* jg16 = nullptr;
+  float* jgs = nullptr;
+  bool have16 = false, geo16 = false, graph32_geo16 = false;
   double* jgk64 = nullptr; // geometry with the metric scaled by a variable coefficient (else op->jg64)
   double* adj_scratch = nullptr;
   double* partials = nullptr;
@@ -434,10 +516,14 @@ Cg::~Cg() {
   if (graph32) cudaGraphExecDestroy(graph32);
   cudaFree(l2g);
   cudaFree(rowptr);
+  cudaFree(asm_rows);
+  cudaFree(asm_cols);
   cudaFree(cols);
   v64.release();
   if (have32) v32.release();
   cudaFree(jg32);
+  cudaFree(jg16);
+  cudaFree(jgs);
   cudaFree(jgk64);
   cudaFree(adj_scratch);
   cudaFree(partials);
@@ -459,7 +545,10 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
   Op* op = cg->op;
   bool ok;
   if constexpr (sizeof(T) == 4) {
-    if (op->dim == 3 && op->deformed && op->variant32 > 0)
+    if (cg->geo16)
+      ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
+                                  v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
+    else if (op->dim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,
                                      xin, v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
     else
@@ -490,7 +579,7 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
     pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
                                            cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg));
-  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, v.yloc, v.s, v.w, skip_ptr(cg),
+  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, skip_ptr(cg),
                                            cg->partials, cg->sc, cg->counter);
   cg->op->ctx->launches += 2;
 }
@@ -527,18 +616,20 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
   pcg_init_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
-  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
+  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
                                            cg->partials);
   scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
   c->launches += 3;
   ITHACA_CUDA(cudaGetLastError());
   cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
   int& len = sizeof(T) == 8 ? cg->graph64_len : cg->graph32_len;
-  if (!ex || len != chunk) {
+  const bool geo_changed = sizeof(T) == 4 && cg->graph32_geo16 != cg->geo16;
+  if (!ex || len != chunk || geo_changed) {
     if (ex) cudaGraphExecDestroy(ex);
     ex = nullptr;
     ex = capture_chunk<T>(cg, v, tab, jg, chunk);
     len = chunk;
+    if (sizeof(T) == 4) cg->graph32_geo16 = cg->geo16;
   }
   // Bounded host loop: at most max_iter / chunk + 2 graph launches.
   const long long max_launches = (long long)max_iter / chunk + 2;
@@ -564,6 +655,49 @@ static void ensure_fp32(Cg* cg) {
   cg->diag_lambda = NAN;  // rebuild so that the FP32 inverse diagonal is filled too
 }
 
+// Half-precision geometry: one CTA per element; for each of the 7 fields the scale is the
+// field's largest magnitude over the element's points and the stored halves are the
+// values divided by it (|half| <= 1, round to nearest).
+__global__ void __launch_bounds__(256) geo16_kernel(int nq, const double* __restrict__ jg, __half* __restrict__ jg16,
+                                                    float* __restrict__ jgs) {
+  __shared__ double red[256 / 32];
+  const int e = blockIdx.x;
+  for (int f = 0; f < 7; ++f) {
+    const double* src = jg + ((size_t)e * 7 + f) * nq;
+    double m = 0;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) m = fmax(m, fabs(src[q]));
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    double mx = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
+    __syncthreads();
+    const double sc = mx > 0 ? mx : 1.0;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) jg16[((size_t)e * 7 + f) * nq + q] = __double2half(src[q] / sc);
+    if (threadIdx.x == 0) jgs[(size_t)e * 8 + f] = (float)sc;
+  }
+  if (threadIdx.x == 0) jgs[(size_t)e * 8 + 7] = 0.f;
+}
+
+static void build_geo16(Cg* cg) {
+  Op* op = cg->op;
+  geo16_kernel<<<op->E, 256, 0, op->ctx->stream>>>(op->nq, geo64(cg), static_cast<__half*>(cg->jg16), cg->jgs);
+  op->ctx->launches++;
+  ITHACA_CUDA(cudaGetLastError());
+}
+
+static void ensure_geo16(Cg* cg) {
+  if (cg->have16) return;
+  Op* op = cg->op;
+  if (!(op->dim == 3 && op->deformed))
+    fail(ITHACA_GPU_ERR_UNSUPPORTED, "16-bit geometry is built for curved (deformed) hexahedra");
+  const size_t njg = (size_t)op->E * 7 * op->nq;
+  ITHACA_CUDA(cudaMalloc(&cg->jg16, sizeof(__half) * njg + kGeoPad));
+  ITHACA_CUDA(cudaMalloc(&cg->jgs, sizeof(float) * 8 * op->E));
+  build_geo16(cg);
+  cg->have16 = true;
+}
+
 // Assembled Jacobi diagonal (sum of element diagonals, sign^2 = 1) and its inverse.
 static void ensure_diag(Cg* cg, double lambda) {
   if (cg->diag_lambda == lambda) return;
@@ -572,7 +706,7 @@ static void ensure_diag(Cg* cg, double lambda) {
   if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
                                 cg->v64.yloc, s))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
-  assemble_dot_kernel<double, false><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
+  assemble_dot_kernel<double, false><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
                                                        nullptr, nullptr, nullptr);
   inv_kernel<<<RB, RT, 0, s>>>(cg->N, cg->v64.s, cg->v64.dinv, cg->have32 ? cg->v32.dinv : nullptr, cg->ndir);
   op->ctx->launches += 3;
@@ -593,7 +727,14 @@ static void fp64_residual(Cg* cg, double lambda, const double* x, const double* 
 static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithaca_gpu_cg_result* res) {
   Ctx* c = cg->op->ctx;
   cudaStream_t s = c->stream;
-  if (o.mode == ITHACA_GPU_SOLVE_MIXED_FP32) ensure_fp32(cg);
+  const bool mixed = o.mode == ITHACA_GPU_SOLVE_MIXED_FP32 || o.mode == ITHACA_GPU_SOLVE_MIXED_FP32_GEO16;
+  if (mixed) ensure_fp32(cg);
+  if (o.mode == ITHACA_GPU_SOLVE_MIXED_FP32_GEO16) ensure_geo16(cg);
+  cg->geo16 = o.mode == ITHACA_GPU_SOLVE_MIXED_FP32_GEO16;
+  struct Geo16Reset {  // the 16-bit geometry is selected for this solve only
+    Cg* c;
+    ~Geo16Reset() { c->geo16 = false; }
+  } geo16_reset{cg};
   ensure_diag(cg, lambda);
   const int chunk = std::max(1, std::min(o.check_every, 64));
   const double tol = std::max(o.tol, 1e-16);  // tolerance floor of NekLinSysIter.cpp:83
@@ -605,7 +746,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
     out.eps = cg->sc_host->eps;
     out.rhs_magnitude = cg->sc_host->rhs_mag;
     status = cg->sc_host->status;
-  } else if (o.mode == ITHACA_GPU_SOLVE_MIXED_FP32) {
+  } else if (mixed) {
     double hs[2];
     // x64 = 0; r64 = b
     ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->N, s));
@@ -727,6 +868,57 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       const int g = l2g[l];
       cols[fill[g]++] = sign[l] > 0 ? (int)l : ~(int)l;
     }
+    // assembly plan: rows by number of entries (class c < kAsmK: c + 1 entries, ELL)
+    AsmPlan plan{};
+    std::vector<int> cls_of(nglobal);
+    long long entries[kAsmK + 1] = {};
+    for (int g = 0; g < nglobal; ++g) {
+      const int k = cnt[g + 1] - cnt[g];
+      if (k == 0) fail(ITHACA_GPU_ERR_ARG, "global dof " + std::to_string(g) + " has no local dof");
+      const int c = k <= kAsmK ? k - 1 : kAsmK;
+      cls_of[g] = c;
+      plan.n[c]++;
+      if (g < ndir) plan.ndir[c]++;
+      entries[c] += k;
+    }
+    long long col_total = 0;
+    for (int c = 0, off = 0; c <= kAsmK; ++c) {
+      plan.rows_off[c] = off;
+      off += plan.n[c];
+      if (c < kAsmK) {
+        plan.col_off[c] = col_total;
+        col_total += entries[c];
+      }
+    }
+    std::vector<int> asm_rows(nglobal), asm_cols((size_t)std::max<long long>(col_total, 1));
+    {
+      int fillc[kAsmK + 1];
+      for (int c = 0; c <= kAsmK; ++c) fillc[c] = 0;
+      for (int g = 0; g < nglobal; ++g) {
+        const int c = cls_of[g], i = fillc[c]++;
+        asm_rows[(size_t)plan.rows_off[c] + i] = g;
+        if (c < kAsmK)
+          for (int j = 0; j <= c; ++j) asm_cols[(size_t)plan.col_off[c] + (size_t)j * plan.n[c] + i] = cols[cnt[g] + j];
+      }
+    }
+    // CTAs per class in proportion to its entries, at least one for a non-empty class
+    {
+      long long total = 0;
+      int nonempty = 0;
+      for (int c = 0; c <= kAsmK; ++c) {
+        total += entries[c];
+        nonempty += plan.n[c] > 0;
+      }
+      int share[kAsmK + 1], used = 0, big = 0;
+      for (int c = 0; c <= kAsmK; ++c) {
+        share[c] = plan.n[c] > 0 ? std::max(1, (int)((double)(RB - nonempty) * entries[c] / std::max(total, 1LL))) : 0;
+        used += share[c];
+        if (entries[c] > entries[big]) big = c;
+      }
+      share[big] += RB - used;  // the rounding remainder goes to the largest class
+      plan.cta0[0] = 0;
+      for (int c = 0; c <= kAsmK; ++c) plan.cta0[c + 1] = plan.cta0[c] + share[c];
+    }
     auto cg = std::make_unique<ithaca_gpu_cg>();
     cg->op = op;
     cg->N = nglobal;
@@ -736,9 +928,15 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     ITHACA_CUDA(cudaMalloc(&cg->l2g, sizeof(int) * nloc));
     ITHACA_CUDA(cudaMalloc(&cg->rowptr, sizeof(int) * (nglobal + 1)));
     ITHACA_CUDA(cudaMalloc(&cg->cols, sizeof(int) * nloc));
+    ITHACA_CUDA(cudaMalloc(&cg->asm_rows, sizeof(int) * nglobal));
+    ITHACA_CUDA(cudaMalloc(&cg->asm_cols, sizeof(int) * asm_cols.size()));
     ITHACA_CUDA(cudaMemcpyAsync(cg->l2g, code.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
     ITHACA_CUDA(cudaMemcpyAsync(cg->rowptr, cnt.data(), sizeof(int) * (nglobal + 1), cudaMemcpyHostToDevice, s));
     ITHACA_CUDA(cudaMemcpyAsync(cg->cols, cols.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+    ITHACA_CUDA(cudaMemcpyAsync(cg->asm_rows, asm_rows.data(), sizeof(int) * nglobal, cudaMemcpyHostToDevice, s));
+    ITHACA_CUDA(
+        cudaMemcpyAsync(cg->asm_cols, asm_cols.data(), sizeof(int) * asm_cols.size(), cudaMemcpyHostToDevice, s));
+    cg->plan = plan;
     cg->v64.alloc(nglobal, nloc);
     ITHACA_CUDA(cudaMalloc(&cg->partials, sizeof(double) * NSLOT * RB));
     ITHACA_CUDA(cudaMalloc(&cg->dscal, sizeof(double) * 8));
@@ -777,7 +975,7 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
     }
     double* dy = on_device ? y : cg->v64.q;
     launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, dx, s, false, nullptr);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
                                                   nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
@@ -799,7 +997,7 @@ int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* globa
       dl = d;
     }
     double* dg = on_device ? global : (double*)c->stage_ptr(1, sizeof(double) * cg->N);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(global, dg, sizeof(double) * cg->N, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaGetLastError());
@@ -890,7 +1088,7 @@ int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing
                                  cg->v64.yloc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
     neg_kernel<<<RB, RT, 0, s>>>(nloc, cg->v64.yloc);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
                                                   nullptr, nullptr);
     c->launches += 3;
     solve_impl(cg, lambda, o, res);
@@ -912,8 +1110,15 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     cudaStream_t s = op->ctx->stream;
-    const bool f32 = mode == ITHACA_GPU_SOLVE_MIXED_FP32;
+    const bool half = mode == ITHACA_GPU_SOLVE_MIXED_FP32_GEO16;
+    const bool f32 = mode == ITHACA_GPU_SOLVE_MIXED_FP32 || half;
     if (f32) ensure_fp32(cg);
+    if (half) ensure_geo16(cg);
+    cg->geo16 = half;
+    struct Geo16Reset {
+      Cg* c;
+      ~Geo16Reset() { c->geo16 = false; }
+    } geo16_reset{cg};
     cudaEvent_t e0, e1;
     ITHACA_CUDA(cudaEventCreate(&e0));
     ITHACA_CUDA(cudaEventCreate(&e1));
@@ -934,10 +1139,12 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
     cudaEventDestroy(e1);
     *avg_ms = ms / reps;
     if (bytes_per_launch) {
-      // per element: l2g index (4 B) + gathered input + output per local dof, geometry per point
-      const double es = f32 ? 4.0 : 8.0;
+      // per element: l2g index (4 B) + gathered input + output per local dof, geometry per
+      // point (+ 8 scales per element for 16-bit geometry)
+      const double es = f32 ? 4.0 : 8.0, gs = half ? 2.0 : es;
       const double npt = op->deformed ? op->nq : 1;
-      *bytes_per_launch = (double)op->E * (op->nm * (4.0 + 2.0 * es) + n_jg(op->dim) * npt * es);
+      *bytes_per_launch =
+          (double)op->E * (op->nm * (4.0 + 2.0 * es) + n_jg(op->dim) * npt * gs + (half ? 32.0 : 0.0));
     }
   });
 }
@@ -977,13 +1184,13 @@ void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, doub
   for (int j = 0; j < ncols; ++j) {
     const double* x = X + (size_t)j * cg->N;
     launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), 0.0, nullptr, x, s, true, nullptr);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc,
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
                                                   LX + (size_t)j * cg->N, nullptr, nullptr, nullptr);
     g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, x, loc);
     if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
         !launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "mass operator: (modes, points) combination not built");
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
+    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
                                                   nullptr, nullptr, nullptr);
     c->launches += 5;
   }
@@ -1037,6 +1244,7 @@ int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_de
       cast_kernel<float><<<RB, RT, 0, s>>>(njg / (op->deformed ? 1 : op->nq), geo64(cg), cg->jg32);
       op->ctx->launches++;
     }
+    if (cg->have16) build_geo16(cg);
     cg->diag_lambda = NAN;
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));
@@ -1075,7 +1283,7 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
                                    cg->v64.yloc, s))
         fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
       double* dg = on_device ? dJdx : cg->v64.q;
-      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->N, 0, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
+      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
                                                     nullptr, nullptr);
       launch_zero_head(cg->ndir, dg, s);
       c->launches += 3;

@@ -25,14 +25,15 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 
 // Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
 // occupancy calculator), never more CTAs than element groups.
-template <typename T, int N, int Q, int EB, int NB>
-static void pipe_nq(int E, const double* hB, const double* hD, const T* jg, T lambda, const T* in, T* out,
-                    const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s) {
+template <typename T, int N, int Q, int EB, int NB, typename TG = T>
+static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T lambda, const T* in, T* out,
+                    const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s,
+                    const float* gscale = nullptr) {
   PTabs<T, N, Q> tab;
   for (int i = 0; i < N * Q; ++i) tab.B[i] = (T)hB[i];
   for (int i = 0; i < Q * Q; ++i) tab.D[i] = (T)hD[i];
-  using L = PipeLayout<T, N, Q, EB, NB>;
-  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB> : helm3_pipe_kernel<T, N, Q, EB, false, NB>;
+  using L = PipeLayout<T, N, Q, EB, NB, TG>;
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG> : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG>;
   static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
   const int gi = l2g ? 1 : 0;
   if (slots[gi] == 0) {
@@ -45,10 +46,27 @@ static void pipe_nq(int E, const double* hB, const double* hD, const T* jg, T la
   }
   const int ngroups = (E + EB - 1) / EB;
   const dim3 block(Q * Q, EB), grid(std::min(ngroups, slots[gi]));
-  k<<<grid, block, L::bytes(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, err);
+  k<<<grid, block, L::bytes(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale);
 }
 
 }  // namespace dev
+
+// Pipelined kernel (one element per group, single buffer) on half-precision geometry
+// with per-element, per-field FP32 scales (8 floats per element).
+bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
+                            const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,
+                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s) {
+  const __half* jg = static_cast<const __half*>(jg16);
+#define X(NN, QQ)                                                                                          \
+  if (n == NN && Q == QQ) {                                                                                \
+    dev::pipe_nq<float, NN, QQ, 1, 1, __half>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, \
+                                              gscale);                                                     \
+    return true;                                                                                           \
+  }
+  X(2, 3) X(3, 4) X(4, 5) X(5, 6) X(6, 7) X(7, 8) X(8, 9) X(9, 10) X(10, 11)
+#undef X
+  return false;
+}
 
 // variant: 2 or 4 = one pass per CTA with a TMA-staged geometry slab and that many
 // elements per CTA; 21 or 22 = the persistent pipelined kernel with 1 or 2 elements per

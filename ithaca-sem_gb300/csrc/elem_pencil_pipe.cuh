@@ -13,29 +13,41 @@
 //     written to shared memory at stage 1 of iteration i+1, where the sign is applied.
 // The arithmetic per element is exactly that of helm3_pencil_kernel (same stages, same
 // tables, same summation order), so both kernels give bit-identical results.
+//
+// TG = __half stores the geometry slab in half precision with one FP32 scale per element
+// and field (value = half * scale, |half| <= 1): half the geometry bytes for a pointwise
+// relative perturbation of the coefficients below 2^-11 of each field's element maximum.
+// The operator stays symmetric positive definite and spectrally equivalent to the FP32
+// one, which is what an inner solve inside FP64 iterative refinement needs.
 #pragma once
+
+#include <cuda_fp16.h>
+
+#include <type_traits>
 
 #include "elem_pencil.cuh"
 
 namespace ithaca {
 namespace dev {
 
-template <typename T, int N, int Q, int EB, int NB>
+template <typename T, int N, int Q, int EB, int NB, typename TG = T>
 struct PipeLayout {
   static constexpr int NQ = Q * Q * Q, GEO = 7 * NQ;
   static constexpr int PJ = Q, PK = pk_stride(Q), FS = PK * Q;
-  static constexpr size_t GEO_BYTES = ((size_t)EB * GEO * sizeof(T) + 32 + 15) / 16 * 16;  // + window slack
+  static constexpr size_t GEO_BYTES = ((size_t)EB * GEO * sizeof(TG) + 32 + 15) / 16 * 16;  // + window slack
   static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
-template <typename T, int N, int Q, int EB, bool GATHER, int NB>
+template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
-                                                               const PTabs<T, N, Q> tab, const T* __restrict__ jg,
+                                                               const PTabs<T, N, Q> tab, const TG* __restrict__ jg,
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
-                                                               const T* __restrict__ lam_ptr, int* __restrict__ err) {
+                                                               const T* __restrict__ lam_ptr, int* __restrict__ err,
+                                                               const float* __restrict__ gscale = nullptr) {
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
-  using L = PipeLayout<T, N, Q, EB, NB>;
+  constexpr bool HALF = !std::is_same<TG, T>::value;
+  using L = PipeLayout<T, N, Q, EB, NB, TG>;
   constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
   constexpr int PJ = L::PJ, PK = L::PK, FS = L::FS;
   constexpr int NPT = (NM + TPE - 1) / TPE;  // coefficients gathered per thread
@@ -59,15 +71,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     const int e0 = grp * EB, ne = min(EB, E - e0);
     const uintptr_t a0 = reinterpret_cast<uintptr_t>(jg + (size_t)e0 * GEO);
     const uintptr_t lo = a0 & ~uintptr_t(15);
-    const uintptr_t hi = (a0 + (size_t)ne * GEO * sizeof(T) + 15) & ~uintptr_t(15);
+    const uintptr_t hi = (a0 + (size_t)ne * GEO * sizeof(TG) + 15) & ~uintptr_t(15);
     mbar_arrive_expect_tx(bar + b, static_cast<uint32_t>(hi - lo));
     tma_bulk_load(geo_base + b * L::GEO_BYTES, reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo),
                   bar + b);
   };
-  auto geometry_of = [&](int grp, int b) -> const T* {
+  auto geometry_of = [&](int grp, int b) -> const TG* {
     const uintptr_t a0 = reinterpret_cast<uintptr_t>(jg + (size_t)grp * EB * GEO);
     const int shift = static_cast<int>(a0 & uintptr_t(15));
-    return reinterpret_cast<const T*>(geo_base + b * L::GEO_BYTES + shift) + el * GEO;
+    return reinterpret_cast<const TG*>(geo_base + b * L::GEO_BYTES + shift) + el * GEO;
   };
 
   // prefetch registers: raw gathered values and a sign mask for the next group
@@ -137,6 +149,12 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       }
     }
     if (has_next) load_codes(nxt);
+    T gs[7];  // per-field scales of this element (half-precision geometry), used at stage 6
+    if constexpr (HALF) {
+      const float* sc = gscale + (size_t)min(e, E - 1) * 8;
+#pragma unroll
+      for (int f = 0; f < 7; ++f) gs[f] = __ldg(sc + f);
+    }
     __syncthreads();
     // ---- 2: BwdTrans along p: pencils (q, r) ----
     if (t < N * N) {
@@ -228,7 +246,13 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       if (NB == 2 && has_next) mbar_wait_bounded(bar + (b ^ 1), ((it + 1) >> 1) & 1, kWaitCycles);
       return;
     }
-    const T* G = geometry_of(grp, b);
+    const TG* G = geometry_of(grp, b);
+    auto geo = [&](int f, int pt) -> T {
+      if constexpr (HALF)
+        return __half2float(G[f * NQ + pt]) * gs[f];
+      else
+        return G[f * NQ + pt];
+    };
     // ---- 6: point-wise metric on columns (i, j) ----
     T v[Q];
     {
@@ -238,9 +262,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         const int s = ci + PJ * cj + PK * k;
         const int pt = ci + Q * cj + Q * Q * k;
         const T g0 = S0[s], g1 = S1[s];
-        const T jw = G[pt];
-        const T m00 = G[NQ + pt], m01 = G[2 * NQ + pt], m02 = G[3 * NQ + pt];
-        const T m11 = G[4 * NQ + pt], m12 = G[5 * NQ + pt], m22 = G[6 * NQ + pt];
+        const T jw = geo(0, pt);
+        const T m00 = geo(1, pt), m01 = geo(2, pt), m02 = geo(3, pt);
+        const T m11 = geo(4, pt), m12 = geo(5, pt), m22 = geo(6, pt);
         S0[s] = fma(m00, g0, fma(m01, g1, m02 * g2[k]));
         S1[s] = fma(m01, g0, fma(m11, g1, m12 * g2[k]));
         f2[k] = fma(m02, g0, fma(m12, g1, m22 * g2[k]));

@@ -71,6 +71,9 @@ struct Ctx {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the legacy default stream
   int* derr = nullptr;  // device error word set by bounded waits in kernels (0 = ok)
   void check_device_error();
+  // dense eigen-solver handle of the POD offline stage, created on first use
+  void* solver = nullptr;
+  void (*solver_free)(void*) = nullptr;
   ~Ctx();
 };
 
@@ -123,6 +126,10 @@ template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s);
+// Half-precision geometry (E x 7 x Q^3 halves) with 8 FP32 scales per element; FP32 hexes.
+bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
+                            const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,
+                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s);
 
 void retain_op(Op* op);
 void release_op(Op* op);    // frees the operator (and releases its context) at zero

@@ -4,7 +4,8 @@
 // EquationSystems/CoupledLinearNS_ROM.cpp:3916-4001): the reference takes a thin SVD of
 // the snapshot matrix S with Eigen's BDCSVD. Here the method of snapshots gives the same
 // subspace: C = S^T S (FP64 split-K GEMM with a fixed-order reduction), C = W L W^T
-// (cyclic Jacobi eigen-solver on the host, ns x ns), V = S W_r L_r^{-1/2}, then two
+// (cuSOLVER's symmetric divide-and-conquer eigen-solver, ns x ns, on the device),
+// V = S W_r L_r^{-1/2}, then two
 // Cholesky-QR passes restore orthonormality (the modes are re-orthogonalised as
 // VelocityCorrectionScheme_iROM.cpp:830-852 does with Gram-Schmidt). Eigenvalues of
 // S^T S far below the largest are not resolved in FP64 (a pass keeps those above 1e-10
@@ -21,6 +22,8 @@
 #include <mutex>
 #include <string>
 #include <vector>
+
+#include <cusolverDn.h>
 
 #include "ithaca_internal.h"
 
@@ -132,47 +135,52 @@ void dgemm_nn(int M, int Nn, int K, const double* A, const double* B, double* C,
   if (launches) *launches += 1;
 }
 
-// ---- host dense helpers (ns x ns, column-major) ----
-// Cyclic Jacobi eigen-decomposition of a symmetric matrix (Golub & Van Loan, Alg. 8.5.3).
-static void jacobi_eigen(int n, std::vector<double>& A, std::vector<double>& V, std::vector<double>& ev) {
-  V.assign((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
-  auto a = [&](int i, int j) -> double& { return A[(size_t)j * n + i]; };
-  double fro = 0;
-  for (double x : A) fro += x * x;
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0;
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < j; ++i) off += 2 * a(i, j) * a(i, j);
-    if (off <= 1e-30 * fro) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = a(p, q);
-        if (std::fabs(apq) < 1e-300) continue;
-        const double theta = (a(q, q) - a(p, p)) / (2 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
-        const double c = 1 / std::sqrt(t * t + 1), s = t * c;
-        for (int k = 0; k < n; ++k) {  // columns p, q
-          const double akp = a(k, p), akq = a(k, q);
-          a(k, p) = c * akp - s * akq;
-          a(k, q) = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {  // rows p, q
-          const double apk = a(p, k), aqk = a(q, k);
-          a(p, k) = c * apk - s * aqk;
-          a(q, k) = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          double& vkp = V[(size_t)p * n + k];
-          double& vkq = V[(size_t)q * n + k];
-          const double x = vkp, y = vkq;
-          vkp = c * x - s * y;
-          vkq = s * x + c * y;
-        }
-      }
+// Device scratch owned by one call.
+struct DevBuf {
+  double* p = nullptr;
+  explicit DevBuf(size_t n) { ITHACA_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
+  ~DevBuf() { cudaFree(p); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+// ---- dense symmetric eigen-decomposition on the device (cuSOLVER syevd) ----
+static void free_solver(void* h) { cusolverDnDestroy(static_cast<cusolverDnHandle_t>(h)); }
+
+static cusolverDnHandle_t ctx_solver(Ctx* ctx) {
+  if (!ctx->solver) {
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) fail(ITHACA_GPU_ERR_CUDA, "cusolverDnCreate failed");
+    ctx->solver = h;
+    ctx->solver_free = free_solver;
   }
+  auto h = static_cast<cusolverDnHandle_t>(ctx->solver);
+  if (cusolverDnSetStream(h, ctx->stream) != CUSOLVER_STATUS_SUCCESS)
+    fail(ITHACA_GPU_ERR_CUDA, "cusolverDnSetStream failed");
+  return h;
+}
+
+// A (n x n, column-major, symmetric, device) -> eigenvectors in place (column j for
+// eigenvalue ev[j], ascending); ev is returned on the host.
+static void sym_eigen(Ctx* ctx, int n, double* A, std::vector<double>& ev) {
+  cusolverDnHandle_t h = ctx_solver(ctx);
+  int lwork = 0;
+  DevBuf dev_w((size_t)n);
+  if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, dev_w.p, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS)
+    fail(ITHACA_GPU_ERR_CUDA, "cusolverDnDsyevd_bufferSize failed");
+  DevBuf work((size_t)std::max(lwork, 1) + 1);  // the last double holds the info word
+  int* info = reinterpret_cast<int*>(work.p + std::max(lwork, 1));
+  if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, dev_w.p, work.p, lwork, info) !=
+      CUSOLVER_STATUS_SUCCESS)
+    fail(ITHACA_GPU_ERR_CUDA, "cusolverDnDsyevd failed");
+  int hinfo = 0;
   ev.resize(n);
-  for (int i = 0; i < n; ++i) ev[i] = a(i, i);
+  ITHACA_CUDA(cudaMemcpyAsync(ev.data(), dev_w.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  ITHACA_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hinfo != 0) fail(ITHACA_GPU_ERR_NUMERIC, "symmetric eigen-solver did not converge (info " +
+                                                   std::to_string(hinfo) + ")");
 }
 
 // Cholesky of an SPD r x r (column-major, lower); returns false if not SPD.
@@ -266,14 +274,6 @@ __global__ void sub_from_kernel(size_t n, const double* __restrict__ s, double* 
     r[i] = s[i] - r[i];
 }
 
-struct DevBuf {
-  double* p = nullptr;
-  explicit DevBuf(size_t n) { ITHACA_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
-  ~DevBuf() { cudaFree(p); }
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-};
-
 }  // namespace ithaca
 
 using namespace ithaca;
@@ -354,10 +354,10 @@ int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, 
     // re-orthonormalises V (two Cholesky-QR passes) and deflates R = S - V (V^T S).
     for (int pass = 0; pass < 8 && r < nmodes; ++pass) {
       dgemm_tn(ns, ns, N, dR.p, dR.p, dC.p, scratch.p, s, &ctx->launches);
-      std::vector<double> C((size_t)ns * ns), W, ev;
-      ITHACA_CUDA(cudaMemcpyAsync(C.data(), dC.p, sizeof(double) * C.size(), cudaMemcpyDeviceToHost, s));
+      std::vector<double> W((size_t)ns * ns), ev;
+      sym_eigen(ctx, ns, dC.p, ev);  // dC now holds the eigenvectors
+      ITHACA_CUDA(cudaMemcpyAsync(W.data(), dC.p, sizeof(double) * W.size(), cudaMemcpyDeviceToHost, s));
       ITHACA_CUDA(cudaStreamSynchronize(s));
-      jacobi_eigen(ns, C, W, ev);
       std::vector<int> order(ns);
       for (int i = 0; i < ns; ++i) order[i] = i;
       std::sort(order.begin(), order.end(), [&](int a, int b) { return ev[a] > ev[b]; });

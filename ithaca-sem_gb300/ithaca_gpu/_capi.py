@@ -15,7 +15,7 @@ ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM = 1, 2, 3, 4
 ERR_NOT_CONVERGED, ERR_GEOMETRY, ERR_TIMEOUT, ERR_NUMERIC = 5, 6, 7, 8
 SHAPE_QUAD, SHAPE_HEX = 4, 8
 FP64, FP32 = 0, 1
-SOLVE_FP64, SOLVE_MIXED_FP32 = 0, 1
+SOLVE_FP64, SOLVE_MIXED_FP32, SOLVE_MIXED_FP32_GEO16 = 0, 1, 2
 
 _ERRNAMES = {1: "ERR_ARG", 2: "ERR_UNSUPPORTED", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_NOT_CONVERGED",
              6: "ERR_GEOMETRY", 7: "ERR_TIMEOUT", 8: "ERR_NUMERIC"}

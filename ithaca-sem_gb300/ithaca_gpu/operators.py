@@ -21,7 +21,7 @@ from . import _capi as C
 
 SHAPES = {"quad": C.SHAPE_QUAD, "hex": C.SHAPE_HEX}
 PRECISIONS = {"fp64": C.FP64, "fp32": C.FP32}
-SOLVE_MODES = {"fp64": C.SOLVE_FP64, "mixed": C.SOLVE_MIXED_FP32}
+SOLVE_MODES = {"fp64": C.SOLVE_FP64, "mixed": C.SOLVE_MIXED_FP32, "mixed_geo16": C.SOLVE_MIXED_FP32_GEO16}
 
 
 def _is_device(a):

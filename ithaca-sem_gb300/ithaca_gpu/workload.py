@@ -87,7 +87,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--mesh", type=int, default=24)
     ap.add_argument("--order", type=int, default=6)
-    ap.add_argument("--mode", choices=["fp64", "mixed"], nargs="*", default=["mixed"])
+    ap.add_argument("--mode", choices=["fp64", "mixed", "mixed_geo16"], nargs="*", default=["mixed"])
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--variant", type=int, default=-1, help="FP32 hex kernel variant (-1: autotune)")
     ap.add_argument("--inner-tol", type=float, nargs="*", default=[1e-2],

@@ -107,6 +107,38 @@ def test_mixed_curved_hex_inner_tolerances(ctx, inner_tol):
     assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
 
 
+@pytest.mark.parametrize("inner_tol", [1e-2, 1e-4])
+def test_mixed_geo16_curved_hex(ctx, inner_tol):
+    """FP32 inner solves on 16-bit (per-element scaled) geometry inside FP64 refinement:
+    the FP64 residual is reached and the solution agrees with the FP64 solve."""
+    c = hex_case(4, 3, 3, 6, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(9).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, _ = sys_.solve(1.0, rhs, tol=1e-12)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed_geo16", inner_tol=inner_tol)
+    assert res.rel_residual < 1e-10
+    assert res.outer_iterations >= 2
+    assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
+    # the FP32-geometry mixed solve afterwards is unaffected (graph re-captured)
+    x2, res2 = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed", inner_tol=inner_tol)
+    assert res2.rel_residual < 1e-10
+    ms, nbytes = sys_.profile_apply(1.0, mode="mixed_geo16", reps=2)
+    assert ms > 0 and nbytes > 0
+
+
+def test_mixed_geo16_rejects_quads(ctx):
+    from ithaca_gpu._capi import ERR_UNSUPPORTED, GpuError
+    c = quad_case(4, 4, 5)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(2).uniform(-1, 1, amap.nglobal)
+    with pytest.raises(GpuError) as ei:
+        sys_.solve(1.0, rhs, tol=1e-10, mode="mixed_geo16")
+    assert ei.value.code == ERR_UNSUPPORTED
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+
+
 def test_helmsolve_matches_analytic(ctx):
     c = quad_case(8, 8, 7, jitter=0.1, seed=0)
     coll, amap, sys_ = _system(ctx, c)
