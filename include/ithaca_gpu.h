@@ -119,12 +119,14 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
  * many elements per CTA (default 4), 21 or 22 = the persistent pencil kernel that
  * prefetches the next group of 1 or 2 elements (geometry by TMA into a double buffer,
  * gathered coefficients into registers) while computing the current one, 31 or 32 =
- * the same with a single geometry buffer refilled right after its metric stage. */
+ * the same with a single geometry buffer refilled right after its metric stage, 41 or
+ * 42 = 31 or 32 with the 1-D contractions on packed FP32 pairs (same results). */
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
 /* Times every variant on the operator's own data and keeps the fastest, like
  * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)
- * picks an implementation type. times_ms (7 entries, may be NULL) receives the average
- * FP32 apply time of variants 0, 2, 4, 21, 22, 31, 32 (-1 where a variant does not apply). */
+ * picks an implementation type. times_ms (9 entries, may be NULL) receives the average
+ * FP32 apply time of variants 0, 2, 4, 21, 22, 31, 32, 41, 42 (-1 where a variant does
+ * not apply). */
 int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* times_ms);
 /* Diagonals of the element Helmholtz matrices (E*n^d), the per-element input of
  * PreconditionerDiagonal::DiagonalPreconditionerSum (PreconditionerDiagonal.cpp:98-161). */

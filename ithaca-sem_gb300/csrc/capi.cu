@@ -432,8 +432,8 @@ int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant) {
   return guarded([&] {
     require(op != nullptr, "null argument");
     require(variant == 0 || variant == 2 || variant == 4 || variant == 21 || variant == 22 || variant == 31 ||
-                variant == 32,
-            "variant must be 0, 2, 4, 21, 22, 31 or 32");
+                variant == 32 || variant == 41 || variant == 42,
+            "variant must be 0, 2, 4, 21, 22, 31, 32, 41 or 42");
     op->variant32 = variant;
   });
 }
@@ -472,10 +472,10 @@ int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* tim
     ITHACA_CUDA(cudaMalloc(&x, sizeof(float) * nm));
     ITHACA_CUDA(cudaMalloc(&y, sizeof(float) * nm));
     ITHACA_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * nm, s));
-    const int variants[7] = {0, 2, 4, 21, 22, 31, 32};
+    const int variants[9] = {0, 2, 4, 21, 22, 31, 32, 41, 42};
     double best = 1e300;
     int best_v = 0;
-    for (int vi = 0; vi < 7; ++vi) {
+    for (int vi = 0; vi < 9; ++vi) {
       const int v = variants[vi];
       double ms_avg = -1;
       if (v == 0 || (op->dim == 3 && op->deformed)) {

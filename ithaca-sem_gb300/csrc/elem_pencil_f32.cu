@@ -25,15 +25,27 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 
 // Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
 // occupancy calculator), never more CTAs than element groups.
-template <typename T, int N, int Q, int EB, int NB, typename TG = T>
+template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool PACK = false>
 static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T lambda, const T* in, T* out,
                     const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s,
                     const float* gscale = nullptr) {
   PTabs<T, N, Q> tab;
   for (int i = 0; i < N * Q; ++i) tab.B[i] = (T)hB[i];
   for (int i = 0; i < Q * Q; ++i) tab.D[i] = (T)hD[i];
+  PTabs2<N, Q> tab2{};
+  constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
+  for (int p = 0; p < N; ++p)
+    for (int i = 0; i < Q; ++i) {
+      tab2.BF[p * QP + i] = (float)hB[p * Q + i];
+      tab2.BT[i * NP + p] = (float)hB[p * Q + i];
+    }
+  for (int k = 0; k < Q; ++k)
+    for (int i = 0; i < Q; ++i) {
+      tab2.DF[k * QP + i] = (float)hD[k * Q + i];  // l_k'(z_i)
+      tab2.DT[i * QP + k] = (float)hD[k * Q + i];
+    }
   using L = PipeLayout<T, N, Q, EB, NB, TG>;
-  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG> : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG>;
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG, PACK> : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG, PACK>;
   static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
   const int gi = l2g ? 1 : 0;
   if (slots[gi] == 0) {
@@ -46,7 +58,7 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
   }
   const int ngroups = (E + EB - 1) / EB;
   const dim3 block(Q * Q, EB), grid(std::min(ngroups, slots[gi]));
-  k<<<grid, block, L::bytes(), s>>>(in, out, tab, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale);
+  k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale);
 }
 
 }  // namespace dev
@@ -59,8 +71,8 @@ bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double*
   const __half* jg = static_cast<const __half*>(jg16);
 #define X(NN, QQ)                                                                                          \
   if (n == NN && Q == QQ) {                                                                                \
-    dev::pipe_nq<float, NN, QQ, 1, 1, __half>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, \
-                                              gscale);                                                     \
+    dev::pipe_nq<float, NN, QQ, 1, 1, __half, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,   \
+                                                    err, s, gscale);                                       \
     return true;                                                                                           \
   }
   X(2, 3) X(3, 4) X(4, 5) X(5, 6) X(6, 7) X(7, 8) X(8, 9) X(9, 10) X(10, 11)
@@ -70,7 +82,8 @@ bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double*
 
 // variant: 2 or 4 = one pass per CTA with a TMA-staged geometry slab and that many
 // elements per CTA; 21 or 22 = the persistent pipelined kernel with 1 or 2 elements per
-// group and a double geometry buffer; 31 or 32 = the same with a single buffer.
+// group and a double geometry buffer; 31 or 32 = the same with a single buffer; 41 or 42 =
+// the single-buffer kernel with its contractions on packed FP32 pairs (fma.rn.f32x2).
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
@@ -89,6 +102,10 @@ bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, cons
       dev::pipe_nq<T, NN, QQ, 1, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
     else if (variant == 32)                                                                                \
       dev::pipe_nq<T, NN, QQ, 2, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+    else if (variant == 41)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 1, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s); \
+    else if (variant == 42)                                                                                \
+      dev::pipe_nq<T, NN, QQ, 2, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s); \
     else                                                                                                   \
       return false;                                                                                        \
     return true;                                                                                           \

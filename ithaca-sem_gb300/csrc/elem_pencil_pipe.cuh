@@ -30,6 +30,53 @@
 namespace ithaca {
 namespace dev {
 
+// ---- packed FP32 pairs (fma.rn.f32x2: two FP32 FMAs per instruction) ----
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// 1-D tables laid out for pairs of outputs: entry (input a, output o) of each table at
+// [a * ld + o] with an even row length ld, so outputs (o, o + 1), o even, are one
+// 8-byte-aligned constant pair. F: forward (BwdTrans / derivative), T: transposed
+// (IProduct / derivative transpose).
+template <int N, int Q>
+struct PTabs2 {
+  static constexpr int QP = Q + (Q & 1), NP = N + (N & 1);
+  alignas(8) float BF[N * QP];  // BF[p * QP + i] = B(p, z_i)
+  alignas(8) float DF[Q * QP];  // DF[k * QP + i] = l_k'(z_i)
+  alignas(8) float BT[Q * NP];  // BT[i * NP + p] = B(p, z_i)
+  alignas(8) float DT[Q * QP];  // DT[i * QP + k] = l_k'(z_i)
+};
+
+// o[x] = sum_{a < NI} W(a, x) c[a] for x < NO, the sum in increasing a (the order of the
+// scalar contractions), two outputs per instruction; with INIT the sums start from o.
+template <int NI, int NO, int LD, bool INIT, typename Get>
+__device__ __forceinline__ void contract2(Get W, const float (&c)[NI], float (&o)[NO]) {
+#pragma unroll
+  for (int x = 0; x + 1 < NO; x += 2) {
+    unsigned long long acc = INIT ? pk2(o[x], o[x + 1]) : pk2(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < NI; ++a) acc = ffma2(pk2(W(a * LD + x), W(a * LD + x + 1)), pk2(c[a], c[a]), acc);
+    upk2(acc, o[x], o[x + 1]);
+  }
+  if constexpr (NO & 1) {
+    float acc = INIT ? o[NO - 1] : 0.f;
+#pragma unroll
+    for (int a = 0; a < NI; ++a) acc = fmaf(W(a * LD + NO - 1), c[a], acc);
+    o[NO - 1] = acc;
+  }
+}
+
 template <typename T, int N, int Q, int EB, int NB, typename TG = T>
 struct PipeLayout {
   static constexpr int NQ = Q * Q * Q, GEO = 7 * NQ;
@@ -38,14 +85,21 @@ struct PipeLayout {
   static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
-template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T>
+template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
-                                                               const PTabs<T, N, Q> tab, const TG* __restrict__ jg,
+                                                               const PTabs<T, N, Q> tab, const PTabs2<N, Q> tab2,
+                                                               const TG* __restrict__ jg,
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
                                                                const T* __restrict__ lam_ptr, int* __restrict__ err,
                                                                const float* __restrict__ gscale = nullptr) {
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
+  static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
+  constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
+  auto BF = [&](int i) { return tab2.BF[i]; };
+  auto DF = [&](int i) { return tab2.DF[i]; };
+  auto BT = [&](int i) { return tab2.BT[i]; };
+  auto DT = [&](int i) { return tab2.DT[i]; };
   constexpr bool HALF = !std::is_same<TG, T>::value;
   using L = PipeLayout<T, N, Q, EB, NB, TG>;
   constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
@@ -82,36 +136,47 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     return reinterpret_cast<const TG*>(geo_base + b * L::GEO_BYTES + shift) + el * GEO;
   };
 
+  // Coefficient slot j of this thread is mode m = t + j TPE (every slot but the last
+  // is always a mode); its shared-memory offset in the (p, q, r) work layout does not
+  // depend on the element, so it is computed once here rather than per element.
+  int soff[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int m = t + j * TPE;
+    soff[j] = m < NM ? (m % N) + PJ * ((m / N) % N) + PK * (m / (N * N)) : -1;
+  }
+  auto slot_ok = [&](int j) { return j < NPT - 1 || soff[j] >= 0; };
+
   // prefetch registers: raw gathered values and a sign mask for the next group
   T xv[NPT];
   int code[NPT];
   unsigned neg = 0;
   auto load_codes = [&](int grp) {
     const int e = grp * EB + el;
+    const int* lp = l2g + (size_t)min(e, E - 1) * NM + t;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
-      const int m = t + j * TPE;
       code[j] = 0;
-      if (e < E && m < NM) {
-        if constexpr (GATHER) code[j] = __ldg(l2g + (size_t)e * NM + m);
+      if (e < E && slot_ok(j)) {
+        if constexpr (GATHER) code[j] = __ldg(lp + j * TPE);
       }
     }
   };
   auto load_values = [&](int grp) {
     const int e = grp * EB + el;
+    const T* ip = in + (size_t)min(e, E - 1) * NM + t;
     neg = 0;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
-      const int m = t + j * TPE;
       xv[j] = T(0);
-      if (e < E && m < NM) {
+      if (e < E && slot_ok(j)) {
         if constexpr (GATHER) {
           const int c = code[j];
           const int g = c >= 0 ? c : ~c;
           if (g >= ndir) xv[j] = in[g];
           neg |= (c < 0 ? 1u : 0u) << j;
         } else {
-          xv[j] = in[(size_t)e * NM + m];
+          xv[j] = ip[j * TPE];
         }
       }
     }
@@ -141,13 +206,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 
     // ---- 1: prefetched coefficients -> S0 as (p, q, r); then the next group's codes ----
 #pragma unroll
-    for (int j = 0; j < NPT; ++j) {
-      const int m = t + j * TPE;
-      if (m < NM) {
-        const int p = m % N, q = (m / N) % N, r = m / (N * N);
-        S0[p + PJ * q + PK * r] = (neg >> j) & 1u ? -xv[j] : xv[j];
-      }
-    }
+    for (int j = 0; j < NPT; ++j)
+      if (slot_ok(j)) S0[soff[j]] = (neg >> j) & 1u ? -xv[j] : xv[j];
     if (has_next) load_codes(nxt);
     T gs[7];  // per-field scales of this element (half-precision geometry), used at stage 6
     if constexpr (HALF) {
@@ -162,12 +222,19 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int p = 0; p < N; ++p) c[p] = S0[p + PJ * q + PK * r];
+      if constexpr (PACK) {
+        T o[Q];
+        contract2<N, Q, QP, false>(BF, c, o);
 #pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        T acc = tab.B[i] * c[0];
+        for (int i = 0; i < Q; ++i) S1[i + PJ * q + PK * r] = o[i];
+      } else {
 #pragma unroll
-        for (int p = 1; p < N; ++p) acc = fma(tab.B[p * Q + i], c[p], acc);
-        S1[i + PJ * q + PK * r] = acc;
+        for (int i = 0; i < Q; ++i) {
+          T acc = tab.B[i] * c[0];
+#pragma unroll
+          for (int p = 1; p < N; ++p) acc = fma(tab.B[p * Q + i], c[p], acc);
+          S1[i + PJ * q + PK * r] = acc;
+        }
       }
     }
     __syncthreads();
@@ -177,12 +244,19 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
+      if constexpr (PACK) {
+        T o[Q];
+        contract2<N, Q, QP, false>(BF, c, o);
 #pragma unroll
-      for (int j = 0; j < Q; ++j) {
-        T acc = tab.B[j] * c[0];
+        for (int j = 0; j < Q; ++j) S0[i + PJ * j + PK * r] = o[j];
+      } else {
 #pragma unroll
-        for (int q = 1; q < N; ++q) acc = fma(tab.B[q * Q + j], c[q], acc);
-        S0[i + PJ * j + PK * r] = acc;
+        for (int j = 0; j < Q; ++j) {
+          T acc = tab.B[j] * c[0];
+#pragma unroll
+          for (int q = 1; q < N; ++q) acc = fma(tab.B[q * Q + j], c[q], acc);
+          S0[i + PJ * j + PK * r] = acc;
+        }
       }
     }
     __syncthreads();
@@ -193,19 +267,24 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int r = 0; r < N; ++r) c[r] = S0[ci + PJ * cj + PK * r];
+      if constexpr (PACK) {
+        contract2<N, Q, QP, false>(BF, c, u);
+        contract2<Q, Q, QP, false>(DF, u, g2);
+      } else {
 #pragma unroll
-      for (int k = 0; k < Q; ++k) {
-        T acc = tab.B[k] * c[0];
+        for (int k = 0; k < Q; ++k) {
+          T acc = tab.B[k] * c[0];
 #pragma unroll
-        for (int r = 1; r < N; ++r) acc = fma(tab.B[r * Q + k], c[r], acc);
-        u[k] = acc;
-      }
+          for (int r = 1; r < N; ++r) acc = fma(tab.B[r * Q + k], c[r], acc);
+          u[k] = acc;
+        }
 #pragma unroll
-      for (int k = 0; k < Q; ++k) {
-        T acc = tab.D[k] * u[0];
+        for (int k = 0; k < Q; ++k) {
+          T acc = tab.D[k] * u[0];
 #pragma unroll
-        for (int c2 = 1; c2 < Q; ++c2) acc = fma(tab.D[c2 * Q + k], u[c2], acc);
-        g2[k] = acc;
+          for (int c2 = 1; c2 < Q; ++c2) acc = fma(tab.D[c2 * Q + k], u[c2], acc);
+          g2[k] = acc;
+        }
       }
 #pragma unroll
       for (int k = 0; k < Q; ++k) SU[ci + PJ * cj + PK * k] = u[k];
@@ -217,22 +296,34 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q];
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = SU[a + PJ * pj + PK * pk];
-#pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        T acc = tab.D[i] * c[0];
-#pragma unroll
-        for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + i], c[a], acc);
-        S0[i + PJ * pj + PK * pk] = acc;
-      }
       const int pi = t % Q;
+      if constexpr (PACK) {
+        T o[Q];
+        contract2<Q, Q, QP, false>(DF, c, o);
 #pragma unroll
-      for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+        for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
 #pragma unroll
-      for (int j = 0; j < Q; ++j) {
-        T acc = tab.D[j] * c[0];
+        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+        contract2<Q, Q, QP, false>(DF, c, o);
 #pragma unroll
-        for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + j], c[a], acc);
-        S1[pi + PJ * j + PK * pk] = acc;
+        for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pk] = o[j];
+      } else {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+          T acc = tab.D[i] * c[0];
+#pragma unroll
+          for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + i], c[a], acc);
+          S0[i + PJ * pj + PK * pk] = acc;
+        }
+#pragma unroll
+        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+          T acc = tab.D[j] * c[0];
+#pragma unroll
+          for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + j], c[a], acc);
+          S1[pi + PJ * j + PK * pk] = acc;
+        }
       }
     }
     // the next group's gather: its codes have had stages 2-5 to arrive
@@ -270,12 +361,16 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         f2[k] = fma(m02, g0, fma(m12, g1, m22 * g2[k]));
         v[k] = lambda * jw * u[k];
       }
+      if constexpr (PACK) {
+        contract2<Q, Q, QP, true>(DT, f2, v);
+      } else {
 #pragma unroll
-      for (int k = 0; k < Q; ++k) {
-        T acc = v[k];
+        for (int k = 0; k < Q; ++k) {
+          T acc = v[k];
 #pragma unroll
-        for (int c2 = 0; c2 < Q; ++c2) acc = fma(tab.D[k * Q + c2], f2[c2], acc);
-        v[k] = acc;
+          for (int c2 = 0; c2 < Q; ++c2) acc = fma(tab.D[k * Q + c2], f2[c2], acc);
+          v[k] = acc;
+        }
       }
     }
     __syncthreads();
@@ -287,24 +382,32 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q], o[Q];
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S0[a + PJ * pj + PK * pk];
+      if constexpr (PACK) {
+        contract2<Q, Q, QP, false>(DT, c, o);
+      } else {
 #pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        T acc = tab.D[i * Q] * c[0];
+        for (int i = 0; i < Q; ++i) {
+          T acc = tab.D[i * Q] * c[0];
 #pragma unroll
-        for (int a = 1; a < Q; ++a) acc = fma(tab.D[i * Q + a], c[a], acc);
-        o[i] = acc;
+          for (int a = 1; a < Q; ++a) acc = fma(tab.D[i * Q + a], c[a], acc);
+          o[i] = acc;
+        }
       }
 #pragma unroll
       for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
       const int pi = t % Q;
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S1[pi + PJ * a + PK * pk];
+      if constexpr (PACK) {
+        contract2<Q, Q, QP, false>(DT, c, o);
+      } else {
 #pragma unroll
-      for (int j = 0; j < Q; ++j) {
-        T acc = tab.D[j * Q] * c[0];
+        for (int j = 0; j < Q; ++j) {
+          T acc = tab.D[j * Q] * c[0];
 #pragma unroll
-        for (int a = 1; a < Q; ++a) acc = fma(tab.D[j * Q + a], c[a], acc);
-        o[j] = acc;
+          for (int a = 1; a < Q; ++a) acc = fma(tab.D[j * Q + a], c[a], acc);
+          o[j] = acc;
+        }
       }
 #pragma unroll
       for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pk] = o[j];
@@ -317,12 +420,19 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         const int s = ci + PJ * cj + PK * k;
         v[k] += S0[s] + S1[s];
       }
+      if constexpr (PACK) {
+        T o[N];
+        contract2<Q, N, NP, false>(BT, v, o);
 #pragma unroll
-      for (int r = 0; r < N; ++r) {
-        T acc = tab.B[r * Q] * v[0];
+        for (int r = 0; r < N; ++r) SU[ci + PJ * cj + PK * r] = o[r];
+      } else {
 #pragma unroll
-        for (int k = 1; k < Q; ++k) acc = fma(tab.B[r * Q + k], v[k], acc);
-        SU[ci + PJ * cj + PK * r] = acc;
+        for (int r = 0; r < N; ++r) {
+          T acc = tab.B[r * Q] * v[0];
+#pragma unroll
+          for (int k = 1; k < Q; ++k) acc = fma(tab.B[r * Q + k], v[k], acc);
+          SU[ci + PJ * cj + PK * r] = acc;
+        }
       }
     }
     __syncthreads();
@@ -332,12 +442,19 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q];
 #pragma unroll
       for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
+      if constexpr (PACK) {
+        T o[N];
+        contract2<Q, N, NP, false>(BT, c, o);
 #pragma unroll
-      for (int q = 0; q < N; ++q) {
-        T acc = tab.B[q * Q] * c[0];
+        for (int q = 0; q < N; ++q) S0[i + PJ * q + PK * r] = o[q];
+      } else {
 #pragma unroll
-        for (int j = 1; j < Q; ++j) acc = fma(tab.B[q * Q + j], c[j], acc);
-        S0[i + PJ * q + PK * r] = acc;
+        for (int q = 0; q < N; ++q) {
+          T acc = tab.B[q * Q] * c[0];
+#pragma unroll
+          for (int j = 1; j < Q; ++j) acc = fma(tab.B[q * Q + j], c[j], acc);
+          S0[i + PJ * q + PK * r] = acc;
+        }
       }
     }
     __syncthreads();
@@ -347,20 +464,27 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q];
 #pragma unroll
       for (int i = 0; i < Q; ++i) c[i] = S0[i + PJ * q + PK * r];
+      if constexpr (PACK) {
+        T o[N];
+        contract2<Q, N, NP, false>(BT, c, o);
 #pragma unroll
-      for (int p = 0; p < N; ++p) {
-        T acc = tab.B[p * Q] * c[0];
+        for (int p = 0; p < N; ++p) S1[p + PJ * q + PK * r] = o[p];
+      } else {
 #pragma unroll
-        for (int i = 1; i < Q; ++i) acc = fma(tab.B[p * Q + i], c[i], acc);
-        S1[p + PJ * q + PK * r] = acc;
+        for (int p = 0; p < N; ++p) {
+          T acc = tab.B[p * Q] * c[0];
+#pragma unroll
+          for (int i = 1; i < Q; ++i) acc = fma(tab.B[p * Q + i], c[i], acc);
+          S1[p + PJ * q + PK * r] = acc;
+        }
       }
     }
     __syncthreads();
     if (active) {
-      for (int m = t; m < NM; m += TPE) {
-        const int p = m % N, q = (m / N) % N, r = m / (N * N);
-        out[(size_t)e * NM + m] = S1[p + PJ * q + PK * r];
-      }
+      T* op = out + (size_t)e * NM + t;
+#pragma unroll
+      for (int j = 0; j < NPT; ++j)
+        if (slot_ok(j)) op[j * TPE] = S1[soff[j]];
     }
     // S0 and S1 are rewritten by the next group's stages 1-2; with NB = 2 the geometry
     // buffer read here is refilled by the copy issued at the top of the iteration after next

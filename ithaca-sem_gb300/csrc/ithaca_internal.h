@@ -113,7 +113,7 @@ struct Op {
   // Helmholtz kernel variant for FP32 hexahedra: 0 = shared-memory kernel (elem.cuh),
   // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA and a
   // TMA-staged geometry slab, 21/22 (31/32) = persistent pipelined pencil kernel with a
-  // double (single) geometry buffer (elem_pencil_pipe.cuh).
+  // double (single) geometry buffer (elem_pencil_pipe.cuh), 41/42 = 31/32 on packed pairs.
   int variant32 = 4;
   ~Op();
 };
