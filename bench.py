@@ -118,9 +118,10 @@ def fp32_kernel_name(variant, n, Q):
 
 
 # DRAM bytes (read + write) per element of one gathered FP32 apply, from the ncu capture
-# of the same kernel on 24^3 hexes (profiles/helm3_pipe_fp32_hex_p6_mesh24.md); the
-# traffic of a launch grows with the number of elements, so the bench scales it by E.
-TRAFFIC_PER_ELEMENT = {}
+# of the same kernel on 28^3 hexes (profiles/inner_loop_kernels_hex_p6_mesh28.md: 387.6 MB
+# per launch over 21,952 elements); a launch's traffic grows with the number of elements,
+# so the bench scales it by E. Keys: (kernel variant, modes, points).
+TRAFFIC_PER_ELEMENT = {(41, 7, 8): 17657}
 
 
 def workload_config(args, n, Q, E, N, ndir):

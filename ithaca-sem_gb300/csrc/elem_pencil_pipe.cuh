@@ -8,9 +8,10 @@
 //     buffer as soon as group i's metric stage has read it (half the shared memory, so
 //     about twice the resident CTAs, for a shorter lead); and
 //   * the gather of group i+1's input coefficients into registers: the signed l2g codes
-//     are loaded right after stage 1 of group i and the dependent x loads are issued
-//     after stage 5, so both latencies hide behind group i's arithmetic; the values are
-//     written to shared memory at stage 1 of iteration i+1, where the sign is applied.
+//     of group i+2 are loaded right after stage 1 of group i, and the dependent x loads
+//     of group i+1 (whose codes arrived a group earlier) are issued after stage 5, so
+//     both latencies hide behind arithmetic; the values are written to shared memory at
+//     stage 1 of iteration i+1, where the sign is applied.
 // The arithmetic per element is exactly that of helm3_pencil_kernel (same stages, same
 // tables, same summation order), so both kernels give bit-identical results.
 //
@@ -147,18 +148,20 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   }
   auto slot_ok = [&](int j) { return j < NPT - 1 || soff[j] >= 0; };
 
-  // prefetch registers: raw gathered values and a sign mask for the next group
+  // prefetch registers: raw gathered values and a sign mask for the next group, the
+  // signed l2g codes of the next group (code) and of the one after (code2): the codes
+  // are loaded two groups ahead, so the dependent value gather never waits on them
   T xv[NPT];
-  int code[NPT];
+  int code[NPT], code2[NPT] = {};
   unsigned neg = 0;
-  auto load_codes = [&](int grp) {
+  auto load_codes = [&](int grp, int (&dst)[NPT]) {
     const int e = grp * EB + el;
     const int* lp = l2g + (size_t)min(e, E - 1) * NM + t;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
-      code[j] = 0;
+      dst[j] = 0;
       if (e < E && slot_ok(j)) {
-        if constexpr (GATHER) code[j] = __ldg(lp + j * TPE);
+        if constexpr (GATHER) dst[j] = __ldg(lp + j * TPE);
       }
     }
   };
@@ -191,8 +194,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   }
   __syncthreads();
   if (tid == 0) issue_geometry(grp, 0);
-  load_codes(grp);
+  load_codes(grp, code);
   load_values(grp);
+  if (grp + (int)gridDim.x < ngroups) load_codes(grp + gridDim.x, code);
 
   for (int it = 0; grp < ngroups; ++it, grp += gridDim.x) {
     const int b = NB == 2 ? (it & 1) : 0;
@@ -208,7 +212,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 #pragma unroll
     for (int j = 0; j < NPT; ++j)
       if (slot_ok(j)) S0[soff[j]] = (neg >> j) & 1u ? -xv[j] : xv[j];
-    if (has_next) load_codes(nxt);
+    const int nxt2 = nxt + gridDim.x;
+    if (nxt2 < ngroups) load_codes(nxt2, code2);
     T gs[7];  // per-field scales of this element (half-precision geometry), used at stage 6
     if constexpr (HALF) {
       const float* sc = gscale + (size_t)min(e, E - 1) * 8;
@@ -326,8 +331,10 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         }
       }
     }
-    // the next group's gather: its codes have had stages 2-5 to arrive
+    // the next group's gather: its codes were loaded a whole group ago
     if (has_next) load_values(nxt);
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) code[j] = code2[j];  // the group after next becomes next
     // geometry of this group must have landed before the point-wise stage
     const bool ok = mbar_wait_bounded(bar + b, parity, kWaitCycles);
     if (!__syncthreads_and(ok)) {
