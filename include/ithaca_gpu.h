@@ -110,17 +110,25 @@ int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_dev
 /* PhysDeriv (Collections/PhysDeriv.cpp:270-415): physical -> d physical derivatives.
  * d2 may be NULL for quads. */
 int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, void* d2, int on_device);
+/* IProductWRTDerivBase (Collections/IProductWRTDerivBase.cpp:446-546): physical
+ * components in_k (E*Q^d each; in2 may be NULL for quads) -> coefficients
+ * out = sum_k (d phi / d x_k, in_k). */
+int ithaca_gpu_iproduct_deriv(ithaca_gpu_op* op, const void* in0, const void* in1, const void* in2, void* out,
+                              int on_device);
 /* Helmholtz (Collections/Helmholtz.cpp:391-430): out = lambda M in + L in, with
  * lambda = factors[eFactorLambda]. Arrays are double for FP64 ops and float for FP32. */
 int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device);
 /* Kernel choice for FP32 hexahedral Helmholtz applies (also used by the FP32 inner
  * solves of a system built on this operator): 0 = shared-memory sum-factorisation
  * kernel, 2 or 4 = register-pencil kernel with a TMA-staged geometry slab and that
- * many elements per CTA (default 4), 21 or 22 = the persistent pencil kernel that
+ * many elements per CTA, 21 or 22 = the persistent pencil kernel that
  * prefetches the next group of 1 or 2 elements (geometry by TMA into a double buffer,
  * gathered coefficients into registers) while computing the current one, 31 or 32 =
  * the same with a single geometry buffer refilled right after its metric stage, 41 or
- * 42 = 31 or 32 with the 1-D contractions on packed FP32 pairs (same results). */
+ * 42 = 31 or 32 with the 1-D contractions on packed FP32 pairs (same results; 41 is the
+ * default). Inside the mixed solver the pipelined variants (21-42) also write the rows of
+ * the global system that have a single local entry themselves, so the assembly that
+ * follows skips them. */
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
 /* Times every variant on the operator's own data and keeps the fastest, like
  * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
   block_partials<2>(v, partials, slots);
 }
 
-__device__ void scalars_iter_body(const double* partials, CgScalars* sc);
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart);
 
 // ---- assembly plan: rows grouped by their number of local entries ----------------
 // Class c < kAsmK holds the rows with exactly c + 1 local entries, stored ELL-style
@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(RT, RB / 152) assemble_dot_kernel(const AsmPla
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
                                                           T* __restrict__ s, const T* __restrict__ w, const int* skip,
                                                           double* partials, CgScalars* fuse_sc = nullptr,
-                                                          unsigned int* counter = nullptr) {
+                                                          unsigned int* counter = nullptr,
+                                                          const double* apart = nullptr, int napart = 0) {
   if (skip != nullptr && *skip) return;
   int c = 0;
   while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(RT, RB / 152) assemble_dot_kernel(const AsmPla
     __syncthreads();
     if (ticket == gridDim.x - 1) {
       __threadfence();
-      scalars_iter_body(partials, fuse_sc);
+      scalars_iter_body(partials, fuse_sc, apart, napart);
       if (threadIdx.x == 0) *counter = 0u;  // re-armed for the next iteration
     }
   }
@@ -360,15 +361,31 @@ __global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials
 
 // Reference loop tail (NekLinSysIterCG.cpp:219-261).
 __global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials, CgScalars* sc) {
-  scalars_iter_body(partials, sc);
+  scalars_iter_body(partials, sc, nullptr, 0);
 }
 
-__device__ void scalars_iter_body(const double* partials, CgScalars* sc) {
+// apart (napart entries): the element kernel's partials of s.w over the rows it
+// assembled itself, added to slot 3 (in a fixed order).
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart) {
   if (sc->done) return;
   const int slots[3] = {0, 1, 3};
   double red[3];
   reduce_slots<3>(partials, slots, red);
-  const double rho_new = red[0], eps = red[1], mu = red[2];
+  double mu_own = 0;
+  if (napart > 0) {
+    __shared__ double sm[RT];
+    double v = 0;
+    for (int i = threadIdx.x; i < napart; i += RT) v += __ldcg(apart + i);
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = RT / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+      __syncthreads();
+    }
+    mu_own = sm[0];
+    __syncthreads();
+  }
+  const double rho_new = red[0], eps = red[1], mu = red[2] + mu_own;
   if (threadIdx.x == 0) {
     sc->eps = eps;
     sc->mu = mu;
@@ -486,6 +503,13 @@ struct Cg {
   int* l2g = nullptr;     // signed-encoded
   int* rowptr = nullptr;  // N + 1
   AsmPlan plan{};           // assembly by row classes (see AsmPlan)
+  // owned rows (one local entry, free): written by the pipelined FP32 element kernel in
+  // the inner iteration, so that iteration's assembly (plan_own) leaves them out
+  bool own_ok = false;
+  int* l2g_own = nullptr;   // l2g with kOwnedBit on the owned rows' local entries
+  AsmPlan plan_own{};
+  double* opart = nullptr;  // per-CTA s.w partials of the element kernel
+  int opart_cap = 0;
   int* asm_rows = nullptr;  // N: global rows, grouped by class
   int* asm_cols = nullptr;  // ELL entries of the classes with at most kAsmK entries
   int* cols = nullptr;    // nloc, signed-encoded local index
@@ -517,6 +541,8 @@ Cg::~Cg() {
   cudaFree(l2g);
   cudaFree(rowptr);
   cudaFree(asm_rows);
+  cudaFree(l2g_own);
+  cudaFree(opart);
   cudaFree(asm_cols);
   cudaFree(cols);
   v64.release();
@@ -539,18 +565,24 @@ static const int* skip_ptr(Cg* cg) { return &cg->sc->done; }
 static const double* geo64(Cg* cg) { return cg->jgk64 ? cg->jgk64 : cg->op->jg64; }
 
 // Gather (signed l2g; ids < ndir read as zero when zero_dir) + element Helmholtz into v.yloc.
+// With own != nullptr (FP32) the pipelined kernels also assemble the owned rows into
+// own->s and report how many partials they wrote in own->ctas (-1: not done, the caller
+// assembles every row).
 template <typename T>
 static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda, const T* lam_ptr, const T* xin,
-                         cudaStream_t s, bool zero_dir, const int* skip) {
+                         cudaStream_t s, bool zero_dir, const int* skip, OwnedRows* own = nullptr) {
   Op* op = cg->op;
   bool ok;
+  if (own != nullptr) own->ctas = -1;
   if constexpr (sizeof(T) == 4) {
+    const int* map = own != nullptr ? cg->l2g_own : cg->l2g;
     if (cg->geo16)
       ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
-                                  v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
+                                  v.yloc, map, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else if (op->dim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,
-                                     xin, v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
+                                     xin, v.yloc, own != nullptr && op->variant32 >= 21 ? map : cg->l2g,
+                                     zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else
       ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
                                zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
@@ -578,9 +610,22 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   else
     pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
                                            cg->partials);
-  launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg));
-  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, skip_ptr(cg),
-                                           cg->partials, cg->sc, cg->counter);
+  OwnedRows own;
+  if constexpr (sizeof(T) == 4) {
+    own.s = v.s;
+    own.part = cg->opart;
+  }
+  const bool try_own = sizeof(T) == 4 && cg->own_ok;
+  launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg), try_own ? &own : nullptr);
+  if (try_own && own.ctas >= 0) {  // the element kernel wrote the owned rows of s
+    if (own.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
+    assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+                                             v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
+                                             cg->opart, own.ctas);
+  } else {
+    assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+                                             v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter);
+  }
   cg->op->ctx->launches += 2;
 }
 
@@ -902,22 +947,41 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       }
     }
     // CTAs per class in proportion to its entries, at least one for a non-empty class
-    {
+    auto split_ctas = [&](AsmPlan& P, const long long* ent) {
       long long total = 0;
       int nonempty = 0;
       for (int c = 0; c <= kAsmK; ++c) {
-        total += entries[c];
-        nonempty += plan.n[c] > 0;
+        total += ent[c];
+        nonempty += P.n[c] > 0;
       }
       int share[kAsmK + 1], used = 0, big = 0;
       for (int c = 0; c <= kAsmK; ++c) {
-        share[c] = plan.n[c] > 0 ? std::max(1, (int)((double)(RB - nonempty) * entries[c] / std::max(total, 1LL))) : 0;
+        share[c] = P.n[c] > 0 ? std::max(1, (int)((double)(RB - nonempty) * ent[c] / std::max(total, 1LL))) : 0;
         used += share[c];
-        if (entries[c] > entries[big]) big = c;
+        if (ent[c] > ent[big]) big = c;
       }
       share[big] += RB - used;  // the rounding remainder goes to the largest class
-      plan.cta0[0] = 0;
-      for (int c = 0; c <= kAsmK; ++c) plan.cta0[c + 1] = plan.cta0[c] + share[c];
+      P.cta0[0] = 0;
+      for (int c = 0; c <= kAsmK; ++c) P.cta0[c + 1] = P.cta0[c] + share[c];
+    };
+    split_ctas(plan, entries);
+    // Owned rows: the free rows with a single local entry. The inner FP32 iteration's
+    // element kernel writes them, so its plan keeps only class 0's Dirichlet rows (which
+    // lead the class and are skipped) and gives class 0's CTAs to the other classes.
+    const bool own_ok = nglobal < kOwnedBit;
+    std::vector<int> code_own;
+    AsmPlan plan_own = plan;
+    if (own_ok) {
+      code_own = code;
+      for (size_t l = 0; l < nloc; ++l) {
+        const int g = l2g[l];
+        if (g >= ndir && cnt[g + 1] - cnt[g] == 1) code_own[l] = sign[l] > 0 ? (g | kOwnedBit) : ~(g | kOwnedBit);
+      }
+      plan_own.n[0] = plan.ndir[0];
+      long long ent_own[kAsmK + 1];
+      for (int c = 0; c <= kAsmK; ++c) ent_own[c] = entries[c];
+      ent_own[0] = plan.ndir[0];
+      split_ctas(plan_own, ent_own);
     }
     auto cg = std::make_unique<ithaca_gpu_cg>();
     cg->op = op;
@@ -929,6 +993,17 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     ITHACA_CUDA(cudaMalloc(&cg->rowptr, sizeof(int) * (nglobal + 1)));
     ITHACA_CUDA(cudaMalloc(&cg->cols, sizeof(int) * nloc));
     ITHACA_CUDA(cudaMalloc(&cg->asm_rows, sizeof(int) * nglobal));
+    if (own_ok) {
+      int dev = 0, sms = 0;
+      ITHACA_CUDA(cudaGetDevice(&dev));
+      ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      cg->opart_cap = sms * 32;  // at most 32 resident CTAs per SM
+      ITHACA_CUDA(cudaMalloc(&cg->l2g_own, sizeof(int) * nloc));
+      ITHACA_CUDA(cudaMalloc(&cg->opart, sizeof(double) * cg->opart_cap));
+      ITHACA_CUDA(cudaMemcpyAsync(cg->l2g_own, code_own.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+      cg->own_ok = true;
+      cg->plan_own = plan_own;
+    }
     ITHACA_CUDA(cudaMalloc(&cg->asm_cols, sizeof(int) * asm_cols.size()));
     ITHACA_CUDA(cudaMemcpyAsync(cg->l2g, code.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
     ITHACA_CUDA(cudaMemcpyAsync(cg->rowptr, cnt.data(), sizeof(int) * (nglobal + 1), cudaMemcpyHostToDevice, s));

@@ -28,7 +28,7 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool PACK = false>
 static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T lambda, const T* in, T* out,
                     const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s,
-                    const float* gscale = nullptr) {
+                    const float* gscale = nullptr, OwnedRows* own = nullptr) {
   PTabs<T, N, Q> tab;
   for (int i = 0; i < N * Q; ++i) tab.B[i] = (T)hB[i];
   for (int i = 0; i < Q * Q; ++i) tab.D[i] = (T)hD[i];
@@ -58,7 +58,15 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
   }
   const int ngroups = (E + EB - 1) / EB;
   const dim3 block(Q * Q, EB), grid(std::min(ngroups, slots[gi]));
-  k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale);
+  T* sown = nullptr;
+  double* opart = nullptr;
+  if (own != nullptr && l2g != nullptr) {
+    sown = own->s;
+    opart = own->part;
+    own->ctas = (int)grid.x;
+  }
+  k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale, sown,
+                                    opart);
 }
 
 }  // namespace dev
@@ -67,12 +75,12 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
 // with per-element, per-field FP32 scales (8 floats per element).
 bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
                             const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,
-                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s) {
+                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s, OwnedRows* own) {
   const __half* jg = static_cast<const __half*>(jg16);
 #define X(NN, QQ)                                                                                          \
   if (n == NN && Q == QQ) {                                                                                \
     dev::pipe_nq<float, NN, QQ, 1, 1, __half, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,   \
-                                                    err, s, gscale);                                       \
+                                                    err, s, gscale, own);                                  \
     return true;                                                                                           \
   }
   X(2, 3) X(3, 4) X(4, 5) X(5, 6) X(6, 7) X(7, 8) X(8, 9) X(9, 10) X(10, 11)
@@ -87,7 +95,8 @@ bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double*
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
-                        cudaStream_t s) {
+                        cudaStream_t s, OwnedRows* own) {
+  if (own != nullptr) own->ctas = -1;  // set by the pipelined kernels only
 #define X(NN, QQ)                                                                                          \
   if (n == NN && Q == QQ) {                                                                                \
     if (variant == 4)                                                                                      \
@@ -95,17 +104,17 @@ bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, cons
     else if (variant == 2)                                                                                 \
       dev::pencil_nq<T, NN, QQ, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);      \
     else if (variant == 21)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 1, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+      dev::pipe_nq<T, NN, QQ, 1, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own);     \
     else if (variant == 22)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 2, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+      dev::pipe_nq<T, NN, QQ, 2, 2>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own);     \
     else if (variant == 31)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 1, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+      dev::pipe_nq<T, NN, QQ, 1, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own);     \
     else if (variant == 32)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 2, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s);     \
+      dev::pipe_nq<T, NN, QQ, 2, 1>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own);     \
     else if (variant == 41)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 1, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s); \
+      dev::pipe_nq<T, NN, QQ, 1, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own); \
     else if (variant == 42)                                                                                \
-      dev::pipe_nq<T, NN, QQ, 2, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s); \
+      dev::pipe_nq<T, NN, QQ, 2, 1, T, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s, nullptr, own); \
     else                                                                                                   \
       return false;                                                                                        \
     return true;                                                                                           \
@@ -117,6 +126,6 @@ bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, cons
 
 template bool launch_helm_pencil<float>(int, int, int, int, const double*, const double*, const float*, float,
                                         const float*, float*, const int*, int, const int*, const float*, int*,
-                                        cudaStream_t);
+                                        cudaStream_t, OwnedRows*);
 
 }  // namespace ithaca

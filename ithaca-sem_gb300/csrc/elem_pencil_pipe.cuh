@@ -93,7 +93,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
                                                                const T* __restrict__ lam_ptr, int* __restrict__ err,
-                                                               const float* __restrict__ gscale = nullptr) {
+                                                               const float* __restrict__ gscale = nullptr,
+                                                               T* __restrict__ sown = nullptr,
+                                                               double* __restrict__ opart = nullptr) {
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
   constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
@@ -154,6 +156,12 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   T xv[NPT];
   int code[NPT], code2[NPT] = {};
   unsigned neg = 0;
+  // owned rows (single local entry, flagged by kOwnedBit in the code): the next group's
+  // global ids and mask, and the current group's ids, signs, mask and gathered values
+  int gnext[NPT], gcur[NPT];
+  T wcur[NPT];
+  unsigned own_next = 0, own_cur = 0, neg_cur = 0;
+  T owned_sw = 0;  // this thread's share of s.w over the owned rows it wrote
   auto load_codes = [&](int grp, int (&dst)[NPT]) {
     const int e = grp * EB + el;
     const int* lp = l2g + (size_t)min(e, E - 1) * NM + t;
@@ -169,15 +177,20 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     const int e = grp * EB + el;
     const T* ip = in + (size_t)min(e, E - 1) * NM + t;
     neg = 0;
+    own_next = 0;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
       xv[j] = T(0);
+      gnext[j] = 0;
       if (e < E && slot_ok(j)) {
         if constexpr (GATHER) {
           const int c = code[j];
-          const int g = c >= 0 ? c : ~c;
+          const int ca = c >= 0 ? c : ~c;
+          const int g = ca & (kOwnedBit - 1);
           if (g >= ndir) xv[j] = in[g];
           neg |= (c < 0 ? 1u : 0u) << j;
+          own_next |= (ca & kOwnedBit ? 1u : 0u) << j;
+          gnext[j] = g;
         } else {
           xv[j] = ip[j * TPE];
         }
@@ -212,6 +225,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 #pragma unroll
     for (int j = 0; j < NPT; ++j)
       if (slot_ok(j)) S0[soff[j]] = (neg >> j) & 1u ? -xv[j] : xv[j];
+    if (sown != nullptr) {  // keep what the output stage needs for the owned rows
+      own_cur = own_next;
+      neg_cur = neg;
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+        gcur[j] = gnext[j];
+        wcur[j] = xv[j];
+      }
+    }
     const int nxt2 = nxt + gridDim.x;
     if (nxt2 < ngroups) load_codes(nxt2, code2);
     T gs[7];  // per-field scales of this element (half-precision geometry), used at stage 6
@@ -490,12 +512,35 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     if (active) {
       T* op = out + (size_t)e * NM + t;
 #pragma unroll
-      for (int j = 0; j < NPT; ++j)
-        if (slot_ok(j)) op[j * TPE] = S1[soff[j]];
+      for (int j = 0; j < NPT; ++j) {
+        if (!slot_ok(j)) continue;
+        const T val = S1[soff[j]];
+        if (sown != nullptr && ((own_cur >> j) & 1u)) {  // owned row: assembled here
+          const T sv = (neg_cur >> j) & 1u ? -val : val;
+          sown[gcur[j]] = sv;
+          owned_sw = fma(sv, wcur[j], owned_sw);
+        } else {
+          op[j * TPE] = val;
+        }
+      }
     }
     // S0 and S1 are rewritten by the next group's stages 1-2; with NB = 2 the geometry
     // buffer read here is refilled by the copy issued at the top of the iteration after next
     __syncthreads();
+  }
+  if (opart != nullptr) {  // this CTA's s.w over its owned rows, summed in FP64
+    double v = (double)owned_sw;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    double* red = reinterpret_cast<double*>(work);  // the work area is free after the loop
+    constexpr int NW = (Q * Q * EB + 31) / 32;
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+      double sum = 0;
+      for (int w = 0; w < NW; ++w) sum += red[w];
+      opart[blockIdx.x] = sum;
+    }
   }
 }
 

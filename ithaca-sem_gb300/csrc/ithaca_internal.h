@@ -114,7 +114,7 @@ struct Op {
   // 2 or 4 = pencil kernel (elem_pencil.cuh) with that many elements per CTA and a
   // TMA-staged geometry slab, 21/22 (31/32) = persistent pipelined pencil kernel with a
   // double (single) geometry buffer (elem_pencil_pipe.cuh), 41/42 = 31/32 on packed pairs.
-  int variant32 = 4;
+  int variant32 = 41;
   ~Op();
 };
 
@@ -122,14 +122,27 @@ struct Op {
 // leaves the allocation.
 constexpr size_t kGeoPad = 64;
 
+// Rows of the global system with a single local entry ("owned" rows, flagged by bit 30
+// of the gather index, see kOwnedBit) can be written by the gathered element kernel
+// itself: s[g] = sign * value, with the partial s.w of each CTA in part[cta]. The
+// pipelined kernels (variants 21-42 and the 16-bit-geometry kernel) accept this; the
+// launcher reports in *ctas how many partials it wrote (-1 where it could not).
+constexpr int kOwnedBit = 1 << 30;
+struct OwnedRows {
+  float* s = nullptr;
+  double* part = nullptr;
+  int ctas = -1;
+};
+
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
-                        cudaStream_t s);
+                        cudaStream_t s, OwnedRows* own = nullptr);
 // Half-precision geometry (E x 7 x Q^3 halves) with 8 FP32 scales per element; FP32 hexes.
 bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
                             const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,
-                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s);
+                            const int* skip, const float* lam_ptr, int* err, cudaStream_t s,
+                            OwnedRows* own = nullptr);
 
 void retain_op(Op* op);
 void release_op(Op* op);    // frees the operator (and releases its context) at zero
@@ -151,6 +164,8 @@ struct ElemApi {
   static bool deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
                     cudaStream_t s);
   static bool diag(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+  static bool iprd(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df, const T* in0,
+                   const T* in1, const T* in2, T* out, cudaStream_t s);
 };
 
 template <typename T>
@@ -178,6 +193,12 @@ inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T
                              T* d0, T* d1, T* d2, cudaStream_t s) {
   return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
                   : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
+}
+template <typename T>
+inline bool launch_iproduct_deriv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df,
+                                  const T* in0, const T* in1, const T* in2, T* out, cudaStream_t s) {
+  return dim == 2 ? ElemApi<T, 2>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s)
+                  : ElemApi<T, 3>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s);
 }
 template <typename T>
 inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,

@@ -107,6 +107,26 @@ def test_mixed_curved_hex_inner_tolerances(ctx, inner_tol):
     assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
 
 
+@pytest.mark.parametrize("variant", [4, 21, 31, 41, 42])
+def test_mixed_kernel_variants_curved_hex(ctx, variant):
+    """Mixed solves with each FP32 hex kernel; the pipelined ones (21-42) also assemble
+    the single-entry rows inside the element kernel. All reach the FP64 residual, agree
+    with the FP64 solve and need the same number of inner iterations within a few (only
+    the summation order of s.w differs)."""
+    c = hex_case(4, 3, 3, 6, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(19).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, _ = sys_.solve(1.0, rhs, tol=1e-12)
+    coll.set_variant(4)
+    _, ref = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    coll.set_variant(variant)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+    assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
+    assert abs(res.iterations - ref.iterations) <= 4, (res.iterations, ref.iterations)
+
+
 @pytest.mark.parametrize("inner_tol", [1e-2, 1e-4])
 def test_mixed_geo16_curved_hex(ctx, inner_tol):
     """FP32 inner solves on 16-bit (per-element scaled) geometry inside FP64 refinement:
