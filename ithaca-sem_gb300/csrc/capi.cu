@@ -401,6 +401,33 @@ int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, 
   });
 }
 
+int ithaca_gpu_iproduct_deriv(ithaca_gpu_op* op, const void* in0, const void* in1, const void* in2, void* out,
+                              int on_device) {
+  return guarded([&] {
+    require(op && in0 && in1 && out, "null argument");
+    require(op->dim == 2 || in2, "in2 is required for hexahedra");
+    StreamOrder order_(op->ctx);
+    Ctx* c = op->ctx;
+    const size_t es = elt(op), nq = (size_t)op->E * op->nq, nm = (size_t)op->E * op->nm;
+    const void* di[3] = {to_device(c, 0, in0, es * nq, on_device), to_device(c, 1, in1, es * nq, on_device),
+                         op->dim == 3 ? to_device(c, 2, in2, es * nq, on_device) : nullptr};
+    void* dout = out_buffer(c, 3, out, es * nm, on_device);
+    bool ok;
+    if (op->precision == ITHACA_GPU_FP64)
+      ok = launch_iproduct_deriv<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
+                                         op->df64, (const double*)di[0], (const double*)di[1], (const double*)di[2],
+                                         (double*)dout, c->stream);
+    else
+      ok = launch_iproduct_deriv<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+                                        op->df32, (const float*)di[0], (const float*)di[1], (const float*)di[2],
+                                        (float*)dout, c->stream);
+    if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTDerivBase: (modes, points) combination not built");
+    c->launches++;
+    from_device(c, out, dout, es * nm, on_device);
+    finish(c, on_device);
+  });
+}
+
 int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void* out, int on_device) {
   return guarded([&] {
     require(op && in && out, "null argument");

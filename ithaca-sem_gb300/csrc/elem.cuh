@@ -322,6 +322,76 @@ __global__ void __launch_bounds__(256) deriv_kernel(const T* __restrict__ in, T*
   }
 }
 
+// IProductWRTDerivBase: out = sum_k (d phi / d x_k, in_k) on each element, i.e. with
+// F_j = J w sum_k (d xi_j / d x_k) in_k at the points, out = sum_j B^T D_j^T F_j (the
+// reference's IProductWRTDerivBase_IterPerExp, Collections/IProductWRTDerivBase.cpp:446-546:
+// tmp[j] = sum_k derivFac[j + k d] in[k], times jac, then StdExpansion::IProductWRTDerivBase
+// per direction). Geometry: df as deriv_kernel reads it, J w as field 0 of jg.
+template <typename T, int DIM, int N, int Q, int TPE, bool DEF>
+__global__ void __launch_bounds__(256) iprd_kernel(const T* __restrict__ in0, const T* __restrict__ in1,
+                                                    const T* __restrict__ in2, T* __restrict__ out,
+                                                    const T* __restrict__ tab, const T* __restrict__ jg,
+                                                    const T* __restrict__ df, int E) {
+  using L = Layout<T, DIM, N, Q>;
+  constexpr int NM = L::NM, NQ = L::NQ, NG = n_jg(DIM), ND = DIM * DIM;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s = reinterpret_cast<T*>(smem_raw);
+  load_tables(s, tab, tables_size(N, Q));
+  const T* sD = s + off_D(N, Q);
+  const T* sw = s + off_w(N, Q);
+  T* U = s + L::TS + threadIdx.y * L::SLAB;
+  T* F0 = U + NQ;
+  T* F1 = F0 + NQ;
+  T* F2 = F1 + NQ;  // DIM 3 only
+  T* C = DIM == 2 ? F1 : F2;
+  const int e = blockIdx.x * blockDim.y + threadIdx.y;
+  const bool active = e < E;
+  const int ee = active ? e : E - 1;
+  const int t = threadIdx.x;
+  const T* gbase = jg + (size_t)ee * NG * (DEF ? NQ : 1);
+  const T* fbase = df + (size_t)ee * ND * (DEF ? NQ : 1);
+  const T* ins[3] = {in0, in1, in2};
+  __syncthreads();  // tables
+  for (int p = t; p < NQ; p += TPE) {
+    const T jw = DEF ? gbase[p] : gbase[0] * wprod<T, DIM, Q>(sw, p);
+    T f[3];
+#pragma unroll
+    for (int kx = 0; kx < DIM; ++kx) f[kx] = ins[kx][(size_t)ee * NQ + p];
+    T* Fs[3] = {F0, F1, F2};
+#pragma unroll
+    for (int jx = 0; jx < DIM; ++jx) {
+      T v = 0;
+#pragma unroll
+      for (int kx = 0; kx < DIM; ++kx) {
+        const T d = DEF ? fbase[(kx * DIM + jx) * NQ + p] : fbase[kx * DIM + jx];
+        v = fma(d, f[kx], v);
+      }
+      Fs[jx][p] = jw * v;
+    }
+  }
+  __syncthreads();
+  for (int p = t; p < NQ; p += TPE) {
+    const int i = p % Q, j = (p / Q) % Q;
+    T v = 0;
+#pragma unroll
+    for (int a = 0; a < Q; ++a) {
+      v = fma(sD[i * Q + a], F0[p + (a - i)], v);
+      v = fma(sD[j * Q + a], F1[p + (a - j) * Q], v);
+    }
+    if constexpr (DIM == 3) {
+      const int k = p / (Q * Q);
+#pragma unroll
+      for (int a = 0; a < Q; ++a) v = fma(sD[k * Q + a], F2[p + (a - k) * Q * Q], v);
+    }
+    U[p] = v;
+  }
+  __syncthreads();
+  ipr_stages<T, DIM, N, Q>(U, F0, F1, C, s + off_Bt(N, Q), t, TPE);
+  __syncthreads();
+  if (active)
+    for (int m = t; m < NM; m += TPE) out[(size_t)e * NM + m] = C[m];
+}
+
 // Diagonal of the element Helmholtz matrix: for mode m = (p, q[, r]),
 //   lambda sum Jw phi_m^2 + sum_ab sum G_ab (d_a phi_m)(d_b phi_m),
 // every term a separable weighted inner product with squared / mixed 1-D tables.

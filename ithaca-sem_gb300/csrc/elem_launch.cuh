@@ -61,6 +61,15 @@ void deriv_nq(int E, int deformed, const T* tab, const T* df, const T* in, T* d0
 }
 
 template <typename T, int DIM, int N, int Q>
+void iprd_nq(int E, int deformed, const T* tab, const T* jg, const T* df, const T* in0, const T* in1, const T* in2,
+             T* out, cudaStream_t s) {
+  using C = Cfg<T, DIM, N, Q>;
+  auto k = deformed ? iprd_kernel<T, DIM, N, Q, C::S::TPE, true> : iprd_kernel<T, DIM, N, Q, C::S::TPE, false>;
+  C::prep(k);
+  k<<<C::grid(E), C::block(), C::smem(), s>>>(in0, in1, in2, out, tab, jg, df, E);
+}
+
+template <typename T, int DIM, int N, int Q>
 void diag_nq(int E, int deformed, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s) {
   using C = Cfg<T, DIM, N, Q>;
   auto k = deformed ? diag_kernel<T, DIM, N, Q, C::S::TPE, true> : diag_kernel<T, DIM, N, Q, C::S::TPE, false>;
@@ -120,6 +129,19 @@ bool ElemApi<T, DIM>::deriv(int n, int Q, int E, int deformed, const T* tab, con
   if (n == NN && Q == QQ) {                                                      \
     dev::deriv_nq<T, DIM, NN, QQ>(E, deformed, tab, df, in, d0, d1, d2, s);      \
     return true;                                                                 \
+  }
+  ITHACA_FOR_EACH_NQ(X)
+#undef X
+  return false;
+}
+
+template <typename T, int DIM>
+bool ElemApi<T, DIM>::iprd(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df, const T* in0,
+                           const T* in1, const T* in2, T* out, cudaStream_t s) {
+#define X(NN, QQ)                                                                        \
+  if (n == NN && Q == QQ) {                                                              \
+    dev::iprd_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, df, in0, in1, in2, out, s);      \
+    return true;                                                                         \
   }
   ITHACA_FOR_EACH_NQ(X)
 #undef X

@@ -11,6 +11,7 @@ Each function restates the composition of the reference MatrixFree kernels:
   iproduct   MatrixFreeOps/IProductKernels.hpp:76-133 (quad), :236-314 (hex)
   physderiv  MatrixFreeOps/PhysDerivKernels.hpp:39-151 (quad), :219-374 (hex)
   helmholtz  MatrixFreeOps/Helmholtz.h:137-275 (quad), :763-993 (hex)
+  iproduct_deriv  Collections/IProductWRTDerivBase.cpp:446-546 (IterPerExp)
 with einsum in place of the SIMD loops (same sums, different summation order).
 """
 import numpy as np
@@ -96,6 +97,26 @@ def metric(df, dim, E, nq):
             m[(a, b)] = sum(dfp[k * dim + a] * dfp[k * dim + b] for k in range(dim))
             m[(b, a)] = m[(a, b)]
     return m
+
+
+def iproduct_deriv(basis, dim, jac, df, comps):
+    """sum_k (d phi / d x_k, comps[k]): IProductWRTDerivBase_IterPerExp
+    (Collections/IProductWRTDerivBase.cpp:446-546) forms tmp[j] = sum_k derivFac[j + k d]
+    comps[k] (derivFac[j + k d] = df[k*d + j] = d xi_j / d x_k), multiplies by jac and
+    takes StdExpansion::IProductWRTDerivBase(j, .), the inner product with the derivative
+    table DB in direction j."""
+    b = basis
+    nq = b.Q ** dim
+    E = np.asarray(comps[0]).size // nq
+    J = _geo_pts(jac, E, nq)
+    dfp = _df_pts(df, dim, E, nq)
+    out = 0
+    for j in range(dim):
+        t = sum(dfp[k * dim + j] * np.asarray(comps[k]).reshape(E, nq) for k in range(dim))
+        tables = [b.B2] * dim
+        tables[j] = b.DB2
+        out = out + iproduct_tables(tables, b.w, dim, J * t)
+    return out
 
 
 def helmholtz(basis, dim, jac, df, lam, coeffs):

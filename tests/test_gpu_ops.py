@@ -78,6 +78,36 @@ def test_bwd_iprod_deriv_fp64(ctx, shape, n, deformed):
         assert rel_err(d, r) < TOL64
 
 
+@pytest.mark.parametrize("shape,n,deformed", _cases())
+def test_iproduct_deriv_fp64(ctx, shape, n, deformed):
+    """IProductWRTDerivBase against the oracle, and of the physical gradient against the
+    Laplacian (lambda = 0 Helmholtz) of the same coefficients."""
+    c = _make(shape, n, deformed)
+    coll = _coll(ctx, c)
+    rng = np.random.default_rng(5)
+    comps = [rng.uniform(-1, 1, c.E * c.nq) for _ in range(c.dim)]
+    out = coll.iproduct_deriv(comps)
+    ref = oops.iproduct_deriv(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, comps)
+    assert rel_err(out, ref) < TOL64
+    u = rng.uniform(-1, 1, c.E * c.nm)
+    lap = coll.iproduct_deriv(coll.physderiv(coll.bwdtrans(u)))
+    assert rel_err(lap, coll.helmholtz(0.0, u)) < TOL64
+
+
+@pytest.mark.parametrize("shape,n", [("quad", 7), ("hex", 6)])
+def test_iproduct_deriv_fp32_and_device(ctx, shape, n):
+    torch = pytest.importorskip("torch")
+    c = _make(shape, n, True)
+    coll = _coll(ctx, c, "fp32")
+    rng = np.random.default_rng(6)
+    comps = [rng.uniform(-1, 1, c.E * c.nq) for _ in range(c.dim)]
+    ref = oops.iproduct_deriv(c.basis, c.dim, c.jac.reshape(c.E, -1), c.df, comps)
+    dev = [torch.from_numpy(x.astype(np.float32)).cuda() for x in comps]
+    out = coll.iproduct_deriv(dev)
+    torch.cuda.synchronize()
+    assert rel_err(out.cpu().numpy(), ref) < TOL32
+
+
 @pytest.mark.parametrize("shape,n,deformed", [("quad", 7, True), ("quad", 9, True), ("hex", 5, True),
                                               ("hex", 7, True), ("hex", 9, True)])
 def test_helmholtz_fp32(ctx, shape, n, deformed):

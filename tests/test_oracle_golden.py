@@ -111,3 +111,17 @@ def test_bilinear_jacobian_is_analytic():
         dx1 = 0.25 * ((1 - xi0)[..., None] * (v[3] - v[0]) + (1 + xi0)[..., None] * (v[2] - v[1]))
         det = dx0[..., 0] * dx1[..., 1] - dx0[..., 1] * dx1[..., 0]
         assert np.max(np.abs(jac[e] - det.reshape(-1))) < 1e-13
+
+
+@pytest.mark.parametrize("fname,n,dim", [("mesh_quad.npz", 7, 2), ("mesh_hex.npz", 5, 3)])
+def test_iproduct_deriv_composes_the_laplacian(fname, n, dim):
+    """IProductWRTDerivBase of the physical gradient is the Laplacian part of the
+    Helmholtz operator, which the golden vectors pin to the compiled reference kernels:
+    sum_k (d phi / d x_k, d u / d x_k) = L u (lambda = 0)."""
+    g = load(fname)
+    b = obasis.Basis1D(n, n + 1)
+    E = g["X"].shape[1]
+    jac = g["jac"].reshape(E, -1)
+    grads = oops.physderiv(b, dim, g["df"], oops.bwdtrans(b, dim, g["u"]))
+    lap = oops.iproduct_deriv(b, dim, jac, g["df"], grads)
+    assert rel_err(lap, oops.helmholtz(b, dim, jac, g["df"], 0.0, g["u"])) < 1e-12
