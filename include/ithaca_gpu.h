@@ -191,6 +191,14 @@ int ithaca_gpu_cg_diagonal(ithaca_gpu_cg* cg, double lambda, double* diag, int o
  * coefficient space (E*n^d): rhs = Assemble(-IProductWRTBase(f)), CG, GlobalToLocal. */
 int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
+/* The same with Dirichlet data: dirichlet holds the ndir global coefficients of the
+ * Dirichlet dofs (numbered first), e.g. the boundary-constrained projections of the
+ * boundary condition that the reference's boundary expansions hold. The solve lifts
+ * them (rhs_F -= (A x_D)_F, ContField.cpp:908-930) and they are the Dirichlet entries
+ * of the result; dirichlet == NULL is homogeneous data. */
+int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const double* forcing, const double* dirichlet,
+                                   double* out_local, const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res,
+                                   int on_device);
 
 /* ---- batched parametric solves ----
  * Many independent C0 Helmholtz systems (own mesh, order, lambda, rhs; homogeneous

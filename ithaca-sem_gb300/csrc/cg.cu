@@ -450,6 +450,12 @@ __global__ void __launch_bounds__(RT) axpy_f32_kernel(int N, int ndir, const dou
   for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) x[g] += sc * (double)d32[g];
 }
 
+// b[g] -= y[g] on the free dofs g >= ndir.
+__global__ void __launch_bounds__(RT) sub_free_kernel(int N, int ndir, const double* __restrict__ y,
+                                                      double* __restrict__ b) {
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) b[g] -= y[g];
+}
+
 __global__ void __launch_bounds__(RT) inv_kernel(int n, const double* __restrict__ d, double* __restrict__ dinv,
                                                  float* __restrict__ dinv32, int ndir) {
   for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += RB * RT) {
@@ -1144,6 +1150,12 @@ int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, dou
 
 int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing, double* out_local,
                          const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device) {
+  return ithaca_gpu_helmsolve_dirichlet(cg, lambda, forcing, nullptr, out_local, opts, res, on_device);
+}
+
+int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const double* forcing, const double* dirichlet,
+                                   double* out_local, const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res,
+                                   int on_device) {
   return cg_guarded([&] {
     req(cg && forcing && out_local, "null argument");
     StreamOrder order_(cg->op->ctx);
@@ -1166,9 +1178,28 @@ int ithaca_gpu_helmsolve(ithaca_gpu_cg* cg, double lambda, const double* forcing
     assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
                                                   nullptr, nullptr);
     c->launches += 3;
+    const double* dvals = nullptr;  // Dirichlet values on the device (ndir entries)
+    if (dirichlet != nullptr && cg->ndir > 0) {
+      // lift (ContField.cpp:908-930): x_D = the given boundary values, b_F -= (A x_D)_F
+      double* xd = cg->v64.p;  // scratch until the solve
+      ITHACA_CUDA(cudaMemsetAsync(xd, 0, sizeof(double) * cg->N, s));
+      ITHACA_CUDA(cudaMemcpyAsync(xd, dirichlet, sizeof(double) * cg->ndir,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+      launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, xd, s, false, nullptr);
+      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
+                                                    cg->cols, cg->v64.yloc, cg->v64.s, nullptr, nullptr, nullptr);
+      sub_free_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.s, cg->v64.b);
+      c->launches += 2;
+      double* keep = (double*)c->stage_ptr(2, sizeof(double) * cg->ndir);  // the solve reuses v64.p
+      ITHACA_CUDA(cudaMemcpyAsync(keep, xd, sizeof(double) * cg->ndir, cudaMemcpyDeviceToDevice, s));
+      dvals = keep;
+    }
     solve_impl(cg, lambda, o, res);
-    // homogeneous Dirichlet values, then GlobalToLocal
-    ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->ndir, s));
+    // Dirichlet values (zero, or the given ones), then GlobalToLocal
+    if (dvals != nullptr)
+      ITHACA_CUDA(cudaMemcpyAsync(cg->v64.x, dvals, sizeof(double) * cg->ndir, cudaMemcpyDeviceToDevice, s));
+    else
+      ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->ndir, s));
     double* dout = on_device ? out_local : (double*)c->stage_ptr(1, sizeof(double) * nloc);
     g2l_kernel<<<RB, RT, 0, s>>>(nloc, cg->l2g, cg->v64.x, dout);
     c->launches++;

@@ -69,6 +69,7 @@ SIGNATURES = {
     "ithaca_gpu_bwdtrans": [_vp, _vp, _vp, _i],
     "ithaca_gpu_iproduct": [_vp, _vp, _vp, _i],
     "ithaca_gpu_physderiv": [_vp, _vp, _vp, _vp, _vp, _i],
+    "ithaca_gpu_iproduct_deriv": [_vp, _vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_helmholtz": [_vp, _d, _vp, _vp, _i],
     "ithaca_gpu_helmholtz_diag": [_vp, _d, _vp, _i],
     "ithaca_gpu_op_set_variant": [_vp, _i],
@@ -82,6 +83,7 @@ SIGNATURES = {
     "ithaca_gpu_cg_assemble": [_vp, _vp, _vp, _i],
     "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_helmsolve_dirichlet": [_vp, _d, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_batch_create": [_vp, _i, _i, ctypes.POINTER(SolveDesc), _pp],
     "ithaca_gpu_batch_destroy": [_vp],
     "ithaca_gpu_batch_solve": [_vp, ctypes.POINTER(CgOpts), _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)],

@@ -180,6 +180,23 @@ class Collection:
         C.call("ithaca_gpu_physderiv", self.handle, pi, ps[0], ps[1], ps[2], d)
         return outs
 
+    def iproduct_deriv(self, ins, out=None):
+        """IProductWRTDerivBase: sum_k (d phi / d x_k, ins[k]) for the d physical components."""
+        ins = list(ins)
+        if len(ins) != self.dim:
+            raise ValueError(f"expected {self.dim} components")
+        out = self._out(out, self.E * self.nm, ins[0])
+        _same_side(*ins, out)
+        ps = []
+        d = 0
+        for a in ins:
+            p, d = _ptr(a, self.dtype if not _is_device(a) else None)
+            ps.append(p)
+        ps += [None] * (3 - len(ps))
+        po, _ = _ptr(out)
+        C.call("ithaca_gpu_iproduct_deriv", self.handle, ps[0], ps[1], ps[2], po, d)
+        return out
+
     def helmholtz(self, lam, inp, out=None):
         out = self._out(out, self.E * self.nm, inp)
         pi, d = _ptr(inp, self.dtype if not _is_device(inp) else None)
@@ -337,14 +354,24 @@ class GlobalLinSysIterativeFullGPU:
         C.call("ithaca_gpu_cg_diagonal", self.handle, ctypes.c_double(lam), po, d)
         return out
 
-    def helmsolve(self, lam, forcing, out=None, **kw):
+    def helmsolve(self, lam, forcing, out=None, dirichlet=None, **kw):
+        """ContField::v_HelmSolve: forcing at the quadrature points -> local coefficients.
+        dirichlet: the ndir Dirichlet global coefficients (None: homogeneous data)."""
         out = out if out is not None else _like(forcing, self.coll.E * self.coll.nm)
-        _same_side(forcing, out)
+        _same_side(forcing, out, dirichlet)
         res = C.CgResult()
         o = self.options(**kw)
         pf, d = _ptr(forcing, np.float64 if not _is_device(forcing) else None)
         po, _ = _ptr(out)
-        C.call("ithaca_gpu_helmsolve", self.handle, ctypes.c_double(lam), pf, po, ctypes.byref(o), ctypes.byref(res), d)
+        if dirichlet is None:
+            C.call("ithaca_gpu_helmsolve", self.handle, ctypes.c_double(lam), pf, po, ctypes.byref(o),
+                   ctypes.byref(res), d)
+        else:
+            if len(dirichlet) != self.amap.ndir:
+                raise ValueError(f"expected {self.amap.ndir} Dirichlet values")
+            pdv, _ = _ptr(dirichlet, np.float64 if not _is_device(dirichlet) else None)
+            C.call("ithaca_gpu_helmsolve_dirichlet", self.handle, ctypes.c_double(lam), pf, pdv, po,
+                   ctypes.byref(o), ctypes.byref(res), d)
         return out, res
 
     def close(self):

@@ -99,10 +99,16 @@ def solve(basis, dim, jac, df, lam, amap, rhs, tol=1e-9, max_iter=5000):
     return cg(lambda v: global_apply(basis, dim, jac, df, lam, m, v), dinv, rhs, m.ndir, tol, max_iter)
 
 
-def helmsolve(basis, dim, jac, df, lam, amap, forcing, tol=1e-9, max_iter=5000):
-    """Homogeneous Dirichlet HelmSolve: returns (local coefficients, iterations)."""
+def helmsolve(basis, dim, jac, df, lam, amap, forcing, tol=1e-9, max_iter=5000, dirichlet=None):
+    """HelmSolve (ContField.cpp:878-945): returns (local coefficients, iterations).
+    dirichlet: the ndir Dirichlet global coefficients (None: homogeneous), lifted as the
+    reference does: rhs_F -= (A x_D)_F, then x_D is the Dirichlet part of the result."""
     m = amap if isinstance(amap, Map) else Map.of(amap)
     rhs = -m.assemble(ops.iproduct(basis, dim, jac, forcing))
+    xd = np.zeros(m.nglobal)
+    if dirichlet is not None:
+        xd[:m.ndir] = dirichlet
+        rhs = rhs - global_apply(basis, dim, jac, df, lam, m, xd, zero_dir=False)
     x, it, _, _ = solve(basis, dim, jac, df, lam, m, rhs, tol, max_iter)
-    x[:m.ndir] = 0.0
+    x[:m.ndir] = xd[:m.ndir]
     return m.gather(x), it

@@ -52,3 +52,35 @@ def rel_err(a, b):
     a = np.asarray(a, dtype=np.float64).reshape(-1)
     b = np.asarray(b, dtype=np.float64).reshape(-1)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def hex_dirichlet(mesh, amap, basis, X, fn):
+    """Dirichlet global coefficients (amap.ndir values) of fn on the boundary of a
+    structured HexMesh: the boundary-constrained projection (oracle.bc) of fn on every
+    boundary face, mapped to the element's modes on that face."""
+    from oracle import bc
+    n, Q, E = basis.n, basis.Q, mesh.E
+    nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
+    L = amap.l2g.reshape(E, n, n, n)    # [e, r, q, p]
+    Xp = X.reshape(3, E, Q, Q, Q)       # [c, e, k, j, i]
+    xd = np.full(amap.ndir, np.nan)
+    for e in range(E):
+        ix, iy, iz = e % nx, (e // nx) % ny, e // (nx * ny)
+        faces = []
+        for axis, idx, cnt in (("i", ix, nx), ("j", iy, ny), ("k", iz, nz)):
+            if idx == 0:
+                faces.append((axis, 0, 0))
+            if idx == cnt - 1:
+                faces.append((axis, Q - 1, 1))
+        for axis, pt, mode in faces:
+            if axis == "k":      # face (a = i, b = j); modes (p = a, q = b, r = mode)
+                P, G = Xp[:, e, pt, :, :], L[e, mode, :, :]
+            elif axis == "j":    # face (a = i, b = k); modes (p = a, q = mode, r = b)
+                P, G = Xp[:, e, :, pt, :], L[e, :, mode, :]
+            else:                # face (a = j, b = k); modes (p = mode, q = a, r = b)
+                P, G = Xp[:, e, :, :, pt], L[e, :, :, mode]
+            C = bc.quad_fwd_bnd(basis, fn(P[0], P[1], P[2]).reshape(-1)).reshape(n, n)
+            assert np.all(G < amap.ndir)
+            xd[G.reshape(-1)] = C.reshape(-1)
+    assert not np.isnan(xd).any()
+    return xd
