@@ -378,6 +378,7 @@ def run_reference(args, rank, world):
     value = 1.0 / (t_iter * iters_full)
     cfg = workload_config(args, n, Q, E, N, ndir)
     cfg["parallelism"] = f"{nth} host threads"
+    cfg["inner"] = "fp64 Jacobi PCG, the reference recurrence (compiled C++ port of the reference kernels)"
     print(json.dumps({
         "metric": METRIC, "impl": "reference", "value": value, "unit": "solves/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3,

@@ -156,7 +156,7 @@ typedef struct {
   int mode;            /* ITHACA_GPU_SOLVE_*                                                         */
   double inner_tol;    /* mixed mode: relative reduction asked of each inner FP32 solve (default 1e-2) */
   int max_outer;       /* mixed mode: maximum refinement steps (default 50)                          */
-  int check_every;     /* iterations per device-side convergence check (default 8)                   */
+  int check_every;     /* iterations per graph launch between host checks (default 16; 8 batched)    */
 } ithaca_gpu_cg_opts;
 
 typedef struct {

@@ -893,7 +893,7 @@ void ithaca_gpu_cg_default_opts(ithaca_gpu_cg_opts* o) {
   o->mode = ITHACA_GPU_SOLVE_FP64;
   o->inner_tol = 1e-2;
   o->max_outer = 50;
-  o->check_every = 8;
+  o->check_every = 16;
 }
 
 int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign, int nglobal, int ndir,
@@ -1228,9 +1228,14 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
     cudaEvent_t e0, e1;
     ITHACA_CUDA(cudaEventCreate(&e0));
     ITHACA_CUDA(cudaEventCreate(&e1));
+    // the FP32 apply exactly as the inner iteration launches it (owned rows included)
+    OwnedRows own;
+    own.s = cg->v32.s;
+    own.part = cg->opart;
     auto run = [&] {
       if (f32)
-        launch_apply<float>(cg, cg->v32, op->t32.base, cg->jg32, (float)lambda, nullptr, cg->v32.w, s, true, nullptr);
+        launch_apply<float>(cg, cg->v32, op->t32.base, cg->jg32, (float)lambda, nullptr, cg->v32.w, s, true, nullptr,
+                            cg->own_ok ? &own : nullptr);
       else
         launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, cg->v64.w, s, true, nullptr);
     };
@@ -1263,7 +1268,7 @@ static ithaca_gpu_cg_opts opts_or_default(const ithaca_gpu_cg_opts* o) {
   if (!o) return d;
   d = *o;
   if (d.max_iter <= 0) d.max_iter = 5000;
-  if (d.check_every <= 0) d.check_every = 8;
+  if (d.check_every <= 0) d.check_every = 16;
   if (d.max_outer <= 0) d.max_outer = 50;
   if (!(d.inner_tol > 0 && d.inner_tol < 1)) d.inner_tol = 1e-2;
   return d;

@@ -253,7 +253,7 @@ class GlobalLinSysIterativeFullGPU:
         self.handle = h
 
     @staticmethod
-    def options(tol=1e-9, max_iter=5000, mode="fp64", inner_tol=1e-2, max_outer=50, check_every=8):
+    def options(tol=1e-9, max_iter=5000, mode="fp64", inner_tol=1e-2, max_outer=50, check_every=16):
         o = C.CgOpts()
         C.lib().ithaca_gpu_cg_default_opts(ctypes.byref(o))
         o.tol, o.max_iter, o.mode = tol, max_iter, SOLVE_MODES[mode]
