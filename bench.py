@@ -107,6 +107,22 @@ def build_workload(mesh_n, order):
     return mesh, n, Q, X, amap, f
 
 
+def max_over_ranks(ms, world, device="cpu"):
+    """The slowest rank's time (ms): every rank's timed region is bracketed by barriers,
+    and the whole job takes as long as its slowest replica."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(steps, ms, world):
+    """Whole-job solves/s of `world` replicas that each ran `steps` solves in `ms`."""
+    return world * steps / (ms / 1e3)
+
+
 def fp32_kernel_name(variant, n, Q):
     """Name of the FP32 hex Helmholtz kernel an autotuner variant launches."""
     if variant == 0:
@@ -219,11 +235,8 @@ def run_gpu(args, rank, world):
     barrier()
     ms = ev0.elapsed_time(ev1)
     launches = ctx.launch_count() - l0
-    if world > 1:
-        t = torch.tensor([ms], device=cuda)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ms, world, cuda)
+    value = replica_throughput(args.steps, ms, world)
     x_mixed = x.clone()
 
     # the other inner-solve variant, for comparison (not the headline)
