@@ -26,6 +26,7 @@
 namespace ithaca {
 
 constexpr int RB = 760;      // reduction CTAs: 5 per SM of 152 (one wave at <= 51 registers per thread)
+constexpr int RBA = 1216;    // assembly CTAs: 8 per SM (<= 32 registers); partial slot 3 holds RBA entries
 constexpr int RT = 256;      // threads per reduction CTA
 constexpr int NSLOT = 4;     // partial-sum slots: 0 r.w, 1 r.r, 2 b.b, 3 s.w
 
@@ -80,7 +81,8 @@ __device__ __forceinline__ void reduce_slots(const double* partials, const int (
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     double s = 0;
-    for (int i = threadIdx.x; i < RB; i += RT) s += __ldcg(partials + slots[k] * RB + i);
+    const int n = slots[k] == 3 ? RBA : RB;  // slot 3 is written by the assembly kernel
+    for (int i = threadIdx.x; i < n; i += RT) s += __ldcg(partials + slots[k] * RB + i);
     sm[k][threadIdx.x] = s;
   }
   __syncthreads();
@@ -234,7 +236,7 @@ __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int 
                                           const int* __restrict__ rows, const int* __restrict__ ecols,
                                           const T* __restrict__ yloc, T* __restrict__ s, const T* __restrict__ w,
                                           T& sw) {
-  constexpr int U = K >= 8 ? 1 : 8 / K;  // rows per thread step
+  constexpr int U = K >= 4 ? 1 : 4 / K;  // rows per thread step (8 CTAs per SM hold the rest in flight)
   const int n = P.n[c];
   const int* R = rows + P.rows_off[c];
   const int* C = ecols + P.col_off[c];
@@ -275,7 +277,7 @@ __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int 
 // `counter`) also runs the loop-tail scalar update, saving one launch per CG iteration;
 // the reduction order of the partial sums does not depend on which CTA that is.
 template <typename T, bool SIGNED = true>
-__global__ void __launch_bounds__(RT, RB / 152) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
+__global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
                                                           const int* __restrict__ ecols, const int* __restrict__ rowptr,
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
                                                           T* __restrict__ s, const T* __restrict__ w, const int* skip,
@@ -418,10 +420,11 @@ __global__ void __launch_bounds__(RT) residual_kernel(int N, int ndir, const int
   double v[2] = {0, 0};
   for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
     double acc = 0;
-    for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
-      const int c = cols[j];
-      acc += c >= 0 ? yloc[c] : -yloc[~c];
-    }
+    if (yloc != nullptr)  // nullptr: x = 0, so r = b
+      for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
+        const int c = cols[j];
+        acc += c >= 0 ? yloc[c] : -yloc[~c];
+      }
     const double rg = b[g] - acc;
     r[g] = rg;
     v[0] += rg * rg;
@@ -625,11 +628,11 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg), try_own ? &own : nullptr);
   if (try_own && own.ctas >= 0) {  // the element kernel wrote the owned rows of s
     if (own.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
-    assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+    assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
                                              v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
                                              cg->opart, own.ctas);
   } else {
-    assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+    assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
                                              v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter);
   }
   cg->op->ctx->launches += 2;
@@ -667,7 +670,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
   pcg_init_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
-  assemble_dot_kernel<T><<<RB, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
+  assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
                                            cg->partials);
   scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
   c->launches += 3;
@@ -757,7 +760,7 @@ static void ensure_diag(Cg* cg, double lambda) {
   if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
                                 cg->v64.yloc, s))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
-  assemble_dot_kernel<double, false><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
+  assemble_dot_kernel<double, false><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
                                                        nullptr, nullptr, nullptr);
   inv_kernel<<<RB, RT, 0, s>>>(cg->N, cg->v64.s, cg->v64.dinv, cg->have32 ? cg->v32.dinv : nullptr, cg->ndir);
   op->ctx->launches += 3;
@@ -766,10 +769,12 @@ static void ensure_diag(Cg* cg, double lambda) {
 }
 
 // FP64 residual r = b - A x over the non-Dirichlet dofs; ||r||^2 -> dscal[0], ||b||^2 -> dscal[1].
+// x == nullptr stands for x = 0 (r = b, no operator apply).
 static void fp64_residual(Cg* cg, double lambda, const double* x, const double* b, double* r) {
   cudaStream_t s = cg->op->ctx->stream;
-  launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, x, s, true, nullptr);
-  residual_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, cg->v64.yloc, b, r, cg->partials);
+  if (x != nullptr) launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, x, s, true, nullptr);
+  residual_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, x != nullptr ? cg->v64.yloc : nullptr, b,
+                                    r, cg->partials);
   reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 1, cg->dscal);
   reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 2, cg->dscal + 1);
   cg->op->ctx->launches += 3;
@@ -801,7 +806,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
     double hs[2];
     // x64 = 0; r64 = b
     ITHACA_CUDA(cudaMemsetAsync(cg->v64.x, 0, sizeof(double) * cg->N, s));
-    fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.r);
+    fp64_residual(cg, lambda, nullptr, cg->v64.b, cg->v64.r);
     ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaStreamSynchronize(s));
     const double bnorm2 = hs[1];
@@ -840,11 +845,12 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
     out.outer_iterations = outer;
     out.eps = rnorm2;
     out.rhs_magnitude = bnorm2 > 1e-6 ? bnorm2 : 1.0;
+    // the last outer step's FP64 residual is the residual of the returned x
+    out.rel_residual = bnorm2 > 0 ? std::sqrt(rnorm2 / bnorm2) : 0.0;
   } else {
     fail(ITHACA_GPU_ERR_ARG, "unknown solve mode");
   }
-  // final FP64 relative residual ||b - A x|| / ||b|| (reported in both modes)
-  {
+  if (!mixed) {  // final FP64 relative residual ||b - A x|| / ||b||
     double hs[2];
     fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.w);
     ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
@@ -962,11 +968,11 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       }
       int share[kAsmK + 1], used = 0, big = 0;
       for (int c = 0; c <= kAsmK; ++c) {
-        share[c] = P.n[c] > 0 ? std::max(1, (int)((double)(RB - nonempty) * ent[c] / std::max(total, 1LL))) : 0;
+        share[c] = P.n[c] > 0 ? std::max(1, (int)((double)(RBA - nonempty) * ent[c] / std::max(total, 1LL))) : 0;
         used += share[c];
         if (ent[c] > ent[big]) big = c;
       }
-      share[big] += RB - used;  // the rounding remainder goes to the largest class
+      share[big] += RBA - used;  // the rounding remainder goes to the largest class
       P.cta0[0] = 0;
       for (int c = 0; c <= kAsmK; ++c) P.cta0[c + 1] = P.cta0[c] + share[c];
     };
@@ -1019,7 +1025,7 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
         cudaMemcpyAsync(cg->asm_cols, asm_cols.data(), sizeof(int) * asm_cols.size(), cudaMemcpyHostToDevice, s));
     cg->plan = plan;
     cg->v64.alloc(nglobal, nloc);
-    ITHACA_CUDA(cudaMalloc(&cg->partials, sizeof(double) * NSLOT * RB));
+    ITHACA_CUDA(cudaMalloc(&cg->partials, sizeof(double) * ((NSLOT - 1) * RB + RBA)));
     ITHACA_CUDA(cudaMalloc(&cg->dscal, sizeof(double) * 8));
     ITHACA_CUDA(cudaMalloc(&cg->counter, sizeof(unsigned int)));
     ITHACA_CUDA(cudaMemset(cg->counter, 0, sizeof(unsigned int)));
@@ -1056,7 +1062,7 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
     }
     double* dy = on_device ? y : cg->v64.q;
     launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, dx, s, false, nullptr);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
+    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
                                                   nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
@@ -1078,7 +1084,7 @@ int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* globa
       dl = d;
     }
     double* dg = on_device ? global : (double*)c->stage_ptr(1, sizeof(double) * cg->N);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
+    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(global, dg, sizeof(double) * cg->N, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaGetLastError());
@@ -1175,7 +1181,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
                                  cg->v64.yloc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
     neg_kernel<<<RB, RT, 0, s>>>(nloc, cg->v64.yloc);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
+    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
                                                   nullptr, nullptr);
     c->launches += 3;
     const double* dvals = nullptr;  // Dirichlet values on the device (ndir entries)
@@ -1186,7 +1192,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
       ITHACA_CUDA(cudaMemcpyAsync(xd, dirichlet, sizeof(double) * cg->ndir,
                                   on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
       launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, xd, s, false, nullptr);
-      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
+      assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
                                                     cg->cols, cg->v64.yloc, cg->v64.s, nullptr, nullptr, nullptr);
       sub_free_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.s, cg->v64.b);
       c->launches += 2;
@@ -1295,13 +1301,13 @@ void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, doub
   for (int j = 0; j < ncols; ++j) {
     const double* x = X + (size_t)j * cg->N;
     launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), 0.0, nullptr, x, s, true, nullptr);
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
+    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
                                                   LX + (size_t)j * cg->N, nullptr, nullptr, nullptr);
     g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, x, loc);
     if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
         !launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "mass operator: (modes, points) combination not built");
-    assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
+    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
                                                   nullptr, nullptr, nullptr);
     c->launches += 5;
   }
@@ -1394,7 +1400,7 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
                                    cg->v64.yloc, s))
         fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
       double* dg = on_device ? dJdx : cg->v64.q;
-      assemble_dot_kernel<double><<<RB, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
+      assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
                                                     nullptr, nullptr);
       launch_zero_head(cg->ndir, dg, s);
       c->launches += 3;
