@@ -57,11 +57,12 @@ __device__ __forceinline__ void block_partials(double (&v)[NC], double* partials
   }
 }
 
-__device__ __forceinline__ double reduce_slot(const double* partials, int slot) {
+// Sum of the first n partials of `slot` (n = the CTA count of the launch that wrote them).
+__device__ __forceinline__ double reduce_slot(const double* partials, int slot, int n) {
   __shared__ double sm[RT];
   double s = 0;
   // L2 loads: the partials may have been written by other CTAs of the same launch
-  for (int i = threadIdx.x; i < RB; i += RT) s += __ldcg(partials + slot * RB + i);
+  for (int i = threadIdx.x; i < n; i += RT) s += __ldcg(partials + slot * RB + i);
   sm[threadIdx.x] = s;
   __syncthreads();
   for (int w = RT / 2; w > 0; w >>= 1) {
@@ -75,13 +76,15 @@ __device__ __forceinline__ double reduce_slot(const double* partials, int slot) 
 
 // Several slots at once (same summation order as reduce_slot for each): the loads of
 // all slots are in flight together and the tree steps are shared.
+// nv: CTAs of the vector kernels (slots 0-2), na: CTAs of the assembly (slot 3).
 template <int NS>
-__device__ __forceinline__ void reduce_slots(const double* partials, const int (&slots)[NS], double (&out)[NS]) {
+__device__ __forceinline__ void reduce_slots(const double* partials, const int (&slots)[NS], double (&out)[NS],
+                                             int nv, int na) {
   __shared__ double sm[NS][RT];
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     double s = 0;
-    const int n = slots[k] == 3 ? RBA : RB;  // slot 3 is written by the assembly kernel
+    const int n = slots[k] == 3 ? na : nv;
     for (int i = threadIdx.x; i < n; i += RT) s += __ldcg(partials + slots[k] * RB + i);
     sm[k][threadIdx.x] = s;
   }
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(RT) pcg_init_kernel(int N, int ndir, const T* 
                                                       T* __restrict__ r, T* __restrict__ w,
                                                       const T* __restrict__ dinv, double* partials) {
   double v[3] = {0, 0, 0};
-  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) {
     const double bg = (double)b[g];
     v[2] += bg * bg;
     if (g >= ndir) {
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(RT) pcg_update_kernel(int N, int ndir, const C
   if (sc->done) return;
   const T alpha = (T)sc->alpha, beta = (T)sc->beta;
   double v[2] = {0, 0};
-  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) {
     const T pg = beta * p[g] + w[g];
     const T qg = beta * q[g] + s[g];
     p[g] = pg;
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
   const float alpha = (float)sc->alpha, beta = (float)sc->beta;
   float rw = 0.f, rr = 0.f;
   const int c0 = ndir >> 2, c1 = (N + 3) >> 2;
-  for (int c = c0 + blockIdx.x * RT + threadIdx.x; c < c1; c += RB * RT) {
+  for (int c = c0 + blockIdx.x * RT + threadIdx.x; c < c1; c += gridDim.x * RT) {
     float4 P = reinterpret_cast<const float4*>(p)[c], W = reinterpret_cast<const float4*>(w)[c];
     float4 Qv = reinterpret_cast<const float4*>(q)[c];
     const float4 S = reinterpret_cast<const float4*>(s)[c];
@@ -205,7 +208,8 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
   block_partials<2>(v, partials, slots);
 }
 
-__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart);
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart, int nv,
+                                  int na);
 
 // ---- assembly plan: rows grouped by their number of local entries ----------------
 // Class c < kAsmK holds the rows with exactly c + 1 local entries, stored ELL-style
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
                                                           T* __restrict__ s, const T* __restrict__ w, const int* skip,
                                                           double* partials, CgScalars* fuse_sc = nullptr,
                                                           unsigned int* counter = nullptr,
-                                                          const double* apart = nullptr, int napart = 0) {
+                                                          const double* apart = nullptr, int napart = 0, int nv = RB) {
   if (skip != nullptr && *skip) return;
   int c = 0;
   while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
@@ -323,17 +327,17 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
     __syncthreads();
     if (ticket == gridDim.x - 1) {
       __threadfence();
-      scalars_iter_body(partials, fuse_sc, apart, napart);
+      scalars_iter_body(partials, fuse_sc, apart, napart, nv, gridDim.x);
       if (threadIdx.x == 0) *counter = 0u;  // re-armed for the next iteration
     }
   }
 }
 
 // Reference initial step (NekLinSysIterCG.cpp:147-190).
-__global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc) {
+__global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc, int nv, int na) {
   const int slots[4] = {0, 1, 2, 3};
   double red[4];
-  reduce_slots<4>(partials, slots, red);
+  reduce_slots<4>(partials, slots, red, nv, na);
   const double rw = red[0], rr = red[1], bb = red[2], sw = red[3];
   if (threadIdx.x == 0) {
     sc->rhs_mag = sc->mag_override > 0 ? sc->mag_override : (bb > 1e-6 ? bb : 1.0);
@@ -362,17 +366,18 @@ __global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials
 }
 
 // Reference loop tail (NekLinSysIterCG.cpp:219-261).
-__global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials, CgScalars* sc) {
-  scalars_iter_body(partials, sc, nullptr, 0);
+__global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials, CgScalars* sc, int nv, int na) {
+  scalars_iter_body(partials, sc, nullptr, 0, nv, na);
 }
 
 // apart (napart entries): the element kernel's partials of s.w over the rows it
 // assembled itself, added to slot 3 (in a fixed order).
-__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart) {
+__device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart, int nv,
+                                  int na) {
   if (sc->done) return;
   const int slots[3] = {0, 1, 3};
   double red[3];
-  reduce_slots<3>(partials, slots, red);
+  reduce_slots<3>(partials, slots, red, nv, na);
   double mu_own = 0;
   if (napart > 0) {
     __shared__ double sm[RT];
@@ -418,7 +423,7 @@ __global__ void __launch_bounds__(RT) residual_kernel(int N, int ndir, const int
                                                       const double* __restrict__ b, double* __restrict__ r,
                                                       double* partials) {
   double v[2] = {0, 0};
-  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) {
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) {
     double acc = 0;
     if (yloc != nullptr)  // nullptr: x = 0, so r = b
       for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
@@ -434,8 +439,8 @@ __global__ void __launch_bounds__(RT) residual_kernel(int N, int ndir, const int
   block_partials<2>(v, partials, slots);
 }
 
-__global__ void reduce_to_kernel(const double* partials, int slot, double* out) {
-  const double v = reduce_slot(partials, slot);
+__global__ void reduce_to_kernel(const double* partials, int slot, int n, double* out) {
+  const double v = reduce_slot(partials, slot, n);
   if (threadIdx.x == 0) *out = v;
 }
 
@@ -443,25 +448,25 @@ __global__ void reduce_to_kernel(const double* partials, int slot, double* out) 
 __global__ void __launch_bounds__(RT) scale_to_f32_kernel(int N, int ndir, const double* __restrict__ r,
                                                           const double* __restrict__ scale_src, float* __restrict__ r32) {
   const double sc = 1.0 / sqrt(*scale_src);
-  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) r32[g] = g >= ndir ? (float)(r[g] * sc) : 0.f;
+  for (int g = blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) r32[g] = g >= ndir ? (float)(r[g] * sc) : 0.f;
 }
 
 // x64 += sqrt(*scale_src) * d32 on g >= ndir.
 __global__ void __launch_bounds__(RT) axpy_f32_kernel(int N, int ndir, const double* __restrict__ scale_src,
                                                       const float* __restrict__ d32, double* __restrict__ x) {
   const double sc = sqrt(*scale_src);
-  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) x[g] += sc * (double)d32[g];
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) x[g] += sc * (double)d32[g];
 }
 
 // b[g] -= y[g] on the free dofs g >= ndir.
 __global__ void __launch_bounds__(RT) sub_free_kernel(int N, int ndir, const double* __restrict__ y,
                                                       double* __restrict__ b) {
-  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += RB * RT) b[g] -= y[g];
+  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) b[g] -= y[g];
 }
 
 __global__ void __launch_bounds__(RT) inv_kernel(int n, const double* __restrict__ d, double* __restrict__ dinv,
                                                  float* __restrict__ dinv32, int ndir) {
-  for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += RB * RT) {
+  for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += gridDim.x * RT) {
     const double v = g >= ndir ? 1.0 / d[g] : 0.0;
     dinv[g] = v;
     if (dinv32) dinv32[g] = (float)v;
@@ -471,19 +476,19 @@ __global__ void __launch_bounds__(RT) inv_kernel(int n, const double* __restrict
 // local[l] = sign * x[g] (AssemblyMapCG::GlobalToLocal), l2g signed-encoded.
 __global__ void __launch_bounds__(RT) g2l_kernel(size_t nloc, const int* __restrict__ l2g,
                                                  const double* __restrict__ x, double* __restrict__ loc) {
-  for (size_t l = (size_t)blockIdx.x * RT + threadIdx.x; l < nloc; l += (size_t)RB * RT) {
+  for (size_t l = (size_t)blockIdx.x * RT + threadIdx.x; l < nloc; l += (size_t)gridDim.x * RT) {
     const int c = l2g[l];
     loc[l] = c >= 0 ? x[c] : -x[~c];
   }
 }
 
 __global__ void __launch_bounds__(RT) neg_kernel(size_t n, double* __restrict__ a) {
-  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)RB * RT) a[i] = -a[i];
+  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) a[i] = -a[i];
 }
 
 template <typename T>
 __global__ void __launch_bounds__(RT) cast_kernel(size_t n, const double* __restrict__ a, T* __restrict__ b) {
-  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)RB * RT) b[i] = (T)a[i];
+  for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) b[i] = (T)a[i];
 }
 
 // ---- solver object --------------------------------------------------------------
@@ -511,6 +516,7 @@ struct Cg {
   size_t nloc = 0;
   int* l2g = nullptr;     // signed-encoded
   int* rowptr = nullptr;  // N + 1
+  int rbv = RB, rba = RBA;  // CTAs of the vector kernels and of the assembly (fewer for small systems)
   AsmPlan plan{};           // assembly by row classes (see AsmPlan)
   // owned rows (one local entry, free): written by the pipelined FP32 element kernel in
   // the inner iteration, so that iteration's assembly (plan_own) leaves them out
@@ -614,10 +620,10 @@ const float* lam_dev<float>(Cg* cg) { return &cg->sc->lambda32; }
 template <typename T>
 static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cudaStream_t s) {
   if constexpr (sizeof(T) == 4)
-    pcg_update_f32x4_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
+    pcg_update_f32x4_kernel<<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
                                               cg->partials);
   else
-    pcg_update_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
+    pcg_update_kernel<T><<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, cg->sc, v.x, v.r, v.w, v.s, v.p, v.q, v.dinv,
                                            cg->partials);
   OwnedRows own;
   if constexpr (sizeof(T) == 4) {
@@ -628,12 +634,13 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg), try_own ? &own : nullptr);
   if (try_own && own.ctas >= 0) {  // the element kernel wrote the owned rows of s
     if (own.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
-    assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+    assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
                                              v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
-                                             cg->opart, own.ctas);
+                                             cg->opart, own.ctas, cg->rbv);
   } else {
-    assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
-                                             v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter);
+    assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+                                             v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
+                                             nullptr, 0, cg->rbv);
   }
   cg->op->ctx->launches += 2;
 }
@@ -668,11 +675,11 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   init.lambda32 = (float)lambda;
   *cg->sc_host = init;
   ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
-  pcg_init_kernel<T><<<RB, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
+  pcg_init_kernel<T><<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
-  assemble_dot_kernel<T><<<RBA, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
+  assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
                                            cg->partials);
-  scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc);
+  scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc, cg->rbv, cg->rba);
   c->launches += 3;
   ITHACA_CUDA(cudaGetLastError());
   cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
@@ -760,7 +767,7 @@ static void ensure_diag(Cg* cg, double lambda) {
   if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
                                 cg->v64.yloc, s))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
-  assemble_dot_kernel<double, false><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
+  assemble_dot_kernel<double, false><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
                                                        nullptr, nullptr, nullptr);
   inv_kernel<<<RB, RT, 0, s>>>(cg->N, cg->v64.s, cg->v64.dinv, cg->have32 ? cg->v32.dinv : nullptr, cg->ndir);
   op->ctx->launches += 3;
@@ -773,10 +780,10 @@ static void ensure_diag(Cg* cg, double lambda) {
 static void fp64_residual(Cg* cg, double lambda, const double* x, const double* b, double* r) {
   cudaStream_t s = cg->op->ctx->stream;
   if (x != nullptr) launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, x, s, true, nullptr);
-  residual_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, x != nullptr ? cg->v64.yloc : nullptr, b,
+  residual_kernel<<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, cg->rowptr, cg->cols, x != nullptr ? cg->v64.yloc : nullptr, b,
                                     r, cg->partials);
-  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 1, cg->dscal);
-  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 2, cg->dscal + 1);
+  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 1, cg->rbv, cg->dscal);
+  reduce_to_kernel<<<1, RT, 0, s>>>(cg->partials, 2, cg->rbv, cg->dscal + 1);
   cg->op->ctx->launches += 3;
 }
 
@@ -823,7 +830,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
         break;
       }
       // r32 = r64 / ||r64||, inner FP32 PCG from zero to relative inner_tol
-      scale_to_f32_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.r, cg->dscal, cg->v32.b);
+      scale_to_f32_kernel<<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.r, cg->dscal, cg->v32.b);
       c->launches++;
       run_pcg<float>(cg, cg->v32, cg->op->t32.base, cg->jg32, lambda, inner2, 1.0, o.max_iter - total_inner, chunk);
       total_inner += cg->sc_host->iters;
@@ -833,7 +840,7 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
         break;
       }
       // x64 += ||r|| d32 ; r64 = b - A x64
-      axpy_f32_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->dscal, cg->v32.x, cg->v64.x);
+      axpy_f32_kernel<<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, cg->dscal, cg->v32.x, cg->v64.x);
       c->launches++;
       fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.r);
       ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
@@ -958,6 +965,14 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
           for (int j = 0; j <= c; ++j) asm_cols[(size_t)plan.col_off[c] + (size_t)j * plan.n[c] + i] = cols[cnt[g] + j];
       }
     }
+    // Grid sizes: the full grids for large systems, about 2 rows per thread for small
+    // ones (enough threads to keep a small system's loads in parallel, without the
+    // partial sums of CTAs that have no rows).
+    int nonempty_all = 0;
+    for (int c = 0; c <= kAsmK; ++c) nonempty_all += plan.n[c] > 0;
+    const long long per2 = ((long long)nglobal + 2 * RT - 1) / (2 * RT);
+    const int rbv = (int)std::min<long long>(RB, std::max<long long>(1, per2));
+    const int rba = (int)std::min<long long>(RBA, std::max<long long>(nonempty_all, per2));
     // CTAs per class in proportion to its entries, at least one for a non-empty class
     auto split_ctas = [&](AsmPlan& P, const long long* ent) {
       long long total = 0;
@@ -968,11 +983,11 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       }
       int share[kAsmK + 1], used = 0, big = 0;
       for (int c = 0; c <= kAsmK; ++c) {
-        share[c] = P.n[c] > 0 ? std::max(1, (int)((double)(RBA - nonempty) * ent[c] / std::max(total, 1LL))) : 0;
+        share[c] = P.n[c] > 0 ? std::max(1, (int)((double)(rba - nonempty) * ent[c] / std::max(total, 1LL))) : 0;
         used += share[c];
         if (ent[c] > ent[big]) big = c;
       }
-      share[big] += RBA - used;  // the rounding remainder goes to the largest class
+      share[big] += rba - used;  // the rounding remainder goes to the largest class
       P.cta0[0] = 0;
       for (int c = 0; c <= kAsmK; ++c) P.cta0[c + 1] = P.cta0[c] + share[c];
     };
@@ -999,6 +1014,8 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     cg->op = op;
     cg->N = nglobal;
     cg->ndir = ndir;
+    cg->rbv = rbv;
+    cg->rba = rba;
     cg->nloc = nloc;
     cudaStream_t s = op->ctx->stream;
     ITHACA_CUDA(cudaMalloc(&cg->l2g, sizeof(int) * nloc));
@@ -1062,7 +1079,7 @@ int ithaca_gpu_cg_apply(ithaca_gpu_cg* cg, double lambda, const double* x, doubl
     }
     double* dy = on_device ? y : cg->v64.q;
     launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, dx, s, false, nullptr);
-    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
+    assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dy, nullptr,
                                                   nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
@@ -1084,7 +1101,7 @@ int ithaca_gpu_cg_assemble(ithaca_gpu_cg* cg, const double* local, double* globa
       dl = d;
     }
     double* dg = on_device ? global : (double*)c->stage_ptr(1, sizeof(double) * cg->N);
-    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
+    assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, dl, dg, nullptr, nullptr, nullptr);
     c->launches++;
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(global, dg, sizeof(double) * cg->N, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaGetLastError());
@@ -1181,7 +1198,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
                                  cg->v64.yloc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
     neg_kernel<<<RB, RT, 0, s>>>(nloc, cg->v64.yloc);
-    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
+    assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.b, nullptr,
                                                   nullptr, nullptr);
     c->launches += 3;
     const double* dvals = nullptr;  // Dirichlet values on the device (ndir entries)
@@ -1192,7 +1209,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
       ITHACA_CUDA(cudaMemcpyAsync(xd, dirichlet, sizeof(double) * cg->ndir,
                                   on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
       launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, xd, s, false, nullptr);
-      assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
+      assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
                                                     cg->cols, cg->v64.yloc, cg->v64.s, nullptr, nullptr, nullptr);
       sub_free_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.s, cg->v64.b);
       c->launches += 2;
@@ -1301,13 +1318,13 @@ void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, doub
   for (int j = 0; j < ncols; ++j) {
     const double* x = X + (size_t)j * cg->N;
     launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), 0.0, nullptr, x, s, true, nullptr);
-    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
+    assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
                                                   LX + (size_t)j * cg->N, nullptr, nullptr, nullptr);
     g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, x, loc);
     if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
         !launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "mass operator: (modes, points) combination not built");
-    assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
+    assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
                                                   nullptr, nullptr, nullptr);
     c->launches += 5;
   }
@@ -1400,7 +1417,7 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
                                    cg->v64.yloc, s))
         fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
       double* dg = on_device ? dJdx : cg->v64.q;
-      assemble_dot_kernel<double><<<RBA, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
+      assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, dg, nullptr,
                                                     nullptr, nullptr);
       launch_zero_head(cg->ndir, dg, s);
       c->launches += 3;
