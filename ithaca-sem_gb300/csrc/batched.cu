@@ -98,7 +98,9 @@ __global__ void __launch_bounds__(BT) bupdate_kernel(const Chunk* __restrict__ c
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const Scal& S = sc[ch.solve];
-    double v[2] = {0, 0};
+    // per-thread sums in T (a chunk gives each thread 16 dofs; FP32 sums keep the
+    // FP32 solve off the slow FP64 pipe), CTA sums in FP64
+    T rw = 0, rr = 0;
     if (!S.done) {
       const T alpha = (T)S.alpha, beta = (T)S.beta;
       for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
@@ -111,10 +113,11 @@ __global__ void __launch_bounds__(BT) bupdate_kernel(const Chunk* __restrict__ c
         r[g] = rg;
         const T wg = dinv[g] * rg;
         w[g] = wg;
-        v[0] += (double)rg * (double)wg;
-        v[1] += (double)rg * (double)rg;
+        rw = fma(rg, wg, rw);
+        rr = fma(rg, rg, rr);
       }
     }
+    double v[2] = {(double)rw, (double)rr};
     block_sum<2>(v, res);
     if (threadIdx.x < 2) part[threadIdx.x * nchunks + c] = res[threadIdx.x];
   }
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
   __shared__ double res[1];
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
-    double v[1] = {0};
+    T sw = 0;  // per-thread s.w in T, CTA sum in FP64
     if (!sc[ch.solve].done) {
       for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
         T acc = 0;
@@ -138,9 +141,10 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
           acc += cc >= 0 ? yloc[cc] : -yloc[~cc];
         }
         s[g] = acc;
-        v[0] += (double)acc * (double)w[g];
+        sw = fma(acc, w[g], sw);
       }
     }
+    double v[1] = {(double)sw};
     block_sum<1>(v, res);
     if (threadIdx.x == 0) part[3 * nchunks + c] = res[0];
   }
