@@ -287,8 +287,10 @@ def run_gpu(args, rank, world):
     gdofs32 = op_rate(coll32, torch.float32, 20)
 
     # ---- end to end through the public HelmSolve call with host buffers ----
-    f_host = np.ascontiguousarray(f)
-    out_host = np.zeros(E * n ** 3)
+    # host buffers in pinned memory (numpy views of pinned torch tensors): the forcing is
+    # copied in and the coefficients copied out by the library inside every timed step
+    f_host = torch.from_numpy(np.ascontiguousarray(f)).pin_memory().numpy()
+    out_host = torch.zeros(E * n ** 3, dtype=torch.float64).pin_memory().numpy()
     sysg.helmsolve(LAMBDA, f_host, out_host, tol=TOL, mode=mode)
     barrier()
     t0 = time.perf_counter()

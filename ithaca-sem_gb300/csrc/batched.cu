@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(BT) binit_kernel(const Chunk* __restrict__ chu
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BT) bupdate_kernel(const Chunk* __restrict__ chunks, int nchunks,
+__global__ void __launch_bounds__(BT, GRID / 152) bupdate_kernel(const Chunk* __restrict__ chunks, int nchunks,
                                                      const Scal* __restrict__ sc, T* __restrict__ x,
                                                      T* __restrict__ r, T* __restrict__ w, const T* __restrict__ s,
                                                      T* __restrict__ p, T* __restrict__ q,
@@ -103,18 +103,39 @@ __global__ void __launch_bounds__(BT) bupdate_kernel(const Chunk* __restrict__ c
     T rw = 0, rr = 0;
     if (!S.done) {
       const T alpha = (T)S.alpha, beta = (T)S.beta;
-      for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
-        const T pg = beta * p[g] + w[g];
-        const T qg = beta * q[g] + s[g];
-        p[g] = pg;
-        q[g] = qg;
-        x[g] += alpha * pg;
-        const T rg = r[g] - alpha * qg;
-        r[g] = rg;
-        const T wg = dinv[g] * rg;
-        w[g] = wg;
-        rw = fma(rg, wg, rw);
-        rr = fma(rg, rg, rr);
+      // U dofs per thread step with their loads issued together (memory-level parallelism)
+      constexpr int U = sizeof(T) == 8 ? 2 : 4;
+      for (int g0 = ch.begin + threadIdx.x; g0 < ch.end; g0 += U * BT) {
+        T pv[U], wv[U], qv[U], sv[U], xv[U], rv[U], dv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int g = g0 + u * BT;
+          const bool in = g < ch.end;
+          pv[u] = in ? p[g] : T(0);
+          wv[u] = in ? w[g] : T(0);
+          qv[u] = in ? q[g] : T(0);
+          sv[u] = in ? s[g] : T(0);
+          xv[u] = in ? x[g] : T(0);
+          rv[u] = in ? r[g] : T(0);
+          dv[u] = in ? dinv[g] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int g = g0 + u * BT;
+          if (g < ch.end) {
+            const T pg = beta * pv[u] + wv[u];
+            const T qg = beta * qv[u] + sv[u];
+            p[g] = pg;
+            q[g] = qg;
+            x[g] = xv[u] + alpha * pg;
+            const T rg = rv[u] - alpha * qg;
+            r[g] = rg;
+            const T wg = dv[u] * rg;
+            w[g] = wg;
+            rw = fma(rg, wg, rw);
+            rr = fma(rg, rg, rr);
+          }
+        }
       }
     }
     double v[2] = {(double)rw, (double)rr};
@@ -134,14 +155,42 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
     const Chunk ch = chunks[c];
     T sw = 0;  // per-thread s.w in T, CTA sum in FP64
     if (!sc[ch.solve].done) {
-      for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
-        T acc = 0;
-        for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
-          const int cc = cols[j];
-          acc += cc >= 0 ? yloc[cc] : -yloc[~cc];
+      // U rows per thread step; each row's entries summed in CSR order, the first
+      // entries of the U rows (and w) loaded together
+      constexpr int U = 4;
+      for (int g0 = ch.begin + threadIdx.x; g0 < ch.end; g0 += U * BT) {
+        int a[U], b[U];
+        T wv[U], acc[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int g = g0 + u * BT;
+          const bool in = g < ch.end;
+          a[u] = in ? rowptr[g] : 0;
+          b[u] = in ? rowptr[g + 1] : 0;
+          wv[u] = in ? w[g] : T(0);
         }
-        s[g] = acc;
-        sw = fma(acc, w[g], sw);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          acc[u] = 0;
+          if (a[u] < b[u]) {
+            const int cc = cols[a[u]];
+            acc[u] = cc >= 0 ? yloc[cc] : -yloc[~cc];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          for (int j = a[u] + 1; j < b[u]; ++j) {
+            const int cc = cols[j];
+            acc[u] += cc >= 0 ? yloc[cc] : -yloc[~cc];
+          }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int g = g0 + u * BT;
+          if (g < ch.end) {
+            s[g] = acc[u];
+            sw = fma(acc[u], wv[u], sw);
+          }
+        }
       }
     }
     double v[1] = {(double)sw};
