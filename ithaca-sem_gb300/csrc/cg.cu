@@ -226,6 +226,7 @@ struct AsmPlan {
   int ndir[kAsmK + 1];       // leading Dirichlet rows per class
   int rows_off[kAsmK + 1];   // first slot of the class in the row list
   long long col_off[kAsmK];  // first ELL entry of the class
+  long long tail_off;        // assembly-ordered buffer: first entry of the tail class
   int cta0[kAsmK + 2];       // CTAs [cta0[c], cta0[c + 1]) work on class c
 };
 
@@ -235,7 +236,7 @@ __device__ __forceinline__ T asm_value(const T* __restrict__ yloc, int c) {
   return yloc[c >= 0 ? c : ~c];  // sign^2 = 1 (diagonal assembly)
 }
 
-template <int K, typename T, bool SIGNED>
+template <int K, typename T, bool SIGNED, bool PERM>
 __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int ncta, bool skip_dir,
                                           const int* __restrict__ rows, const int* __restrict__ ecols,
                                           const T* __restrict__ yloc, T* __restrict__ s, const T* __restrict__ w,
@@ -243,25 +244,41 @@ __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int 
   constexpr int U = K >= 4 ? 1 : 4 / K;  // rows per thread step (8 CTAs per SM hold the rest in flight)
   const int n = P.n[c];
   const int* R = rows + P.rows_off[c];
-  const int* C = ecols + P.col_off[c];
   const int stride = ncta * RT;
   for (int i = (skip_dir ? P.ndir[c] : 0) + cta * RT + threadIdx.x; i < n; i += U * stride) {
-    int g[U], idx[U][K];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int ii = i + u * stride;
-      const bool in = ii < n;
-      g[u] = in ? R[ii] : -1;
-#pragma unroll
-      for (int j = 0; j < K; ++j) idx[u][j] = in ? C[(size_t)j * n + ii] : 0;
-    }
-    // second level: every local value and w[g] of the U rows, all loads in flight
+    int g[U];
     T val[U][K], wg[U];
+    if constexpr (PERM) {
+      // signed local values in the ELL layout: the row ids and the values load together
+      const T* Y = yloc + P.col_off[c];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
+      for (int u = 0; u < U; ++u) {
+        const int ii = i + u * stride;
+        const bool in = ii < n;
+        g[u] = in ? R[ii] : -1;
 #pragma unroll
-      for (int j = 0; j < K; ++j) val[u][j] = g[u] >= 0 ? asm_value<T, SIGNED>(yloc, idx[u][j]) : T(0);
-      wg[u] = (w != nullptr && g[u] >= 0) ? w[g[u]] : T(0);
+        for (int j = 0; j < K; ++j) val[u][j] = in ? Y[(size_t)j * n + ii] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) wg[u] = (w != nullptr && g[u] >= 0) ? w[g[u]] : T(0);
+    } else {
+      const int* C = ecols + P.col_off[c];
+      int idx[U][K];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int ii = i + u * stride;
+        const bool in = ii < n;
+        g[u] = in ? R[ii] : -1;
+#pragma unroll
+        for (int j = 0; j < K; ++j) idx[u][j] = in ? C[(size_t)j * n + ii] : 0;
+      }
+      // second level: every local value and w[g] of the U rows, all loads in flight
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) val[u][j] = g[u] >= 0 ? asm_value<T, SIGNED>(yloc, idx[u][j]) : T(0);
+        wg[u] = (w != nullptr && g[u] >= 0) ? w[g[u]] : T(0);
+      }
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -277,10 +294,11 @@ __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int 
 }
 
 // s[g] = sum_{local l of g} sign_l * yloc[l] over all rows (skip_dir: free rows only);
-// partial s.w in slot 3. With fuse_sc != nullptr the last CTA to finish (ticket on
+// partial s.w in slot 3. PERM: yloc is the assembly-ordered buffer of signed local values
+// (ELL layout of P, tail rows at P.tail_off + rowptr[slot]), ecols and cols are unused. With fuse_sc != nullptr the last CTA to finish (ticket on
 // `counter`) also runs the loop-tail scalar update, saving one launch per CG iteration;
 // the reduction order of the partial sums does not depend on which CTA that is.
-template <typename T, bool SIGNED = true>
+template <typename T, bool SIGNED = true, bool PERM = false>
 __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
                                                           const int* __restrict__ ecols, const int* __restrict__ rowptr,
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
@@ -294,21 +312,26 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
   const int cta = blockIdx.x - P.cta0[c], ncta = P.cta0[c + 1] - P.cta0[c];
   T sw = 0;  // per-thread s.w in T (FP32 sums stay off the slow FP64 pipe); CTA sum in FP64
   switch (c) {
-    case 0: asm_class<1, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 1: asm_class<2, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 2: asm_class<3, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 3: asm_class<4, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 4: asm_class<5, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 5: asm_class<6, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 6: asm_class<7, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
-    case 7: asm_class<8, T, SIGNED>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 0: asm_class<1, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 1: asm_class<2, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 2: asm_class<3, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 3: asm_class<4, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 4: asm_class<5, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 5: asm_class<6, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 6: asm_class<7, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
+    case 7: asm_class<8, T, SIGNED, PERM>(P, c, cta, ncta, skip_dir, rows, ecols, yloc, s, w, sw); break;
     default: {  // longer rows: CSR
       const int n = P.n[kAsmK];
       const int* R = rows + P.rows_off[kAsmK];
       for (int i = (skip_dir ? P.ndir[kAsmK] : 0) + cta * RT + threadIdx.x; i < n; i += ncta * RT) {
         const int g = R[i];
         T acc = 0;
-        for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) acc += asm_value<T, SIGNED>(yloc, cols[j]);
+        if constexpr (PERM) {
+          const T* Y = yloc + P.tail_off;
+          for (int j = rowptr[i]; j < rowptr[i + 1]; ++j) acc += Y[j];
+        } else {
+          for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) acc += asm_value<T, SIGNED>(yloc, cols[j]);
+        }
         s[g] = acc;
         if (w) sw = fma(acc, w[g], sw);
       }
@@ -518,10 +541,14 @@ struct Cg {
   int* rowptr = nullptr;  // N + 1
   int rbv = RB, rba = RBA;  // CTAs of the vector kernels and of the assembly (fewer for small systems)
   AsmPlan plan{};           // assembly by row classes (see AsmPlan)
-  // owned rows (one local entry, free): written by the pipelined FP32 element kernel in
-  // the inner iteration, so that iteration's assembly (plan_own) leaves them out
+  // Scattered output of the inner iteration's pipelined FP32 element kernel: it writes
+  // the owned rows (one local entry, free) into s itself and every other signed local
+  // value into its slot of the assembly-ordered buffer (the ELL layout of plan, then the
+  // tail rows' entries at plan.tail_off + tail_ptr[slot] + j), which the assembly
+  // (plan_own: the same classes without the owned rows) reads with unit stride.
   bool own_ok = false;
-  int* l2g_own = nullptr;   // l2g with kOwnedBit on the owned rows' local entries
+  int* ocode = nullptr;     // nloc output codes (see OwnedRows)
+  int* tail_ptr = nullptr;  // rows of the tail class + 1: first slot of each row's entries
   AsmPlan plan_own{};
   double* opart = nullptr;  // per-CTA s.w partials of the element kernel
   int opart_cap = 0;
@@ -556,7 +583,8 @@ Cg::~Cg() {
   cudaFree(l2g);
   cudaFree(rowptr);
   cudaFree(asm_rows);
-  cudaFree(l2g_own);
+  cudaFree(ocode);
+  cudaFree(tail_ptr);
   cudaFree(opart);
   cudaFree(asm_cols);
   cudaFree(cols);
@@ -590,13 +618,14 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
   bool ok;
   if (own != nullptr) own->ctas = -1;
   if constexpr (sizeof(T) == 4) {
-    const int* map = own != nullptr ? cg->l2g_own : cg->l2g;
+    const int* map = cg->l2g;
+    if (own != nullptr) own->ocode = cg->ocode;
     if (cg->geo16)
       ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
                                   v.yloc, map, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else if (op->dim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,
-                                     xin, v.yloc, own != nullptr && op->variant32 >= 21 ? map : cg->l2g,
+                                     xin, v.yloc, map,
                                      zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else
       ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
@@ -634,9 +663,9 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg), try_own ? &own : nullptr);
   if (try_own && own.ctas >= 0) {  // the element kernel wrote the owned rows of s
     if (own.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
-    assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
-                                             v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
-                                             cg->opart, own.ctas, cg->rbv);
+    assemble_dot_kernel<T, true, true><<<cg->rba, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, nullptr, cg->tail_ptr,
+                                                         nullptr, v.yloc, v.s, v.w, skip_ptr(cg), cg->partials,
+                                                         cg->sc, cg->counter, cg->opart, own.ctas, cg->rbv);
   } else {
     assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
                                              v.yloc, v.s, v.w, skip_ptr(cg), cg->partials, cg->sc, cg->counter,
@@ -954,6 +983,13 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
         col_total += entries[c];
       }
     }
+    plan.tail_off = col_total;
+    // Output codes of the scattered inner apply (see OwnedRows): owned rows (free, one
+    // local entry) -> g | kOwnedBit; other free rows -> the entry's slot in the
+    // assembly-ordered buffer (the ELL position of asm_cols, or tail_off + tail_ptr[i] + j);
+    // Dirichlet rows -> -1. The slots number the local entries once, so they fit in nloc.
+    const bool own_ok = nglobal < kOwnedBit && nloc < (size_t)kOwnedBit;
+    std::vector<int> ocode(own_ok ? nloc : 0, -1), tail_ptr(plan.n[kAsmK] + 1, 0);
     std::vector<int> asm_rows(nglobal), asm_cols((size_t)std::max<long long>(col_total, 1));
     {
       int fillc[kAsmK + 1];
@@ -961,8 +997,17 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       for (int g = 0; g < nglobal; ++g) {
         const int c = cls_of[g], i = fillc[c]++;
         asm_rows[(size_t)plan.rows_off[c] + i] = g;
-        if (c < kAsmK)
-          for (int j = 0; j <= c; ++j) asm_cols[(size_t)plan.col_off[c] + (size_t)j * plan.n[c] + i] = cols[cnt[g] + j];
+        const int k = cnt[g + 1] - cnt[g];
+        if (c == kAsmK) tail_ptr[i + 1] = tail_ptr[i] + k;
+        for (int j = 0; j < k; ++j) {
+          const long long pos = c < kAsmK ? plan.col_off[c] + (long long)j * plan.n[c] + i
+                                          : plan.tail_off + tail_ptr[i] + j;
+          if (c < kAsmK) asm_cols[(size_t)pos] = cols[cnt[g] + j];
+          if (own_ok && g >= ndir) {
+            const int cl = cols[cnt[g] + j], l = cl >= 0 ? cl : ~cl;
+            ocode[(size_t)l] = k == 1 ? (g | kOwnedBit) : (int)pos;
+          }
+        }
       }
     }
     // Grid sizes: the full grids for large systems, about 2 rows per thread for small
@@ -995,15 +1040,8 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     // Owned rows: the free rows with a single local entry. The inner FP32 iteration's
     // element kernel writes them, so its plan keeps only class 0's Dirichlet rows (which
     // lead the class and are skipped) and gives class 0's CTAs to the other classes.
-    const bool own_ok = nglobal < kOwnedBit;
-    std::vector<int> code_own;
     AsmPlan plan_own = plan;
     if (own_ok) {
-      code_own = code;
-      for (size_t l = 0; l < nloc; ++l) {
-        const int g = l2g[l];
-        if (g >= ndir && cnt[g + 1] - cnt[g] == 1) code_own[l] = sign[l] > 0 ? (g | kOwnedBit) : ~(g | kOwnedBit);
-      }
       plan_own.n[0] = plan.ndir[0];
       long long ent_own[kAsmK + 1];
       for (int c = 0; c <= kAsmK; ++c) ent_own[c] = entries[c];
@@ -1027,9 +1065,12 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       ITHACA_CUDA(cudaGetDevice(&dev));
       ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       cg->opart_cap = sms * 32;  // at most 32 resident CTAs per SM
-      ITHACA_CUDA(cudaMalloc(&cg->l2g_own, sizeof(int) * nloc));
+      ITHACA_CUDA(cudaMalloc(&cg->ocode, sizeof(int) * nloc));
+      ITHACA_CUDA(cudaMalloc(&cg->tail_ptr, sizeof(int) * tail_ptr.size()));
       ITHACA_CUDA(cudaMalloc(&cg->opart, sizeof(double) * cg->opart_cap));
-      ITHACA_CUDA(cudaMemcpyAsync(cg->l2g_own, code_own.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+      ITHACA_CUDA(cudaMemcpyAsync(cg->ocode, ocode.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
+      ITHACA_CUDA(cudaMemcpyAsync(cg->tail_ptr, tail_ptr.data(), sizeof(int) * tail_ptr.size(),
+                                  cudaMemcpyHostToDevice, s));
       cg->own_ok = true;
       cg->plan_own = plan_own;
     }
@@ -1273,12 +1314,14 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
     cudaEventDestroy(e1);
     *avg_ms = ms / reps;
     if (bytes_per_launch) {
-      // per element: l2g index (4 B) + gathered input + output per local dof, geometry per
-      // point (+ 8 scales per element for 16-bit geometry)
+      // per element: l2g index (4 B) + gathered input + output per local dof (+ the output
+      // code, 4 B, of the scattered FP32 output), geometry per point (+ 8 scales per
+      // element for 16-bit geometry)
       const double es = f32 ? 4.0 : 8.0, gs = half ? 2.0 : es;
       const double npt = op->deformed ? op->nq : 1;
+      const double oc = f32 && own.ctas >= 0 ? 4.0 : 0.0;
       *bytes_per_launch =
-          (double)op->E * (op->nm * (4.0 + 2.0 * es) + n_jg(op->dim) * npt * gs + (half ? 32.0 : 0.0));
+          (double)op->E * (op->nm * (4.0 + oc + 2.0 * es) + n_jg(op->dim) * npt * gs + (half ? 32.0 : 0.0));
     }
   });
 }

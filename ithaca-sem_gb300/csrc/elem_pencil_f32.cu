@@ -60,13 +60,15 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
   const dim3 block(Q * Q, EB), grid(std::min(ngroups, slots[gi]));
   T* sown = nullptr;
   double* opart = nullptr;
-  if (own != nullptr && l2g != nullptr) {
+  const int* ocode = nullptr;
+  if (own != nullptr && l2g != nullptr && own->ocode != nullptr) {
     sown = own->s;
     opart = own->part;
+    ocode = own->ocode;
     own->ctas = (int)grid.x;
   }
   k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale, sown,
-                                    opart);
+                                    opart, ocode);
 }
 
 }  // namespace dev

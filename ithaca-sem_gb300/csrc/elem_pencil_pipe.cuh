@@ -15,6 +15,11 @@
 // The arithmetic per element is exactly that of helm3_pencil_kernel (same stages, same
 // tables, same summation order), so both kernels give bit-identical results.
 //
+// Output: element-ordered (out[e * NM + m], unsigned), or, with per-local-dof output
+// codes, scattered: owned rows (free global rows with a single local entry) are written
+// straight into the assembled vector, the other signed local values into the slots of
+// an assembly-ordered buffer, so that the assembly reads them with unit stride.
+//
 // TG = __half stores the geometry slab in half precision with one FP32 scale per element
 // and field (value = half * scale, |half| <= 1): half the geometry bytes for a pointwise
 // relative perturbation of the coefficients below 2^-11 of each field's element maximum.
@@ -95,7 +100,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
                                                                const T* __restrict__ lam_ptr, int* __restrict__ err,
                                                                const float* __restrict__ gscale = nullptr,
                                                                T* __restrict__ sown = nullptr,
-                                                               double* __restrict__ opart = nullptr) {
+                                                               double* __restrict__ opart = nullptr,
+                                                               const int* __restrict__ ocode = nullptr) {
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
   constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
@@ -156,11 +162,13 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   T xv[NPT];
   int code[NPT], code2[NPT] = {};
   unsigned neg = 0;
-  // owned rows (single local entry, flagged by kOwnedBit in the code): the next group's
-  // global ids and mask, and the current group's ids, signs, mask and gathered values
-  int gnext[NPT], gcur[NPT];
+  // scattered output (ocode != nullptr): the current group's output codes, signs and
+  // gathered values; an output code is g | kOwnedBit for an owned row (a free row with a
+  // single local entry, written to sown[g] here), the position of the signed local
+  // value in the assembly-ordered buffer `out` otherwise, or negative (not written)
+  int gcur[NPT];
   T wcur[NPT];
-  unsigned own_next = 0, own_cur = 0, neg_cur = 0;
+  unsigned neg_cur = 0;
   T owned_sw = 0;  // this thread's share of s.w over the owned rows it wrote
   auto load_codes = [&](int grp, int (&dst)[NPT]) {
     const int e = grp * EB + el;
@@ -177,20 +185,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     const int e = grp * EB + el;
     const T* ip = in + (size_t)min(e, E - 1) * NM + t;
     neg = 0;
-    own_next = 0;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
       xv[j] = T(0);
-      gnext[j] = 0;
       if (e < E && slot_ok(j)) {
         if constexpr (GATHER) {
           const int c = code[j];
-          const int ca = c >= 0 ? c : ~c;
-          const int g = ca & (kOwnedBit - 1);
+          const int g = c >= 0 ? c : ~c;
           if (g >= ndir) xv[j] = in[g];
           neg |= (c < 0 ? 1u : 0u) << j;
-          own_next |= (ca & kOwnedBit ? 1u : 0u) << j;
-          gnext[j] = g;
         } else {
           xv[j] = ip[j * TPE];
         }
@@ -225,12 +228,12 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 #pragma unroll
     for (int j = 0; j < NPT; ++j)
       if (slot_ok(j)) S0[soff[j]] = (neg >> j) & 1u ? -xv[j] : xv[j];
-    if (sown != nullptr) {  // keep what the output stage needs for the owned rows
-      own_cur = own_next;
-      neg_cur = neg;
+    if (ocode != nullptr) {  // what the scattered output stage needs; the codes arrive
+      neg_cur = neg;         // during the stages below
+      const int* cp = ocode + (size_t)(active ? e : 0) * NM + t;
 #pragma unroll
       for (int j = 0; j < NPT; ++j) {
-        gcur[j] = gnext[j];
+        gcur[j] = active && slot_ok(j) ? __ldg(cp + j * TPE) : -1;
         wcur[j] = xv[j];
       }
     }
@@ -515,10 +518,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       for (int j = 0; j < NPT; ++j) {
         if (!slot_ok(j)) continue;
         const T val = S1[soff[j]];
-        if (sown != nullptr && ((own_cur >> j) & 1u)) {  // owned row: assembled here
+        if (ocode != nullptr) {
+          const int oc = gcur[j];
           const T sv = (neg_cur >> j) & 1u ? -val : val;
-          sown[gcur[j]] = sv;
-          owned_sw = fma(sv, wcur[j], owned_sw);
+          if (oc >= 0 && (oc & kOwnedBit)) {  // owned row: assembled here
+            sown[oc & (kOwnedBit - 1)] = sv;
+            owned_sw = fma(sv, wcur[j], owned_sw);
+          } else if (oc >= 0) {
+            out[oc] = sv;
+          }
         } else {
           op[j * TPE] = val;
         }

@@ -122,15 +122,21 @@ struct Op {
 // leaves the allocation.
 constexpr size_t kGeoPad = 64;
 
-// Rows of the global system with a single local entry ("owned" rows, flagged by bit 30
-// of the gather index, see kOwnedBit) can be written by the gathered element kernel
-// itself: s[g] = sign * value, with the partial s.w of each CTA in part[cta]. The
-// pipelined kernels (variants 21-42 and the 16-bit-geometry kernel) accept this; the
-// launcher reports in *ctas how many partials it wrote (-1 where it could not).
+// Scattered output of the gathered element kernel, one output code per local dof:
+//   g | kOwnedBit  the free global row g has this single local entry ("owned" row): the
+//                  kernel writes s[g] = sign * value and adds s[g] w[g] to its CTA's
+//                  partial part[cta] (w = the gathered input);
+//   pos >= 0       the signed local value goes to out[pos], a slot of the
+//                  assembly-ordered buffer that the assembly then reads with unit stride;
+//   negative       not written (Dirichlet rows).
+// The pipelined kernels (variants 21-42 and the 16-bit-geometry kernel) accept this; the
+// launcher reports in ctas how many partials it wrote (-1 where it could not, and the
+// output is element-ordered as usual).
 constexpr int kOwnedBit = 1 << 30;
 struct OwnedRows {
   float* s = nullptr;
   double* part = nullptr;
+  const int* ocode = nullptr;
   int ctas = -1;
 };
 

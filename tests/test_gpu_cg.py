@@ -127,6 +127,46 @@ def test_mixed_kernel_variants_curved_hex(ctx, variant):
     assert abs(res.iterations - ref.iterations) <= 4, (res.iterations, ref.iterations)
 
 
+def _merged_map(amap):
+    """The map with a few free global dofs merged: three interior vertices into one row
+    of 24 local entries (longer than the ELL classes), a face dof into an edge dof (6
+    entries). Any map whose every global dof has a local entry assembles an SPD system."""
+    from ithaca_gpu.mesh import AssemblyMap
+    l2g = amap.l2g.astype(np.int64).copy()
+    cnt = np.bincount(l2g, minlength=amap.nglobal)
+    free = np.arange(amap.ndir, amap.nglobal)
+    v8, k4, k2 = free[cnt[free] == 8], free[cnt[free] == 4], free[cnt[free] == 2]
+    l2g[np.isin(l2g, v8[1:3])] = v8[0]
+    l2g[l2g == k2[0]] = k4[0]
+    ids = np.unique(l2g)
+    l2g = np.searchsorted(ids, l2g)
+    return AssemblyMap(l2g, amap.sign, ids.size, amap.ndir)
+
+
+@pytest.mark.parametrize("variant", [4, 41, 42])
+def test_mixed_long_rows(ctx, variant):
+    """Rows of 1, 2, 4, 6, 8 and 24 local entries: the FP64 solve against the oracle, and
+    the mixed solve with the element-ordered (4) and the scattered (41, 42: owned rows
+    and assembly-ordered slots) output of the inner apply."""
+    from ithaca_gpu.operators import Collection, GlobalLinSysIterativeFullGPU
+    c = hex_case(4, 3, 3, 4, amp=0.08)
+    amap = _merged_map(c.mesh.assembly(c.n))
+    counts = np.bincount(amap.l2g, minlength=amap.nglobal)
+    assert counts.max() == 24 and 6 in counts
+    coll = Collection(ctx, c.shape, c.n, c.Q, c.E, c.jac, c.df, deformed=c.deformed)
+    sys_ = GlobalLinSysIterativeFullGPU(coll, amap)
+    rhs = np.random.default_rng(23).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, res64 = sys_.solve(1.0, rhs, tol=1e-12)
+    xo, it_o, _, _ = osolve.solve(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, amap, rhs, tol=1e-12)
+    assert abs(res64.iterations - it_o) <= 1, (res64.iterations, it_o)
+    assert rel_err(x64[amap.ndir:], xo[amap.ndir:]) < 1e-9
+    coll.set_variant(variant)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+    assert rel_err(x[amap.ndir:], xo[amap.ndir:]) < 1e-8
+
+
 @pytest.mark.parametrize("inner_tol", [1e-2, 1e-4])
 def test_mixed_geo16_curved_hex(ctx, inner_tol):
     """FP32 inner solves on 16-bit (per-element scaled) geometry inside FP64 refinement:
