@@ -57,21 +57,53 @@ __device__ __forceinline__ void block_partials(double (&v)[NC], double* partials
   }
 }
 
+// Deterministic CTA sums of one double per thread and slot: warp shuffles, then the
+// warps' sums in warp order. Every thread receives the totals.
+template <int NS>
+__device__ __forceinline__ void block_sum(double (&acc)[NS], double (&out)[NS]) {
+  __shared__ double sm[NS][RT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+    if (lane == 0) sm[k][warp] = acc[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    double t = sm[k][0];
+#pragma unroll
+    for (int w = 1; w < RT / 32; ++w) t += sm[k][w];
+    out[k] = t;
+  }
+  __syncthreads();
+}
+
+// This thread's share of the first n entries of p (entries threadIdx.x + i RT): the first
+// M loads are all issued before the first add (L2 loads: the entries may have been
+// written by other CTAs of the same launch); entries beyond M RT follow in a loop.
+template <int M>
+__device__ __forceinline__ double thread_partials(const double* p, int n) {
+  double v[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    const int j = threadIdx.x + i * RT;
+    v[i] = j < n ? __ldcg(p + j) : 0.0;
+  }
+  double t = v[0];
+#pragma unroll
+  for (int i = 1; i < M; ++i) t += v[i];
+  for (int j = threadIdx.x + M * RT; j < n; j += RT) t += __ldcg(p + j);
+  return t;
+}
+constexpr int kMaxP = (RBA + RT - 1) / RT;  // partials per thread of a full slot
+
 // Sum of the first n partials of `slot` (n = the CTA count of the launch that wrote them).
 __device__ __forceinline__ double reduce_slot(const double* partials, int slot, int n) {
-  __shared__ double sm[RT];
-  double s = 0;
-  // L2 loads: the partials may have been written by other CTAs of the same launch
-  for (int i = threadIdx.x; i < n; i += RT) s += __ldcg(partials + slot * RB + i);
-  sm[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = RT / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
-    __syncthreads();
-  }
-  const double r = sm[0];
-  __syncthreads();
-  return r;
+  double a[1] = {thread_partials<kMaxP>(partials + slot * RB, n)}, o[1];
+  block_sum<1>(a, o);
+  return o[0];
 }
 
 // Several slots at once (same summation order as reduce_slot for each): the loads of
@@ -80,25 +112,10 @@ __device__ __forceinline__ double reduce_slot(const double* partials, int slot, 
 template <int NS>
 __device__ __forceinline__ void reduce_slots(const double* partials, const int (&slots)[NS], double (&out)[NS],
                                              int nv, int na) {
-  __shared__ double sm[NS][RT];
+  double a[NS];
 #pragma unroll
-  for (int k = 0; k < NS; ++k) {
-    double s = 0;
-    const int n = slots[k] == 3 ? na : nv;
-    for (int i = threadIdx.x; i < n; i += RT) s += __ldcg(partials + slots[k] * RB + i);
-    sm[k][threadIdx.x] = s;
-  }
-  __syncthreads();
-  for (int w = RT / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-#pragma unroll
-      for (int k = 0; k < NS; ++k) sm[k][threadIdx.x] += sm[k][threadIdx.x + w];
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int k = 0; k < NS; ++k) out[k] = sm[k][0];
-  __syncthreads();
+  for (int k = 0; k < NS; ++k) a[k] = thread_partials<kMaxP>(partials + slots[k] * RB, slots[k] == 3 ? na : nv);
+  block_sum<NS>(a, out);
 }
 
 // ---- PCG vector kernels (T = double or float; reductions in double) ----------
@@ -344,9 +361,10 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
   }
   if (fuse_sc != nullptr) {
     __shared__ unsigned int ticket;
-    __threadfence();  // this CTA's partial is visible before it takes a ticket
-    __syncthreads();
-    if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+    if (threadIdx.x == 0) {  // thread 0 wrote this CTA's partial: visible before its ticket
+      __threadfence();
+      ticket = atomicAdd(counter, 1u);
+    }
     __syncthreads();
     if (ticket == gridDim.x - 1) {
       __threadfence();
@@ -398,24 +416,13 @@ __global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials
 __device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart, int nv,
                                   int na) {
   if (sc->done) return;
-  const int slots[3] = {0, 1, 3};
-  double red[3];
-  reduce_slots<3>(partials, slots, red, nv, na);
-  double mu_own = 0;
-  if (napart > 0) {
-    __shared__ double sm[RT];
-    double v = 0;
-    for (int i = threadIdx.x; i < napart; i += RT) v += __ldcg(apart + i);
-    sm[threadIdx.x] = v;
-    __syncthreads();
-    for (int w = RT / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
-      __syncthreads();
-    }
-    mu_own = sm[0];
-    __syncthreads();
-  }
-  const double rho_new = red[0], eps = red[1], mu = red[2] + mu_own;
+  // slots 0, 1 and 3 and the element kernel's partials, all loads in flight together
+  double a[4] = {thread_partials<kMaxP>(partials + 0 * RB, nv), thread_partials<kMaxP>(partials + 1 * RB, nv),
+                 thread_partials<kMaxP>(partials + 3 * RB, na),
+                 napart > 0 ? thread_partials<kMaxP>(apart, napart) : 0.0};
+  double red[4];
+  block_sum<4>(a, red);
+  const double rho_new = red[0], eps = red[1], mu = red[2] + red[3];
   if (threadIdx.x == 0) {
     sc->eps = eps;
     sc->mu = mu;
