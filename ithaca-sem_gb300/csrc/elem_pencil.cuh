@@ -23,8 +23,10 @@ namespace dev {
 
 // k-stride of a padded Q^3 work field (index i + Q j + PK k): at most 2-way bank
 // conflicts for the column (i, j), pencil-i (j, k) and pencil-j (i, k) lane layouts.
+// Q = 8: 73 = 9 (mod 32), which with the pipelined kernel's lane maps leaves 2-way
+// conflicts only in its two pencil-j stages.
 __host__ __device__ constexpr int pk_stride(int Q) {
-  return Q == 2 ? 5 : Q == 3 ? 9 : Q == 4 ? 19 : Q == 5 ? 25 : Q == 6 ? 36 : Q == 7 ? 51 : Q == 8 ? 69
+  return Q == 2 ? 5 : Q == 3 ? 9 : Q == 4 ? 19 : Q == 5 ? 25 : Q == 6 ? 36 : Q == 7 ? 51 : Q == 8 ? 73
        : Q == 9 ? 81 : Q == 10 ? 101 : 121;
 }
 

@@ -114,6 +114,11 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
   constexpr int PJ = L::PJ, PK = L::PK, FS = L::FS;
   constexpr int NPT = (NM + TPE - 1) / TPE;  // coefficients gathered per thread
+  // Q = 8: pencils along the unit-stride index go to threads (t / 8, t % 8) rather than
+  // (t % 8, t / 8). With row stride 8 and plane stride 73 (= 9 mod 32) the 32 lanes of
+  // a warp then hit 32 different shared-memory banks in every stage but the two
+  // j-direction derivative stages (2-way); same arithmetic per pencil either way.
+  constexpr bool M8 = (Q == 8);
   if (skip != nullptr && *skip) return;  // converged solve: the whole CTA leaves together
   if (lam_ptr != nullptr) lambda = *lam_ptr;
 
@@ -247,8 +252,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 2: BwdTrans along p: pencils (q, r) ----
-    if (t < N * N) {
-      const int q = t % N, r = t / N;
+    if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
+      const int q = M8 ? t / 8 : t % N, r = M8 ? t % 8 : t / N;
       T c[N];
 #pragma unroll
       for (int p = 0; p < N; ++p) c[p] = S0[p + PJ * q + PK * r];
@@ -269,8 +274,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 3: along q: pencils (i, r) ----
-    if (t < Q * N) {
-      const int i = t % Q, r = t / Q;
+    if (M8 ? t % 8 < N : t < Q * N) {
+      const int i = M8 ? t / 8 : t % Q, r = M8 ? t % 8 : t / Q;
       T c[N];
 #pragma unroll
       for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
@@ -322,21 +327,21 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     __syncthreads();
     // ---- 5: d/dxi_0 on pencils (j, k) -> S0 ; d/dxi_1 on pencils (i, k) -> S1 ----
     {
-      const int pj = t % Q, pk = t / Q;
+      const int pj = M8 ? t / 8 : t % Q, pk = M8 ? t % 8 : t / Q;
       T c[Q];
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = SU[a + PJ * pj + PK * pk];
-      const int pi = t % Q;
+      const int pi = t % Q, pkb = t / Q;
       if constexpr (PACK) {
         T o[Q];
         contract2<Q, Q, QP, false>(DF, c, o);
 #pragma unroll
         for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
 #pragma unroll
-        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pkb];
         contract2<Q, Q, QP, false>(DF, c, o);
 #pragma unroll
-        for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pk] = o[j];
+        for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pkb] = o[j];
       } else {
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
@@ -346,13 +351,13 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
           S0[i + PJ * pj + PK * pk] = acc;
         }
 #pragma unroll
-        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pk];
+        for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pkb];
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
           T acc = tab.D[j] * c[0];
 #pragma unroll
           for (int a = 1; a < Q; ++a) acc = fma(tab.D[a * Q + j], c[a], acc);
-          S1[pi + PJ * j + PK * pk] = acc;
+          S1[pi + PJ * j + PK * pkb] = acc;
         }
       }
     }
@@ -410,7 +415,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     if (NB == 1 && tid == 0 && has_next) issue_geometry(nxt, 0);
     // ---- 7: D^T along i on pencils (j, k) in S0, along j on pencils (i, k) in S1 ----
     {
-      const int pj = t % Q, pk = t / Q;
+      const int pj = M8 ? t / 8 : t % Q, pk = M8 ? t % 8 : t / Q;
       T c[Q], o[Q];
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S0[a + PJ * pj + PK * pk];
@@ -427,9 +432,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       }
 #pragma unroll
       for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
-      const int pi = t % Q;
+      const int pi = t % Q, pkb = t / Q;
 #pragma unroll
-      for (int a = 0; a < Q; ++a) c[a] = S1[pi + PJ * a + PK * pk];
+      for (int a = 0; a < Q; ++a) c[a] = S1[pi + PJ * a + PK * pkb];
       if constexpr (PACK) {
         contract2<Q, Q, QP, false>(DT, c, o);
       } else {
@@ -442,7 +447,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         }
       }
 #pragma unroll
-      for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pk] = o[j];
+      for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pkb] = o[j];
     }
     __syncthreads();
     // ---- 8: sum the three directions on columns, IProduct along k -> SU as (i, j, r) ----
@@ -469,8 +474,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 9: along j: pencils (i, r) -> S0 as (i, q, r) ----
-    if (t < Q * N) {
-      const int i = t % Q, r = t / Q;
+    if (M8 ? t % 8 < N : t < Q * N) {
+      const int i = M8 ? t / 8 : t % Q, r = M8 ? t % 8 : t / Q;
       T c[Q];
 #pragma unroll
       for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
@@ -491,8 +496,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 10: along i: pencils (q, r) -> S1 as (p, q, r) ----
-    if (t < N * N) {
-      const int q = t % N, r = t / N;
+    if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
+      const int q = M8 ? t / 8 : t % N, r = M8 ? t % 8 : t / N;
       T c[Q];
 #pragma unroll
       for (int i = 0; i < Q; ++i) c[i] = S0[i + PJ * q + PK * r];
