@@ -9,7 +9,7 @@ Jacobi-preconditioned CG solve of the assembled C0 system to an FP64 relative re
 Inputs are synthetic and seeded; no dataset is involved.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--order P] [--mesh M]
-  python bench.py --config quad2d|mixed2d|batched|pod|adjoint|all   (secondary workloads)
+  python bench.py --config quad2d|mixed2d|hex_orders|batched|pod|adjoint|all   (secondary workloads)
 
 `--impl reference` times the reference path's CPU implementation on the host cores
 (the compiled C++ port of the reference kernels and CG recurrence, oracle/cport).
@@ -635,8 +635,57 @@ def suite_adjoint(args):
           dtype="f64", J=J, grad_max=float(g.abs().max()))
 
 
-SUITES = {"quad2d": suite_quad2d, "mixed2d": suite_mixed2d, "batched": suite_batched, "pod": suite_pod,
-          "adjoint": suite_adjoint}
+def suite_hex_orders(args):
+    """Config 2 as a sweep: 32^3 curved hexes at P = 4, 6, 8 (Q = P + 2): the four
+    operators (GDOF/s, Ndof = E n^3; Helmholtz also in FP32 with the autotuned kernel)
+    and Jacobi PCG to 1e-12, FP64 (the reference recurrence) and mixed."""
+    import torch
+    from ithaca_gpu.operators import Collection
+    from ithaca_gpu.workload import hex_workload
+    rows = []
+    for P in (4, 6, 8):
+        w = hex_workload(32, P)
+        ctx, coll, sysg, amap = w["ctx"], w["coll"], w["system"], w["amap"]
+        E, n, Q, N, ndir = w["mesh"].E, w["n"], w["Q"], amap.nglobal, amap.ndir
+        stream = torch.cuda.ExternalStream(ctx.stream, device="cuda:0")
+        gen = torch.Generator(device="cuda").manual_seed(P)
+        u = torch.rand(E * n ** 3, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+        phys = torch.empty(E * Q ** 3, dtype=torch.float64, device="cuda")
+        coef = torch.empty_like(u)
+        d = [torch.empty_like(phys) for _ in range(3)]
+        coll.bwdtrans(u, phys)
+        ops = {"bwdtrans": lambda: coll.bwdtrans(u, phys), "iproduct": lambda: coll.iproduct(phys, coef),
+               "physderiv": lambda: coll.physderiv(phys, d), "helmholtz": lambda: coll.helmholtz(1.0, u, coef)}
+        gdofs = {k: E * n ** 3 / (_time_device(torch, stream, f, 10, 2) / 1e3) / 1e9 for k, f in ops.items()}
+        coll32 = Collection(ctx, "hex", n, Q, E, w["jac"], w["df"], deformed=True, precision="fp32")
+        v32, _ = coll32.autotune(reps=5)
+        u32, o32 = u.float(), torch.empty(E * n ** 3, dtype=torch.float32, device="cuda")
+        gdofs["helmholtz_fp32"] = E * n ** 3 / (
+            _time_device(torch, stream, lambda: coll32.helmholtz(1.0, u32, o32), 20, 3) / 1e3) / 1e9
+        sysg.autotune_inner(1.0, reps=5)
+        b, x = w["b"], torch.zeros_like(w["b"])
+        solves = {}
+        for mode in ("fp64", "mixed"):
+            reps = 1 if (mode == "fp64" and P == 8) else min(args.steps, 2)
+            ms = _time_device(torch, stream, lambda: sysg.solve(1.0, b, x, tol=1e-12, mode=mode), reps, 1)
+            _, res = sysg.solve(1.0, b, x, tol=1e-12, mode=mode)
+            solves[mode] = {"solves_per_s": 1e3 / ms, "ms": ms, "iterations": res.iterations,
+                            "outer": res.outer_iterations, "rel_residual": res.rel_residual}
+        rows.append({"P": P, "n": n, "Q": Q, "global_dofs": N, "solve_dofs": N - ndir, "gdofs": gdofs,
+                     "fp32_helmholtz_variant": v32, "solve_1e-12": solves})
+        del w, coll, coll32, sysg, u, phys, coef, d, u32, o32, b, x
+        ctx.close()
+        torch.cuda.empty_cache()
+    cfg = {"workload": "3-D Helmholtz, 32^3 hexes curved by x + 0.05 sin(2 pi y) sin(2 pi z), P = 4, 6, 8, "
+                       "Q = P + 2, lambda = 1, Jacobi PCG to 1e-12",
+           "elements": 32768, "l2": "operands exceed L2 at every order (geometry >= 200 MB)"}
+    _line("config 2: 3-D Helmholtz operator GDOF/s and CG solves/s (1e-12) at P = 4, 6, 8",
+          rows[1]["solve_1e-12"]["mixed"]["solves_per_s"], "solves/s", args, cfg, dtype="f64 / f32 inner",
+          orders=rows)
+
+
+SUITES = {"quad2d": suite_quad2d, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
+          "pod": suite_pod, "adjoint": suite_adjoint}
 
 
 def main():

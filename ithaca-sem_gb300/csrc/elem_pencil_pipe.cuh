@@ -141,8 +141,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     const uintptr_t lo = a0 & ~uintptr_t(15);
     const uintptr_t hi = (a0 + (size_t)ne * GEO * sizeof(TG) + 15) & ~uintptr_t(15);
     mbar_arrive_expect_tx(bar + b, static_cast<uint32_t>(hi - lo));
-    tma_bulk_load(geo_base + b * L::GEO_BYTES, reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo),
-                  bar + b);
+    // the geometry is read once per launch: evict it from L2 first
+    tma_bulk_load_hint(geo_base + b * L::GEO_BYTES, reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo),
+                       bar + b, l2_evict_first_policy());
   };
   auto geometry_of = [&](int grp, int b) -> const TG* {
     const uintptr_t a0 = reinterpret_cast<uintptr_t>(jg + (size_t)grp * EB * GEO);
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     for (int j = 0; j < NPT; ++j) {
       dst[j] = 0;
       if (e < E && slot_ok(j)) {
-        if constexpr (GATHER) dst[j] = __ldg(lp + j * TPE);
+        if constexpr (GATHER) dst[j] = __ldcs(lp + j * TPE);  // read once per launch
       }
     }
   };
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       const int* cp = ocode + (size_t)(active ? e : 0) * NM + t;
 #pragma unroll
       for (int j = 0; j < NPT; ++j) {
-        gcur[j] = active && slot_ok(j) ? __ldg(cp + j * TPE) : -1;
+        gcur[j] = active && slot_ok(j) ? __ldcs(cp + j * TPE) : -1;
         wcur[j] = xv[j];
       }
     }
