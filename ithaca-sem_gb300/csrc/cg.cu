@@ -57,6 +57,29 @@ __device__ __forceinline__ void block_partials(double (&v)[NC], double* partials
   }
 }
 
+// The same from FP32 per-thread values: the warp sums in FP32 (shuffles), only the sum of
+// a CTA's warp sums in FP64, by one thread per slot. FP64 arithmetic runs at ~1/60 of the
+// FP32 rate on this GPU, so FP64 shuffle trees over every lane of every CTA cost several
+// microseconds at the end of each kernel.
+template <int NC>
+__device__ __forceinline__ void block_partials(float (&v)[NC], double* partials, const int* slots) {
+  __shared__ double sm[NC][RT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    if (lane == 0) sm[c][warp] = (double)v[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double s = sm[threadIdx.x][0];
+#pragma unroll
+    for (int w = 1; w < RT / 32; ++w) s += sm[threadIdx.x][w];
+    partials[slots[threadIdx.x] * RB + blockIdx.x] = s;
+  }
+}
+
 // Deterministic CTA sums of one double per thread and slot: warp shuffles, then the
 // warps' sums in warp order. Every thread receives the totals.
 template <int NS>
@@ -220,7 +243,7 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
     reinterpret_cast<float4*>(r)[c] = R;
     reinterpret_cast<float4*>(w)[c] = W;
   }
-  double v[2] = {(double)rw, (double)rr};
+  float v[2] = {rw, rr};
   const int slots[2] = {0, 1};
   block_partials<2>(v, partials, slots);
 }
@@ -354,8 +377,8 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
       }
     }
   }
-  double v[1] = {(double)sw};
-  if (partials) {
+  T v[1] = {sw};
+  if (partials != nullptr && w != nullptr) {  // without w the element kernel summed s.w
     const int slots[1] = {3};
     block_partials<1>(v, partials, slots);
   }
@@ -368,7 +391,7 @@ __global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPl
     __syncthreads();
     if (ticket == gridDim.x - 1) {
       __threadfence();
-      scalars_iter_body(partials, fuse_sc, apart, napart, nv, gridDim.x);
+      scalars_iter_body(partials, fuse_sc, apart, napart, nv, w != nullptr ? (int)gridDim.x : 0);
       if (threadIdx.x == 0) *counter = 0u;  // re-armed for the next iteration
     }
   }
@@ -411,17 +434,37 @@ __global__ void __launch_bounds__(RT) scalars_iter_kernel(const double* partials
   scalars_iter_body(partials, sc, nullptr, 0, nv, na);
 }
 
-// apart (napart entries): the element kernel's partials of s.w over the rows it
-// assembled itself, added to slot 3 (in a fixed order).
+// apart (napart entries): partials of s.w summed by the element kernel (the whole dot
+// when it wrote the scattered output, the assembly's slot 3 then holding zeros), added
+// to slot 3 (in a fixed order).
 __device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart, int nv,
                                   int na) {
   if (sc->done) return;
-  // slots 0, 1 and 3 and the element kernel's partials, all loads in flight together
-  double a[4] = {thread_partials<kMaxP>(partials + 0 * RB, nv), thread_partials<kMaxP>(partials + 1 * RB, nv),
-                 thread_partials<kMaxP>(partials + 3 * RB, na),
-                 napart > 0 ? thread_partials<kMaxP>(apart, napart) : 0.0};
+  // Few FP64 instructions (one CTA does this between two kernels): each thread sums its
+  // share of slots 0, 1, 3 and of the element kernel's partials (loads in flight
+  // together, empty sources skipped), then warp 0 sums the 256 shares of each.
+  constexpr int MV = (RB + RT - 1) / RT;
+  double a[4];
+  a[0] = thread_partials<MV>(partials + 0 * RB, nv);
+  a[1] = thread_partials<MV>(partials + 1 * RB, nv);
+  a[2] = na > 0 ? thread_partials<kMaxP>(partials + 3 * RB, na) : 0.0;
+  a[3] = napart > 0 ? thread_partials<MV>(apart, napart) : 0.0;
+  __shared__ double sh[4][RT];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] = a[k];
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  constexpr int PER = RT / 32;
   double red[4];
-  block_sum<4>(a, red);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double t = sh[k][threadIdx.x * PER];
+#pragma unroll
+    for (int i = 1; i < PER; ++i) t += sh[k][threadIdx.x * PER + i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+    red[k] = t;
+  }
   const double rho_new = red[0], eps = red[1], mu = red[2] + red[3];
   if (threadIdx.x == 0) {
     sc->eps = eps;
@@ -670,8 +713,9 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, skip_ptr(cg), try_own ? &own : nullptr);
   if (try_own && own.ctas >= 0) {  // the element kernel wrote the owned rows of s
     if (own.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
+    // the element kernel summed the whole s.w (its partials in opart): no w here
     assemble_dot_kernel<T, true, true><<<cg->rba, RT, 0, s>>>(cg->plan_own, true, cg->asm_rows, nullptr, cg->tail_ptr,
-                                                         nullptr, v.yloc, v.s, v.w, skip_ptr(cg), cg->partials,
+                                                         nullptr, v.yloc, v.s, nullptr, skip_ptr(cg), cg->partials,
                                                          cg->sc, cg->counter, cg->opart, own.ctas, cg->rbv);
   } else {
     assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,

@@ -175,7 +175,10 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   int gcur[NPT];
   T wcur[NPT];
   unsigned neg_cur = 0;
-  T owned_sw = 0;  // this thread's share of s.w over the owned rows it wrote
+  // this thread's share of s.w: with s = P^T y (assembly) and the gathered input P w,
+  // s.w = y.(P w), the local values times their signed gathered inputs (zero on
+  // Dirichlet rows), so the whole dot is summed here and the assembly needs no w
+  T loc_sw = 0;
   auto load_codes = [&](int grp, int (&dst)[NPT]) {
     const int e = grp * EB + el;
     const int* lp = l2g + (size_t)min(e, E - 1) * NM + t;
@@ -527,12 +530,11 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         if (ocode != nullptr) {
           const int oc = gcur[j];
           const T sv = (neg_cur >> j) & 1u ? -val : val;
-          if (oc >= 0 && (oc & kOwnedBit)) {  // owned row: assembled here
+          if (oc >= 0 && (oc & kOwnedBit))  // owned row: assembled here
             sown[oc & (kOwnedBit - 1)] = sv;
-            owned_sw = fma(sv, wcur[j], owned_sw);
-          } else if (oc >= 0) {
+          else if (oc >= 0)
             out[oc] = sv;
-          }
+          loc_sw = fma(sv, wcur[j], loc_sw);
         } else {
           op[j * TPE] = val;
         }
@@ -542,17 +544,23 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     // buffer read here is refilled by the copy issued at the top of the iteration after next
     __syncthreads();
   }
-  if (opart != nullptr) {  // this CTA's s.w over its owned rows, summed in FP64
-    double v = (double)owned_sw;
+  if (opart != nullptr) {  // this CTA's share of s.w: warp sums in T, the CTA sum in FP64
+    // Q^2 EB threads need not fill the last warp: shuffle among its existing lanes only
+    constexpr int NT = Q * Q * EB, NW = (NT + 31) / 32;
+    const int nl = min(32, NT - (tid & ~31)), lane = tid & 31;
+    const unsigned mask = nl == 32 ? 0xffffffffu : (1u << nl) - 1u;
+    T v = loc_sw;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    for (int off = 16; off > 0; off >>= 1) {
+      const T o = __shfl_down_sync(mask, v, off);
+      if (lane + off < nl) v += o;
+    }
     double* red = reinterpret_cast<double*>(work);  // the work area is free after the loop
-    constexpr int NW = (Q * Q * EB + 31) / 32;
-    if ((tid & 31) == 0) red[tid >> 5] = v;
+    if ((tid & 31) == 0) red[tid >> 5] = (double)v;
     __syncthreads();
     if (tid == 0) {
-      double sum = 0;
-      for (int w = 0; w < NW; ++w) sum += red[w];
+      double sum = red[0];
+      for (int w = 1; w < NW; ++w) sum += red[w];
       opart[blockIdx.x] = sum;
     }
   }

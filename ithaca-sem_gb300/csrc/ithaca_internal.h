@@ -124,11 +124,13 @@ constexpr size_t kGeoPad = 64;
 
 // Scattered output of the gathered element kernel, one output code per local dof:
 //   g | kOwnedBit  the free global row g has this single local entry ("owned" row): the
-//                  kernel writes s[g] = sign * value and adds s[g] w[g] to its CTA's
-//                  partial part[cta] (w = the gathered input);
+//                  kernel writes s[g] = sign * value;
 //   pos >= 0       the signed local value goes to out[pos], a slot of the
 //                  assembly-ordered buffer that the assembly then reads with unit stride;
 //   negative       not written (Dirichlet rows).
+// Every CTA also writes part[cta], its share of s.w = y.(P w) over all its local values
+// (w = the gathered input, P the signed gather), i.e. the whole dot product of the
+// assembled output with the input.
 // The pipelined kernels (variants 21-42 and the 16-bit-geometry kernel) accept this; the
 // launcher reports in ctas how many partials it wrote (-1 where it could not, and the
 // output is element-ordered as usual).
