@@ -61,6 +61,30 @@ __device__ __forceinline__ void block_sum(double (&v)[NC], double* out /* NC val
   __syncthreads();
 }
 
+// FP32 per-thread values: warp sums in FP32 (shuffles) and only the sum of the warp sums
+// in FP64. FP64 runs at ~1/60 of the FP32 rate on this GPU, and an FP64 shuffle tree over
+// every lane for every chunk keeps the SMs' FP64 pipes busy for tens of microseconds
+// per iteration of the batch.
+template <int NC>
+__device__ __forceinline__ void block_sum(float (&v)[NC], double* out /* NC values */) {
+  __shared__ double sm[NC][BT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    if (lane == 0) sm[c][warp] = (double)v[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double t = sm[threadIdx.x][0];
+#pragma unroll
+    for (int w = 1; w < BT / 32; ++w) t += sm[threadIdx.x][w];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
 // part layout: part[slot * nchunks + chunk]; slots 0 r.w, 1 r.r, 2 b.b, 3 s.w
 template <typename T>
 __global__ void __launch_bounds__(BT) binit_kernel(const Chunk* __restrict__ chunks, int nchunks,
@@ -138,7 +162,7 @@ __global__ void __launch_bounds__(BT, GRID / 152) bupdate_kernel(const Chunk* __
         }
       }
     }
-    double v[2] = {(double)rw, (double)rr};
+    T v[2] = {rw, rr};
     block_sum<2>(v, res);
     if (threadIdx.x < 2) part[threadIdx.x * nchunks + c] = res[threadIdx.x];
   }
@@ -193,25 +217,35 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
         }
       }
     }
-    double v[1] = {(double)sw};
+    T v[1] = {sw};
     block_sum<1>(v, res);
     if (threadIdx.x == 0) part[3 * nchunks + c] = res[0];
   }
 }
 
-__device__ __forceinline__ double sum_range(const double* part, int nchunks, int slot, int c0, int c1) {
-  __shared__ double sm[BT];
-  double s = 0;
-  for (int c = c0 + threadIdx.x; c < c1; c += BT) s += part[slot * nchunks + c];
-  sm[threadIdx.x] = s;
+// Sums over chunks [c0, c1) of several partial slots at once: every load of a thread in
+// flight together, one shared-memory tree (one barrier per level) for all slots.
+template <int NS>
+__device__ __forceinline__ void sum_ranges(const double* part, int nchunks, const int (&slots)[NS], int c0, int c1,
+                                           double (&out)[NS]) {
+  __shared__ double sm[NS][BT];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    double t = 0;
+    for (int c = c0 + threadIdx.x; c < c1; c += BT) t += part[slots[k] * nchunks + c];
+    sm[k][threadIdx.x] = t;
+  }
   __syncthreads();
   for (int wdt = BT / 2; wdt > 0; wdt >>= 1) {
-    if (threadIdx.x < wdt) sm[threadIdx.x] += sm[threadIdx.x + wdt];
+    if (threadIdx.x < wdt) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) sm[k][threadIdx.x] += sm[k][threadIdx.x + wdt];
+    }
     __syncthreads();
   }
-  const double r = sm[0];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) out[k] = sm[k][0];
   __syncthreads();
-  return r;
 }
 
 // One CTA per solve: the reference's initial step (NekLinSysIterCG.cpp:147-190).
@@ -221,8 +255,10 @@ __global__ void __launch_bounds__(BT) bscalars_init_kernel(Scal* __restrict__ sc
   Scal& S = sc[sv];
   if (S.done) return;  // solves that need no (more) work were flagged on entry
   const int c0 = cstart[sv], c1 = cstart[sv + 1];
-  const double rw = sum_range(part, nchunks, 0, c0, c1), rr = sum_range(part, nchunks, 1, c0, c1);
-  const double bb = sum_range(part, nchunks, 2, c0, c1) + S.bb_dir, sw = sum_range(part, nchunks, 3, c0, c1);
+  const int slots[4] = {0, 1, 2, 3};
+  double red[4];
+  sum_ranges<4>(part, nchunks, slots, c0, c1, red);
+  const double rw = red[0], rr = red[1], bb = red[2] + S.bb_dir, sw = red[3];
   if (threadIdx.x == 0) {
     S.rhs_mag = S.mag_override > 0 ? S.mag_override : (bb > 1e-6 ? bb : 1.0);
     S.eps = rr;
@@ -255,8 +291,10 @@ __global__ void __launch_bounds__(BT) bscalars_iter_kernel(Scal* __restrict__ sc
   Scal& S = sc[sv];
   if (S.done) return;
   const int c0 = cstart[sv], c1 = cstart[sv + 1];
-  const double rho_new = sum_range(part, nchunks, 0, c0, c1), eps = sum_range(part, nchunks, 1, c0, c1);
-  const double mu = sum_range(part, nchunks, 3, c0, c1);
+  const int slots[3] = {0, 1, 3};
+  double red[3];
+  sum_ranges<3>(part, nchunks, slots, c0, c1, red);
+  const double rho_new = red[0], eps = red[1], mu = red[2];
   if (threadIdx.x == 0) {
     S.eps = eps;
     S.mu = mu;
@@ -314,7 +352,10 @@ __global__ void __launch_bounds__(BT) bouter_kernel(Scal* __restrict__ outer, Sc
                                                     int max_iter_inner) {
   const int sv = blockIdx.x;
   const int c0 = cstart[sv], c1 = cstart[sv + 1];
-  const double rr = sum_range(part, nchunks, 1, c0, c1), bb = sum_range(part, nchunks, 2, c0, c1);
+  const int slots[2] = {1, 2};
+  double red[2];
+  sum_ranges<2>(part, nchunks, slots, c0, c1, red);
+  const double rr = red[0], bb = red[1];
   if (threadIdx.x == 0) {
     Scal& O = outer[sv];
     O.rn2 = rr;
