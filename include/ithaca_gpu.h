@@ -150,6 +150,13 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* op, const int* l2g, const double* sign, 
                          ithaca_gpu_cg** cg);
 int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg);
 
+/* Solver path for 2-D systems. mode -1 (default): systems of at most 2^20 global dofs run
+ * the persistent solver, one cooperative launch per (inner) PCG with the phases separated
+ * by bounded grid barriers; larger ones the graph-captured kernels. 0: always the
+ * graph-captured kernels. 1: always the persistent solver for 2-D systems. Both paths run
+ * the same recurrence (NekLinSysIterCG.cpp:104-263); 3-D systems always use the graph. */
+int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode);
+
 typedef struct {
   double tol;          /* IterativeSolverTolerance (default 1e-9); stop when ||r||^2 < tol^2 ||b||^2 */
   int max_iter;        /* NekLinSysMaxIterations (default 5000)                                      */

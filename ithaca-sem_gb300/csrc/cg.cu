@@ -21,6 +21,7 @@
 
 #include <cuda_fp16.h>
 
+#include "cg_shared.h"
 #include "ithaca_internal.h"
 
 namespace ithaca {
@@ -29,13 +30,10 @@ constexpr int RB = 760;      // reduction CTAs: 5 per SM of 152 (one wave at <= 
 constexpr int RBA = 1216;    // assembly CTAs: 8 per SM (<= 32 registers); partial slot 3 holds RBA entries
 constexpr int RT = 256;      // threads per reduction CTA
 constexpr int NSLOT = 4;     // partial-sum slots: 0 r.w, 1 r.r, 2 b.b, 3 s.w
+// 2-D systems up to this many global dofs run the persistent solver by default: below it
+// the graph-captured kernels are bound by launch and drain rather than by their work
+constexpr int kPersistMaxN = 1 << 20;
 
-struct CgScalars {
-  double alpha, beta, rho, mu, eps, rhs_mag, tol2, mag_override;
-  double lambda;
-  float lambda32, pad0;
-  int iters, k, done, status, max_iter, pad1;
-};
 
 // ---- reductions -------------------------------------------------------------
 template <int NC>
@@ -250,25 +248,6 @@ __global__ void __launch_bounds__(RT) pcg_update_f32x4_kernel(int N, int ndir, c
 
 __device__ void scalars_iter_body(const double* partials, CgScalars* sc, const double* apart, int napart, int nv,
                                   int na);
-
-// ---- assembly plan: rows grouped by their number of local entries ----------------
-// Class c < kAsmK holds the rows with exactly c + 1 local entries, stored ELL-style
-// (entry j of row slot i at cols[col_off + j * n + i], entries in increasing local
-// index, as the reference's scatter-add visits them); class kAsmK holds the rows with
-// more entries, which are read through the CSR arrays. Inside a class the rows are in
-// increasing global order, so the Dirichlet rows (numbered first) lead each class.
-// The CTAs of a launch are split among the classes in proportion to their entries, so
-// every CTA (and warp) handles rows of one length: no divergence, and each thread keeps
-// up to kAsmK independent entry loads in flight.
-constexpr int kAsmK = 8;
-struct AsmPlan {
-  int n[kAsmK + 1];          // rows per class
-  int ndir[kAsmK + 1];       // leading Dirichlet rows per class
-  int rows_off[kAsmK + 1];   // first slot of the class in the row list
-  long long col_off[kAsmK];  // first ELL entry of the class
-  long long tail_off;        // assembly-ordered buffer: first entry of the tail class
-  int cta0[kAsmK + 2];       // CTAs [cta0[c], cta0[c + 1]) work on class c
-};
 
 template <typename T, bool SIGNED>
 __device__ __forceinline__ T asm_value(const T* __restrict__ yloc, int c) {
@@ -600,6 +579,11 @@ struct Cg {
   int* ocode = nullptr;     // nloc output codes (see OwnedRows)
   int* tail_ptr = nullptr;  // rows of the tail class + 1: first slot of each row's entries
   AsmPlan plan_own{};
+  // persistent small-system solver (2-D, cg_persist.cu): -1 automatic (N <= kPersistMaxN),
+  // 0 off, 1 whenever the system is 2-D; grid-barrier state; SM count
+  int persist = -1;
+  unsigned* bar = nullptr;
+  int sms = 0;
   double* opart = nullptr;  // per-CTA s.w partials of the element kernel
   int opart_cap = 0;
   int* asm_rows = nullptr;  // N: global rows, grouped by class
@@ -635,6 +619,7 @@ Cg::~Cg() {
   cudaFree(asm_rows);
   cudaFree(ocode);
   cudaFree(tail_ptr);
+  cudaFree(bar);
   cudaFree(opart);
   cudaFree(asm_cols);
   cudaFree(cols);
@@ -755,6 +740,43 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   init.lambda32 = (float)lambda;
   *cg->sc_host = init;
   ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
+  Op* op = cg->op;
+  const bool persist = op->dim == 2 && cg->own_ok && cg->bar != nullptr && !cg->geo16 &&
+                       (cg->persist == 1 || (cg->persist < 0 && cg->N <= kPersistMaxN));
+  if (persist) {  // the whole solve in one cooperative launch (cg_persist.cu)
+    PersistArgs<T> a{};
+    a.N = cg->N;
+    a.ndir = cg->ndir;
+    a.E = op->E;
+    a.deformed = op->deformed;
+    a.l2g = cg->l2g;
+    a.ocode = cg->ocode;
+    a.asm_rows = cg->asm_rows;
+    a.tail_ptr = cg->tail_ptr;
+    a.plan = cg->plan;
+    a.x = v.x;
+    a.r = v.r;
+    a.w = v.w;
+    a.s = v.s;
+    a.p = v.p;
+    a.q = v.q;
+    a.yslot = v.yloc;
+    a.b = v.b;
+    a.dinv = v.dinv;
+    a.tab = tab;
+    a.jg = jg;
+    a.part = cg->partials;
+    a.bar = cg->bar;
+    a.err = c->derr;
+    a.sc = cg->sc;
+    if (launch_cg2_persistent<T>(op->n, op->Q, a, cg->sms, s)) {
+      c->launches++;
+      ITHACA_CUDA(cudaMemcpyAsync(cg->sc_host, cg->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
+      ITHACA_CUDA(cudaStreamSynchronize(s));
+      c->check_device_error();
+      return;
+    }
+  }
   pcg_init_kernel<T><<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
   launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
   assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
@@ -1116,6 +1138,8 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       ITHACA_CUDA(cudaGetDevice(&dev));
       ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       cg->opart_cap = sms * 32;  // at most 32 resident CTAs per SM
+      cg->sms = sms;
+      ITHACA_CUDA(cudaMalloc(&cg->bar, 2 * sizeof(unsigned)));
       ITHACA_CUDA(cudaMalloc(&cg->ocode, sizeof(int) * nloc));
       ITHACA_CUDA(cudaMalloc(&cg->tail_ptr, sizeof(int) * tail_ptr.size()));
       ITHACA_CUDA(cudaMalloc(&cg->opart, sizeof(double) * cg->opart_cap));
@@ -1144,6 +1168,14 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     ITHACA_CUDA(cudaStreamSynchronize(s));
     retain_op(op);  // the solver holds its operator (and through it the context)
     *out = cg.release();
+  });
+}
+
+int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode) {
+  return cg_guarded([&] {
+    req(cg != nullptr, "null solver");
+    req(mode >= -1 && mode <= 1, "persistent mode must be -1, 0 or 1");
+    cg->persist = mode;
   });
 }
 

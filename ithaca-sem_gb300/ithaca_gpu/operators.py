@@ -326,6 +326,11 @@ class GlobalLinSysIterativeFullGPU:
         C.call("ithaca_gpu_kappa_gradient", self.handle, px, pp, pg, d)
         return grad
 
+    def set_persistent(self, mode):
+        """Solver path of 2-D systems: -1 automatic (persistent up to 2^20 dofs), 0 the
+        graph-captured kernels, 1 the persistent single-launch solver."""
+        C.call("ithaca_gpu_cg_set_persistent", self.handle, int(mode))
+
     def profile_apply(self, lam, mode="mixed", reps=20):
         """Average device time (ms) of the gather + element-apply kernel the solver
         launches for `mode`, timed with CUDA events on the context stream, and the
