@@ -136,6 +136,9 @@ __global__ void __launch_bounds__(256) helm_kernel(const T* __restrict__ in, T* 
   const int ee = e < E ? e : E - 1;
   // batched solves: elements of converged solves (skip[esolve[e] * skip_stride] != 0) do no I/O
   const bool active = e < E && !(esolve != nullptr && skip[(size_t)esolve[ee] * skip_stride] != 0);
+  // a CTA whose elements all belong to converged solves leaves at once (as the batched
+  // vector kernels skip converged chunks), so late iterations cost little
+  if (esolve != nullptr && !__syncthreads_or(active)) return;
 
   const int t = threadIdx.x;
 
