@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(BT) binit_kernel(const Chunk* __restrict__ chu
   __shared__ double res[3];
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
+    if (sc[ch.solve].done) continue;  // converged (or idle) solve: no work, no partials
     double v[3] = {0, 0, 0};
     if (!sc[ch.solve].done) {
       for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(BT, GRID / 152) bupdate_kernel(const Chunk* __
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const Scal& S = sc[ch.solve];
+    if (S.done) continue;  // converged solve: no work, no partials (its scalars step skips it)
     // per-thread sums in T (a chunk gives each thread 16 dofs; FP32 sums keep the
     // FP32 solve off the slow FP64 pipe), CTA sums in FP64
     T rw = 0, rr = 0;
@@ -177,6 +179,7 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
   __shared__ double res[1];
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
+    if (sc[ch.solve].done) continue;  // converged solve: no work, no partials
     T sw = 0;  // per-thread s.w in T, CTA sum in FP64
     if (!sc[ch.solve].done) {
       // U rows per thread step; each row's entries summed in CSR order, the first
