@@ -322,15 +322,18 @@ __global__ void __launch_bounds__(BT) bscalars_iter_kernel(Scal* __restrict__ sc
 }
 
 // ---- mixed-precision outer step kernels (FP64) ----
-// r = b - sum yloc on the free dofs of solves not yet converged; partial r.r (slot 1), b.b (slot 2)
+// r = b - sum yloc on the free dofs; partial r.r (slot 1), b.b (slot 2). With skip_done the
+// solves already converged (outer_done) are left out: their x no longer changes, and their
+// norms stay as the outer kernel last recorded them.
 __global__ void __launch_bounds__(BT) bresidual_kernel(const Chunk* __restrict__ chunks, int nchunks,
                                                        const Scal* __restrict__ sc, const int* __restrict__ rowptr,
                                                        const int* __restrict__ cols, const double* __restrict__ yloc,
                                                        const double* __restrict__ b, double* __restrict__ r,
-                                                       double* __restrict__ part) {
+                                                       double* __restrict__ part, int skip_done) {
   __shared__ double res[2];
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
+    if (skip_done && sc[ch.solve].outer_done) continue;
     double v[2] = {0, 0};
     for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
       double acc = 0;
@@ -352,18 +355,21 @@ __global__ void __launch_bounds__(BT) bresidual_kernel(const Chunk* __restrict__
 __global__ void __launch_bounds__(BT) bouter_kernel(Scal* __restrict__ outer, Scal* __restrict__ inner,
                                                     const double* __restrict__ part, int nchunks,
                                                     const int* __restrict__ cstart, double tol2, double inner_tol2,
-                                                    int max_iter_inner) {
+                                                    int max_iter_inner, int skip_done) {
   const int sv = blockIdx.x;
   const int c0 = cstart[sv], c1 = cstart[sv + 1];
+  const bool was_done = skip_done && outer[sv].outer_done;  // its residual was not recomputed
   const int slots[2] = {1, 2};
   double red[2];
   sum_ranges<2>(part, nchunks, slots, c0, c1, red);
   const double rr = red[0], bb = red[1];
   if (threadIdx.x == 0) {
     Scal& O = outer[sv];
-    O.rn2 = rr;
-    O.bn2 = bb;
-    if (!isfinite(rr)) O.status = ITHACA_GPU_ERR_NUMERIC;
+    if (!was_done) {
+      O.rn2 = rr;
+      O.bn2 = bb;
+    }
+    if (!was_done && !isfinite(rr)) O.status = ITHACA_GPU_ERR_NUMERIC;
     O.outer_done = (O.outer_done || !(rr > tol2 * bb) || bb == 0 || O.status != ITHACA_GPU_OK) ? 1 : 0;
     Scal I = Scal{};
     I.tol2 = inner_tol2;
