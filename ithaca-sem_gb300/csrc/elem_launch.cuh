@@ -4,6 +4,7 @@
 #pragma once
 
 #include "elem.cuh"
+#include "elem2_pencil.cuh"
 
 namespace ithaca {
 namespace dev {
@@ -24,9 +25,39 @@ struct Cfg {
   }
 };
 
+// 1-D tables of (N, Q) as kernel parameters, computed on the host once per instantiation.
+template <typename T, int N, int Q>
+const PTabs<T, N, Q>& host_ptabs() {
+  static const PTabs<T, N, Q> t = [] {
+    const BasisTables b = make_basis(N, Q);
+    PTabs<T, N, Q> r{};
+    for (int i = 0; i < N * Q; ++i) r.B[i] = (T)b.B[i];
+    for (int i = 0; i < Q * Q; ++i) r.D[i] = (T)b.D[i];
+    return r;
+  }();
+  return t;
+}
+
 template <typename T, int DIM, int N, int Q>
 void helm_nq(int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g, int ndir,
              const int* skip, const T* lam_ptr, const int* esolve, int skip_stride, cudaStream_t s) {
+  // FP32 deformed quads: the register-pencil kernel (elem2_pencil.cuh). FP64 stays on the
+  // shared-memory kernel: FP64 arithmetic bounds both, and the latter's smaller CTAs
+  // spread small meshes over more SMs.
+  if constexpr (DIM == 2 && sizeof(T) == 4) {
+    if (deformed) {
+      using P = Pencil2<T, N, Q>;
+      auto k = l2g ? helm2_pencil_kernel<T, N, Q, true> : helm2_pencil_kernel<T, N, Q, false>;
+      static bool prepared[2] = {false, false};
+      if (!prepared[l2g ? 1 : 0]) {
+        ITHACA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::bytes()));
+        prepared[l2g ? 1 : 0] = true;
+      }
+      k<<<(E + P::EB - 1) / P::EB, dim3(Q, P::EB), P::bytes(), s>>>(in, out, host_ptabs<T, N, Q>(), jg, lambda, E, l2g,
+                                                                 ndir, skip, lam_ptr, esolve, skip_stride);
+      return;
+    }
+  }
   using C = Cfg<T, DIM, N, Q>;
   constexpr int TPE = C::S::TPE;
   auto k = deformed ? (l2g ? helm_kernel<T, DIM, N, Q, TPE, true, true> : helm_kernel<T, DIM, N, Q, TPE, true, false>)
