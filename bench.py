@@ -496,7 +496,7 @@ def suite_quad2d(args):
                    "sample": f"3 full FP64 solves ({res_c[1]} iterations)"}
     except Exception as ex:
         cpu = {"value": None, "error": str(ex)[:200]}
-    _line("config 1: 2-D Helmholtz CG solves/s (FP64, 1e-12) and operator GDOF/s", out["fp64"]["solves_per_s"],
+    _line("2-D Helmholtz, 32x32 jittered quads P=6: CG solves/s (FP64, 1e-12) and operator GDOF/s", out["fp64"]["solves_per_s"],
           "solves/s", args, cfg, dtype="f64", helmholtz_gdofs_fp64=gdofs, solve=out, cpu_baseline=cpu)
 
 
@@ -524,7 +524,7 @@ def suite_mixed2d(args):
     head = [r for r in rows if r["P"] == 6 and r["lambda"] == 1.0][0]
     cfg = {"workload": "2-D Helmholtz, 32x32 jittered quads, P in {6, 8}, lambda in {0.1, 1, 10}, "
                        "FP32 inner PCG in FP64 refinement to 1e-10", "l2": "L2-resident (latency-bound)"}
-    _line("config 3: mixed-precision solves/s (P=6, lambda=1; all cases in 'cases')",
+    _line("2-D mixed-precision solves/s, 32x32 jittered quads (P=6, lambda=1; all cases in 'cases')",
           head["mixed"]["solves_per_s"], "solves/s", args, cfg, dtype="f64 (outer) / f32 (inner)", cases=rows)
 
 
@@ -550,13 +550,13 @@ def suite_batched(args):
     cfg = {"workload": "256 2-D Helmholtz solves, lambda = 10^U(-2,2), E ~ U{500..8000} jittered quads, "
                        "P ~ U{3..9}, Q = P+2, tol 1e-10, one graph-captured batch",
            "solve_dofs_total": ndof, "host_setup_s": setup_s}
-    _line("config 4: batched parametric solves/s (256 solves, mixed)", out["mixed"]["solves_per_s"], "solves/s", args,
+    _line("batched parametric solves/s (256 2-D solves, mixed)", out["mixed"]["solves_per_s"], "solves/s", args,
           cfg, dtype="f64 (outer) / f32 (inner)", batch=out,
           speedup_mixed_vs_fp64=out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"])
 
 
 def suite_pod(args):
-    """POD on the config-1 FOM (32x32 quads, P=6): 256 lambda snapshots (one batch), 50
+    """POD on the 32x32-quad, P=6 full-order model: 256 lambda snapshots (one batch), 50
     modes by the method of snapshots, reduced operators, 4096 online FP64 LU solves."""
     import torch
     from ithaca_gpu import pod
@@ -632,12 +632,12 @@ def suite_adjoint(args):
     cfg = {"workload": "variable-coefficient Helmholtz, 64x64 jittered quads, P=6, kappa = 1 + 0.5 g (8 seeded "
                        "Fourier modes), J = sum Jw (u - u_t)^2, adjoint gradient, FP64 CG to 1e-12",
            "quadrature_points": int(kappa.numel())}
-    _line("config 5: adjoint gradients/s (forward + adjoint solve + dJ/dkappa)", 1e3 / ms, "gradients/s", args, cfg,
+    _line("adjoint gradients/s, 64x64 quads P=6 (forward + adjoint solve + dJ/dkappa)", 1e3 / ms, "gradients/s", args, cfg,
           dtype="f64", J=J, grad_max=float(g.abs().max()))
 
 
 def suite_hex_orders(args):
-    """Config 2 as a sweep: 32^3 curved hexes at P = 4, 6, 8 (Q = P + 2): the four
+    """The 3-D sweep: 32^3 curved hexes at P = 4, 6, 8 (Q = P + 2): the four
     operators (GDOF/s, Ndof = E n^3; Helmholtz also in FP32 with the autotuned kernel)
     and Jacobi PCG to 1e-12, FP64 (the reference recurrence) and mixed."""
     import torch
@@ -680,7 +680,7 @@ def suite_hex_orders(args):
     cfg = {"workload": "3-D Helmholtz, 32^3 hexes curved by x + 0.05 sin(2 pi y) sin(2 pi z), P = 4, 6, 8, "
                        "Q = P + 2, lambda = 1, Jacobi PCG to 1e-12",
            "elements": 32768, "l2": "operands exceed L2 at every order (geometry >= 200 MB)"}
-    _line("config 2: 3-D Helmholtz operator GDOF/s and CG solves/s (1e-12) at P = 4, 6, 8",
+    _line("3-D Helmholtz, 32^3 curved hexes at P = 4, 6, 8: operator GDOF/s and CG solves/s (1e-12)",
           rows[1]["solve_1e-12"]["mixed"]["solves_per_s"], "solves/s", args, cfg, dtype="f64 / f32 inner",
           orders=rows)
 
