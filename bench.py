@@ -135,8 +135,8 @@ def fp32_kernel_name(variant, n, Q):
 
 # DRAM bytes (read + write) per element of one gathered FP32 apply as the inner iteration
 # launches it (scattered output: owned rows and assembly-ordered slots), from ncu captures
-# of the same kernels on 28^3 hexes (profiles/inner_loop_kernels_hex_p6_mesh28.md: 398.9 MB
-# per launch for variant 41, 399.3 MB for 42, means of two launches, over 21,952 elements);
+# of the same kernels on 28^3 hexes (398.9 MB per launch for variant 41, 399.3 MB for 42,
+# means of two launches, over 21,952 elements);
 # a launch's traffic grows with the number of elements, so the bench scales it by E.
 # Keys: (kernel variant, modes, points).
 TRAFFIC_PER_ELEMENT = {(41, 7, 8): 18171, (42, 7, 8): 18190}

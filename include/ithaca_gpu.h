@@ -157,6 +157,16 @@ int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg);
  * the same recurrence (NekLinSysIterCG.cpp:104-263); 3-D systems always use the graph. */
 int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode);
 
+/* Test hooks of the persistent solver's failure path (no reference counterpart; the
+ * reference has no device waits). barrier_polls: polls of ~64 ns before a grid-barrier
+ * wait gives up (0: the default, about 1 s; at most 2^24). drop_cta: that CTA never
+ * arrives at its first barrier, so every wait runs out and the solve returns
+ * ITHACA_GPU_ERR_TIMEOUT with the context still usable (-1: none). delay_ns: every third
+ * CTA pauses that long after each barrier, so the others run ahead into the next phase
+ * (a race stress; 0: none, at most 1e6). All three stay set until changed; a solve uses
+ * 0, -1, 0. */
+int ithaca_gpu_cg_set_wait_test(ithaca_gpu_cg* cg, long long barrier_polls, int drop_cta, int delay_ns);
+
 typedef struct {
   double tol;          /* IterativeSolverTolerance (default 1e-9); stop when ||r||^2 < tol^2 ||b||^2 */
   int max_iter;        /* NekLinSysMaxIterations (default 5000)                                      */
@@ -275,18 +285,22 @@ int ithaca_gpu_pod_reconstruct(ithaca_gpu_ctx* ctx, int N, int r, const double* 
                                double* u, int on_device);
 
 /* Allocation-free Gram matrix C = S^T S (no counterpart in the reference). For callers
- * that cannot allocate device memory where they need it: a ROM step recorded inside a
- * CUDA graph capture (cudaMalloc/cudaFree are not allowed while a stream is captured), or
- * a host that reserves its device memory up front and forbids allocation in its loop.
+ * that cannot allocate device memory where they need it: a host application that
+ * reserves its device memory up front in its own pool and forbids allocation in its
+ * solve loop, or a time-stepping loop that must not stall on the device-wide
+ * synchronisation that cudaFree implies.
  * S (N x ns, column-major) and C (ns x ns) are device pointers owned by the caller; work
  * is queued on `stream` (a cudaStream_t, NULL for the legacy default stream) and not
  * waited for. The split-K scratch is a fixed 2 MiB device array in the library, held on
  * every device that loads it until the process exits, so ns <= 128 (larger ns returns
  * ITHACA_GPU_ERR_ARG). Nothing in the array needs to start at zero: every partial sum is
  * written before it is read. The first call on a device looks that array up
- * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
- * array: calls whose work overlaps on the GPU race and must be serialised by the caller.
- * It calls no cudaMalloc or cudaFree and needs no context. */
+ * (cudaGetSymbolAddress) and should come before any stream capture; the address is kept
+ * for the life of the process, so calls after a cudaDeviceReset of that device are not
+ * supported. All calls share the array: calls whose work overlaps on the GPU race and
+ * must be serialised by the caller. A CUDA error already pending from earlier work is
+ * reported (ITHACA_GPU_ERR_CUDA) and left pending, and nothing is queued. It calls no
+ * cudaMalloc or cudaFree and needs no context. */
 int ithaca_gpu_pod_gram_noalloc(int N, int ns, const double* S, double* C, void* stream);
 
 /* Measurement hook (no reference counterpart): runs the gather + element-Helmholtz

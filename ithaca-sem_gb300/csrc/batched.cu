@@ -27,7 +27,9 @@ namespace batch {
 
 constexpr int BT = 256;        // threads per CTA
 constexpr int CH = 4096;       // dofs per reduction chunk
-constexpr int GRID = 152 * 4;  // CTAs of the chunk kernels
+constexpr int kChunkPerSM = 4;  // CTAs per SM of the chunk kernels
+// CTAs of a full chunk-kernel grid on the current device
+inline int chunk_grid() { return kChunkPerSM * device_sm_count(); }
 
 struct Scal {
   double alpha, beta, rho, mu, eps, rhs_mag, tol2, mag_override, bb_dir;
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(BT) binit_kernel(const Chunk* __restrict__ chu
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BT, GRID / 152) bupdate_kernel(const Chunk* __restrict__ chunks, int nchunks,
+__global__ void __launch_bounds__(BT, kChunkPerSM) bupdate_kernel(const Chunk* __restrict__ chunks, int nchunks,
                                                      const Scal* __restrict__ sc, T* __restrict__ x,
                                                      T* __restrict__ r, T* __restrict__ w, const T* __restrict__ s,
                                                      T* __restrict__ p, T* __restrict__ q,

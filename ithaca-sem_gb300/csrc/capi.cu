@@ -23,6 +23,20 @@ void check_cuda(cudaError_t e, const char* what) {
   }
 }
 
+int device_sm_count() {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices] = {};
+  int dev = 0;
+  ITHACA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) fail(ITHACA_GPU_ERR_ARG, "device ordinal out of range");
+  int sms = cache[dev].load();
+  if (sms <= 0) {
+    ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cache[dev].store(sms);
+  }
+  return sms;
+}
+
 void* Ctx::stage_ptr(int slot, size_t bytes) {
   if (bytes > stage_bytes[slot]) {
     if (stage[slot]) ITHACA_CUDA(cudaFree(stage[slot]));

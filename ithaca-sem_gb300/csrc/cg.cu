@@ -26,8 +26,11 @@
 
 namespace ithaca {
 
-constexpr int RB = 760;      // reduction CTAs: 5 per SM of 152 (one wave at <= 51 registers per thread)
-constexpr int RBA = 1216;    // assembly CTAs: 8 per SM (<= 32 registers); partial slot 3 holds RBA entries
+// Grids of the vector and assembly kernels: 5 and 8 CTAs per SM of the device (one wave at
+// <= 51 and <= 32 registers per thread), capped at the partial-sum capacities below
+constexpr int kRedPerSM = 5, kAsmPerSM = 8;
+constexpr int RB = 760;      // capacity of a partial-sum slot of the vector kernels (5 x 152 SMs)
+constexpr int RBA = 1216;    // capacity of slot 3 (assembly partials; 8 x 152 SMs)
 constexpr int RT = 256;      // threads per reduction CTA
 constexpr int NSLOT = 4;     // partial-sum slots: 0 r.w, 1 r.r, 2 b.b, 3 s.w
 // 2-D systems up to this many global dofs run the persistent solver by default: below it
@@ -318,7 +321,7 @@ __device__ __forceinline__ void asm_class(const AsmPlan& P, int c, int cta, int 
 // `counter`) also runs the loop-tail scalar update, saving one launch per CG iteration;
 // the reduction order of the partial sums does not depend on which CTA that is.
 template <typename T, bool SIGNED = true, bool PERM = false>
-__global__ void __launch_bounds__(RT, RBA / 152) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
+__global__ void __launch_bounds__(RT, kAsmPerSM) assemble_dot_kernel(const AsmPlan P, bool skip_dir, const int* __restrict__ rows,
                                                           const int* __restrict__ ecols, const int* __restrict__ rowptr,
                                                           const int* __restrict__ cols, const T* __restrict__ yloc,
                                                           T* __restrict__ s, const T* __restrict__ w, const int* skip,
@@ -582,6 +585,8 @@ struct Cg {
   // persistent small-system solver (2-D, cg_persist.cu): -1 automatic (N <= kPersistMaxN),
   // 0 off, 1 whenever the system is 2-D; grid-barrier state; SM count
   int persist = -1;
+  long long dbg_polls = 0;            // failure-path test hooks of the persistent solver
+  int dbg_drop = -1, dbg_delay = 0;   // (PersistArgs); zero / -1 in a solve
   unsigned* bar = nullptr;
   int sms = 0;
   double* opart = nullptr;  // per-CTA s.w partials of the element kernel
@@ -769,6 +774,9 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
     a.bar = cg->bar;
     a.err = c->derr;
     a.sc = cg->sc;
+    a.dbg_polls = cg->dbg_polls;
+    a.dbg_drop_cta = cg->dbg_drop;
+    a.dbg_delay_ns = cg->dbg_delay;
     if (launch_cg2_persistent<T>(op->n, op->Q, a, cg->sms, s)) {
       c->launches++;
       ITHACA_CUDA(cudaMemcpyAsync(cg->sc_host, cg->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
@@ -1088,9 +1096,13 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     // partial sums of CTAs that have no rows).
     int nonempty_all = 0;
     for (int c = 0; c <= kAsmK; ++c) nonempty_all += plan.n[c] > 0;
+    int dev = 0, sms = 0;
+    ITHACA_CUDA(cudaGetDevice(&dev));
+    ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const long long per2 = ((long long)nglobal + 2 * RT - 1) / (2 * RT);
-    const int rbv = (int)std::min<long long>(RB, std::max<long long>(1, per2));
-    const int rba = (int)std::min<long long>(RBA, std::max<long long>(nonempty_all, per2));
+    const int rb_full = std::min(RB, kRedPerSM * sms), rba_full = std::min(RBA, kAsmPerSM * sms);
+    const int rbv = (int)std::min<long long>(rb_full, std::max<long long>(1, per2));
+    const int rba = (int)std::min<long long>(std::max(rba_full, nonempty_all), std::max<long long>(nonempty_all, per2));
     // CTAs per class in proportion to its entries, at least one for a non-empty class
     auto split_ctas = [&](AsmPlan& P, const long long* ent) {
       long long total = 0;
@@ -1134,9 +1146,6 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     ITHACA_CUDA(cudaMalloc(&cg->cols, sizeof(int) * nloc));
     ITHACA_CUDA(cudaMalloc(&cg->asm_rows, sizeof(int) * nglobal));
     if (own_ok) {
-      int dev = 0, sms = 0;
-      ITHACA_CUDA(cudaGetDevice(&dev));
-      ITHACA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       cg->opart_cap = sms * 32;  // at most 32 resident CTAs per SM
       cg->sms = sms;
       ITHACA_CUDA(cudaMalloc(&cg->bar, 2 * sizeof(unsigned)));
@@ -1176,6 +1185,18 @@ int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode) {
     req(cg != nullptr, "null solver");
     req(mode >= -1 && mode <= 1, "persistent mode must be -1, 0 or 1");
     cg->persist = mode;
+  });
+}
+
+int ithaca_gpu_cg_set_wait_test(ithaca_gpu_cg* cg, long long barrier_polls, int drop_cta, int delay_ns) {
+  return cg_guarded([&] {
+    req(cg != nullptr, "null solver");
+    req(barrier_polls >= 0 && barrier_polls <= (1LL << 24), "barrier_polls must be in [0, 2^24]");
+    req(drop_cta >= -1, "drop_cta must be -1 or a CTA index");
+    req(delay_ns >= 0 && delay_ns <= 1000000, "delay_ns must be in [0, 1e6]");
+    cg->dbg_polls = barrier_polls;
+    cg->dbg_drop = drop_cta;
+    cg->dbg_delay = delay_ns;
   });
 }
 

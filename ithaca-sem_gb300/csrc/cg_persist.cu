@@ -36,21 +36,27 @@ constexpr int RC = 4;                         // free rows per thread kept in re
 constexpr long long kBarrierPolls = 1 << 24;  // ~1 s of polling at 64 ns per poll
 
 // Grid barrier (arrival counter + generation). Returns false on timeout in any thread.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
+// polls bounds the wait (kBarrierPolls unless a test hook shortens it). A CTA with
+// drop set does not arrive: it reports the timeout at once, and every other CTA's wait
+// then runs out (the failure-path test hook; never set in a solve).
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, long long polls_max, bool drop = false) {
   __syncthreads();
   bool ok = true;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     volatile unsigned* gen = bar + 1;
     const unsigned g = *gen;
     __threadfence();  // this CTA's writes are visible before it arrives
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+    if (drop) {
+      ok = false;
+      if (err != nullptr) atomicExch(err, ITHACA_GPU_ERR_TIMEOUT);
+    } else if (atomicAdd(bar, 1u) == gridDim.x - 1) {
       bar[0] = 0u;
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
       long long polls = 0;
       while (*gen == g) {
-        if (++polls > kBarrierPolls) {
+        if (++polls > polls_max) {
           ok = false;
           if (err != nullptr) atomicExch(err, ITHACA_GPU_ERR_TIMEOUT);
           break;
@@ -63,13 +69,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
   return __syncthreads_and(ok) != 0;
 }
 
-// Sums of NS per-CTA partials (part[k * G + cta]) in a fixed order; every thread of
-// every CTA gets the same values.
+// Sums of NS per-CTA partials (part[slot[k] * G + cta]) in a fixed order; every thread
+// of every CTA gets the same values.
 template <int NS>
-__device__ __forceinline__ void sum_partials(const double* part, int G, double (&out)[NS], double* sh) {
+__device__ __forceinline__ void sum_partials(const double* part, const int (&slot)[NS], int G, double (&out)[NS],
+                                             double* sh) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
 #pragma unroll
-  for (int k = 0; k < NS; ++k) sh[k * PT + tid] = tid < G ? __ldcg(part + k * G + tid) : 0.0;
+  for (int k = 0; k < NS; ++k) sh[k * PT + tid] = tid < G ? __ldcg(part + slot[k] * G + tid) : 0.0;
   __syncthreads();
   if (tid < 32) {
 #pragma unroll
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(PT) cg2_persist_kernel(const PersistArgs<T> a)
       const T bg = a.b[g];
       v[2] = fma(bg, bg, v[2]);
     }
-    cta_partials<T, 3>(v, a.part, G, sh);  // slots 0 r.w, 1 r.r, 2 b.b
+    cta_partials<T, 3>(v, a.part, G, sh);  // slots 0 r.w, 1 r.r (parity 0), 2 b.b
   }
 
   // ---- phase A: s = A w on the elements, scattered output, the CTA's share of s.w ----
@@ -278,7 +285,7 @@ __global__ void __launch_bounds__(PT) cg2_persist_kernel(const PersistArgs<T> a)
   };
 
   // ---- phase B: assemble this thread's non-owned rows and update its rows ----
-  auto phase_b = [&](T alpha, T beta) {
+  auto phase_b = [&](T alpha, T beta, int parity) {
     T rw = 0, rrs = 0;
 #pragma unroll
     for (int k = 0; k < RC; ++k) {
@@ -308,7 +315,7 @@ __global__ void __launch_bounds__(PT) cg2_persist_kernel(const PersistArgs<T> a)
       }
     }
     T v[2] = {rw, rrs};
-    cta_partials<T, 2>(v, a.part, G, sh);  // slots 0 r.w, 1 r.r
+    cta_partials<T, 2>(v, a.part + (parity ? 4 : 0) * G, G, sh);  // slots 0, 1 or 4, 5: r.w, r.r
   };
 
   // Every CTA's copy of the recurrence's scalars, in shared memory: thread 0 updates it
@@ -319,14 +326,28 @@ __global__ void __launch_bounds__(PT) cg2_persist_kernel(const PersistArgs<T> a)
   };
   __shared__ State st;
   if (tid == 0) st = State{0, 0, 0, 0, 0, 1, 0, 0, 0, ITHACA_GPU_OK};
-  bool ok = grid_barrier(a.bar, a.err);  // also publishes st to the CTA
+  // Test hooks (zero in a solve): a shorter barrier wait, one CTA that never arrives,
+  // and a pause of some CTAs right after each barrier, which lets the others run ahead.
+  const long long polls = a.dbg_polls > 0 ? a.dbg_polls : kBarrierPolls;
+  const bool drop = a.dbg_drop_cta == (int)blockIdx.x;
+  auto lag = [&]() {
+    if (a.dbg_delay_ns > 0 && blockIdx.x % 3 == 1) __nanosleep(a.dbg_delay_ns);
+  };
+  // r.w and r.r alternate between slots {0, 1} and {4, 5} from one iteration to the
+  // next: a CTA that leaves the second barrier early writes its next phase-B partials
+  // while slower CTAs may still be summing this iteration's, and the parity keeps the two
+  // apart. The writes of the iteration after next come behind two more barriers, which
+  // every CTA reaches only after its sums.
+  int parity = 0;
+  bool ok = grid_barrier(a.bar, a.err, polls, drop);  // also publishes st to the CTA
   if (ok) {
     phase_a();
-    ok = grid_barrier(a.bar, a.err);
+    ok = grid_barrier(a.bar, a.err, polls);
   }
   if (ok) {  // the reference's initial step
+    lag();
     double red[4];
-    sum_partials<4>(a.part, G, red, sh);
+    sum_partials<4>(a.part, {0, 1, 2, 3}, G, red, sh);
     if (tid == 0) {
       const double rw = red[0], rrs = red[1], bb = red[2], swv = red[3];
       st.rhs_mag = in.mag_override > 0 ? in.mag_override : (bb > 1e-6 ? bb : 1.0);
@@ -351,15 +372,20 @@ __global__ void __launch_bounds__(PT) cg2_persist_kernel(const PersistArgs<T> a)
     __syncthreads();
   }
   while (ok && !st.done) {
-    phase_b((T)st.alpha, (T)st.beta);
-    ok = grid_barrier(a.bar, a.err);
+    parity ^= 1;
+    phase_b((T)st.alpha, (T)st.beta, parity);
+    ok = grid_barrier(a.bar, a.err, polls);
     if (!ok) break;
     phase_a();
-    ok = grid_barrier(a.bar, a.err);
+    ok = grid_barrier(a.bar, a.err, polls);
     if (!ok) break;
-    // the reference loop tail: slots 0 r.w, 1 r.r (phase B), 3 s.w (phase A)
+    lag();
+    // the reference loop tail: r.w, r.r (phase B, this parity's slots), 3 s.w (phase A)
     double red[4];
-    sum_partials<4>(a.part, G, red, sh);
+    if (parity)
+      sum_partials<4>(a.part, {4, 5, 2, 3}, G, red, sh);
+    else
+      sum_partials<4>(a.part, {0, 1, 2, 3}, G, red, sh);
     if (tid == 0) {
       const double rho_new = red[0];
       st.eps = red[1];

@@ -45,10 +45,15 @@ struct PersistArgs {
   AsmPlan plan;         // the full plan (class 0 free rows are the owned rows)
   T *x, *r, *w, *s, *p, *q, *yslot;
   const T *b, *dinv, *tab, *jg;
-  double* part;         // 4 x gridDim.x partial sums
+  double* part;         // 6 x gridDim.x partial sums (slots: r.w, r.r, b.b, s.w, r.w', r.r')
   unsigned* bar;        // grid barrier: arrival count, generation (zeroed before launch)
   int* err;             // device error word
   CgScalars* sc;        // in: tol2, mag_override, max_iter, lambda; out: the final state
+  // failure-path test hooks, zero in a solve: barrier poll limit (0: the default),
+  // a CTA that never arrives at its first barrier (-1: none), and a pause in ns of every
+  // third CTA after each barrier (0: none)
+  long long dbg_polls;
+  int dbg_drop_cta, dbg_delay_ns;
 };
 
 // Launches the persistent solver for quads with n modes and Q = n + 1 points; returns

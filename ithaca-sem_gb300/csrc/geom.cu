@@ -77,7 +77,7 @@ void launch_geom_factors(int dim, int Q, int E, const double* D, const double* c
                          int* bad, cudaStream_t s) {
   const size_t total = (size_t)E * (dim == 2 ? Q * Q : Q * Q * Q);
   const int threads = 256;
-  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, 152 * 32);
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
   geom_factors_kernel<<<blocks, threads, 0, s>>>(dim, Q, E, D, coords, jac, df, bad);
 }
 
@@ -120,7 +120,7 @@ void launch_build_jg(int dim, int Q, int E, int deformed, const double* w, const
                      T* jg, T* dfo, cudaStream_t s) {
   const size_t total = (size_t)E * (deformed ? (dim == 2 ? Q * Q : Q * Q * Q) : 1);
   const int threads = 256;
-  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, 152 * 32);
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
   build_jg_kernel<T><<<blocks, threads, 0, s>>>(dim, Q, E, deformed, w, jac, df, jg, dfo);
 }
 

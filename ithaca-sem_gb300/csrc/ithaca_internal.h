@@ -24,6 +24,9 @@ void set_last_error(const std::string& msg);
 void check_cuda(cudaError_t e, const char* what);
 #define ITHACA_CUDA(x) ::ithaca::check_cuda((x), #x)
 
+// Number of SMs of the current device (queried once per device); grids are sized from it.
+int device_sm_count();
+
 // ---------------------------------------------------------------------------
 // Basis tables (host, FP64), see basis.cpp.
 struct BasisTables {

@@ -99,7 +99,7 @@ __global__ void sum_parts_kernel(size_t n, int nparts, const double* __restrict_
 
 // Split count and chunk for a K-long reduction.
 static void split_k(int K, int tiles, int* nsplit, int* kchunk) {
-  const int target = std::max(1, (152 * 4) / std::max(1, tiles));
+  const int target = std::max(1, (device_sm_count() * 4) / std::max(1, tiles));
   int ns = std::max(1, std::min(target, (K + 255) / 256));
   int kc = (K + ns - 1) / ns;
   kc = (kc + GK - 1) / GK * GK;
@@ -509,12 +509,11 @@ int ithaca_gpu_pod_rb_size(int ns, const double* sigma, double pod_tolerance, in
 // ---------------------------------------------------------------------------
 // Gram matrix without any device allocation.
 //
-// Some callers cannot allocate device memory at the point where they need S^T S: a
-// reduced-order model that rebuilds its Gram matrix inside a CUDA graph being captured
-// (cudaMalloc and cudaFree are not allowed during stream capture), or a host that
-// reserves all device memory up front for a fixed-budget pool and forbids further
-// allocations in its solve loop. ithaca_gpu_pod_gram allocates its split-K partial sums
-// per call; this variant keeps them in a fixed, file-scope device array instead.
+// Some callers cannot allocate device memory at the point where they need S^T S: a host
+// that reserves all device memory up front for a fixed-budget pool and forbids further
+// allocations in its solve loop, or a time-stepping loop that must not stall on the
+// device-wide synchronisation cudaFree implies. ithaca_gpu_pod_gram allocates its split-K
+// partial sums per call; this variant keeps them in a fixed, file-scope device array.
 //
 // The array holds kNoAllocGramDoubles doubles (2 MiB), allocated when the library is
 // loaded on a device and held until the process exits. It bounds the problem: ns <= 128
@@ -532,7 +531,8 @@ constexpr size_t kNoAllocGramDoubles = (size_t)kNoAllocMaxSplits * kNoAllocMaxSn
 static __device__ __align__(256) double g_gram_scratch[kNoAllocGramDoubles];
 
 // Device address of g_gram_scratch on the current device, looked up once per device
-// (the host-side name of a __device__ array is only a stand-in, not a device address).
+// (the host-side name of a __device__ array is only a stand-in, not a device address)
+// and kept for the life of the process: a cudaDeviceReset of that device is not supported.
 static double* gram_scratch_on_current_device() {
   constexpr int kMaxDevices = 64;
   static double* cache[kMaxDevices] = {};
@@ -562,6 +562,11 @@ extern "C" int ithaca_gpu_pod_gram_noalloc(int N, int ns, const double* S, doubl
       fail(ITHACA_GPU_ERR_ARG, "ithaca_gpu_pod_gram_noalloc: ns = " + std::to_string(ns) + " exceeds the " +
                                    std::to_string(kNoAllocMaxSnapshots) +
                                    " snapshots its fixed scratch holds (use ithaca_gpu_pod_gram)");
+    // an error left by the caller's earlier work is reported as such and stays pending
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+      fail(ITHACA_GPU_ERR_CUDA, std::string("ithaca_gpu_pod_gram_noalloc: a CUDA error from earlier work is pending (") +
+                                    cudaGetErrorString(pending) + "); nothing was queued");
     double* scratch = gram_scratch_on_current_device();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const dim3 grid((ns + GT - 1) / GT, (ns + GT - 1) / GT, 1);

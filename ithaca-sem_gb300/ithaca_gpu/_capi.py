@@ -77,6 +77,7 @@ SIGNATURES = {
     "ithaca_gpu_cg_create": [_vp, _vp, _vp, _i, _i, _pp],
     "ithaca_gpu_cg_destroy": [_vp],
     "ithaca_gpu_cg_set_persistent": [_vp, _i],
+    "ithaca_gpu_cg_set_wait_test": [_vp, ctypes.c_longlong, _i, _i],
     "ithaca_gpu_cg_default_opts": [ctypes.POINTER(CgOpts)],
     "ithaca_gpu_cg_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_cg_apply": [_vp, _d, _vp, _vp, _i],

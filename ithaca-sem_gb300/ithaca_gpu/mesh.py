@@ -179,21 +179,22 @@ class HexMesh:
                 y + a * np.sin(tp * z) * np.sin(tp * x),
                 z + a * np.sin(tp * x) * np.sin(tp * y))
 
-    def coords(self, Q):
+    def coords(self, Q, elements=None):
         """Coordinates at the Q^3 GLL points, shape (3, E, Q^3), point (k*Q + j)*Q + i.
-        Element e = (kz*ny + jy)*nx + ix."""
+        Element e = (kz*ny + jy)*nx + ix. `elements`: only these element ids (in order)."""
         nx, ny, nz = self.nx, self.ny, self.nz
         z = gll_points(Q)
         t = 0.5 * (1 + z)
-        ix = np.arange(self.E) % nx
-        iy = (np.arange(self.E) // nx) % ny
-        iz = np.arange(self.E) // (nx * ny)
+        eids = np.arange(self.E) if elements is None else np.asarray(elements, dtype=np.int64)
+        ix = eids % nx
+        iy = (eids // nx) % ny
+        iz = eids // (nx * ny)
         X0 = ((ix[:, None] + t[None, :]) / nx)[:, None, None, :]
         X1 = ((iy[:, None] + t[None, :]) / ny)[:, None, :, None]
         X2 = ((iz[:, None] + t[None, :]) / nz)[:, :, None, None]
         X0, X1, X2 = np.broadcast_arrays(X0, X1, X2)
         Y = self._map(X0, X1, X2)
-        return np.stack([c.reshape(self.E, Q ** 3) for c in Y], axis=0)
+        return np.stack([c.reshape(eids.size, Q ** 3) for c in Y], axis=0)
 
     def assembly(self, n):
         """Aligned structured hexes: the C0 dof of local mode (p, q, r) is the tensor

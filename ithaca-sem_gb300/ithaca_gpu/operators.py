@@ -331,6 +331,12 @@ class GlobalLinSysIterativeFullGPU:
         graph-captured kernels, 1 the persistent single-launch solver."""
         C.call("ithaca_gpu_cg_set_persistent", self.handle, int(mode))
 
+    def set_wait_test(self, barrier_polls=0, drop_cta=-1, delay_ns=0):
+        """Failure-path test hooks of the persistent solver: a shorter grid-barrier wait,
+        a CTA that never arrives (every wait then runs out: ERR_TIMEOUT), and a pause of
+        every third CTA after each barrier. The defaults restore a normal solve."""
+        C.call("ithaca_gpu_cg_set_wait_test", self.handle, int(barrier_polls), int(drop_cta), int(delay_ns))
+
     def profile_apply(self, lam, mode="mixed", reps=20):
         """Average device time (ms) of the gather + element-apply kernel the solver
         launches for `mode`, timed with CUDA events on the context stream, and the

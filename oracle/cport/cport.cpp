@@ -124,6 +124,27 @@ struct QuadOp {
       }
     }
   }
+  // single operators of one element (BwdTrans, IProductWRTBase, PhysDeriv)
+  static void bwd_e(const Tab& t, const double* c, double* u) { bwd(t.B.data(), c, u); }
+  static void ipr_e(const Tab& t, const double* jac, bool def, const double* u, double* out) {
+    ipr(t.B.data(), t.B.data(), t.w.data(), jac, def, u, out, 1.0, false);
+  }
+  // du/dx_k = sum_j df[k*2+j] du/dxi_j (collocation derivatives, PhysDerivQuadKernel)
+  static void deriv_e(const Tab& t, const double* df, bool def, const double* u, double* const* d) {
+    const double* D = t.D.data();
+    for (int j = 0; j < Q; ++j)
+      for (int i = 0; i < Q; ++i) {
+        double a = 0, b = 0;
+        for (int k = 0; k < Q; ++k) {
+          a += D[k * Q + i] * u[j * Q + k];
+          b += u[k * Q + i] * D[k * Q + j];
+        }
+        const int c = j * Q + i;
+        const double* f = def ? df + 4 * c : df;
+        d[0][c] = f[0] * a + f[1] * b;
+        d[1][c] = f[2] * a + f[3] * b;
+      }
+  }
   static void apply(const Tab& t, const double* jac, const double* df, bool def, double lam, const double* in,
                     double* out) {
     constexpr int nq = Q * Q;
@@ -208,6 +229,29 @@ struct HexOp {
       }
     }
   }
+  static void bwd_e(const Tab& t, const double* c, double* u) { bwd(t.B.data(), c, u); }
+  static void ipr_e(const Tab& t, const double* jac, bool def, const double* u, double* out) {
+    ipr(t.B.data(), t.B.data(), t.B.data(), t.w.data(), jac, def, u, out, 1.0, false);
+  }
+  // du/dx_k = sum_j df[k*3+j] du/dxi_j (collocation derivatives, PhysDerivHexKernel)
+  static void deriv_e(const Tab& t, const double* df, bool def, const double* u, double* const* d) {
+    const double* D = t.D.data();
+    for (int k = 0; k < Q; ++k)
+      for (int j = 0; j < Q; ++j)
+        for (int i = 0; i < Q; ++i) {
+          double a = 0, b = 0, c = 0;
+          for (int m = 0; m < Q; ++m) {
+            a += D[m * Q + i] * u[(k * Q + j) * Q + m];
+            b += u[(k * Q + m) * Q + i] * D[m * Q + j];
+            c += u[(m * Q + j) * Q + i] * D[m * Q + k];
+          }
+          const int o = (k * Q + j) * Q + i;
+          const double* f = def ? df + 9 * o : df;
+          d[0][o] = f[0] * a + f[1] * b + f[2] * c;
+          d[1][o] = f[3] * a + f[4] * b + f[5] * c;
+          d[2][o] = f[6] * a + f[7] * b + f[8] * c;
+        }
+  }
   static void apply(const Tab& t, const double* jac, const double* df, bool def, double lam, const double* in,
                     double* out) {
     constexpr int nq = Q * Q * Q;
@@ -251,6 +295,24 @@ struct HexOp {
 };
 
 using ApplyFn = void (*)(const Tab&, const double*, const double*, bool, double, const double*, double*);
+using BwdFn = void (*)(const Tab&, const double*, double*);
+using IprFn = void (*)(const Tab&, const double*, bool, const double*, double*);
+using DerivFn = void (*)(const Tab&, const double*, bool, const double*, double* const*);
+struct ElemFns {
+  BwdFn bwd;
+  IprFn ipr;
+  DerivFn deriv;
+};
+
+ElemFns pick_elem(int dim, int n, int Q) {
+#define P(NN, QQ)                                                                           \
+  if (n == NN && Q == QQ)                                                                   \
+    return dim == 2 ? ElemFns{&QuadOp<NN, QQ>::bwd_e, &QuadOp<NN, QQ>::ipr_e, &QuadOp<NN, QQ>::deriv_e} \
+                    : ElemFns{&HexOp<NN, QQ>::bwd_e, &HexOp<NN, QQ>::ipr_e, &HexOp<NN, QQ>::deriv_e};
+  P(2, 3) P(3, 4) P(4, 5) P(5, 6) P(6, 7) P(7, 8) P(8, 9) P(9, 10) P(10, 11)
+#undef P
+  return ElemFns{nullptr, nullptr, nullptr};
+}
 
 ApplyFn pick(int dim, int n, int Q) {
 #define P(NN, QQ) \
@@ -307,6 +369,49 @@ int cport_helmholtz(int dim, int n, int Q, int E, const double* jac, const doubl
   parallel(E, nthreads, [&](long long a, long long b, int) {
     for (long long e = a; e < b; ++e)
       f(t, &g.jac[e * npt], &g.df[e * npt * dim * dim], deformed != 0, lambda, in + e * nm, out + e * nm);
+  });
+  return 0;
+}
+
+// BwdTrans: coefficients (E n^d) -> physical values (E Q^d).
+int cport_bwdtrans(int dim, int n, int Q, int E, const double* in, double* out, int nthreads) {
+  ElemFns f = pick_elem(dim, n, Q);
+  if (!f.bwd) return 1;
+  Tab t(n, Q);
+  const int nm = dim == 2 ? n * n : n * n * n, nq = dim == 2 ? Q * Q : Q * Q * Q;
+  parallel(E, nthreads, [&](long long a, long long b, int) {
+    for (long long e = a; e < b; ++e) f.bwd(t, in + e * nm, out + e * nq);
+  });
+  return 0;
+}
+
+// IProductWRTBase: physical values -> coefficients, weighted by J w.
+int cport_iproduct(int dim, int n, int Q, int E, const double* jac, int deformed, const double* in, double* out,
+                   int nthreads) {
+  ElemFns f = pick_elem(dim, n, Q);
+  if (!f.ipr) return 1;
+  Tab t(n, Q);
+  const int nm = dim == 2 ? n * n : n * n * n, nq = dim == 2 ? Q * Q : Q * Q * Q, npt = deformed ? nq : 1;
+  parallel(E, nthreads, [&](long long a, long long b, int) {
+    for (long long e = a; e < b; ++e) f.ipr(t, jac + e * npt, deformed != 0, in + e * nq, out + e * nm);
+  });
+  return 0;
+}
+
+// PhysDeriv: physical values -> d arrays of physical derivatives (d2 unused in 2-D).
+int cport_physderiv(int dim, int n, int Q, int E, const double* df, int deformed, const double* in, double* d0,
+                    double* d1, double* d2, int nthreads) {
+  ElemFns f = pick_elem(dim, n, Q);
+  if (!f.deriv) return 1;
+  Tab t(n, Q);
+  const int nq = dim == 2 ? Q * Q : Q * Q * Q, npt = deformed ? nq : 1;
+  Geo g = regroup(dim, nq, E, deformed != 0, df, df);  // jac unused: df regrouped per point
+  const int ndf = dim * dim;
+  parallel(E, nthreads, [&](long long a, long long b, int) {
+    for (long long e = a; e < b; ++e) {
+      double* d[3] = {d0 + e * nq, d1 + e * nq, dim == 3 ? d2 + e * nq : nullptr};
+      f.deriv(t, &g.df[e * npt * ndf], deformed != 0, in + e * nq, d);
+    }
   });
   return 0;
 }

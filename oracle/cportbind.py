@@ -43,6 +43,36 @@ def helmholtz(dim, n, Q, E, jac, df, deformed, lam, coeffs, nthreads=1, out=None
     return out
 
 
+def bwdtrans(dim, n, Q, E, coeffs, nthreads=1):
+    out = np.zeros(E * Q ** dim)
+    c, cp = _d(coeffs)
+    rc = lib().cport_bwdtrans(dim, n, Q, E, cp, out.ctypes.data_as(_dp), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"cport_bwdtrans returned {rc}")
+    return out
+
+
+def iproduct(dim, n, Q, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n ** dim)
+    j, jp = _d(jac)
+    f, fp = _d(phys)
+    rc = lib().cport_iproduct(dim, n, Q, E, jp, int(deformed), fp, out.ctypes.data_as(_dp), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"cport_iproduct returned {rc}")
+    return out
+
+
+def physderiv(dim, n, Q, E, df, deformed, phys, nthreads=1):
+    outs = [np.zeros(E * Q ** dim) for _ in range(3 if dim == 3 else 2)]
+    f, fp = _d(df)
+    u, up = _d(phys)
+    ptrs = [o.ctypes.data_as(_dp) for o in outs] + ([None] if dim == 2 else [])
+    rc = lib().cport_physderiv(dim, n, Q, E, fp, int(deformed), up, *ptrs, nthreads)
+    if rc != 0:
+        raise RuntimeError(f"cport_physderiv returned {rc}")
+    return outs
+
+
 def cg_solve(dim, n, Q, E, jac, df, deformed, lam, l2g, sign, nglobal, ndir, dinv, rhs, tol, max_iter, nthreads=1):
     x = np.zeros(nglobal)
     eps = ctypes.c_double(0.0)

@@ -138,3 +138,50 @@ def test_set_persistent_rejects_bad_mode(ctx):
     coll, amap, sys_ = _system(ctx, c)
     with pytest.raises(GpuError):
         sys_.set_persistent(2)
+
+
+def test_persistent_barrier_timeout_then_solves(ctx):
+    """A CTA that never arrives at the grid barrier: every bounded wait runs out, the
+    solve returns ERR_TIMEOUT, and the next solve on the same context converges."""
+    from ithaca_gpu._capi import ERR_TIMEOUT, GpuError
+    c = quad_case(12, 10, 7)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = _rhs(amap, 11)
+    sys_.set_persistent(1)
+    x0, r0 = sys_.solve(1.0, rhs, tol=1e-11)
+    sys_.set_wait_test(barrier_polls=20000, drop_cta=0)  # ~1 ms waits
+    with pytest.raises(GpuError) as ei:
+        sys_.solve(1.0, rhs, tol=1e-11)
+    assert ei.value.code == ERR_TIMEOUT
+    sys_.set_wait_test()
+    x1, r1 = sys_.solve(1.0, rhs, tol=1e-11)
+    assert r1.iterations == r0.iterations and np.array_equal(x1, x0)
+
+
+@pytest.mark.parametrize("delay_ns", [2000, 50000])
+def test_persistent_partials_race_stress(ctx, delay_ns):
+    """Every third CTA pauses after each grid barrier while the others run ahead into the
+    next phase and write their next partial sums. All CTAs must still read the same
+    partials: the solve is bitwise identical to an undisturbed one."""
+    c = quad_case(32, 32, 7)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = _rhs(amap, 12)
+    sys_.set_persistent(1)
+    x0, r0 = sys_.solve(1.0, rhs, tol=1e-11)
+    try:
+        sys_.set_wait_test(delay_ns=delay_ns)
+        for _ in range(3):
+            x1, r1 = sys_.solve(1.0, rhs, tol=1e-11)
+            assert r1.iterations == r0.iterations
+            assert np.array_equal(x1, x0)
+    finally:
+        sys_.set_wait_test()
+
+
+def test_wait_test_hook_rejects_bad_values(ctx):
+    from ithaca_gpu._capi import GpuError
+    c = quad_case(2, 2, 3)
+    coll, amap, sys_ = _system(ctx, c)
+    for kw in ({"barrier_polls": -1}, {"drop_cta": -2}, {"delay_ns": 2_000_000}):
+        with pytest.raises(GpuError):
+            sys_.set_wait_test(**kw)

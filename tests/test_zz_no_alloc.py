@@ -1,7 +1,8 @@
 """The allocation-free Gram entry point (ithaca_gpu_pod_gram_noalloc) against ithaca_gpu_pod_gram.
 
-Callers that cannot allocate device memory where they need S^T S (a ROM step inside a
-CUDA graph being captured, or a host with a fixed device-memory budget) call the
+Callers that cannot allocate device memory where they need S^T S (a host whose device
+memory is reserved up front in its own pool, or a loop that must not stall on the
+device-wide synchronisation of cudaFree) call the
 no-allocation variant with their own device input and output; its split-K scratch is a
 fixed 2 MiB device array inside the library (ns <= 128). This file is collected last so
 that a run stopping at the first failure has already run every other test; it passes alone
