@@ -8,9 +8,14 @@ Jacobi-preconditioned CG solve of the assembled C0 system to an FP64 relative re
 ||b - A x||_2 / ||b||_2 < 1e-10, FP32 inner solves inside FP64 iterative refinement.
 Inputs are synthetic and seeded; no dataset is involved.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--order P] [--mesh M]
-  python bench.py --config quad2d|mixed2d|hex_orders|batched|pod|adjoint|all   (secondary workloads)
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--order P] [--mesh M] [--full 0|1]
+  python bench.py --config quad2d|mixed2d|hex_orders|batched|pod|adjoint|inner_apply|peaks|all   (secondary workloads)
 
+The default line also carries the metric's other configurations measured in the same
+run (--full 1): the same hexes at P = 8, the 32 x 32 quad mesh at P = 6 and 8 with
+lambda in {0.1, 1, 10} (mixed vs FP64), and the 256-solve parametric batch; and, as its
+CPU baseline, one full solve of the headline workload by the compiled CPU port of the
+reference path with the GPU FP64 solution's difference from it.
 `--impl reference` times the reference path's CPU implementation on the host cores
 (the compiled C++ port of the reference kernels and CG recurrence, oracle/cport).
 Under torchrun (N > 1) every rank solves its own copy (replicas: the single solve has
@@ -134,12 +139,11 @@ def fp32_kernel_name(variant, n, Q):
 
 
 # DRAM bytes (read + write) per element of one gathered FP32 apply as the inner iteration
-# launches it (scattered output: owned rows and assembly-ordered slots), from ncu captures
-# of the same kernels on 28^3 hexes (398.9 MB per launch for variant 41, 399.3 MB for 42,
-# means of two launches, over 21,952 elements);
-# a launch's traffic grows with the number of elements, so the bench scales it by E.
-# Keys: (kernel variant, modes, points).
-TRAFFIC_PER_ELEMENT = {(41, 7, 8): 18171, (42, 7, 8): 18190}
+# launches it (scattered output: owned rows and assembly-ordered slots), from an ncu
+# capture of the kernel on 28^3 hexes (394.1 MB read + 5.4 MB written per launch over
+# 21,952 elements, variant 42); a launch's traffic grows with the number of elements, so
+# the bench scales it by E. Keys: (kernel variant, modes, points).
+TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200}
 
 
 def workload_config(args, n, Q, E, N, ndir):
@@ -150,34 +154,108 @@ def workload_config(args, n, Q, E, N, ndir):
             "l2": "inputs larger than L2 (geometry and vectors exceed 129 MB)", "parallelism": "replicas"}
 
 
-def cpu_baseline_sample(args, n, Q, E, jac, df, amap, rhs, iters_full, nthreads, budget_s=20.0):
-    """Time the compiled CPU port of the reference CG (oracle/cport) on a bounded number
-    of iterations of the same workload; scale to solves/s with the iteration count of the
-    full reference recurrence (iters_full)."""
+def cpu_full_solve(n, Q, E, jac, df, amap, b, dinv, nthreads):
+    """One full FP64 solve of the workload by the compiled CPU port of the reference
+    kernels and CG recurrence (oracle/cport, pinned to the reference build by the golden
+    tests): its own iteration count, solution and wall time."""
     from oracle import cportbind
-    from oracle import solve as osolve
-    if not cportbind.available():
-        return None
-    dinv = np.ascontiguousarray(1.0 / rhs["diag"]) if "diag" in rhs else None
     t0 = time.perf_counter()
-    cportbind.cg_solve(3, n, Q, E, jac, df, True, LAMBDA, amap.l2g, amap.sign, amap.nglobal, amap.ndir, dinv,
-                       rhs["b"], TOL, 1, nthreads)
-    t1 = time.perf_counter()
-    base = t1 - t0  # setup + 2 operator applications
-    k = 4
-    while True:
+    x, it, eps = cportbind.cg_solve(3, n, Q, E, jac, df, True, LAMBDA, amap.l2g, amap.sign, amap.nglobal, amap.ndir,
+                                    dinv, b, TOL, 5000, nthreads)
+    return x, it, time.perf_counter() - t0
+
+
+def _solve_rate(torch, stream, fn, reps):
+    """Solves/s of fn (one solve per call) over reps calls, CUDA events on `stream`."""
+    a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        out = fn()
+    z.record(stream)
+    z.synchronize()
+    return reps / (a.elapsed_time(z) / 1e3), out
+
+
+def hex_order8_fields(torch, cuda):
+    """32^3 curved hexes at P = 8 (n = 9, Q = 10), lambda = 1, to 1e-10: mixed and FP64
+    solves/s (the largest order of the 3-D sweep)."""
+    from ithaca_gpu.workload import hex_workload
+    w = hex_workload(32, 8)
+    ctx, sysg, b = w["ctx"], w["system"], w["b"]
+    stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
+    variant, _ = sysg.autotune_inner(LAMBDA, reps=5)
+    x = torch.zeros_like(b)
+    sysg.solve(LAMBDA, b, x, tol=TOL, mode="mixed")
+    mixed, (_, rm) = _solve_rate(torch, stream, lambda: sysg.solve(LAMBDA, b, x, tol=TOL, mode="mixed"), 2)
+    xm = x.clone()
+    fp64, (_, r64) = _solve_rate(torch, stream, lambda: sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64"), 1)
+    out = {"workload": "32^3 curved hexes, P=8 (n=9, Q=10), lambda=1, to 1e-10",
+           "solve_dofs": w["amap"].nglobal - w["amap"].ndir, "fp32_kernel_variant": variant,
+           "mixed": {"solves_per_s": mixed, "iterations": rm.iterations, "outer": rm.outer_iterations,
+                     "rel_residual": rm.rel_residual},
+           "fp64": {"solves_per_s": fp64, "iterations": r64.iterations, "rel_residual": r64.rel_residual,
+                    "timed": "1 solve (FP64 graph captured by the first call inside it)"},
+           "speedup_mixed_vs_fp64": mixed / fp64,
+           "max_rel_diff_mixed_vs_fp64": float((x - xm).abs().max() / x.abs().max())}
+    del w, sysg, b, x, xm
+    ctx.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def quad_mixed_fields(torch, cuda):
+    """The 32 x 32 jittered-quad mesh at P = 6 and 8, lambda in {0.1, 1, 10}, to 1e-10:
+    mixed vs FP64 solves/s, one system at a time, and the difference of the mixed
+    solution from the FP64 one."""
+    from ithaca_gpu.workload import quad_workload
+    rows = []
+    for P in (6, 8):
+        w = quad_workload(32, P)
+        sysg, ctx = w["system"], w["ctx"]
+        stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
+        b = torch.from_numpy(w["b"]).to(cuda)
+        x = torch.zeros_like(b)
+        for lam in (0.1, 1.0, 10.0):
+            row = {"P": P, "lambda": lam}
+            for mode in ("fp64", "mixed"):
+                for _ in range(3):
+                    sysg.solve(lam, b, x, tol=TOL, mode=mode)
+                rate, (_, res) = _solve_rate(torch, stream, lambda: sysg.solve(lam, b, x, tol=TOL, mode=mode), 10)
+                row[mode] = {"solves_per_s": rate, "iterations": res.iterations, "outer": res.outer_iterations,
+                             "rel_residual": res.rel_residual}
+                if mode == "fp64":
+                    x64 = x.clone()
+            row["speedup"] = row["mixed"]["solves_per_s"] / row["fp64"]["solves_per_s"]
+            row["max_rel_diff_mixed_vs_fp64"] = float((x - x64).abs().max() / x64.abs().max())
+            rows.append(row)
+        ctx.close()
+    return rows
+
+
+def batched_fields():
+    """256 parametric 2-D solves (lambda = 10^U(-2, 2), E ~ U{500..8000}, P ~ U{3..9}) in
+    one batch to 1e-10: mixed vs FP64 solves/s."""
+    from ithaca_gpu.batched import BatchedHelmholtz, parametric_quad_problems
+    from ithaca_gpu.operators import Context
+    ctx = Context(0)
+    t0 = time.perf_counter()
+    probs = parametric_quad_problems(ctx, nsolve=256)
+    setup_s = time.perf_counter() - t0
+    bt = BatchedHelmholtz(ctx, "quad", probs)
+    out = {"workload": "256 2-D Helmholtz solves, lambda = 10^U(-2,2), E ~ U{500..8000} jittered quads, "
+                       "P ~ U{3..9}, Q = P+2, to 1e-10, one batch", "host_setup_s": setup_s}
+    for mode in ("fp64", "mixed"):
+        bt.solve(mode=mode, tol=TOL, want_x=False)  # warm-up (graph capture)
         t0 = time.perf_counter()
-        cportbind.cg_solve(3, n, Q, E, jac, df, True, LAMBDA, amap.l2g, amap.sign, amap.nglobal, amap.ndir, dinv,
-                           rhs["b"], TOL, k + 1, nthreads)
-        dt = time.perf_counter() - t0
-        if dt > budget_s / 2 or k >= 64:
-            break
-        k *= 2
-    t_iter = max(dt - base, 1e-9) / k
-    return {"value": 1.0 / (t_iter * iters_full), "unit": "solves/s", "cores": nthreads, "kind": "port",
-            "sample": f"{k} CG iterations of the full workload ({t_iter * 1e3:.1f} ms/iteration, setup excluded), "
-                      f"scaled by the {iters_full} iterations of the FP64 reference recurrence",
-            "ms_per_iteration": t_iter * 1e3}
+        res = bt.solve(mode=mode, tol=TOL, want_x=False)
+        ms = (time.perf_counter() - t0) * 1e3
+        out[mode] = {"solves_per_s": 256 / (ms / 1e3), "batch_ms": ms,
+                     "max_rel_residual": float(res["rel_residual"].max()),
+                     "iterations_median": float(np.median(res["iterations"]))}
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    bt.close()
+    ctx.close()
+    return out
 
 
 def run_gpu(args, rank, world):
@@ -242,14 +320,8 @@ def run_gpu(args, rank, world):
 
     # the other inner-solve variant, for comparison (not the headline)
     other = "mixed" if mode == "mixed_geo16" else "mixed_geo16"
-    _, res_o = sysg.solve(LAMBDA, b, x, tol=TOL, mode=other)
-    eo0, eo1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    eo0.record(stream)
-    for _ in range(2):
-        _, res_o = sysg.solve(LAMBDA, b, x, tol=TOL, mode=other)
-    eo1.record(stream)
-    eo1.synchronize()
-    other_solves = 2 / (eo0.elapsed_time(eo1) / 1e3)
+    sysg.solve(LAMBDA, b, x, tol=TOL, mode=other)
+    other_solves, (_, res_o) = _solve_rate(torch, stream, lambda: sysg.solve(LAMBDA, b, x, tol=TOL, mode=other), 2)
 
     # ---- dominant kernel: the FP32 gather + element Helmholtz of the inner solve ----
     k_ms, k_bytes = sysg.profile_apply(LAMBDA, mode=mode, reps=20)
@@ -257,16 +329,10 @@ def run_gpu(args, rank, world):
     achieved = k_bytes / (k_ms / 1e3) / 1e9
 
     # ---- FP64 reference recurrence on the GPU ----
-    _, res64 = sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64")
-    torch.cuda.synchronize()
-    k64 = max(1, min(2, args.steps))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(k64):
-        _, res64 = sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64")
-    e1.record(stream)
-    e1.synchronize()
-    fp64_solves = k64 / (e0.elapsed_time(e1) / 1e3)
+    sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64")
+    fp64_solves, (_, res64) = _solve_rate(torch, stream, lambda: sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64"),
+                                          max(1, min(2, args.steps)))
+    x64_gpu = x.clone()
     sol_diff = float((x - x_mixed).abs().max() / x.abs().max())
     k64_ms, k64_bytes = sysg.profile_apply(LAMBDA, mode="fp64", reps=5)
 
@@ -303,10 +369,14 @@ def run_gpu(args, rank, world):
 
     if rank != 0:
         return
+    # host copies for the CPU reference solve below, then free the headline workload
+    jac_h, df_h, b_h = jac.cpu().numpy(), df.cpu().numpy(), b.cpu().numpy()
+    dinv_h = 1.0 / sysg.diagonal(LAMBDA)
+    x64_h = x64_gpu.cpu().numpy()
     cfg = workload_config(args, n, Q, E, N, ndir)
-    tkey = ("geo16" if mode == "mixed_geo16" else variant, n, Q)
     cfg["fp32_kernel_variant"] = variant
     cfg["autotune_ms"] = {str(k): round(v, 4) for k, v in variant_ms.items()}
+    launches_total = int(launches)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -323,35 +393,57 @@ def run_gpu(args, rank, world):
         "helmholtz_gdofs": {"fp64": gdofs64, "fp32": gdofs32},
         "solver_gdofs": {"mixed": value / world * (N - ndir) / 1e9, "fp64": fp64_solves * (N - ndir) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (TRAFFIC_PER_ELEMENT[tkey] * E if tkey in TRAFFIC_PER_ELEMENT else None),
+                     "traffic": (TRAFFIC_PER_ELEMENT[(variant, n, Q)] * E
+                                 if mode == "mixed" and (variant, n, Q) in TRAFFIC_PER_ELEMENT else None),
                      "kernel": (f"helm3_pipe_kernel<float,{n},{Q},1,gather,1,half,packed>" if mode == "mixed_geo16"
                                 else fp32_kernel_name(variant, n, Q)) + " gather (inner FP32 apply)",
-                     "kernel_ms": k_ms, "bytes_per_launch": k_bytes, "peak_source": peak_kind},
+                     "kernel_ms": k_ms, "bytes_per_launch": k_bytes,
+                     "bytes_rule": "per element 4 (2 n^3 + 7 Q^3) + 4 n^3: FP32 coefficients in and out, J w and the "
+                                   "six metric terms per point, the signed index per local dof",
+                     "layout_overhead_bytes_per_launch": 4.0 * E * n ** 3,
+                     "peak_source": peak_kind},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_host.nbytes),
                 "d2h_bytes_per_step": int(out_host.nbytes), "rel_residual": rese.rel_residual},
-        "gpu_launches": int(launches),
+        "gpu_launches": launches_total,
         "clocks": clk.summary(),
     }
     # FP64 flop rate of the FP64 apply (collocation-form operation count per element)
     fl = 2 * (2 * (Q * n ** 3 + Q * Q * n * n + Q ** 3 * n) + 6 * Q ** 4 + 11 * Q ** 3)
     line["fp64"]["apply_fp64_tflops"] = E * fl / (k64_ms / 1e3) / 1e12
-    # CPU baseline: compiled port of the reference path on the host cores, bounded sample
+    del coll, coll32, sysg, jac, df, b, x, x_mixed, x64_gpu, loc, fd
+    ctx.close()
+    torch.cuda.empty_cache()
+    # the other configurations of the metric, measured in the same run
+    if args.full:
+        for key, fn in (("hex_p8", lambda: hex_order8_fields(torch, cuda)),
+                        ("quad_32x32_mixed_sweep", lambda: quad_mixed_fields(torch, cuda)),
+                        ("batched_256", batched_fields)):
+            try:
+                line[key] = fn()
+            except Exception as ex:  # one failing secondary field does not void the headline
+                line[key] = {"error": str(ex)[:300]}
+    # CPU baseline: one full solve of the same workload by the compiled port of the
+    # reference path on the host cores, and the GPU FP64 solution's difference from it
     try:
-        jac_h, df_h = jac.cpu().numpy(), df.cpu().numpy()
-        diag = sysg.diagonal(LAMBDA)
-        full = np.zeros(N)
-        full[ndir:] = diag
-        rhs = {"b": b.cpu().numpy(), "diag": diag}
-        line["cpu_baseline"] = cpu_baseline_sample(args, n, Q, E, jac_h, df_h, amap, rhs, res64.iterations,
-                                                   os.cpu_count() or 1)
-    except Exception as ex:  # the GPU numbers stand even if the CPU sample fails
+        nth = os.cpu_count() or 1
+        xc, it_c, dt_c = cpu_full_solve(n, Q, E, jac_h, df_h, amap, b_h, dinv_h, nth)
+        line["cpu_baseline"] = {"value": 1.0 / dt_c, "unit": "solves/s", "cores": nth, "kind": "port",
+                                "sample": f"one full FP64 Jacobi PCG solve of the workload to {TOL:g} "
+                                          f"({it_c} iterations, {dt_c:.1f} s, setup included)",
+                                "iterations": it_c}
+        line["fp64"]["max_rel_diff_vs_cpu_reference"] = float(
+            np.max(np.abs(x64_h[ndir:] - xc[ndir:])) / np.max(np.abs(xc[ndir:])))
+        line["fp64"]["cpu_reference_iterations"] = it_c
+    except Exception as ex:  # the GPU numbers stand even if the CPU solve fails
         line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
     print(json.dumps(line))
 
 
 def run_reference(args, rank, world):
     """CPU arm: the compiled port of the reference kernels + CG (oracle/cport), all host
-    threads, on the same workload; each step is a bounded sample of CG iterations."""
+    threads, on the same workload. One full solve (untimed for the steps) gives the
+    recurrence's own iteration count; each timed step is a bounded sample of CG
+    iterations, and solves/s = 1 / (time per iteration x that iteration count)."""
     if rank != 0:
         return
     from oracle import basis as obasis
@@ -371,7 +463,9 @@ def run_reference(args, rank, world):
     ip = oops.iproduct(b1, 3, jac.reshape(E, -1), f)
     rhs = -m.assemble(ip)
     dinv = osolve.jacobi_inverse(b1, 3, jac.reshape(E, -1), df, LAMBDA, m)
-    iters_full = REF_ITERATIONS.get((args.mesh, args.order))
+    _, iters_full, full_s = cpu_full_solve(n, Q, E, jac, df, amap, rhs, dinv, nth)
+    if iters_full <= 0:
+        raise RuntimeError(f"the CPU reference solve did not converge ({iters_full})")
     per_step = 8
 
     def run(k):
@@ -387,11 +481,6 @@ def run_reference(args, rank, world):
         step()
     times = [step() for _ in range(args.steps)]
     t_iter = max(statistics.median(times), 1e-9) / per_step
-    if iters_full is None:
-        iters_full = 1
-        unit_note = "per CG iteration (no iteration count recorded for this mesh/order)"
-    else:
-        unit_note = f"scaled by the {iters_full} iterations of the FP64 reference recurrence"
     value = 1.0 / (t_iter * iters_full)
     cfg = workload_config(args, n, Q, E, N, ndir)
     cfg["parallelism"] = f"{nth} host threads"
@@ -401,16 +490,13 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": cfg,
+        "iterations": iters_full,
+        "full_solve": {"seconds": full_s, "solves_per_s": 1.0 / full_s, "iterations": iters_full},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nth, "kind": "port",
-                         "sample": f"{per_step} CG iterations per step on the full workload, setup excluded, "
-                                   + unit_note},
+                         "sample": f"{per_step} CG iterations per step on the full workload, setup excluded, scaled "
+                                   f"by the {iters_full} iterations of this port's own full solve to {TOL:g}"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
-
-
-# Iterations of the FP64 reference recurrence (Jacobi PCG, tol 1e-10) on the bench
-# workloads, as counted by the GPU FP64 path (which reproduces the recurrence).
-REF_ITERATIONS = {(32, 6): 961}
 
 
 # ---------------------------------------------------------------------------------
@@ -685,8 +771,46 @@ def suite_hex_orders(args):
           orders=rows)
 
 
+def suite_inner_apply(args):
+    """The solver's gathered element applies alone, on --mesh^3 curved hexes at P =
+    --order: the FP32 inner apply of the mixed solve (the --variant kernel, or the
+    autotuned one) and the FP64 apply, CUDA-event time per launch against the algorithmic
+    bytes. A small mesh keeps it a case the kernel captures can take."""
+    from ithaca_gpu.workload import hex_workload
+    w = hex_workload(args.mesh, args.order)
+    sysg, E, n, Q = w["system"], w["mesh"].E, w["n"], w["Q"]
+    if args.variant < 0:
+        variant, _ = sysg.autotune_inner(LAMBDA, reps=3)
+    else:
+        variant = args.variant
+        w["coll"].set_variant(variant)
+    ms32, by32 = sysg.profile_apply(LAMBDA, mode="mixed", reps=args.steps)
+    ms64, by64 = sysg.profile_apply(LAMBDA, mode="fp64", reps=args.steps)
+    peak, kind = load_peaks()
+    cfg = {"workload": f"gathered element Helmholtz applies of the solver, {args.mesh}^3 curved hexes, P={args.order}",
+           "elements": E, "fp32_kernel_variant": variant}
+    _line("inner FP32 gathered apply: algorithmic GB/s", by32 / (ms32 / 1e3) / 1e9, "GB/s", args, cfg, dtype="f32",
+          fp32={"kernel": fp32_kernel_name(variant, n, Q), "ms": ms32, "bytes": by32,
+                "frac_of_hbm": by32 / (ms32 / 1e3) / 1e9 / peak, "peak_source": kind},
+          fp64={"ms": ms64, "bytes": by64, "gbs": by64 / (ms64 / 1e3) / 1e9})
+
+
+def suite_peaks(args):
+    """The device's arithmetic-pipe peaks (FP64 FMA, FP64 MMA, FP32 FMA), measured by the
+    library: the compute roofs of the FP64 and FP32 element operators."""
+    from ithaca_gpu.operators import Context
+    ctx = Context(0)
+    runs = [ctx.pipe_peaks() for _ in range(max(1, args.steps))]
+    best = {k: max(r[k] for r in runs) for k in runs[0]}
+    _line("arithmetic pipe peaks (FP64 FMA, FP64 MMA m8n8k4, FP32 FMA)", best["fp64_fma_tflops"], "TFLOP/s", args,
+          {"workload": "independent FMA / MMA chains on every SM, 8 CTAs of 256 threads per SM"}, dtype="f64/f32",
+          peaks=best, runs=runs)
+    ctx.close()
+
+
 SUITES = {"quad2d": suite_quad2d, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
-          "pod": suite_pod, "adjoint": suite_adjoint}
+          "pod": suite_pod, "adjoint": suite_adjoint, "inner_apply": suite_inner_apply,
+          "peaks": suite_peaks}
 
 
 def main():
@@ -699,6 +823,9 @@ def main():
     ap.add_argument("--mesh", type=int, default=32)
     ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed",
                     help="inner solve of the headline: FP32 on FP32 geometry, or FP32 on 16-bit geometry")
+    ap.add_argument("--variant", type=int, default=-1, help="inner_apply: FP32 hex kernel variant (-1: autotune)")
+    ap.add_argument("--full", type=int, default=1,
+                    help="1: add the P=8 hexes, the 2-D mixed sweep and the 256-solve batch to the line")
     ap.add_argument("--config", choices=["hex"] + list(SUITES) + ["all"], default="hex",
                     help="hex: the headline workload (default); the others: secondary workloads, one line each")
     args = ap.parse_args()

@@ -157,6 +157,18 @@ int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg);
  * the same recurrence (NekLinSysIterCG.cpp:104-263); 3-D systems always use the graph. */
 int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode);
 
+/* Successive right-hand sides: projection onto previous solutions (P. F. Fischer,
+ * Comput. Methods Appl. Mech. Engrg. 163, 1998), as GlobalLinSysIterative::DoProjection /
+ * UpdateKnownSolutions (MultiRegions/GlobalLinSysIterative.cpp:156-482) with the session
+ * parameter SuccessiveRHS (AssemblyMap.cpp:168-175). nsuccessive > 0 keeps that many
+ * A-conjugate normalised solutions, < 0 keeps |nsuccessive| solutions with the basis
+ * A x / ||A x||, 0 turns the projection off (at most 64). Each later ithaca_gpu_cg_solve /
+ * ithaca_gpu_helmsolve* call projects its right-hand side onto the stored solutions,
+ * runs CG on the remainder (iterations in the result count that CG) and stores the new
+ * solution. The stored solutions belong to one operator: a solve with another lambda, or
+ * ithaca_gpu_cg_set_varcoeff, starts the buffer afresh. Resets the buffer. */
+int ithaca_gpu_cg_set_successive_rhs(ithaca_gpu_cg* cg, int nsuccessive);
+
 /* Test hooks of the persistent solver's failure path (no reference counterpart; the
  * reference has no device waits). barrier_polls: polls of ~64 ns before a grid-barrier
  * wait gives up (0: the default, about 1 s; at most 2^24). drop_cta: that CTA never
@@ -223,6 +235,33 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
  * the ITHACA offline phase (CoupledLinearNS_ROM.cpp:1208-1283, one FOM HelmSolve per
  * parameter) as one graph-captured batch. Every solve follows the reference CG
  * recurrence with its own scalars. Host arrays, layouts as ithaca_gpu_cg_create. */
+/* ---- statically condensed global system (GlobalSysSoln = IterativeStaticCond) ----
+ * GlobalLinSysIterativeStaticCond (MultiRegions/GlobalLinSysIterativeStaticCond.cpp) with
+ * GlobalLinSysStaticCond::v_Solve (GlobalLinSysStaticCond.cpp:104-238): per element the
+ * Helmholtz matrix is condensed onto its boundary modes (vertex, edge, face: any modal
+ * index below 2), the assembled Schur-complement system is solved by the reference CG
+ * recurrence with its diagonal as Jacobi preconditioner
+ * (PreconditionerDiagonal::StaticCondDiagonalPreconditionerSum, :164-189), and the
+ * interior modes follow element by element. Same map arguments as ithaca_gpu_cg_create
+ * (the interior modes of an element must be private to it; Dirichlet dofs are boundary
+ * modes); the element blocks are built on the first solve with a given lambda, from the
+ * operator's own element apply (FP64, deformed collections). */
+typedef struct ithaca_gpu_sc ithaca_gpu_sc;
+int ithaca_gpu_sc_create(ithaca_gpu_op* op, const int* l2g, const double* sign, int nglobal, int ndir,
+                         ithaca_gpu_sc** out);
+int ithaca_gpu_sc_destroy(ithaca_gpu_sc* sc);
+/* Sizes: global boundary dofs, the Dirichlet ones among them, boundary and interior modes
+ * per element. */
+int ithaca_gpu_sc_info(ithaca_gpu_sc* sc, int* nbnd_global, int* ndir_bnd, int* nbnd_local, int* nint_local);
+/* v_Solve on local (element) arrays of E*n^d entries: loc_rhs the element forcing
+ * (e.g. -IProductWRTBase(f)), loc_inout the boundary values already known (Dirichlet
+ * data, initial guess) in, the solution out. opts->mode must be ITHACA_GPU_SOLVE_FP64.
+ * The CG's rhs magnitude is that of the assembled boundary forcing, smoothed 0.9 / 0.1
+ * with the previous solve's as v_PreSolve does (:431-460); res->rel_residual is the
+ * boundary system's sqrt(eps / rhs magnitude). */
+int ithaca_gpu_sc_solve(ithaca_gpu_sc* sc, double lambda, const double* loc_rhs, double* loc_inout,
+                        const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res, int on_device);
+
 typedef struct ithaca_gpu_batch ithaca_gpu_batch;
 typedef struct {
   int nmodes, npoints, nelmt;
@@ -303,10 +342,19 @@ int ithaca_gpu_pod_reconstruct(ithaca_gpu_ctx* ctx, int N, int r, const double* 
  * cudaMalloc or cudaFree and needs no context. */
 int ithaca_gpu_pod_gram_noalloc(int N, int ns, const double* S, double* C, void* stream);
 
+/* Measurement hook (no reference counterpart): the device's FP64 FMA, FP64 tensor-core
+ * (mma.sync m8n8k4 f64) and FP32 FMA throughput in TFLOP/s, each from one timed launch of
+ * independent FMA / MMA chains on every SM (after a warm-up launch) on the context
+ * stream; the compute roofs of the FP64 and FP32 element operators. */
+int ithaca_gpu_measure_pipe_peaks(ithaca_gpu_ctx* ctx, double* fp64_fma_tflops, double* fp64_mma_tflops,
+                                  double* fp32_fma_tflops);
+
 /* Measurement hook (no reference counterpart): runs the gather + element-Helmholtz
  * kernel that ithaca_gpu_cg_solve launches for `mode` `reps` times on the context
  * stream and returns its average device time in ms (CUDA events) and the algorithmic
- * bytes of one launch (local-vector, index and geometry traffic). */
+ * bytes of one launch: per element, the signed index (4 B) plus input and output per
+ * local dof, and J w with the symmetric metric per quadrature point, at the mode's
+ * element size (the scattered output's per-dof output codes are not counted). */
 int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int reps, double* avg_ms,
                                 double* bytes_per_launch);
 

@@ -546,7 +546,84 @@ __global__ void __launch_bounds__(RT) cast_kernel(size_t n, const double* __rest
   for (size_t i = (size_t)blockIdx.x * RT + threadIdx.x; i < n; i += (size_t)gridDim.x * RT) b[i] = (T)a[i];
 }
 
+// ---- successive right-hand sides: small dense products with the stored solutions ----
+constexpr int kMaxSuccessive = 64;
+struct ProjCoef {
+  double c[kMaxSuccessive];
+};
+
+// part[v * gridDim.x + cta] = this CTA's share of sum_i V[v ld + i] y[i], i < n (one
+// CTA row of the grid per stored vector v = blockIdx.y; fixed summation order).
+__global__ void __launch_bounds__(RT) multidot_part_kernel(int n, const double* __restrict__ V, size_t ld,
+                                                           const double* __restrict__ y, double* part) {
+  const double* v = V + (size_t)blockIdx.y * ld;
+  double acc = 0;
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) acc = fma(v[i], y[i], acc);
+  __shared__ double sh[RT / 32];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < RT / 32; ++w) t += sh[w];
+    part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// out[v] = sum of the nparts partials of vector v (one CTA per v, fixed order).
+__global__ void __launch_bounds__(RT) multidot_final_kernel(const double* part, int nparts, double* out) {
+  const double* p = part + (size_t)blockIdx.x * nparts;
+  double acc = 0;
+  for (int i = threadIdx.x; i < nparts; i += RT) acc += p[i];
+  __shared__ double sh[RT / 32];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < RT / 32; ++w) t += sh[w];
+    out[blockIdx.x] = t;
+  }
+}
+
+// out[i] = sum_{v < nv} coef[v] V[v ld + i] for i < n.
+__global__ void __launch_bounds__(RT) combine_kernel(int n, int nv, const double* __restrict__ V, size_t ld,
+                                                     const ProjCoef coef, double* __restrict__ out) {
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) {
+    double acc = 0;
+    for (int v = 0; v < nv; ++v) acc = fma(coef.c[v], V[(size_t)v * ld + i], acc);
+    out[i] = acc;
+  }
+}
+
+// dst[i] = a * src[i] (i < n); dst[i] += src[i] when add.
+__global__ void __launch_bounds__(RT) scale_copy_kernel(int n, double a, const double* __restrict__ src,
+                                                        double* __restrict__ dst, int add) {
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) dst[i] = add ? dst[i] + src[i] : a * src[i];
+}
+
 // ---- solver object --------------------------------------------------------------
+// State of the successive-right-hand-side projection (GlobalLinSysIterative.cpp:156-482):
+// up to m stored solutions (free part only, nf = N - ndir values each), normalised as
+// the reference normalises them, and the symmetric coefficient matrix of their products.
+struct SuccessiveRhs {
+  int m = 0;             // buffer size (0: off)
+  bool aconj = true;     // A-conjugate basis (the reference's positive SuccessiveRHS)
+  int nprev = 0;         // solutions accepted so far (m_numPrevSols)
+  int nstored = 0;       // vectors in the buffer (m_prevBasis.size())
+  double lambda = NAN;   // the operator the stored solutions belong to
+  std::vector<int> slot; // slot[i]: storage column of the reference's vector i
+  std::vector<double> M; // coefficient matrix, nstored x nstored, row-major
+  double* sols = nullptr;   // m x nf: x_i / norm_i
+  double* basis = nullptr;  // m x nf: A x_i / ||A x_i|| (non-conjugate mode only)
+  double *px = nullptr, *ax = nullptr, *bsave = nullptr, *part = nullptr, *dots = nullptr;
+  int nparts = 0;
+  void release() {
+    for (double* p : {sols, basis, px, ax, bsave, part, dots}) cudaFree(p);
+    sols = basis = px = ax = bsave = part = dots = nullptr;
+  }
+};
+
 template <typename T>
 struct Vecs {
   T *x = nullptr, *r = nullptr, *w = nullptr, *s = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr,
@@ -613,10 +690,12 @@ struct Cg {
   double diag_lambda = NAN;
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int graph64_len = 0, graph32_len = 0;
+  SuccessiveRhs proj;
   ~Cg();
 };
 
 Cg::~Cg() {
+  proj.release();
   if (graph64) cudaGraphExecDestroy(graph64);
   if (graph32) cudaGraphExecDestroy(graph32);
   cudaFree(l2g);
@@ -981,6 +1060,221 @@ static void solve_impl(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithac
   if (status != ITHACA_GPU_OK) fail(status, "NaN or Inf in the CG recurrence");
 }
 
+// ---- successive right-hand sides (GlobalLinSysIterative.cpp:156-482) ----------------
+constexpr double kZeroTol = 1.0e-12;          // NekConstants::kNekZeroTol
+constexpr double kSparseNonZeroTol = 1e-16;   // NekConstants::kNekSparseNonZeroTol
+
+// Solves M x = y (n x n, row-major, symmetric) by LDL^T without pivoting, in place in y.
+// The reference factorises with Bunch-Kaufman (Lapack Dsptrf); the matrix here is SPD
+// with a unit diagonal unless the stored solutions are dependent, and a non-positive
+// pivot is treated as the reference treats a failed factorisation.
+static bool ldlt_solve(const std::vector<double>& M, int n, std::vector<double>& y) {
+  std::vector<double> L((size_t)n * n, 0.0), d(n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    double dj = M[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) dj -= L[(size_t)j * n + k] * L[(size_t)j * n + k] * d[k];
+    if (!(dj > 0.0)) return false;
+    d[j] = dj;
+    L[(size_t)j * n + j] = 1.0;
+    for (int i = j + 1; i < n; ++i) {
+      double v = M[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) v -= L[(size_t)i * n + k] * L[(size_t)j * n + k] * d[k];
+      L[(size_t)i * n + j] = v / dj;
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < i; ++k) y[i] -= L[(size_t)i * n + k] * y[k];
+  for (int i = 0; i < n; ++i) y[i] /= d[i];
+  for (int i = n - 1; i >= 0; --i)
+    for (int k = i + 1; k < n; ++k) y[i] -= L[(size_t)k * n + i] * y[k];
+  return true;
+}
+
+static void proj_alloc(Cg* cg) {
+  SuccessiveRhs& P = cg->proj;
+  if (P.sols) return;
+  const size_t nf = (size_t)(cg->N - cg->ndir), N = cg->N;
+  P.nparts = std::max(1, std::min(device_sm_count() * 2, (int)((nf + RT - 1) / RT)));
+  ITHACA_CUDA(cudaMalloc(&P.sols, sizeof(double) * P.m * std::max<size_t>(nf, 1)));
+  if (!P.aconj) ITHACA_CUDA(cudaMalloc(&P.basis, sizeof(double) * P.m * std::max<size_t>(nf, 1)));
+  ITHACA_CUDA(cudaMalloc(&P.px, sizeof(double) * N));
+  ITHACA_CUDA(cudaMalloc(&P.ax, sizeof(double) * N));
+  ITHACA_CUDA(cudaMalloc(&P.bsave, sizeof(double) * N));
+  ITHACA_CUDA(cudaMalloc(&P.part, sizeof(double) * P.nparts * P.m));
+  ITHACA_CUDA(cudaMalloc(&P.dots, sizeof(double) * P.m));
+  ITHACA_CUDA(cudaMemset(P.px, 0, sizeof(double) * N));
+}
+
+// Stored vector i of the reference's m_prevBasis (the solutions themselves when A-conjugate).
+static double* proj_basis(Cg* cg) { return cg->proj.aconj ? cg->proj.sols : cg->proj.basis; }
+
+// <V_i, y> over the free dofs for the nv stored vectors V (host result).
+static std::vector<double> proj_dots(Cg* cg, const double* V, int nv, const double* yfree) {
+  SuccessiveRhs& P = cg->proj;
+  std::vector<double> out(nv, 0.0);
+  if (nv == 0) return out;
+  cudaStream_t s = cg->op->ctx->stream;
+  const int nf = cg->N - cg->ndir;
+  multidot_part_kernel<<<dim3(P.nparts, nv), RT, 0, s>>>(nf, V, (size_t)nf, yfree, P.part);
+  multidot_final_kernel<<<nv, RT, 0, s>>>(P.part, P.nparts, P.dots);
+  cg->op->ctx->launches += 2;
+  ITHACA_CUDA(cudaMemcpyAsync(out.data(), P.dots, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+  ITHACA_CUDA(cudaStreamSynchronize(s));
+  return out;
+}
+
+// ResetKnownSolutionsToLatestOne (:272-289): keep only the latest stored vector (moved to
+// column 0, with its unit diagonal entry).
+static int proj_reset_to_latest(Cg* cg) {
+  SuccessiveRhs& P = cg->proj;
+  if (P.nprev == 0) return -1;
+  const int latest = (P.nprev - 1 + P.m) % P.m;
+  const size_t nf = (size_t)(cg->N - cg->ndir);
+  cudaStream_t s = cg->op->ctx->stream;
+  if (latest != 0) {
+    ITHACA_CUDA(cudaMemcpyAsync(P.sols, P.sols + latest * nf, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+    if (!P.aconj)
+      ITHACA_CUDA(cudaMemcpyAsync(P.basis, P.basis + latest * nf, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+  }
+  P.nstored = 1;
+  P.M.assign(1, 1.0);
+  P.nprev = 1;
+  return latest;
+}
+
+// A x over the free dofs into P.ax (x gathered with its Dirichlet part read as zero).
+static void proj_apply(Cg* cg, double lambda, const double* x) {
+  cudaStream_t s = cg->op->ctx->stream;
+  launch_apply<double>(cg, cg->v64, cg->op->t64.base, geo64(cg), lambda, nullptr, x, s, true, nullptr);
+  assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+                                                  cg->v64.yloc, cg->proj.ax, nullptr, nullptr, nullptr);
+  cg->op->ctx->launches++;
+}
+
+// UpdateKnownSolutions (:295-482) with the solution in cg->v64.x.
+static void proj_update(Cg* cg, double lambda) {
+  SuccessiveRhs& P = cg->proj;
+  const int m = P.m, nf = cg->N - cg->ndir, nd = cg->ndir;
+  cudaStream_t s = cg->op->ctx->stream;
+  const int grid = std::max(1, std::min(RB, (nf + RT - 1) / RT));
+  int insert = P.nprev % m;
+  bool full = P.nstored == m;
+  proj_apply(cg, lambda, cg->v64.x);
+  double* axf = P.ax + nd;
+  const double* xf = cg->v64.x + nd;
+  const double sol_norm = proj_dots(cg, P.aconj ? xf : axf, 1, axf)[0];
+  if (sol_norm < 22.2 * kSparseNonZeroTol) return;
+  const double inv = 1.0 / std::sqrt(sol_norm);
+  scale_copy_kernel<<<grid, RT, 0, s>>>(nf, inv, axf, axf, 0);
+  cg->op->ctx->launches++;
+  const std::vector<double> all = proj_dots(cg, proj_basis(cg), P.nstored, axf);
+  std::vector<double> y;
+  for (int i = 0; i < P.nstored; ++i)
+    if (i != insert) y.push_back(all[i]);
+  // the coefficient matrix without the vector about to be replaced
+  int nt = 0;
+  std::vector<double> tilM;
+  if (full && m > 1) {
+    nt = m - 1;
+    tilM.resize((size_t)nt * nt);
+    for (int i = 0, a = 0; i < m; ++i) {
+      if (i == insert) continue;
+      for (int j = 0, b = 0; j < m; ++j) {
+        if (j == insert) continue;
+        tilM[(size_t)a * nt + b++] = P.M[(size_t)i * m + j];
+      }
+      ++a;
+    }
+  } else if (!full && P.nstored > 0) {
+    nt = P.nstored;
+    tilM = P.M;
+  }
+  std::vector<double> invy = y;
+  bool ok = true;
+  if (!y.empty()) ok = ldlt_solve(tilM, nt, invy);
+  if (!ok) {
+    const int latest = proj_reset_to_latest(cg);
+    y.assign(1, y[latest - (latest > insert)]);
+    invy = y;
+    insert = P.nprev % m;
+    full = P.nstored == m;
+  }
+  double residual = 1.0;
+  for (int i = 0; i < P.nstored - (full ? 1 : 0); ++i) residual -= y[i] * invy[i];
+  if (residual < 10.0 * kZeroTol) return;
+  // new coefficient matrix
+  const int nn = full ? m : P.nstored + 1;
+  std::vector<double> newM((size_t)nn * nn, 0.0);
+  const int no = P.nstored;
+  for (int i = 0; i < no; ++i)
+    for (int j = 0; j < no; ++j) newM[(size_t)i * nn + j] = P.M[(size_t)i * no + j];
+  newM[(size_t)insert * nn + insert] = 1.0;
+  for (int i = 0; i < nn; ++i) {
+    if (i == insert) continue;
+    const double v = y[i - (i > insert)];
+    newM[(size_t)insert * nn + i] = newM[(size_t)i * nn + insert] = v;
+  }
+  std::vector<double> probe(nn, 1.0);
+  if (!ldlt_solve(newM, nn, probe)) return;
+  // accept: store x / sqrt(solNorm) (and A x / sqrt(solNorm) for the non-conjugate basis)
+  scale_copy_kernel<<<grid, RT, 0, s>>>(nf, inv, xf, P.sols + (size_t)insert * nf, 0);
+  if (!P.aconj) ITHACA_CUDA(cudaMemcpyAsync(P.basis + (size_t)insert * nf, axf, sizeof(double) * nf,
+                                            cudaMemcpyDeviceToDevice, s));
+  cg->op->ctx->launches++;
+  if (P.nstored < m) P.nstored++;
+  P.M = newM;
+  P.nprev++;
+}
+
+// DoProjection (:156-266) around solve_impl: rhs in cg->v64.b, solution into cg->v64.x.
+static void solve_projected(Cg* cg, double lambda, const ithaca_gpu_cg_opts& o, ithaca_gpu_cg_result* res) {
+  SuccessiveRhs& P = cg->proj;
+  if (P.m == 0) {
+    solve_impl(cg, lambda, o, res);
+    return;
+  }
+  if (!(P.lambda == lambda)) {  // another operator: the stored solutions do not apply
+    P.nprev = P.nstored = 0;
+    P.M.clear();
+    P.lambda = lambda;
+  }
+  proj_alloc(cg);
+  const int nf = cg->N - cg->ndir, nd = cg->ndir;
+  cudaStream_t s = cg->op->ctx->stream;
+  const int grid = std::max(1, std::min(RB, (nf + RT - 1) / RT));
+  ithaca_gpu_cg_result r{};
+  if (P.nprev == 0) {
+    solve_impl(cg, lambda, o, &r);
+  } else {
+    ITHACA_CUDA(cudaMemcpyAsync(P.bsave, cg->v64.b, sizeof(double) * cg->N, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> alpha = proj_dots(cg, proj_basis(cg), P.nstored, P.bsave + nd);
+    const std::vector<double> alphaback = alpha;
+    if (!ldlt_solve(P.M, P.nstored, alpha)) {
+      const int latest = proj_reset_to_latest(cg);
+      alpha.assign(1, alphaback[latest]);
+    }
+    ProjCoef coef{};
+    for (int i = 0; i < P.nstored; ++i) coef.c[i] = alpha[i];
+    combine_kernel<<<grid, RT, 0, s>>>(nf, P.nstored, P.sols, (size_t)nf, coef, P.px + nd);
+    cg->op->ctx->launches++;
+    // pb = b - A px on the free dofs, zero on the Dirichlet ones
+    if (nd > 0) ITHACA_CUDA(cudaMemsetAsync(cg->v64.b, 0, sizeof(double) * nd, s));
+    fp64_residual(cg, lambda, P.px, P.bsave, cg->v64.b);
+    solve_impl(cg, lambda, o, &r);
+    // x = tmpx + px; the reported residual is that of x against the given rhs
+    scale_copy_kernel<<<grid, RT, 0, s>>>(nf, 1.0, P.px + nd, cg->v64.x + nd, 1);
+    ITHACA_CUDA(cudaMemcpyAsync(cg->v64.b, P.bsave, sizeof(double) * cg->N, cudaMemcpyDeviceToDevice, s));
+    cg->op->ctx->launches++;
+    double hs[2];
+    fp64_residual(cg, lambda, cg->v64.x, cg->v64.b, cg->v64.w);
+    ITHACA_CUDA(cudaMemcpyAsync(hs, cg->dscal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+    r.rel_residual = hs[1] > 0 ? std::sqrt(hs[0] / hs[1]) : 0.0;
+  }
+  if (r.iterations > 0) proj_update(cg, lambda);
+  if (res) *res = r;
+}
+
 }  // namespace ithaca
 
 using namespace ithaca;
@@ -1188,6 +1482,18 @@ int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode) {
   });
 }
 
+int ithaca_gpu_cg_set_successive_rhs(ithaca_gpu_cg* cg, int nsuccessive) {
+  return cg_guarded([&] {
+    req(cg != nullptr, "null solver");
+    req(std::abs(nsuccessive) <= kMaxSuccessive, "at most 64 stored solutions");
+    cudaStreamSynchronize(cg->op->ctx->stream);
+    cg->proj.release();
+    cg->proj = SuccessiveRhs{};
+    cg->proj.m = std::abs(nsuccessive);
+    cg->proj.aconj = nsuccessive > 0;
+  });
+}
+
 int ithaca_gpu_cg_set_wait_test(ithaca_gpu_cg* cg, long long barrier_polls, int drop_cta, int delay_ns) {
   return cg_guarded([&] {
     req(cg != nullptr, "null solver");
@@ -1312,7 +1618,7 @@ int ithaca_gpu_cg_solve(ithaca_gpu_cg* cg, double lambda, const double* rhs, dou
         cudaStreamSynchronize(cg->op->ctx->stream);
       }
     } cb{cg, x, on_device, (size_t)cg->ndir, sizeof(double) * (cg->N - cg->ndir)};
-    solve_impl(cg, lambda, o, res);
+    solve_projected(cg, lambda, o, res);
   });
 }
 
@@ -1362,7 +1668,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
       ITHACA_CUDA(cudaMemcpyAsync(keep, xd, sizeof(double) * cg->ndir, cudaMemcpyDeviceToDevice, s));
       dvals = keep;
     }
-    solve_impl(cg, lambda, o, res);
+    solve_projected(cg, lambda, o, res);
     // Dirichlet values (zero, or the given ones), then GlobalToLocal
     if (dvals != nullptr)
       ITHACA_CUDA(cudaMemcpyAsync(cg->v64.x, dvals, sizeof(double) * cg->ndir, cudaMemcpyDeviceToDevice, s));
@@ -1418,14 +1724,14 @@ int ithaca_gpu_cg_profile_apply(ithaca_gpu_cg* cg, int mode, double lambda, int 
     cudaEventDestroy(e1);
     *avg_ms = ms / reps;
     if (bytes_per_launch) {
-      // per element: l2g index (4 B) + gathered input + output per local dof (+ the output
-      // code, 4 B, of the scattered FP32 output), geometry per point (+ 8 scales per
-      // element for 16-bit geometry)
+      // algorithmic bytes per element: the signed l2g index (4 B), the gathered input and
+      // the output per local dof, and J w plus the symmetric metric per point (+ 8 scales
+      // per element for 16-bit geometry). The output codes of the scattered FP32 output
+      // (4 B per local dof) are this kernel's layout choice and are not counted.
       const double es = f32 ? 4.0 : 8.0, gs = half ? 2.0 : es;
       const double npt = op->deformed ? op->nq : 1;
-      const double oc = f32 && own.ctas >= 0 ? 4.0 : 0.0;
       *bytes_per_launch =
-          (double)op->E * (op->nm * (4.0 + oc + 2.0 * es) + n_jg(op->dim) * npt * gs + (half ? 32.0 : 0.0));
+          (double)op->E * (op->nm * (4.0 + 2.0 * es) + n_jg(op->dim) * npt * gs + (half ? 32.0 : 0.0));
     }
   });
 }
@@ -1527,6 +1833,7 @@ int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_de
     }
     if (cg->have16) build_geo16(cg);
     cg->diag_lambda = NAN;
+    cg->proj.lambda = NAN;  // a new operator: stored solutions of the old one no longer apply
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));
   });

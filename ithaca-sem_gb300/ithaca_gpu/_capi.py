@@ -77,6 +77,7 @@ SIGNATURES = {
     "ithaca_gpu_cg_create": [_vp, _vp, _vp, _i, _i, _pp],
     "ithaca_gpu_cg_destroy": [_vp],
     "ithaca_gpu_cg_set_persistent": [_vp, _i],
+    "ithaca_gpu_cg_set_successive_rhs": [_vp, _i],
     "ithaca_gpu_cg_set_wait_test": [_vp, ctypes.c_longlong, _i, _i],
     "ithaca_gpu_cg_default_opts": [ctypes.POINTER(CgOpts)],
     "ithaca_gpu_cg_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
@@ -86,6 +87,11 @@ SIGNATURES = {
     "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_helmsolve_dirichlet": [_vp, _d, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_sc_create": [_vp, _vp, _vp, _i, _i, _pp],
+    "ithaca_gpu_sc_destroy": [_vp],
+    "ithaca_gpu_sc_info": [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "ithaca_gpu_sc_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_batch_create": [_vp, _i, _i, ctypes.POINTER(SolveDesc), _pp],
     "ithaca_gpu_batch_destroy": [_vp],
     "ithaca_gpu_batch_solve": [_vp, ctypes.POINTER(CgOpts), _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)],
@@ -99,6 +105,8 @@ SIGNATURES = {
     "ithaca_gpu_pod_project": [_vp, _i, _vp, _vp, _vp, _i],
     "ithaca_gpu_pod_online": [_vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _i],
     "ithaca_gpu_pod_reconstruct": [_vp, _i, _i, _vp, _i, _vp, _vp, _i],
+    "ithaca_gpu_measure_pipe_peaks": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double)],
     "ithaca_gpu_cg_profile_apply": [_vp, _i, _d, _i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
 }
 

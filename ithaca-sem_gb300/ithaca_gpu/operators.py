@@ -82,6 +82,12 @@ class Context:
         C.call("ithaca_gpu_ctx_launch_count", self.handle, ctypes.byref(n))
         return n.value
 
+    def pipe_peaks(self):
+        """Measured FP64 FMA, FP64 MMA (DMMA) and FP32 FMA throughput, TFLOP/s."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        C.call("ithaca_gpu_measure_pipe_peaks", self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {"fp64_fma_tflops": a.value, "fp64_mma_tflops": b.value, "fp32_fma_tflops": c.value}
+
     def close(self):
         if self.handle:
             C.call("ithaca_gpu_ctx_destroy", self.handle)
@@ -331,6 +337,11 @@ class GlobalLinSysIterativeFullGPU:
         graph-captured kernels, 1 the persistent single-launch solver."""
         C.call("ithaca_gpu_cg_set_persistent", self.handle, int(mode))
 
+    def set_successive_rhs(self, nsuccessive):
+        """SuccessiveRHS projection of later solves onto up to |nsuccessive| previous
+        solutions (> 0 A-conjugate, < 0 residual-minimising, 0 off); resets the buffer."""
+        C.call("ithaca_gpu_cg_set_successive_rhs", self.handle, int(nsuccessive))
+
     def set_wait_test(self, barrier_polls=0, drop_cta=-1, delay_ns=0):
         """Failure-path test hooks of the persistent solver: a shorter grid-barrier wait,
         a CTA that never arrives (every wait then runs out: ERR_TIMEOUT), and a pause of
@@ -388,6 +399,69 @@ class GlobalLinSysIterativeFullGPU:
     def close(self):
         if getattr(self, "handle", None):
             C.call("ithaca_gpu_cg_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GlobalLinSysIterativeStaticCondGPU:
+    """Statically condensed C0 system + Jacobi-preconditioned CG on the boundary modes
+    (GlobalLinSysIterativeStaticCond), on the GPU."""
+
+    def __init__(self, coll, amap):
+        if coll.precision != "fp64":
+            raise ValueError("the global system needs an FP64 collection")
+        self.coll, self.amap = coll, amap
+        l2g = np.ascontiguousarray(amap.l2g, dtype=np.int32)
+        sign = np.ascontiguousarray(amap.sign, dtype=np.float64)
+        h = ctypes.c_void_p()
+        C.call("ithaca_gpu_sc_create", coll.handle, ctypes.c_void_p(l2g.ctypes.data),
+               ctypes.c_void_p(sign.ctypes.data), amap.nglobal, amap.ndir, ctypes.byref(h))
+        self.handle = h
+
+    def info(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        C.call("ithaca_gpu_sc_info", self.handle, *[ctypes.byref(x) for x in v])
+        return dict(nbnd_global=v[0].value, ndir_bnd=v[1].value, nbnd_local=v[2].value, nint_local=v[3].value)
+
+    def solve_local(self, lam, loc_rhs, loc_inout=None, **kw):
+        """GlobalLinSysStaticCond::v_Solve: local forcing -> local solution; loc_inout holds
+        the known boundary values (Dirichlet data) and receives the solution."""
+        n = self.coll.E * self.coll.nm
+        if loc_inout is None:
+            loc_inout = _like(loc_rhs, n)
+        _same_side(loc_rhs, loc_inout)
+        res = C.CgResult()
+        o = GlobalLinSysIterativeFullGPU.options(**kw)
+        pr, d = _ptr(loc_rhs, np.float64 if not _is_device(loc_rhs) else None)
+        pio, _ = _ptr(loc_inout)
+        C.call("ithaca_gpu_sc_solve", self.handle, ctypes.c_double(lam), pr, pio, ctypes.byref(o), ctypes.byref(res), d)
+        return loc_inout, res
+
+    def helmsolve(self, lam, forcing, dirichlet=None, **kw):
+        """ContField::v_HelmSolve with this solve: forcing at the quadrature points ->
+        local coefficients; dirichlet: the ndir Dirichlet global coefficients or None."""
+        loc_rhs = self.coll.iproduct(forcing)
+        loc_rhs = -loc_rhs
+        n = self.coll.E * self.coll.nm
+        if dirichlet is None:
+            inout = _like(forcing, n)
+        else:
+            xg = np.zeros(self.amap.nglobal)
+            xg[:self.amap.ndir] = np.asarray(dirichlet)
+            inout = self.amap.sign * xg[self.amap.l2g]
+            if _is_device(forcing):
+                import torch
+                inout = torch.from_numpy(inout).to(forcing.device)
+        return self.solve_local(lam, loc_rhs, inout, **kw)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.call("ithaca_gpu_sc_destroy", self.handle)
             self.handle = None
 
     def __del__(self):

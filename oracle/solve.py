@@ -50,8 +50,10 @@ def jacobi_inverse(basis, dim, jac, df, lam, amap):
     return 1.0 / d[m.ndir:]
 
 
-def cg(apply_fn, dinv, rhs, ndir, tol=1e-9, max_iter=5000):
-    """Returns (x, iterations, eps, rhs_mag); x has zeros on the Dirichlet part."""
+def cg(apply_fn, dinv, rhs, ndir, tol=1e-9, max_iter=5000, rhs_mag=None):
+    """Returns (x, iterations, eps, rhs_mag); x has zeros on the Dirichlet part.
+    rhs_mag: a magnitude set by the caller (GlobalLinSysIterative::Set_Rhs_Magnitude, as
+    the static-condensation solve sets it); None: ||rhs||^2 with the 1e-6 floor."""
     N = rhs.size
     nnd = N - ndir
     x = np.zeros(N)
@@ -60,8 +62,9 @@ def cg(apply_fn, dinv, rhs, ndir, tol=1e-9, max_iter=5000):
     p = np.zeros(nnd)
     q = np.zeros(nnd)
     eps = r @ r
-    bb = rhs @ rhs
-    rhs_mag = bb if bb > 1e-6 else 1.0
+    if rhs_mag is None:
+        bb = rhs @ rhs
+        rhs_mag = bb if bb > 1e-6 else 1.0
     tol = max(tol, 1e-16)
     if eps < tol * tol * rhs_mag:
         return x, 0, eps, rhs_mag
@@ -112,3 +115,141 @@ def helmsolve(basis, dim, jac, df, lam, amap, forcing, tol=1e-9, max_iter=5000, 
     x, it, _, _ = solve(basis, dim, jac, df, lam, m, rhs, tol, max_iter)
     x[:m.ndir] = xd[:m.ndir]
     return m.gather(x), it
+
+
+# ---------------------------------------------------------------------------------
+# Successive right-hand sides: projection onto previous solutions (Fischer 1998), as
+# GlobalLinSysIterative::DoProjection / UpdateKnownSolutions / ResetKnownSolutionsToLatestOne
+# (MultiRegions/GlobalLinSysIterative.cpp:156-482). nsucc > 0: A-conjugate basis of
+# A-normalised solutions; nsucc < 0: the basis A x / ||A x|| (least squares in the
+# Euclidean norm of the residual). The reference factorises the small symmetric
+# coefficient matrix with Bunch-Kaufman (Lapack Dsptrf/Dsptrs); here an LDL^T without
+# pivoting (the matrix is SPD with unit diagonal unless the basis is dependent, which
+# the same tests reject).
+# ---------------------------------------------------------------------------------
+ZERO_TOL = 1.0e-12          # NekConstants::kNekZeroTol
+SPARSE_NONZERO_TOL = 1e-16  # NekConstants::kNekSparseNonZeroTol
+
+
+def ldlt_solve(M, y):
+    """Solve M x = y by LDL^T without pivoting; returns None where a pivot is not positive."""
+    n = M.shape[0]
+    L = np.eye(n)
+    d = np.zeros(n)
+    for j in range(n):
+        d[j] = M[j, j] - np.dot(L[j, :j] ** 2, d[:j])
+        if not d[j] > 0.0:
+            return None
+        for i in range(j + 1, n):
+            L[i, j] = (M[i, j] - np.dot(L[i, :j] * L[j, :j], d[:j])) / d[j]
+    z = np.zeros(n)
+    for i in range(n):
+        z[i] = y[i] - np.dot(L[i, :i], z[:i])
+    z /= d
+    x = np.zeros(n)
+    for i in range(n - 1, -1, -1):
+        x[i] = z[i] - np.dot(L[i + 1:, i], x[i + 1:])
+    return x
+
+
+class SuccessiveRHS:
+    def __init__(self, nsucc):
+        self.aconj = nsucc > 0
+        self.m = abs(int(nsucc))
+        self.basis, self.sols = [], []
+        self.M = np.zeros((0, 0))
+        self.nprev = 0
+
+    def _reset_to_latest(self):
+        """ResetKnownSolutionsToLatestOne (:272-289)."""
+        if self.nprev == 0:
+            return -1
+        latest = (self.nprev - 1 + self.m) % self.m
+        self.basis, self.sols = [self.basis[latest]], [self.sols[latest]]
+        self.M = np.ones((1, 1))  # the unit diagonal entry of the kept vector
+        self.nprev = 1
+        return latest
+
+    def solve(self, apply_fn, dinv, rhs, ndir, tol=1e-9, max_iter=5000):
+        """DoProjection (:156-266): returns (x, iterations of the CG on the projected rhs)."""
+        if self.nprev == 0:
+            x, it, _, _ = cg(apply_fn, dinv, rhs, ndir, tol, max_iter)
+        else:
+            b = rhs[ndir:]
+            alpha = np.array([v @ b for v in self.basis])
+            a = ldlt_solve(self.M, alpha)
+            if a is None:
+                latest = self._reset_to_latest()
+                a = np.array([alpha[latest]])
+            px = np.zeros(rhs.size)
+            for ai, xi in zip(a, self.sols):
+                px[ndir:] += ai * xi
+            pb = np.zeros(rhs.size)
+            pb[ndir:] = b - apply_fn(px)[ndir:]
+            tmpx, it, _, _ = cg(apply_fn, dinv, pb, ndir, tol, max_iter)
+            x = np.zeros(rhs.size)
+            x[ndir:] = tmpx[ndir:] + px[ndir:]
+        if it:
+            self._update(apply_fn, x, ndir)
+        return x, it
+
+    def _update(self, apply_fn, newx, ndir):
+        """UpdateKnownSolutions (:295-482)."""
+        m = self.m
+        insert = self.nprev % m
+        full = len(self.basis) == m
+        ax = apply_fn(newx)[ndir:]
+        xb = newx[ndir:]
+        new_basis = xb if self.aconj else ax
+        sol_norm = new_basis @ ax
+        if sol_norm < 22.2 * SPARSE_NONZERO_TOL:
+            return
+        axn = ax / np.sqrt(sol_norm)
+        y = np.array([self.basis[i] @ axn for i in range(len(self.basis)) if i != insert])
+        if full and m > 1:
+            keep = [i for i in range(m) if i != insert]
+            tilM = self.M[np.ix_(keep, keep)]
+        elif not full and len(self.basis):
+            tilM = self.M.copy()
+        else:
+            tilM = np.zeros((0, 0))
+        ok = True
+        inv_y = np.zeros(y.size)
+        if y.size:
+            s = ldlt_solve(tilM, y)
+            ok = s is not None
+            if ok:
+                inv_y = s
+        if not ok:
+            latest = self._reset_to_latest()
+            y = np.array([y[latest - (latest > insert)]])
+            inv_y = y.copy()
+            insert = self.nprev % m
+            full = len(self.basis) == m
+        residual = 1.0 - float(np.dot(y[:len(self.basis) - full], inv_y[:len(self.basis) - full]))
+        if residual < 10.0 * ZERO_TOL:
+            return
+        if full:
+            newM = self.M.copy()
+            newM[insert, insert] = 1.0
+            for i in range(m):
+                if i == insert:
+                    continue
+                newM[insert, i] = newM[i, insert] = y[i - (i > insert)]
+        else:
+            k = len(self.basis)
+            newM = np.zeros((k + 1, k + 1))
+            newM[:k, :k] = self.M
+            newM[insert, insert] = 1.0
+            for i in range(k):
+                newM[insert, i] = newM[i, insert] = y[i]
+        if ldlt_solve(newM, np.ones(newM.shape[0])) is None:
+            return
+        xs = xb / np.sqrt(sol_norm)
+        if len(self.basis) < m:
+            self.basis.append(None)
+            self.sols.append(None)
+        self.sols[insert] = xs
+        self.basis[insert] = xs if self.aconj else axn
+        self.M = newM
+        self.nprev += 1
