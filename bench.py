@@ -242,8 +242,11 @@ def batched_fields():
     probs = parametric_quad_problems(ctx, nsolve=256)
     setup_s = time.perf_counter() - t0
     bt = BatchedHelmholtz(ctx, "quad", probs)
+    tiles = bt.autotune(reps=3)
     out = {"workload": "256 2-D Helmholtz solves, lambda = 10^U(-2,2), E ~ U{500..8000} jittered quads, "
-                       "P ~ U{3..9}, Q = P+2, to 1e-10, one batch", "host_setup_s": setup_s}
+                       "P ~ U{3..9}, Q = P+2, to 1e-10, one batch, each solve one graph launch",
+           "host_setup_s": setup_s,
+           "tile_variants": {str(n): {"fp32": c["fp32"][0], "fp64": c["fp64"][0]} for n, c in tiles.items()}}
     for mode in ("fp64", "mixed"):
         bt.solve(mode=mode, tol=TOL, want_x=False)  # warm-up (graph capture)
         t0 = time.perf_counter()
@@ -253,6 +256,43 @@ def batched_fields():
                      "max_rel_residual": float(res["rel_residual"].max()),
                      "iterations_median": float(np.median(res["iterations"]))}
     out["speedup_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    bt.close()
+    ctx.close()
+    return out
+
+
+def quad_sweep_batched_fields():
+    """The 32 x 32 jittered-quad mesh's lambda sweep (P = 6 and 8, lambda in {0.1, 1, 10}:
+    six systems) solved as one batch to 1e-10: mixed vs FP64 solves/s, each batch solve one
+    graph launch."""
+    from ithaca_gpu.batched import BatchedHelmholtz
+    from ithaca_gpu.operators import Context
+    from ithaca_gpu.workload import quad_workload
+    ctx = Context(0)
+    probs = []
+    for P in (6, 8):
+        w = quad_workload(32, P, ctx=ctx)
+        for lam in (0.1, 1.0, 10.0):
+            probs.append(dict(nmodes=w["n"], npoints=w["Q"], jac=w["jac"], df=w["df"], amap=w["amap"], lam=lam,
+                              rhs=w["b"]))
+    bt = BatchedHelmholtz(ctx, "quad", probs)
+    bt.autotune(reps=5)
+    out = {"workload": "32x32 jittered quads, P in {6, 8} x lambda in {0.1, 1, 10}: 6 systems in one batch, to 1e-10"}
+    xs = {}
+    for mode in ("fp64", "mixed"):
+        bt.solve(mode=mode, tol=TOL, want_x=False)
+        reps = 10
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = bt.solve(mode=mode, tol=TOL, want_x=False)
+        ms = (time.perf_counter() - t0) * 1e3 / reps
+        xs[mode] = bt.solve(mode=mode, tol=TOL)["x"]
+        out[mode] = {"solves_per_s": len(probs) / (ms / 1e3), "batch_ms": ms,
+                     "max_rel_residual": float(res["rel_residual"].max()),
+                     "iterations": [int(i) for i in res["iterations"]]}
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["max_rel_diff_mixed_vs_fp64"] = max(float(np.max(np.abs(a - b_)) / np.max(np.abs(b_)))
+                                            for a, b_ in zip(xs["mixed"], xs["fp64"]))
     bt.close()
     ctx.close()
     return out
@@ -417,6 +457,7 @@ def run_gpu(args, rank, world):
     if args.full:
         for key, fn in (("hex_p8", lambda: hex_order8_fields(torch, cuda)),
                         ("quad_32x32_mixed_sweep", lambda: quad_mixed_fields(torch, cuda)),
+                        ("quad_32x32_sweep_batched", quad_sweep_batched_fields),
                         ("batched_256", batched_fields)):
             try:
                 line[key] = fn()
@@ -616,7 +657,8 @@ def suite_mixed2d(args):
 
 def suite_batched(args):
     """256 parametric solves (lambda log-uniform, E ~ U{500..8000}, P ~ U{3..9}) in one
-    batch, FP64 and mixed."""
+    batch, FP64 and mixed: host-checked chunk launches, one graph launch per solve, and
+    one launch with the per-order autotuned tile shapes."""
     from ithaca_gpu.batched import BatchedHelmholtz, parametric_quad_problems
     from ithaca_gpu.operators import Context
     ctx = Context(0)
@@ -625,20 +667,29 @@ def suite_batched(args):
     setup_s = time.perf_counter() - t0
     bt = BatchedHelmholtz(ctx, "quad", probs)
     out = {}
-    for mode in ("fp64", "mixed"):
-        bt.solve(mode=mode, tol=1e-10, want_x=False)  # warm-up (graph capture)
-        ms, res = _time_host(lambda: bt.solve(mode=mode, tol=1e-10, want_x=False), 1, 0)
-        it = res["iterations"]
-        out[mode] = {"solves_per_s": 256 / (ms / 1e3), "batch_ms": ms, "device_ms": res["elapsed_ms"],
-                     "iterations": {"min": int(it.min()), "median": float(np.median(it)), "max": int(it.max())},
-                     "max_rel_residual": float(res["rel_residual"].max())}
+    tiles = None
+    for name, one, tune in (("host_checked", 0, False), ("one_launch", 1, False), ("one_launch_tuned", 1, True)):
+        bt.set_one_launch(one)
+        if tune:
+            tiles = bt.autotune(reps=3)
+        row = {}
+        for mode in ("fp64", "mixed"):
+            bt.solve(mode=mode, tol=1e-10, want_x=False)  # warm-up (graph build)
+            ms, res = _time_host(lambda: bt.solve(mode=mode, tol=1e-10, want_x=False), max(1, args.steps // 2), 0)
+            it = res["iterations"]
+            row[mode] = {"solves_per_s": 256 / (ms / 1e3), "batch_ms": ms, "device_ms": res["elapsed_ms"],
+                         "iterations": {"min": int(it.min()), "median": float(np.median(it)), "max": int(it.max())},
+                         "max_rel_residual": float(res["rel_residual"].max())}
+        row["speedup_mixed_vs_fp64"] = row["mixed"]["solves_per_s"] / row["fp64"]["solves_per_s"]
+        out[name] = row
     ndof = int(sum(p["amap"].nglobal - p["amap"].ndir for p in probs))
     cfg = {"workload": "256 2-D Helmholtz solves, lambda = 10^U(-2,2), E ~ U{500..8000} jittered quads, "
-                       "P ~ U{3..9}, Q = P+2, tol 1e-10, one graph-captured batch",
-           "solve_dofs_total": ndof, "host_setup_s": setup_s}
-    _line("batched parametric solves/s (256 2-D solves, mixed)", out["mixed"]["solves_per_s"], "solves/s", args,
-          cfg, dtype="f64 (outer) / f32 (inner)", batch=out,
-          speedup_mixed_vs_fp64=out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"])
+                       "P ~ U{3..9}, Q = P+2, tol 1e-10, one batch",
+           "solve_dofs_total": ndof, "host_setup_s": setup_s,
+           "tile_variants": {str(n): {"fp32": c["fp32"], "fp64": c["fp64"]} for n, c in tiles.items()}}
+    best = out["one_launch_tuned"]
+    _line("batched parametric solves/s (256 2-D solves, mixed)", best["mixed"]["solves_per_s"], "solves/s", args,
+          cfg, dtype="f64 (outer) / f32 (inner)", batch=out, speedup_mixed_vs_fp64=best["speedup_mixed_vs_fp64"])
 
 
 def suite_pod(args):

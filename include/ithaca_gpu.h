@@ -282,6 +282,24 @@ int ithaca_gpu_batch_destroy(ithaca_gpu_batch* batch);
  * elapsed_ms: device time of the whole batch (CUDA events on the context stream). */
 int ithaca_gpu_batch_solve(ithaca_gpu_batch* batch, const ithaca_gpu_cg_opts* opts, double* const* x,
                            int* iterations, int* outer, double* rel_res, double* elapsed_ms);
+/* Launch structure of ithaca_gpu_batch_solve (the snapshot loop of
+ * CoupledLinearNS_ROM.cpp:1208-1283 has no counterpart: it solves one system at a time).
+ * on = 1 (default): the whole solve is one CUDA graph launch whose loops are conditional
+ * graph nodes (device-side WHILE over chunks of iterations, and in mixed mode over the
+ * refinement steps), so the host waits once. on = 0: the host launches a captured chunk
+ * of iterations, reads the scalars and decides whether to launch again. Both run the same
+ * kernels in the same order and give the same results. */
+int ithaca_gpu_batch_set_one_launch(ithaca_gpu_batch* batch, int on);
+/* Tile shapes per polynomial order, chosen by timing as CollectionOptimisation::
+ * SetWithTimings chooses implementation types (Collections/CollectionOptimisation.cpp:
+ * 321-469): for each order group and precision the gathered element apply is timed `reps`
+ * times with each element-kernel variant (0 shared-memory kernel; 1 / 2 register-pencil
+ * kernel with 256 / 128 threads per CTA) on the group's own data, and the fastest is used
+ * from then on. Outputs (any may be NULL): the number of groups, each group's modes, the
+ * chosen FP32 and FP64 variants, and the times ms[(group * 2 + precision) * 3 + variant]
+ * (precision 0 FP32, 1 FP64; at most 11 groups). */
+int ithaca_gpu_batch_autotune(ithaca_gpu_batch* batch, int reps, int* ngroups, int* nmodes, int* variant32,
+                              int* variant64, double* ms);
 
 /* ---- variable coefficient and adjoint gradient ----
  * Isotropic diffusion coefficient kappa at the quadrature points (E*Q^d) of a deformed
@@ -289,6 +307,15 @@ int ithaca_gpu_batch_solve(ithaca_gpu_batch* batch, const ithaca_gpu_cg_opts* op
  * LaplacianMatrixOp_MatFree with eVarCoeffD00 = eVarCoeffD11 [= D22] = kappa
  * (StdRegions/StdExpansion.cpp:664-717). kappa == NULL restores kappa = 1. */
 int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_device);
+/* Anisotropic coefficient: the symmetric tensor K at the quadrature points of a deformed
+ * collection, d(d+1)/2 arrays of E*Q^d values in the order of the reference's
+ * eVarCoeffD00, D01, (D02,) D11, (D12, D22) (StdRegions/StdExpansion.cpp:664-717, where
+ * LaplacianMatrixOp_MatFree(k1, k2) scales d u / d x_k2 by the (k1, k2) component before
+ * IProductWRTDerivBase(k1)). The solver's operator becomes lambda M + sum_{k1,k2}
+ * (d phi / d x_k1, K_k1k2 d u / d x_k2): the metric of each point is rebuilt as
+ * J w (d xi / d x)^T K (d xi / d x). ithaca_gpu_cg_set_varcoeff(cg, NULL, 1) restores K = I;
+ * ithaca_gpu_kappa_gradient is defined for the isotropic coefficient only. */
+int ithaca_gpu_cg_set_varcoeff_tensor(ithaca_gpu_cg* cg, const double* K, int on_device);
 /* Misfit J = sum_q Jw_q (u(x_q) - u_target_q)^2 of the global vector x (Dirichlet
  * values taken as zero) and, if dJdx != NULL, its gradient w.r.t. x (nglobal entries,
  * zero on Dirichlet dofs). No reference counterpart (the reference has no adjoint). */

@@ -83,9 +83,50 @@ __global__ void zero_head_kernel(int n, double* __restrict__ a) {
   for (int i = blockIdx.x * AT + threadIdx.x; i < n; i += AB * AT) a[i] = 0.0;
 }
 
+// Anisotropic coefficient: the metric of the Laplacian term becomes
+// J w sum_{k,l} (dxi_a/dx_k) K_kl (dxi_b/dx_l), with K the symmetric tensor at each point
+// (K components in the order D00, D01, (D02,) D11, (D12, D22), each E*nq values; df per
+// element dfe[e][k*d+a][p] = dxi_a/dx_k). dst keeps J w in field 0 and the d(d+1)/2 metric
+// terms (upper triangle, row-major) after it.
+__global__ void tensor_metric_kernel(int E, int dim, int nq, const double* __restrict__ jg,
+                                     const double* __restrict__ dfe, const double* __restrict__ K,
+                                     double* __restrict__ dst) {
+  const size_t total = (size_t)E * nq;
+  const int ng = 1 + dim * (dim + 1) / 2, nd = dim * dim;
+  for (size_t i = (size_t)blockIdx.x * AT + threadIdx.x; i < total; i += (size_t)AB * AT) {
+    const size_t e = i / nq;
+    const int p = (int)(i % nq);
+    const double jw = jg[e * ng * nq + p];
+    double f[9], k[3][3];
+    for (int c = 0; c < nd; ++c) f[c] = dfe[(e * nd + c) * nq + p];
+    int t = 0;
+    for (int a = 0; a < dim; ++a)
+      for (int b = a; b < dim; ++b) {
+        k[a][b] = k[b][a] = K[(size_t)t * total + i];
+        ++t;
+      }
+    double* out = dst + e * ng * nq + p;
+    out[0] = jw;
+    int cnt = 1;
+    for (int a = 0; a < dim; ++a)
+      for (int b = a; b < dim; ++b) {
+        double s = 0;
+        for (int kk = 0; kk < dim; ++kk)
+          for (int l = 0; l < dim; ++l) s += f[kk * dim + a] * k[kk][l] * f[l * dim + b];
+        out[(size_t)cnt * nq] = jw * s;
+        ++cnt;
+      }
+  }
+}
+
 }  // namespace ithaca
 
 namespace ithaca {
+
+void launch_tensor_metric(int E, int dim, int nq, const double* jg, const double* dfe, const double* K, double* dst,
+                          cudaStream_t s) {
+  tensor_metric_kernel<<<AB, AT, 0, s>>>(E, dim, nq, jg, dfe, K, dst);
+}
 
 void launch_scale_metric(int E, int ng, int nq, const double* src, const double* kappa, double* dst,
                          cudaStream_t s) {

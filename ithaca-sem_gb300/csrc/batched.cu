@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -406,6 +407,48 @@ __global__ void __launch_bounds__(BT) baxpy_kernel(const Chunk* __restrict__ chu
   }
 }
 
+// ---- device-side loop control of the one-launch solve ----
+// One CTA: is any solve of any group still active (inner loop: !done; outer loop:
+// !outer_done)? Advances the loop counter and sets the conditional node(s) to
+// (active && counter < bound): the bound makes every device-side loop finite even if a
+// flag were never set.
+__global__ void __launch_bounds__(BT) bactive_kernel(Scal* const* __restrict__ scs, const int* __restrict__ nsolve,
+                                                     int ngroups, int outer, unsigned* counter, unsigned bound,
+                                                     cudaGraphConditionalHandle h, cudaGraphConditionalHandle h2,
+                                                     int set2) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    const Scal* sc = scs[g];
+    for (int k = threadIdx.x; k < nsolve[g]; k += BT) mine |= outer ? !sc[k].outer_done : !sc[k].done;
+  }
+  if (mine) any = 1;  // every writer stores the same value
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned c = ++*counter;
+    const unsigned v = (any && c < bound) ? 1u : 0u;
+    cudaGraphSetConditional(h, v);
+    if (set2) cudaGraphSetConditional(h2, v);
+  }
+}
+
+// Sets a conditional handle. A WHILE node nested in another conditional's body keeps the
+// value its loop ended with (the handle's default is applied at the top-level graph
+// launch only), so each entry into the inner loop re-arms it first.
+__global__ void bset_cond_kernel(cudaGraphConditionalHandle h, unsigned v) { cudaGraphSetConditional(h, v); }
+
+// After an inner solve of the mixed mode: its iterations into the outer scalars' totals
+// (iters: inner iterations, k: refinement steps that iterated), and a NaN/Inf status.
+__global__ void baccum_kernel(Scal* __restrict__ outer, const Scal* __restrict__ inner, int n) {
+  for (int k = blockIdx.x * BT + threadIdx.x; k < n; k += gridDim.x * BT) {
+    outer[k].iters += inner[k].iters;
+    if (inner[k].iters > 0) outer[k].k += 1;
+    if (inner[k].status == ITHACA_GPU_ERR_NUMERIC) outer[k].status = ITHACA_GPU_ERR_NUMERIC;
+  }
+}
+
 // ---- setup kernels ----
 __global__ void scale_jw_kernel(int E, int ng, int nq, double lambda, double* __restrict__ jg) {
   const size_t total = (size_t)E * nq;
@@ -473,6 +516,9 @@ struct Group {
   Vec<float> v32;
   cudaStream_t stream = nullptr;
   cudaEvent_t done_ev = nullptr;
+  // element-kernel variant of the group's applies (tile shape; -1 the default), chosen
+  // per order by ithaca_gpu_batch_autotune
+  int var32 = -1, var64 = -1;
   size_t nloc() const { return (size_t)E * nm; }
   ~Group() {
     cudaFree(t64);
@@ -520,10 +566,28 @@ struct Batch {
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int graph64_len = 0, graph32_len = 0;
   cudaEvent_t fork = nullptr;
+  // the whole solve as one graph launch with device-side loops (conditional nodes):
+  // 1 (default) on, 0 the host-checked chunk launches
+  int one_launch = 1;
+  cudaGraphExec_t solve64 = nullptr, solve_mixed = nullptr;
+  long long solve64_key = -1, solve_mixed_key = -1;  // chunk, bounds the graphs were built for
+  cudaStream_t cap[3] = {nullptr, nullptr, nullptr};  // capture streams of the loop bodies
+  batch::Scal** d_sc = nullptr;      // per group: inner scalars
+  batch::Scal** d_outer = nullptr;   // per group: outer scalars
+  int* d_nsolve = nullptr;
+  unsigned* d_counter = nullptr;     // [0] inner loop, [1] outer loop
   ~Batch() {
     if (graph64) cudaGraphExecDestroy(graph64);
     if (graph32) cudaGraphExecDestroy(graph32);
+    if (solve64) cudaGraphExecDestroy(solve64);
+    if (solve_mixed) cudaGraphExecDestroy(solve_mixed);
     if (fork) cudaEventDestroy(fork);
+    for (cudaStream_t c : cap)
+      if (c) cudaStreamDestroy(c);
+    cudaFree(d_sc);
+    cudaFree(d_outer);
+    cudaFree(d_nsolve);
+    cudaFree(d_counter);
   }
 };
 

@@ -681,6 +681,7 @@ struct Cg {
   float* jgs = nullptr;
   bool have16 = false, geo16 = false, graph32_geo16 = false;
   double* jgk64 = nullptr; // geometry with the metric scaled by a variable coefficient (else op->jg64)
+  bool aniso = false;       // jgk64 holds an anisotropic (tensor) coefficient
   double* adj_scratch = nullptr;
   double* partials = nullptr;
   double* dscal = nullptr;  // scratch doubles (norms)
@@ -1786,6 +1787,8 @@ void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, doub
 
 // adjoint.cu
 void launch_scale_metric(int E, int ng, int nq, const double* src, const double* kappa, double* dst, cudaStream_t s);
+void launch_tensor_metric(int E, int dim, int nq, const double* jg, const double* dfe, const double* K, double* dst,
+                          cudaStream_t s);
 void launch_misfit(int E, int ng, int nq, const double* jg, double* u, const double* t, double* partial, double* out,
                    cudaStream_t s);
 void launch_kappa_grad(int E, int ng, int nq, int dim, const double* jg, const double* du, const double* dp,
@@ -1834,6 +1837,38 @@ int ithaca_gpu_cg_set_varcoeff(ithaca_gpu_cg* cg, const double* kappa, int on_de
     if (cg->have16) build_geo16(cg);
     cg->diag_lambda = NAN;
     cg->proj.lambda = NAN;  // a new operator: stored solutions of the old one no longer apply
+    cg->aniso = false;
+    ITHACA_CUDA(cudaGetLastError());
+    ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ithaca_gpu_cg_set_varcoeff_tensor(ithaca_gpu_cg* cg, const double* K, int on_device) {
+  return cg_guarded([&] {
+    req(cg != nullptr && K != nullptr, "null argument");
+    StreamOrder order_(cg->op->ctx);
+    Op* op = cg->op;
+    req(op->deformed != 0, "a quadrature-point coefficient needs a deformed (per-point) collection");
+    cudaStream_t s = op->ctx->stream;
+    const int dim = op->dim, nk = dim * (dim + 1) / 2;
+    const size_t npts = (size_t)op->E * op->nq, njg = (size_t)op->E * n_jg(dim) * op->nq;
+    const double* dk = K;
+    if (!on_device) {
+      double* d = (double*)op->ctx->stage_ptr(0, sizeof(double) * nk * npts);
+      ITHACA_CUDA(cudaMemcpyAsync(d, K, sizeof(double) * nk * npts, cudaMemcpyHostToDevice, s));
+      dk = d;
+    }
+    if (!cg->jgk64) ITHACA_CUDA(cudaMalloc(&cg->jgk64, sizeof(double) * njg));
+    launch_tensor_metric(op->E, dim, op->nq, op->jg64, op->df64, dk, cg->jgk64, s);
+    op->ctx->launches++;
+    if (cg->have32) {
+      cast_kernel<float><<<RB, RT, 0, s>>>(njg, geo64(cg), cg->jg32);
+      op->ctx->launches++;
+    }
+    if (cg->have16) build_geo16(cg);
+    cg->diag_lambda = NAN;
+    cg->proj.lambda = NAN;
+    cg->aniso = true;
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));
   });
@@ -1887,6 +1922,7 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
 int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* psi, double* grad, int on_device) {
   return cg_guarded([&] {
     req(cg && x && psi && grad, "null argument");
+    if (cg->aniso) fail(ITHACA_GPU_ERR_UNSUPPORTED, "the kappa gradient is for an isotropic coefficient");
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     Ctx* c = op->ctx;

@@ -22,22 +22,22 @@
 namespace ithaca {
 namespace dev {
 
-template <typename T, int N, int Q>
+template <typename T, int N, int Q, int CT = 256>
 struct Pencil2 {
-  static constexpr int EB = 256 / Q;        // elements per CTA (threadIdx.y)
+  static constexpr int EB = CT / Q;         // elements per CTA (threadIdx.y) of CT threads
   static constexpr int PAD = Q + 1;         // row stride of a work field
   static constexpr int FS = Q * PAD;        // one work field
   static constexpr size_t bytes() { return sizeof(T) * (size_t)EB * 2 * FS; }
 };
 
-template <typename T, int N, int Q, bool GATHER>
-__global__ void __launch_bounds__(256) helm2_pencil_kernel(const T* __restrict__ in, T* __restrict__ out,
+template <typename T, int N, int Q, bool GATHER, int CT = 256>
+__global__ void __launch_bounds__(CT) helm2_pencil_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                            const PTabs<T, N, Q> tab, const T* __restrict__ jg,
                                                            T lambda, int E, const int* __restrict__ l2g, int ndir,
                                                            const int* __restrict__ skip,
                                                            const T* __restrict__ lam_ptr,
                                                            const int* __restrict__ esolve, int skip_stride) {
-  using L = Pencil2<T, N, Q>;
+  using L = Pencil2<T, N, Q, CT>;
   constexpr int NM = N * N, NQ = Q * Q, PAD = L::PAD, FS = L::FS;
   if (esolve == nullptr && skip != nullptr && *skip) return;  // a converged solve: the whole CTA leaves
   if (lam_ptr != nullptr) lambda = *lam_ptr;

@@ -38,24 +38,39 @@ const PTabs<T, N, Q>& host_ptabs() {
   return t;
 }
 
+// The register-pencil kernel for deformed quads with CT threads per CTA (CT / Q elements).
+template <typename T, int N, int Q, int CT>
+void helm2_pencil_launch(int E, const T* jg, T lambda, const T* in, T* out, const int* l2g, int ndir, const int* skip,
+                         const T* lam_ptr, const int* esolve, int skip_stride, cudaStream_t s) {
+  using P = Pencil2<T, N, Q, CT>;
+  auto k = l2g ? helm2_pencil_kernel<T, N, Q, true, CT> : helm2_pencil_kernel<T, N, Q, false, CT>;
+  static bool prepared[2] = {false, false};
+  if (!prepared[l2g ? 1 : 0]) {
+    ITHACA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::bytes()));
+    prepared[l2g ? 1 : 0] = true;
+  }
+  k<<<(E + P::EB - 1) / P::EB, dim3(Q, P::EB), P::bytes(), s>>>(in, out, host_ptabs<T, N, Q>(), jg, lambda, E, l2g,
+                                                             ndir, skip, lam_ptr, esolve, skip_stride);
+}
+
+// variant (deformed quads; ignored elsewhere): -1 the default (FP32: the register-pencil
+// kernel with 256 threads per CTA; FP64: the shared-memory kernel, as FP64 arithmetic
+// bounds both and its smaller CTAs spread small meshes over more SMs), 0 the
+// shared-memory kernel, 1 / 2 the register-pencil kernel with 256 / 128 threads per CTA.
 template <typename T, int DIM, int N, int Q>
 void helm_nq(int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g, int ndir,
-             const int* skip, const T* lam_ptr, const int* esolve, int skip_stride, cudaStream_t s) {
-  // FP32 deformed quads: the register-pencil kernel (elem2_pencil.cuh). FP64 stays on the
-  // shared-memory kernel: FP64 arithmetic bounds both, and the latter's smaller CTAs
-  // spread small meshes over more SMs.
-  if constexpr (DIM == 2 && sizeof(T) == 4) {
+             const int* skip, const T* lam_ptr, const int* esolve, int skip_stride, cudaStream_t s, int variant) {
+  if constexpr (DIM == 2) {
     if (deformed) {
-      using P = Pencil2<T, N, Q>;
-      auto k = l2g ? helm2_pencil_kernel<T, N, Q, true> : helm2_pencil_kernel<T, N, Q, false>;
-      static bool prepared[2] = {false, false};
-      if (!prepared[l2g ? 1 : 0]) {
-        ITHACA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::bytes()));
-        prepared[l2g ? 1 : 0] = true;
+      const int v = variant >= 0 ? variant : (sizeof(T) == 4 ? 1 : 0);
+      if (v == 1) {
+        helm2_pencil_launch<T, N, Q, 256>(E, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve, skip_stride, s);
+        return;
       }
-      k<<<(E + P::EB - 1) / P::EB, dim3(Q, P::EB), P::bytes(), s>>>(in, out, host_ptabs<T, N, Q>(), jg, lambda, E, l2g,
-                                                                 ndir, skip, lam_ptr, esolve, skip_stride);
-      return;
+      if (v == 2 && Q <= 128) {
+        helm2_pencil_launch<T, N, Q, 128>(E, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve, skip_stride, s);
+        return;
+      }
     }
   }
   using C = Cfg<T, DIM, N, Q>;
@@ -116,11 +131,11 @@ void diag_nq(int E, int deformed, const T* tab, const T* jg, T lambda, T* out, c
 template <typename T, int DIM>
 bool ElemApi<T, DIM>::helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in,
                            T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, const int* esolve,
-                           int skip_stride, cudaStream_t s) {
+                           int skip_stride, cudaStream_t s, int variant) {
 #define X(NN, QQ)                                                                                  \
   if (n == NN && Q == QQ) {                                                                        \
     dev::helm_nq<T, DIM, NN, QQ>(E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve,           \
-                                 skip_stride, s);                                                                  \
+                                 skip_stride, s, variant);                                                         \
     return true;                                                                                   \
   }
   ITHACA_FOR_EACH_NQ(X)

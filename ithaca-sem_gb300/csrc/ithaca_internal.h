@@ -169,7 +169,7 @@ template <typename T, int DIM>
 struct ElemApi {
   static bool helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out,
                    const int* l2g, int ndir, const int* skip, const T* lam_ptr, const int* esolve, int skip_stride,
-                   cudaStream_t s);
+                   cudaStream_t s, int variant = -1);
   static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
   static bool ipr(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
   static bool deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
@@ -183,11 +183,11 @@ template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
                              const int* skip = nullptr, const T* lam_ptr = nullptr, const int* esolve = nullptr,
-                             int skip_stride = 0) {
+                             int skip_stride = 0, int variant = -1) {
   return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
-                                        esolve, skip_stride, s)
+                                        esolve, skip_stride, s, variant)
                   : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
-                                        esolve, skip_stride, s);
+                                        esolve, skip_stride, s, variant);
 }
 template <typename T>
 inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {

@@ -94,8 +94,11 @@ SIGNATURES = {
     "ithaca_gpu_sc_solve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_batch_create": [_vp, _i, _i, ctypes.POINTER(SolveDesc), _pp],
     "ithaca_gpu_batch_destroy": [_vp],
+    "ithaca_gpu_batch_set_one_launch": [_vp, _i],
+    "ithaca_gpu_batch_autotune": [_vp, _i, ctypes.POINTER(ctypes.c_int), _vp, _vp, _vp, _vp],
     "ithaca_gpu_batch_solve": [_vp, ctypes.POINTER(CgOpts), _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double)],
     "ithaca_gpu_cg_set_varcoeff": [_vp, _vp, _i],
+    "ithaca_gpu_cg_set_varcoeff_tensor": [_vp, _vp, _i],
     "ithaca_gpu_misfit": [_vp, _vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_kappa_gradient": [_vp, _vp, _vp, _vp, _i],
     "ithaca_gpu_pod_gram": [_vp, _i, _i, _vp, _vp, _i],

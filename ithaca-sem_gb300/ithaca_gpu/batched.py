@@ -54,6 +54,25 @@ class BatchedHelmholtz:
                ctypes.c_void_p(outer.ctypes.data), ctypes.c_void_p(rel.ctypes.data), ctypes.byref(ms))
         return dict(x=xs, iterations=its, outer=outer, rel_residual=rel, elapsed_ms=ms.value)
 
+    def autotune(self, reps=5):
+        """Times the element-kernel variants (tile shapes) of every order group in FP32 and
+        FP64 and keeps the fastest. Returns {nmodes: {"fp32": (variant, [ms per variant]),
+        "fp64": (...)}}."""
+        ng = ctypes.c_int()
+        nm, v32, v64 = (np.zeros(11, dtype=np.int32) for _ in range(3))
+        ms = np.zeros(11 * 2 * 3)
+        C.call("ithaca_gpu_batch_autotune", self.handle, int(reps), ctypes.byref(ng),
+               *[ctypes.c_void_p(a.ctypes.data) for a in (nm, v32, v64, ms)])
+        out = {}
+        for g in range(ng.value):
+            t = ms[g * 6:(g + 1) * 6]
+            out[int(nm[g])] = {"fp32": (int(v32[g]), list(t[:3])), "fp64": (int(v64[g]), list(t[3:]))}
+        return out
+
+    def set_one_launch(self, on):
+        """1: each solve is one graph launch with device-side loops; 0: host-checked chunks."""
+        C.call("ithaca_gpu_batch_set_one_launch", self.handle, int(on))
+
     def close(self):
         if getattr(self, "handle", None):
             C.call("ithaca_gpu_batch_destroy", self.handle)

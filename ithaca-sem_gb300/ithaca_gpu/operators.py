@@ -310,6 +310,13 @@ class GlobalLinSysIterativeFullGPU:
         pk, d = _ptr(kappa, np.float64 if not _is_device(kappa) else None)
         C.call("ithaca_gpu_cg_set_varcoeff", self.handle, pk, d)
 
+    def set_varcoeff_tensor(self, K):
+        """Anisotropic coefficient: K has d(d+1)/2 rows (D00, D01, (D02,) D11, (D12, D22)) of
+        E*Q^d values at the quadrature points."""
+        K = K if _is_device(K) else np.ascontiguousarray(K, dtype=np.float64)
+        pk, d = _ptr(K, np.float64 if not _is_device(K) else None)
+        C.call("ithaca_gpu_cg_set_varcoeff_tensor", self.handle, pk, d)
+
     def misfit(self, x, u_target, J=None, dJdx=None):
         """J = sum Jw (u - u_target)^2 at the points and dJ/dx (global)."""
         dev = _is_device(x)

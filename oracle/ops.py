@@ -187,3 +187,25 @@ def helmholtz_diag(basis, dim, jac, df, lam):
             out = out + iproduct_tables(tables, b.w, dim, J * m[(a, c)])
     return out
 
+
+
+def helmholtz_varcoeff_tensor(basis, dim, jac, df, lam, K, coeffs):
+    """lambda M u + sum_{k1,k2} IProductWRTDerivBase(k1, K[k1,k2] du/dx_k2), as
+    StdRegions/StdExpansion.cpp:664-717 composes LaplacianMatrixOp_MatFree(k1, k2) with the
+    symmetric coefficients eVarCoeffD00, D01, (D02,) D11, (D12, D22) given in K (rows in that
+    order, each at the quadrature points)."""
+    b = basis
+    E = coeffs.size // b.n ** dim
+    nq = b.Q ** dim
+    J = _geo_pts(jac, E, nq)
+    u = bwdtrans(b, dim, coeffs)
+    out = lam * iproduct_tables([b.B2] * dim, b.w, dim, J * u)
+    d = physderiv(b, dim, df, u)
+    Kf = np.asarray(K).reshape(dim * (dim + 1) // 2, E, nq)
+    idx, t = {}, 0
+    for a in range(dim):
+        for c in range(a, dim):
+            idx[(a, c)] = idx[(c, a)] = t
+            t += 1
+    comps = [sum(Kf[idx[(k1, k2)]] * d[k2] for k2 in range(dim)) for k1 in range(dim)]
+    return out + iproduct_deriv(b, dim, jac, df, comps)

@@ -66,3 +66,68 @@ def test_batched_mixed_reaches_fp64_residual(family):
     for i, p in enumerate(probs):
         nd = p["amap"].ndir
         assert rel_err(res["x"][i][nd:], ref["x"][i][nd:]) < 1e-8
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_one_launch_matches_host_checked_path(family, mode):
+    """The whole solve as one graph launch (device-side loops) runs the same kernels in
+    the same order as the host-checked chunk launches: identical iterations and
+    solutions, bit for bit, on two solves in a row."""
+    from ithaca_gpu.batched import BatchedHelmholtz
+    ctx, probs = family
+    b = BatchedHelmholtz(ctx, "quad", probs)
+    b.set_one_launch(0)
+    ref = b.solve(mode=mode, tol=1e-10)
+    b.set_one_launch(1)
+    l0 = ctx.launch_count()
+    for _ in range(2):
+        res = b.solve(mode=mode, tol=1e-10)
+        assert np.array_equal(res["iterations"], ref["iterations"])
+        assert np.array_equal(res["outer"], ref["outer"])
+        for x, xr in zip(res["x"], ref["x"]):
+            assert np.array_equal(x, xr)
+        assert np.array_equal(res["rel_residual"], ref["rel_residual"])
+    # one graph launch per solve, plus the final FP64 residual's few launches
+    assert ctx.launch_count() - l0 < 2 * (1 + 3 * 8)
+
+
+def test_one_launch_reports_iteration_limit(family):
+    from ithaca_gpu._capi import ERR_NOT_CONVERGED, GpuError
+    from ithaca_gpu.batched import BatchedHelmholtz
+    ctx, probs = family
+    b = BatchedHelmholtz(ctx, "quad", probs[:3])
+    with pytest.raises(GpuError) as ei:
+        b.solve(mode="fp64", tol=1e-12, max_iter=4)
+    assert ei.value.code == ERR_NOT_CONVERGED
+    with pytest.raises(GpuError) as ei:
+        b.solve(mode="mixed", tol=1e-12, max_outer=1)
+    assert ei.value.code == ERR_NOT_CONVERGED
+    res = b.solve(mode="mixed", tol=1e-10)  # the batch stays usable
+    assert np.all(res["rel_residual"] < 1e-10)
+
+
+def test_autotuned_tile_shapes_keep_the_results(family):
+    """The per-order tile-shape autotuner picks, for every order group and precision, the
+    fastest element-kernel variant; the solves keep their FP64 residuals and iteration
+    counts (within one: the variants sum in a different order)."""
+    from ithaca_gpu.batched import BatchedHelmholtz
+    ctx, probs = family
+    b = BatchedHelmholtz(ctx, "quad", probs)
+    ref = b.solve(mode="fp64", tol=1e-11)
+    refm = b.solve(mode="mixed", tol=1e-10)
+    choice = b.autotune(reps=3)
+    assert sorted(choice) == sorted({p["nmodes"] for p in probs})
+    for n, c in choice.items():
+        for prec in ("fp32", "fp64"):
+            v, times = c[prec]
+            assert v in (0, 1, 2) and times[v] == min(times) and all(t > 0 for t in times)
+    res = b.solve(mode="fp64", tol=1e-11)
+    assert np.all(np.abs(res["iterations"] - ref["iterations"]) <= 1)
+    for x, xr, p in zip(res["x"], ref["x"], probs):
+        nd = p["amap"].ndir
+        assert rel_err(x[nd:], xr[nd:]) < 1e-10
+    resm = b.solve(mode="mixed", tol=1e-10)
+    assert np.all(resm["rel_residual"] < 1e-10)
+    for x, xr, p in zip(resm["x"], refm["x"], probs):
+        nd = p["amap"].ndir
+        assert rel_err(x[nd:], xr[nd:]) < 1e-8
