@@ -261,6 +261,107 @@ def batched_fields():
     return out
 
 
+# FP64 FMA issue rate of this machine's GB300 (2 flops per FMA), measured by
+# ithaca_gpu_measure_pipe_peaks (bench.py --config peaks).
+FP64_FMA_PEAK_TF = 1.254
+
+
+def tri_helm_flops(n):
+    """FP64 operations of one triangle Helmholtz apply in the kernel's collocation form:
+    BwdTrans (2 NC Q1 + 2 N NQ), collocation derivatives and their transposes
+    (4 NQ (Q0 + Q1)), 8 per point (metric products and the mass term), the inner
+    product (2 N NQ + 2 NC Q1) and the top-vertex terms (4 Q1)."""
+    Q0, Q1, nc = n + 1, n, n * (n + 1) // 2
+    nq = Q0 * Q1
+    return 4 * nc * Q1 + 4 * n * nq + 4 * nq * (Q0 + Q1) + 8 * nq + 4 * Q1
+
+
+def tri_fields(torch, cuda, mesh=128, P=6):
+    """Curved, jittered triangles (mesh x mesh cells, two triangles each) at order P:
+    the four operators (FP64 GDOF/s), the FP64 Helmholtz apply against the FP64 pipe,
+    FP32 apply, and Jacobi PCG to 1e-10 (FP64 and mixed); CPU: the compiled port of
+    HelmholtzTriImpl on the host cores."""
+    from ithaca_gpu.mesh import TriMesh
+    from ithaca_gpu.operators import Collection, Context, GlobalLinSysIterativeFullGPU, geom_factors
+    n = P + 1
+    Q = n + 1
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
+    m = TriMesh(mesh, mesh, jitter=0.15, seed=7, curve_amp=0.05)
+    E = m.E
+    X = m.coords(n)
+    jac, df = geom_factors(ctx, "tri", Q, X)
+    coll = Collection(ctx, "tri", n, Q, E, jac, df)
+    coll32 = Collection(ctx, "tri", n, Q, E, jac, df, precision="fp32")
+    nc, nq = coll.nm, coll.nq
+    rng = np.random.default_rng(11)
+    u = torch.from_numpy(rng.uniform(-1, 1, E * nc)).to(cuda)
+    u32 = u.float()
+    phys = torch.empty(E * nq, dtype=torch.float64, device=cuda)
+    coef = torch.empty_like(u)
+    coef32 = torch.empty_like(u32)
+    d0, d1 = torch.empty_like(phys), torch.empty_like(phys)
+    coll.bwdtrans(u, phys)
+    reps = 50
+    ms = {"bwdtrans": _time_device(torch, stream, lambda: coll.bwdtrans(u, phys), reps),
+          "iproduct": _time_device(torch, stream, lambda: coll.iproduct(phys, coef), reps),
+          "physderiv": _time_device(torch, stream, lambda: coll.physderiv(phys, [d0, d1]), reps),
+          "helmholtz": _time_device(torch, stream, lambda: coll.helmholtz(1.0, u, coef), reps)}
+    ms32 = _time_device(torch, stream, lambda: coll32.helmholtz(1.0, u32, coef32), reps)
+    fl = tri_helm_flops(n)
+    tflops = E * fl / (ms["helmholtz"] / 1e3) / 1e12
+    amap = m.assembly(n)
+    sysg = GlobalLinSysIterativeFullGPU(coll, amap)
+    f = (np.sin(np.pi * X[0]) * np.sin(np.pi * X[1])).reshape(-1) * -(1.0 + 2 * np.pi ** 2)
+    loc = coll.iproduct(f)
+    b_h = -amap.assemble(loc)
+    b_h[:amap.ndir] = 0.0
+    b = torch.from_numpy(b_h).to(cuda)
+    x = torch.zeros_like(b)
+    out = {"workload": f"{mesh}x{mesh} cells as {E} curved jittered triangles, P={P} (n={n}: {nc} modes, "
+                       f"{Q}x{n} points), lambda=1, per-point geometry",
+           "elements": E, "local_dofs": E * nc, "solve_dofs": amap.nglobal - amap.ndir,
+           "fp64_gdofs": {k: E * nc / (v / 1e3) / 1e9 for k, v in ms.items()},
+           "fp32_helmholtz_gdofs": E * nc / (ms32 / 1e3) / 1e9,
+           "helmholtz_fp64": {"ms": ms["helmholtz"], "flop_per_element": fl, "tflops": tflops,
+                              "bound": "fp64 pipe (2.8 flop per byte of per-point geometry and coefficients)",
+                              "peak_tflops": FP64_FMA_PEAK_TF, "frac": tflops / FP64_FMA_PEAK_TF,
+                              "peak_source": "measured FP64 FMA issue rate (bench.py --config peaks)"}}
+    for mode in ("fp64", "mixed"):
+        sysg.solve(1.0, b, x, tol=TOL, mode=mode)
+        rate, (_, res) = _solve_rate(torch, stream, lambda: sysg.solve(1.0, b, x, tol=TOL, mode=mode), 3)
+        out[mode] = {"solves_per_s": rate, "iterations": res.iterations, "outer": res.outer_iterations,
+                     "rel_residual": res.rel_residual}
+        if mode == "fp64":
+            x64 = x.clone()
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["max_rel_diff_mixed_vs_fp64"] = float((x - x64).abs().max() / x64.abs().max())
+    uh = coll.bwdtrans(sysg.global_to_local(x64.cpu().numpy()))
+    out["max_error_vs_exact_sin_sin"] = float(np.max(np.abs(uh - (np.sin(np.pi * X[0]) * np.sin(np.pi * X[1])).reshape(-1))))
+    try:
+        from oracle import cportbind
+        from oracle import tri as otri
+        if cportbind.available():
+            nth = os.cpu_count() or 1
+            tb = otri.TriBasis(n)
+            Es = min(E, 8192)
+            jh = np.asarray(jac).reshape(E, -1)[:Es].reshape(-1)
+            dh = np.asarray(df).reshape(4, E, -1)[:, :Es].reshape(4, -1)
+            uh_ = u.cpu().numpy()[:Es * nc]
+            ms_c, _ = _time_host(lambda: cportbind.tri_helmholtz(tb, Es, jh, dh, True, 1.0, uh_, nthreads=nth), 5)
+            out["cpu_baseline"] = {"value": Es * nc / (ms_c / 1e3) / 1e9, "unit": "GDOF/s (FP64 Helmholtz apply)",
+                                   "cores": nth, "kind": "port",
+                                   "sample": f"5 applies to the first {Es} triangles (HelmholtzTriImpl restated)"}
+    except Exception as ex:
+        out["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    sysg.close()
+    coll.close()
+    coll32.close()
+    ctx.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def quad_sweep_batched_fields():
     """The 32 x 32 jittered-quad mesh's lambda sweep (P = 6 and 8, lambda in {0.1, 1, 10}:
     six systems) solved as one batch to 1e-10: mixed vs FP64 solves/s, each batch solve one
@@ -458,7 +559,8 @@ def run_gpu(args, rank, world):
         for key, fn in (("hex_p8", lambda: hex_order8_fields(torch, cuda)),
                         ("quad_32x32_mixed_sweep", lambda: quad_mixed_fields(torch, cuda)),
                         ("quad_32x32_sweep_batched", quad_sweep_batched_fields),
-                        ("batched_256", batched_fields)):
+                        ("batched_256", batched_fields),
+                        ("tri_128x128_p6", lambda: tri_fields(torch, cuda))):
             try:
                 line[key] = fn()
             except Exception as ex:  # one failing secondary field does not void the headline
@@ -859,7 +961,16 @@ def suite_peaks(args):
     ctx.close()
 
 
-SUITES = {"quad2d": suite_quad2d, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
+def suite_tri(args):
+    """Triangles: 128 x 128 cells (32768 curved triangles) at P = 6."""
+    import torch
+    out = tri_fields(torch, "cuda:0")
+    _line("2-D Helmholtz on curved triangles, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
+          out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", tri=out,
+          cpu_baseline=out.get("cpu_baseline"))
+
+
+SUITES = {"quad2d": suite_quad2d, "tri": suite_tri, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
           "pod": suite_pod, "adjoint": suite_adjoint, "inner_apply": suite_inner_apply,
           "peaks": suite_peaks}
 

@@ -41,8 +41,8 @@ enum {
   ITHACA_GPU_ERR_NUMERIC = 8        /* NaN / Inf met in a reduction                      */
 };
 
-/* LibUtilities::ShapeType values of the two supported shapes. */
-enum { ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_HEX = 8 };
+/* LibUtilities::ShapeType values of the supported shapes (LibUtilities/BasicUtils/ShapeType.hpp). */
+enum { ITHACA_GPU_SHAPE_TRI = 3, ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_HEX = 8 };
 
 /* Arithmetic of an element operator. */
 enum { ITHACA_GPU_FP64 = 0, ITHACA_GPU_FP32 = 1 };
@@ -81,12 +81,26 @@ int ithaca_gpu_ctx_launch_count(ithaca_gpu_ctx* ctx, long long* count);
  * z, w: Q; D: Q*Q with D[k*Q+i] = l_k'(z_i); B, DB: n*Q with B[p*Q+i]. Host arrays. */
 int ithaca_gpu_basis_modA(int nmodes, int npoints, double* z, double* w, double* D, double* B, double* DB);
 
+/* ---- triangle basis: eModified_A on Q0 = nmodes + 1 GLL points (direction 0) and
+ *      eModified_B on Q1 = nmodes Gauss-Radau-Jacobi (alpha 1, beta 0) points (direction
+ *      1), the default keys of SpatialDomains/MeshGraph.cpp:1665-1681; Polylib.cpp:119-144
+ *      zwgrjm, :589-626 Dgrjm; Basis.cpp:423-507 eModified_B ----
+ * Direction 0 as ithaca_gpu_basis_modA(nmodes, nmodes + 1). Direction 1: z1, w1 (Q1, the
+ * weights as Basis::GetW holds them, without the collapsed map's factor 1/2), D1 (Q1*Q1,
+ * D1[l*Q1+j] = l_l'(z1_j)), B1 and DB1 (nc*Q1 with nc = nmodes (nmodes+1)/2, mode
+ * m(p, q) with q fastest: B1[m*Q1 + j]). Host arrays; any pointer may be NULL. */
+int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double* B0, double* DB0, double* z1,
+                         double* w1, double* D1, double* B1, double* DB1);
+
 /* ---- geometry (SpatialDomains/GeomFactors.cpp:168-475 ComputeDeriv/ComputeJac/
  *      ComputeDerivFactors) ----
  * coords: d arrays of E*Q^d physical coordinates at the GLL quadrature points,
  * stored one after another (coordinate k at coords[k*E*Q^d]). Writes jac (E*Q^d)
  * and df (d*d*E*Q^d) in the deformed layout above. Returns ITHACA_GPU_ERR_GEOMETRY
- * if any Jacobian is not positive. */
+ * if any Jacobian is not positive. Triangles (shape 3): npoints = Q0, the coordinates
+ * at the Q0 x Q1 collapsed points (point j*Q0 + i, Q1 = Q0 - 1), 2 arrays of E*Q0*Q1;
+ * the derivatives are taken in collapsed coordinates and mapped by the chain rule of
+ * StdTriExp::v_PhysDeriv. */
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device);
 
@@ -96,11 +110,17 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
  * MatrixFree::Operator (MatrixFreeOps/Operator.hpp:21-201) with its SetJac/SetDF.
  * Basis: ModifiedA with `nmodes` modes on `npoints` GLL points in every direction
  * (the homogeneous case MatrixFreeOps/Helmholtz.h:42-44 requires). Supported:
- * npoints == nmodes + 1, 2 <= nmodes <= 10. `precision` selects the arithmetic. */
+ * npoints == nmodes + 1, 2 <= nmodes <= 10. `precision` selects the arithmetic.
+ * Triangles (shape 3): the basis of ithaca_gpu_basis_tri with npoints = Q0 = nmodes + 1;
+ * per element nmodes (nmodes + 1) / 2 coefficients and Q0 (Q0 - 1) points, geometry
+ * (jac, df with d = 2) per point on those points or per element (MatrixFreeOps/
+ * Helmholtz.h:290-330, 505-635; BwdTrans.h:540-570; IProduct.h:560-590;
+ * PhysDeriv.h:470-500; IProductWRTDerivBase.h:671-1060). */
 int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
                          const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op);
 int ithaca_gpu_op_destroy(ithaca_gpu_op* op);
-/* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282). */
+/* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282); nelmt * nmodes (nmodes+1)/2
+ * for triangles. */
 int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof);
 
 /* BwdTrans (Collections/BwdTrans.cpp:143-240): coefficients -> physical values. */

@@ -1,7 +1,7 @@
 // Implementation type "GPU" for the Collections operators (Collections/Operator.h:113-165,
 // registrations as Collections/Helmholtz.cpp:484-503): BwdTrans, IProductWRTBase,
-// PhysDeriv, IProductWRTDerivBase and Helmholtz of quadrilateral and hexahedral
-// collections run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
+// PhysDeriv, IProductWRTDerivBase and Helmholtz of triangular, quadrilateral and
+// hexahedral collections run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
 // keeps the reference's element-contiguous layouts and CoalescedGeomData's geometry.
 #include <Collections/Operator.h>
 
@@ -19,8 +19,9 @@ class GpuOperatorBase : public Operator {
   GpuOperatorBase(std::vector<StdRegions::StdExpansionSharedPtr> pCollExp, CoalescedGeomDataSharedPtr pGeomData)
       : Operator(pCollExp, pGeomData) {
     const auto shape = pCollExp[0]->DetShapeType();
-    if (shape != LibUtilities::eQuadrilateral && shape != LibUtilities::eHexahedron)
-      NEKERROR(ErrorUtil::efatal, "GPU operators are built for quadrilaterals and hexahedra");
+    if (shape != LibUtilities::eTriangle && shape != LibUtilities::eQuadrilateral &&
+        shape != LibUtilities::eHexahedron)
+      NEKERROR(ErrorUtil::efatal, "GPU operators are built for triangles, quadrilaterals and hexahedra");
     const int nm = pCollExp[0]->GetBasis(0)->GetNumModes();
     const int nq = pCollExp[0]->GetBasis(0)->GetNumPoints();
     const Array<OneD, const NekDouble>& jac = pGeomData->GetJac(pCollExp);
@@ -28,7 +29,7 @@ class GpuOperatorBase : public Operator {
     Check(ithaca_gpu_op_create(GpuAdapter::GpuContext(), (int)shape, nm, nq, (int)m_numElmt, jac.get(), df.get(),
                                m_isDeformed ? 1 : 0, ITHACA_GPU_FP64, 0, &m_op));
     GpuAdapter::OperatorRegistry()[pCollExp[0].get()] = m_op;
-    m_dim = shape == LibUtilities::eQuadrilateral ? 2 : 3;
+    m_dim = shape == LibUtilities::eHexahedron ? 3 : 2;
   }
   ~GpuOperatorBase() override {
     if (m_op) ithaca_gpu_op_destroy(m_op);
@@ -111,6 +112,8 @@ class Helmholtz_GPU final : public GpuOperatorBase {
 
 #define ITHACA_GPU_REGISTER(cls, op, name)                                                                      \
   OperatorKey cls::m_typeArr[] = {                                                                            \
+      GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eTriangle, op, eGPU, false),      \
+                                                   cls::create, name "_Tri"),                                  \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eQuadrilateral, op, eGPU, false), \
                                                    cls::create, name "_Quad"),                                 \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eHexahedron, op, eGPU, false),    \

@@ -8,6 +8,13 @@
 //   ModifiedA modes B, DB = D B  -- LibUtilities/Foundations/Basis.cpp:392-421
 // Points: Newton iteration on (1 - z^2) P'_{Q-1}(z) from Chebyshev-Gauss-Lobatto
 // guesses; weights 2 / (Q (Q-1) P_{Q-1}(z)^2); D by the Lagrange-derivative formula.
+//
+// Triangles add direction 1 of the collapsed coordinates:
+//   Gauss-Radau-Jacobi points with z_0 = -1, alpha 1, beta 0 (Polylib.cpp:119-144 zwgrjm):
+//     interior points the zeros of P_{Q-1}^{(1,1)} (Newton with deflation from
+//     Chebyshev-Gauss guesses), weights 2 (1 - z_i) / (Q (Q+1) P_{Q-1}^{(1,0)}(z_i)^2)
+//   derivative matrix by the barycentric Lagrange formula (Polylib.cpp:589-626 Dgrjm)
+//   ModifiedB modes B1 (n (n+1)/2 of them, q fastest), DB1 = D1 B1 (Basis.cpp:423-507)
 #include "ithaca_internal.h"
 
 #include <cmath>
@@ -98,6 +105,93 @@ void modA_tables(int n, int Q, const double* z, const double* D, double* B, doub
       for (int k = 0; k < Q; ++k) s += D[k * Q + i] * B[p * Q + k];
       DB[p * Q + i] = s;
     }
+}
+
+// Zeros of P_m^{(a,b)}: Newton with deflation from Chebyshev-Gauss guesses.
+static void jacobi_zeros(int m, double a, double b, double* x) {
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < m; ++k) {
+    double r = -std::cos((2.0 * k + 1.0) * pi / (2.0 * m));
+    if (k > 0) r = 0.5 * (r + x[k - 1]);
+    for (int it = 0; it < 200; ++it) {
+      const double p = jacobi(m, a, b, r);
+      const double dp = 0.5 * (m + a + b + 1.0) * jacobi(m - 1, a + 1.0, b + 1.0, r);
+      double defl = 0.0;
+      for (int j = 0; j < k; ++j) defl += 1.0 / (r - x[j]);
+      const double step = p / (dp - p * defl);
+      r -= step;
+      if (std::fabs(step) < 1e-16) break;
+    }
+    x[k] = r;
+  }
+}
+
+static void radau_points(int Q, double* z, double* w) {
+  if (Q == 1) { z[0] = 0.0; w[0] = 2.0; return; }
+  z[0] = -1.0;
+  jacobi_zeros(Q - 1, 1.0, 1.0, z + 1);
+  for (int i = 0; i < Q; ++i) {
+    const double p = jacobi(Q - 1, 1.0, 0.0, z[i]);
+    w[i] = 2.0 * (1.0 - z[i]) / (Q * (Q + 1.0) * p * p);
+  }
+}
+
+// D[k*Q + i] = l_k'(z_i) for any distinct points.
+static void lagrange_derivative(int Q, const double* z, double* D) {
+  std::vector<double> c(Q, 1.0);
+  for (int i = 0; i < Q; ++i)
+    for (int j = 0; j < Q; ++j)
+      if (j != i) c[i] *= z[i] - z[j];
+  for (int i = 0; i < Q; ++i) {
+    double diag = 0.0;
+    for (int k = 0; k < Q; ++k) {
+      if (k == i) continue;
+      D[k * Q + i] = c[i] / (c[k] * (z[i] - z[k]));
+      diag += 1.0 / (z[i] - z[k]);
+    }
+    D[i * Q + i] = diag;
+  }
+}
+
+static void modB_tables(int n, int Q, const double* z, const double* D, double* B, double* DB) {
+  int m = 0;
+  for (int p = 0; p < n; ++p)
+    for (int q = 0; q < n - p; ++q, ++m)
+      for (int i = 0; i < Q; ++i) {
+        const double lo = 0.5 * (1.0 - z[i]), hi = 0.5 * (1.0 + z[i]);
+        double v;
+        if (p == 0)
+          v = q == 0 ? lo : (q == 1 ? hi : lo * hi * jacobi(q - 2, 1.0, 1.0, z[i]));
+        else if (q == 0)
+          v = std::pow(lo, p);
+        else
+          v = std::pow(lo, p) * hi * jacobi(q - 1, 2.0 * p - 1.0, 1.0, z[i]);
+        B[m * Q + i] = v;
+      }
+  for (int mm = 0; mm < m; ++mm)
+    for (int i = 0; i < Q; ++i) {
+      double s = 0.0;
+      for (int k = 0; k < Q; ++k) s += D[k * Q + i] * B[mm * Q + k];
+      DB[mm * Q + i] = s;
+    }
+}
+
+TriBasisTables make_tri_basis(int n) {
+  TriBasisTables t;
+  t.n = n;
+  t.Q0 = n + 1;
+  t.Q1 = n;
+  t.nc = n * (n + 1) / 2;
+  t.a = make_basis(n, n + 1);
+  t.z1.resize(t.Q1);
+  t.w1.resize(t.Q1);
+  t.D1.resize(t.Q1 * t.Q1);
+  t.B1.resize((size_t)t.nc * t.Q1);
+  t.DB1.resize((size_t)t.nc * t.Q1);
+  radau_points(t.Q1, t.z1.data(), t.w1.data());
+  lagrange_derivative(t.Q1, t.z1.data(), t.D1.data());
+  modB_tables(n, t.Q1, t.z1.data(), t.D1.data(), t.B1.data(), t.DB1.data());
+  return t;
 }
 
 BasisTables make_basis(int n, int Q) {

@@ -98,9 +98,45 @@ static int guarded(F f) {
 }
 
 static int shape_dim(int shape) {
-  if (shape == ITHACA_GPU_SHAPE_QUAD) return 2;
+  if (shape == ITHACA_GPU_SHAPE_QUAD || shape == ITHACA_GPU_SHAPE_TRI) return 2;
   if (shape == ITHACA_GPU_SHAPE_HEX) return 3;
-  fail(ITHACA_GPU_ERR_UNSUPPORTED, "shape must be quadrilateral (4) or hexahedron (8)");
+  fail(ITHACA_GPU_ERR_UNSUPPORTED, "shape must be triangle (3), quadrilateral (4) or hexahedron (8)");
+}
+
+// Packed triangle tables (layout tri_off in ithaca_internal.h), host FP64.
+static std::vector<double> pack_tri_tables(const TriBasisTables& b) {
+  const TriOff o = tri_off(b.n);
+  const int n = b.n, Q0 = b.Q0, Q1 = b.Q1, nc = b.nc;
+  std::vector<double> h(o.size);
+  for (int i = 0; i < n * Q0; ++i) {
+    h[o.B0 + i] = b.a.B[i];
+    h[o.DB0 + i] = b.a.DB[i];
+  }
+  for (int i = 0; i < Q0 * Q0; ++i) h[o.D0 + i] = b.a.D[i];
+  for (int i = 0; i < Q0; ++i) {
+    h[o.w0 + i] = b.a.w[i];
+    h[o.h0 + i] = 0.5 * (1.0 + b.a.z[i]);
+  }
+  for (int i = 0; i < nc * Q1; ++i) {
+    h[o.B1 + i] = b.B1[i];
+    h[o.DB1 + i] = b.DB1[i];
+  }
+  for (int i = 0; i < Q1 * Q1; ++i) h[o.D1 + i] = b.D1[i];
+  for (int j = 0; j < Q1; ++j) {
+    h[o.w1 + j] = 0.5 * b.w1[j];  // MatrixFreeOps/Operator.hpp:245-248
+    h[o.h1 + j] = 2.0 / (1.0 - b.z1[j]);
+  }
+  return h;
+}
+
+template <typename T>
+static void upload_tri_tables(DevTables<T>& dt, const TriBasisTables& b) {
+  const std::vector<double> h = pack_tri_tables(b);
+  std::vector<T> ht(h.begin(), h.end());
+  dt.n = b.n;
+  dt.Q = b.Q0;
+  ITHACA_CUDA(cudaMalloc(&dt.base, ht.size() * sizeof(T)));
+  ITHACA_CUDA(cudaMemcpy(dt.base, ht.data(), ht.size() * sizeof(T), cudaMemcpyHostToDevice));
 }
 
 template <typename T>
@@ -244,6 +280,25 @@ int ithaca_gpu_basis_modA(int nmodes, int npoints, double* z, double* w, double*
   });
 }
 
+int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double* B0, double* DB0, double* z1,
+                         double* w1, double* D1, double* B1, double* DB1) {
+  return guarded([&] {
+    require(nmodes >= 2 && nmodes <= 16, "need 2 <= nmodes <= 16");
+    const TriBasisTables t = make_tri_basis(nmodes);
+    const int n = nmodes, Q0 = t.Q0, Q1 = t.Q1, nc = t.nc;
+    if (z0) std::memcpy(z0, t.a.z.data(), sizeof(double) * Q0);
+    if (w0) std::memcpy(w0, t.a.w.data(), sizeof(double) * Q0);
+    if (D0) std::memcpy(D0, t.a.D.data(), sizeof(double) * Q0 * Q0);
+    if (B0) std::memcpy(B0, t.a.B.data(), sizeof(double) * n * Q0);
+    if (DB0) std::memcpy(DB0, t.a.DB.data(), sizeof(double) * n * Q0);
+    if (z1) std::memcpy(z1, t.z1.data(), sizeof(double) * Q1);
+    if (w1) std::memcpy(w1, t.w1.data(), sizeof(double) * Q1);
+    if (D1) std::memcpy(D1, t.D1.data(), sizeof(double) * Q1 * Q1);
+    if (B1) std::memcpy(B1, t.B1.data(), sizeof(double) * nc * Q1);
+    if (DB1) std::memcpy(DB1, t.DB1.data(), sizeof(double) * nc * Q1);
+  });
+}
+
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device) {
   return guarded([&] {
@@ -251,6 +306,31 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
     StreamOrder order_(ctx);
     require(nelmt > 0 && npoints >= 2 && npoints <= 16, "bad sizes");
     const int dim = shape_dim(shape);
+    if (shape == ITHACA_GPU_SHAPE_TRI) {  // npoints = Q0 = n + 1 GLL points; Q1 = n Gauss-Radau
+      const int n = npoints - 1;
+      const size_t tot = (size_t)nelmt * npoints * n;
+      const std::vector<double> h = pack_tri_tables(make_tri_basis(n));
+      double* dtab = nullptr;
+      int* dbad = nullptr;
+      ITHACA_CUDA(cudaMalloc(&dtab, sizeof(double) * h.size()));
+      std::unique_ptr<double, decltype(&cudaFree)> g1(dtab, cudaFree);
+      ITHACA_CUDA(cudaMalloc(&dbad, sizeof(int)));
+      std::unique_ptr<int, decltype(&cudaFree)> g2(dbad, cudaFree);
+      ITHACA_CUDA(cudaMemcpyAsync(dtab, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+      ITHACA_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+      const double* X = (const double*)to_device(ctx, 0, coords, sizeof(double) * 2 * tot, on_device);
+      double* J = (double*)out_buffer(ctx, 1, jac, sizeof(double) * tot, on_device);
+      double* F = (double*)out_buffer(ctx, 2, df, sizeof(double) * 4 * tot, on_device);
+      launch_geom_factors_tri(n, nelmt, dtab, X, J, F, dbad, ctx->stream);
+      ctx->launches++;
+      from_device(ctx, jac, J, sizeof(double) * tot, on_device);
+      from_device(ctx, df, F, sizeof(double) * 4 * tot, on_device);
+      int hbad = 0;
+      ITHACA_CUDA(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (hbad) fail(ITHACA_GPU_ERR_GEOMETRY, "non-positive Jacobian at a quadrature point");
+      return;
+    }
     const int Q = npoints;
     const size_t nq = dim == 2 ? (size_t)Q * Q : (size_t)Q * Q * Q;
     const size_t tot = (size_t)nelmt * nq;
@@ -293,35 +373,62 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     o->ctx = ctx;
     o->shape = shape;
     o->dim = dim;
+    o->kdim = shape == ITHACA_GPU_SHAPE_TRI ? kTriKernels : dim;
     o->n = nmodes;
     o->Q = npoints;
     o->E = nelmt;
     o->deformed = deformed ? 1 : 0;
     o->precision = precision;
-    o->nm = dim == 2 ? nmodes * nmodes : nmodes * nmodes * nmodes;
-    o->nq = dim == 2 ? npoints * npoints : npoints * npoints * npoints;
-    BasisTables b = make_basis(nmodes, npoints);
-    upload_tables(o->t64, b);
-    upload_tables(o->t32, b);
-    o->hB = b.B;
-    o->hD = b.D;
-    const size_t npt = o->deformed ? (size_t)o->nq : 1;
-    const size_t njg = (size_t)nelmt * n_jg(dim) * npt, ndf = (size_t)nelmt * dim * dim * npt;
-    const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * npt, on_device);
-    const double* F = (const double*)to_device(ctx, 1, df, sizeof(double) * dim * dim * nelmt * npt, on_device);
-    double* dw = nullptr;
-    ITHACA_CUDA(cudaMalloc(&dw, sizeof(double) * npoints));
-    std::unique_ptr<double, decltype(&cudaFree)> gw(dw, cudaFree);
-    ITHACA_CUDA(cudaMemcpyAsync(dw, b.w.data(), sizeof(double) * npoints, cudaMemcpyHostToDevice, ctx->stream));
-    ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
-    ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * ndf));
-    launch_build_jg<double>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg64, o->df64, ctx->stream);
-    ctx->launches++;
-    if (precision == ITHACA_GPU_FP32) {
-      ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
-      ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
-      launch_build_jg<float>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg32, o->df32, ctx->stream);
+    const size_t npt = o->deformed ? (size_t)(dim == 2 ? npoints * npoints : npoints * npoints * npoints) : 1;
+    if (shape == ITHACA_GPU_SHAPE_TRI) {
+      // ModifiedA x ModifiedB: n (n + 1) / 2 modes on (n + 1) x n collapsed points
+      o->nm = tri_nc(nmodes);
+      o->nq = npoints * nmodes;
+      const TriBasisTables tb = make_tri_basis(nmodes);
+      upload_tri_tables(o->t64, tb);
+      upload_tri_tables(o->t32, tb);
+      const size_t tp = o->deformed ? (size_t)o->nq : 1;
+      const size_t njg = (size_t)nelmt * 4 * tp;
+      const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * tp, on_device);
+      const double* F = (const double*)to_device(ctx, 1, df, sizeof(double) * 4 * nelmt * tp, on_device);
+      ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * njg));
+      launch_build_jg_tri<double>(nmodes, nelmt, o->deformed, o->t64.base, J, F, o->jg64, o->df64, ctx->stream);
       ctx->launches++;
+      if (precision == ITHACA_GPU_FP32) {
+        ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
+        ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * njg));
+        launch_build_jg_tri<float>(nmodes, nelmt, o->deformed, o->t64.base, J, F, o->jg32, o->df32, ctx->stream);
+        ctx->launches++;
+      }
+    } else {
+      o->nm = dim == 2 ? nmodes * nmodes : nmodes * nmodes * nmodes;
+      o->nq = dim == 2 ? npoints * npoints : npoints * npoints * npoints;
+      BasisTables b = make_basis(nmodes, npoints);
+      upload_tables(o->t64, b);
+      upload_tables(o->t32, b);
+      o->hB = b.B;
+      o->hD = b.D;
+      const size_t njg = (size_t)nelmt * n_jg(dim) * npt, ndf = (size_t)nelmt * dim * dim * npt;
+      const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * npt, on_device);
+      const double* F =
+          (const double*)to_device(ctx, 1, df, sizeof(double) * dim * dim * nelmt * npt, on_device);
+      double* dw = nullptr;
+      ITHACA_CUDA(cudaMalloc(&dw, sizeof(double) * npoints));
+      std::unique_ptr<double, decltype(&cudaFree)> gw(dw, cudaFree);
+      ITHACA_CUDA(cudaMemcpyAsync(dw, b.w.data(), sizeof(double) * npoints, cudaMemcpyHostToDevice, ctx->stream));
+      ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * ndf));
+      launch_build_jg<double>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg64, o->df64, ctx->stream);
+      ctx->launches++;
+      if (precision == ITHACA_GPU_FP32) {
+        ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
+        ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
+        launch_build_jg<float>(dim, npoints, nelmt, o->deformed, dw, J, F, o->jg32, o->df32, ctx->stream);
+        ctx->launches++;
+      }
+      // the stream must finish with dw before it is freed
+      ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -355,10 +462,10 @@ int ithaca_gpu_bwdtrans(ithaca_gpu_op* op, const void* in, void* out, int on_dev
     void* dout = out_buffer(c, 1, out, es * nout, on_device);
     bool ok;
     if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, (const double*)din, (double*)dout,
+      ok = launch_bwdtrans<double>(op->kdim, op->n, op->Q, op->E, op->t64.base, (const double*)din, (double*)dout,
                                    c->stream);
     else
-      ok = launch_bwdtrans<float>(op->dim, op->n, op->Q, op->E, op->t32.base, (const float*)din, (float*)dout,
+      ok = launch_bwdtrans<float>(op->kdim, op->n, op->Q, op->E, op->t32.base, (const float*)din, (float*)dout,
                                   c->stream);
     if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "BwdTrans: (modes, points) combination not built");
     c->launches++;
@@ -377,10 +484,10 @@ int ithaca_gpu_iproduct(ithaca_gpu_op* op, const void* in, void* out, int on_dev
     void* dout = out_buffer(c, 1, out, es * nout, on_device);
     bool ok;
     if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
+      ok = launch_iproduct<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
                                    (const double*)din, (double*)dout, c->stream);
     else
-      ok = launch_iproduct<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+      ok = launch_iproduct<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
                                   (const float*)din, (float*)dout, c->stream);
     if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
     c->launches++;
@@ -401,10 +508,10 @@ int ithaca_gpu_physderiv(ithaca_gpu_op* op, const void* in, void* d0, void* d1, 
                   op->dim == 3 ? out_buffer(c, 3, d2, es * nq, on_device) : nullptr};
     bool ok;
     if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_physderiv<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->df64,
+      ok = launch_physderiv<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->df64,
                                     (const double*)din, (double*)o[0], (double*)o[1], (double*)o[2], c->stream);
     else
-      ok = launch_physderiv<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->df32,
+      ok = launch_physderiv<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->df32,
                                    (const float*)din, (float*)o[0], (float*)o[1], (float*)o[2], c->stream);
     if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "PhysDeriv: (modes, points) combination not built");
     c->launches++;
@@ -428,11 +535,11 @@ int ithaca_gpu_iproduct_deriv(ithaca_gpu_op* op, const void* in0, const void* in
     void* dout = out_buffer(c, 3, out, es * nm, on_device);
     bool ok;
     if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_iproduct_deriv<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
+      ok = launch_iproduct_deriv<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64,
                                          op->df64, (const double*)di[0], (const double*)di[1], (const double*)di[2],
                                          (double*)dout, c->stream);
     else
-      ok = launch_iproduct_deriv<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+      ok = launch_iproduct_deriv<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
                                         op->df32, (const float*)di[0], (const float*)di[1], (const float*)di[2],
                                         (float*)dout, c->stream);
     if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTDerivBase: (modes, points) combination not built");
@@ -452,14 +559,14 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
     void* dout = out_buffer(c, 1, out, es * nm, on_device);
     bool ok;
     if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_helmholtz<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
+      ok = launch_helmholtz<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
                                     (const double*)din, (double*)dout, nullptr, 0, c->stream);
     else if (op->dim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), op->jg32,
                                      (float)lambda, (const float*)din, (float*)dout, nullptr, 0, nullptr, nullptr,
                                      c->derr, c->stream);
     else
-      ok = launch_helmholtz<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
+      ok = launch_helmholtz<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, op->jg32,
                                    (float)lambda, (const float*)din, (float*)dout, nullptr, 0, c->stream);
     if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
     c->launches++;
@@ -521,7 +628,7 @@ int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* tim
       double ms_avg = -1;
       if (v == 0 || (op->dim == 3 && op->deformed)) {
         auto run = [&] {
-          bool ok = v == 0 ? launch_helmholtz<float>(op->dim, op->n, op->Q, op->E, op->deformed, op->t32.base, jg,
+          bool ok = v == 0 ? launch_helmholtz<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, jg,
                                                      1.0f, x, y, nullptr, 0, s)
                            : launch_helm_pencil<float>(op->n, op->Q, op->E, v, op->hB.data(), op->hD.data(), jg,
                                                        1.0f, x, y, nullptr, 0, nullptr, nullptr, c->derr, s);
@@ -556,7 +663,7 @@ int ithaca_gpu_helmholtz_diag(ithaca_gpu_op* op, double lambda, double* out, int
     Ctx* c = op->ctx;
     const size_t nm = (size_t)op->E * op->nm;
     double* dout = (double*)out_buffer(c, 1, out, sizeof(double) * nm, on_device);
-    if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda, dout,
+    if (!launch_helm_diag<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda, dout,
                                   c->stream))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
     c->launches++;

@@ -691,6 +691,10 @@ struct Cg {
   double diag_lambda = NAN;
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int graph64_len = 0, graph32_len = 0;
+  // geometry each graph was captured with: the kernels' parameters hold the pointer, so a
+  // coefficient set later (a new geometry buffer) needs a new capture
+  const void* graph64_geo = nullptr;
+  const void* graph32_geo = nullptr;
   SuccessiveRhs proj;
   ~Cg();
 };
@@ -748,10 +752,10 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
                                      xin, v.yloc, map,
                                      zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else
-      ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+      ok = launch_helmholtz<T>(op->kdim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
                                zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
   } else {
-    ok = launch_helmholtz<T>(op->dim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+    ok = launch_helmholtz<T>(op->kdim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
                              zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
   }
   if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
@@ -826,7 +830,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   *cg->sc_host = init;
   ITHACA_CUDA(cudaMemcpyAsync(cg->sc, cg->sc_host, sizeof(CgScalars), cudaMemcpyHostToDevice, s));
   Op* op = cg->op;
-  const bool persist = op->dim == 2 && cg->own_ok && cg->bar != nullptr && !cg->geo16 &&
+  const bool persist = op->kdim == 2 && cg->own_ok && cg->bar != nullptr && !cg->geo16 &&
                        (cg->persist == 1 || (cg->persist < 0 && cg->N <= kPersistMaxN));
   if (persist) {  // the whole solve in one cooperative launch (cg_persist.cu)
     PersistArgs<T> a{};
@@ -874,12 +878,14 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   ITHACA_CUDA(cudaGetLastError());
   cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
   int& len = sizeof(T) == 8 ? cg->graph64_len : cg->graph32_len;
-  const bool geo_changed = sizeof(T) == 4 && cg->graph32_geo16 != cg->geo16;
+  const void*& geo = sizeof(T) == 8 ? cg->graph64_geo : cg->graph32_geo;
+  const bool geo_changed = (sizeof(T) == 4 && cg->graph32_geo16 != cg->geo16) || geo != (const void*)jg;
   if (!ex || len != chunk || geo_changed) {
     if (ex) cudaGraphExecDestroy(ex);
     ex = nullptr;
     ex = capture_chunk<T>(cg, v, tab, jg, chunk);
     len = chunk;
+    geo = jg;
     if (sizeof(T) == 4) cg->graph32_geo16 = cg->geo16;
   }
   // Bounded host loop: at most max_iter / chunk + 2 graph launches.
@@ -954,7 +960,7 @@ static void ensure_diag(Cg* cg, double lambda) {
   if (cg->diag_lambda == lambda) return;
   Op* op = cg->op;
   cudaStream_t s = op->ctx->stream;
-  if (!launch_helm_diag<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
+  if (!launch_helm_diag<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, geo64(cg), lambda,
                                 cg->v64.yloc, s))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz diagonal: (modes, points) combination not built");
   assemble_dot_kernel<double, false><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc, cg->v64.s,
@@ -1646,7 +1652,7 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
       f = d;
     }
     // wsp = -IProductWRTBase(f) (ContField.cpp:895-900); b = Assemble(wsp)
-    if (!launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, f,
+    if (!launch_iproduct<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, f,
                                  cg->v64.yloc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
     neg_kernel<<<RB, RT, 0, s>>>(nloc, cg->v64.yloc);
@@ -1775,8 +1781,8 @@ void cg_apply_LM(ithaca_gpu_cg* cg, int ncols, const double* X, double* LX, doub
     assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, cg->v64.yloc,
                                                   LX + (size_t)j * cg->N, nullptr, nullptr, nullptr);
     g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, x, loc);
-    if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
-        !launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
+    if (!launch_bwdtrans<double>(op->kdim, op->n, op->Q, op->E, op->t64.base, loc, phys, s) ||
+        !launch_iproduct<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys, loc, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "mass operator: (modes, points) combination not built");
     assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, loc, MX + (size_t)j * cg->N,
                                                   nullptr, nullptr, nullptr);
@@ -1849,6 +1855,8 @@ int ithaca_gpu_cg_set_varcoeff_tensor(ithaca_gpu_cg* cg, const double* K, int on
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     req(op->deformed != 0, "a quadrature-point coefficient needs a deformed (per-point) collection");
+    if (op->shape == ITHACA_GPU_SHAPE_TRI)
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "the coefficient tensor is built for quadrilaterals and hexahedra");
     cudaStream_t s = op->ctx->stream;
     const int dim = op->dim, nk = dim * (dim + 1) / 2;
     const size_t npts = (size_t)op->E * op->nq, njg = (size_t)op->E * n_jg(dim) * op->nq;
@@ -1878,6 +1886,8 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
                       int on_device) {
   return cg_guarded([&] {
     req(cg && x && u_target && J, "null argument");
+    if (cg->op->shape == ITHACA_GPU_SHAPE_TRI)
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "the adjoint misfit is built for quadrilaterals and hexahedra");
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     Ctx* c = op->ctx;
@@ -1896,13 +1906,13 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
     ITHACA_CUDA(cudaMemcpyAsync(cg->v64.q, dx, sizeof(double) * cg->N, cudaMemcpyDeviceToDevice, s));
     launch_zero_head(cg->ndir, cg->v64.q, s);
     g2l_kernel<<<RB, RT, 0, s>>>(cg->nloc, cg->l2g, cg->v64.q, cg->v64.yloc);
-    if (!launch_bwdtrans<double>(op->dim, op->n, op->Q, op->E, op->t64.base, cg->v64.yloc, phys, s))
+    if (!launch_bwdtrans<double>(op->kdim, op->n, op->Q, op->E, op->t64.base, cg->v64.yloc, phys, s))
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "BwdTrans: (modes, points) combination not built");
     launch_misfit(op->E, n_jg(op->dim), op->nq, op->jg64, phys, tgt, cg->partials, cg->dscal + 2, s);
     c->launches += 5;
     if (dJdx) {
       // dJ/dx = Assemble(IProduct(2 (u - t))), zero on Dirichlet dofs
-      if (!launch_iproduct<double>(op->dim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys,
+      if (!launch_iproduct<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, phys,
                                    cg->v64.yloc, s))
         fail(ITHACA_GPU_ERR_UNSUPPORTED, "IProductWRTBase: (modes, points) combination not built");
       double* dg = on_device ? dJdx : cg->v64.q;
@@ -1923,6 +1933,8 @@ int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* 
   return cg_guarded([&] {
     req(cg && x && psi && grad, "null argument");
     if (cg->aniso) fail(ITHACA_GPU_ERR_UNSUPPORTED, "the kappa gradient is for an isotropic coefficient");
+    if (cg->op->shape == ITHACA_GPU_SHAPE_TRI)
+      fail(ITHACA_GPU_ERR_UNSUPPORTED, "the kappa gradient is built for quadrilaterals and hexahedra");
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     Ctx* c = op->ctx;

@@ -129,4 +129,101 @@ template void launch_build_jg<double>(int, int, int, int, const double*, const d
 template void launch_build_jg<float>(int, int, int, int, const double*, const double*, const double*, float*,
                                      float*, cudaStream_t);
 
+// ---- triangles ----
+// Coordinates at the Q0 x Q1 collapsed points -> J and df per point: the collapsed
+// derivatives mapped by d/dxi0 = h1 d/deta0, d/dxi1 = h0 h1 d/deta0 + d/deta1 (the chain
+// rule of StdRegions/StdTriExp.cpp v_PhysDeriv), J = det(dx/dxi), df = its inverse
+// (df[k*2 + j] = dxi_j / dx_k). Flags non-positive Jacobians (inverted triangles).
+__global__ void geom_factors_tri_kernel(int n, int E, const double* __restrict__ tab, const double* __restrict__ X,
+                                        double* __restrict__ jac, double* __restrict__ df, int* bad) {
+  const TriOff o = tri_off(n);
+  const int Q0 = n + 1, Q1 = n, nq = Q0 * Q1;
+  const size_t total = (size_t)E * nq;
+  for (size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (size_t)gridDim.x * blockDim.x) {
+    const int e = (int)(gid / nq), p = (int)(gid % nq);
+    const int j = p / Q0, i = p - j * Q0;
+    double dx[2][2];  // dx[c][a] = dx_c / dxi_a
+    for (int c = 0; c < 2; ++c) {
+      const double* x = X + (size_t)c * total + (size_t)e * nq;
+      double d0 = 0, d1 = 0;
+      for (int a = 0; a < Q0; ++a) d0 += tab[o.D0 + a * Q0 + i] * x[j * Q0 + a];
+      for (int a = 0; a < Q1; ++a) d1 += tab[o.D1 + a * Q1 + j] * x[a * Q0 + i];
+      const double x0 = tab[o.h1 + j] * d0;
+      dx[c][0] = x0;
+      dx[c][1] = d1 + tab[o.h0 + i] * x0;
+    }
+    const double det = dx[0][0] * dx[1][1] - dx[0][1] * dx[1][0];
+    if (!(det > 0.0)) atomicOr(bad, 1);
+    jac[gid] = det;
+    df[0 * total + gid] = dx[1][1] / det;
+    df[1 * total + gid] = -dx[1][0] / det;
+    df[2 * total + gid] = -dx[0][1] / det;
+    df[3 * total + gid] = dx[0][0] / det;
+  }
+}
+
+void launch_geom_factors_tri(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                             int* bad, cudaStream_t s) {
+  const size_t total = (size_t)E * (n + 1) * n;
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
+  geom_factors_tri_kernel<<<blocks, threads, 0, s>>>(n, E, tab, coords, jac, df, bad);
+}
+
+// Deformed triangles: per point Jw = J w0_i w1_j (w1 with its factor 1/2) and Jw m^{ab}
+// with the collapsed metric of HelmholtzTriImpl (MatrixFreeOps/Helmholtz.h:581-605):
+//   a = h1 (df0 + h0 df1), b = h1 (df2 + h0 df3),
+//   m00 = a^2 + b^2, m01 = a df1 + b df3, m11 = df1^2 + df3^2.
+// Regular triangles: per element J and J g^{ab} as for quads.
+template <typename T>
+__global__ void build_jg_tri_kernel(int n, int E, int deformed, const double* __restrict__ tab,
+                                    const double* __restrict__ jac, const double* __restrict__ df,
+                                    T* __restrict__ jg, T* __restrict__ dfo) {
+  const TriOff o = tri_off(n);
+  const int Q0 = n + 1, nq = (n + 1) * n;
+  const int npt = deformed ? nq : 1;
+  const size_t total = (size_t)E * npt;
+  for (size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (size_t)gridDim.x * blockDim.x) {
+    const int e = (int)(gid / npt), p = (int)(gid % npt);
+    double f[4];
+    for (int c = 0; c < 4; ++c) f[c] = df[(size_t)c * total + gid];
+    T* out = jg + (size_t)e * 4 * npt + p;
+    if (deformed) {
+      const int j = p / Q0, i = p - j * Q0;
+      const double h0 = tab[o.h0 + i], h1 = tab[o.h1 + j];
+      const double jw = jac[gid] * tab[o.w0 + i] * tab[o.w1 + j];
+      const double a = h1 * (f[0] + h0 * f[1]);
+      const double b = h1 * (f[2] + h0 * f[3]);
+      out[0] = (T)jw;
+      out[(size_t)npt] = (T)(jw * (a * a + b * b));
+      out[(size_t)2 * npt] = (T)(jw * (a * f[1] + b * f[3]));
+      out[(size_t)3 * npt] = (T)(jw * (f[1] * f[1] + f[3] * f[3]));
+    } else {
+      const double J = jac[gid];
+      out[0] = (T)J;
+      out[1] = (T)(J * (f[0] * f[0] + f[2] * f[2]));
+      out[2] = (T)(J * (f[0] * f[1] + f[2] * f[3]));
+      out[3] = (T)(J * (f[1] * f[1] + f[3] * f[3]));
+    }
+    T* o2 = dfo + (size_t)e * 4 * npt + p;
+    for (int c = 0; c < 4; ++c) o2[(size_t)c * npt] = (T)f[c];
+  }
+}
+
+template <typename T>
+void launch_build_jg_tri(int n, int E, int deformed, const double* tab, const double* jac, const double* df, T* jg,
+                         T* dfo, cudaStream_t s) {
+  const size_t total = (size_t)E * (deformed ? (n + 1) * n : 1);
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
+  build_jg_tri_kernel<T><<<blocks, threads, 0, s>>>(n, E, deformed, tab, jac, df, jg, dfo);
+}
+
+template void launch_build_jg_tri<double>(int, int, int, const double*, const double*, const double*, double*,
+                                          double*, cudaStream_t);
+template void launch_build_jg_tri<float>(int, int, int, const double*, const double*, const double*, float*,
+                                         float*, cudaStream_t);
+
 }  // namespace ithaca

@@ -36,6 +36,46 @@ struct BasisTables {
 BasisTables make_basis(int n, int Q);
 double jacobi(int m, double a, double b, double x);
 
+// Triangle tables (host, FP64), basis.cpp: direction 0 is make_basis(n, n + 1)
+// (ModifiedA on GLL points); direction 1 the Gauss-Radau-Jacobi (alpha 1, beta 0) points
+// z1 and weights w1, D1[l*Q1 + j] = l_l'(z1_j) and the ModifiedB tables B1, DB1 of the
+// nc = n (n + 1) / 2 modes m(p, q) (q fastest), each Q1 = n values long.
+struct TriBasisTables {
+  int n = 0, Q0 = 0, Q1 = 0, nc = 0;
+  BasisTables a;
+  std::vector<double> z1, w1, D1, B1, DB1;
+};
+TriBasisTables make_tri_basis(int n);
+
+// Packed device tables of a triangle expansion (offsets in elements):
+//   B0 [p*Q0 + i]  D0 [k*Q0 + i]  w0 [i]  h0 [i] = (1 + z0_i)/2
+//   B1 [m*Q1 + j]  D1 [l*Q1 + j]  w1 [j] = w1_j / 2 (the collapsed map's factor)
+//   h1 [j] = 2/(1 - z1_j)          DB0 [p*Q0 + i]   DB1 [m*Q1 + j]
+struct TriOff {
+  int B0, D0, w0, h0, B1, D1, w1, h1, DB0, DB1, size;
+};
+inline __host__ __device__ constexpr int tri_nc(int n) { return n * (n + 1) / 2; }
+inline __host__ __device__ constexpr TriOff tri_off(int n) {
+  const int Q0 = n + 1, Q1 = n, nc = n * (n + 1) / 2;
+  TriOff o{};
+  o.B0 = 0;
+  o.D0 = o.B0 + n * Q0;
+  o.w0 = o.D0 + Q0 * Q0;
+  o.h0 = o.w0 + Q0;
+  o.B1 = o.h0 + Q0;
+  o.D1 = o.B1 + nc * Q1;
+  o.w1 = o.D1 + Q1 * Q1;
+  o.h1 = o.w1 + Q1;
+  o.DB0 = o.h1 + Q1;
+  o.DB1 = o.DB0 + n * Q0;
+  o.size = o.DB1 + nc * Q1;
+  return o;
+}
+
+// Kernel family passed where the launchers below take `dim`: 2 (quads), 3 (hexes) or
+// kTriKernels (triangles; their geometry has the 2-D layout).
+constexpr int kTriKernels = 23;
+
 // Device copy of the 1-D tables for one (n, Q), packed for the kernels:
 //   B  [p*Q + i]   Bt  [i*n + p]   DB [p*Q + i]   DBt [i*n + p]
 //   D  [k*Q + i] = l_k'(z_i)        Dt  [i*Q + k] = D[k*Q + i]       w [i]
@@ -103,6 +143,7 @@ struct Op {
   std::atomic<int> refs{1};
   Ctx* ctx = nullptr;
   int shape = 0, dim = 0, n = 0, Q = 0, E = 0;
+  int kdim = 0;  // kernel family for the launchers: dim, or kTriKernels for triangles
   int deformed = 1, precision = ITHACA_GPU_FP64;
   int nm = 0, nq = 0;  // modes / points per element
   DevTables<double> t64;
@@ -179,11 +220,29 @@ struct ElemApi {
                    const T* in1, const T* in2, T* out, cudaStream_t s);
 };
 
+// Triangles (elem_tri.cuh): the same entry points; Q is the direction-0 point count n + 1.
+template <typename T>
+struct TriApi {
+  static bool helm(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, const T* in, T* out,
+                   const int* l2g, int ndir, const int* skip, const T* lam_ptr, const int* esolve, int skip_stride,
+                   cudaStream_t s);
+  static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
+  static bool ipr(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
+  static bool deriv(int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in, T* d0, T* d1,
+                    cudaStream_t s);
+  static bool diag(int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+  static bool iprd(int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df, const T* in0,
+                   const T* in1, T* out, cudaStream_t s);
+};
+
 template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
                              const int* skip = nullptr, const T* lam_ptr = nullptr, const int* esolve = nullptr,
                              int skip_stride = 0, int variant = -1) {
+  if (dim == kTriKernels)
+    return TriApi<T>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve,
+                           skip_stride, s);
   return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
                                         esolve, skip_stride, s, variant)
                   : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
@@ -191,29 +250,34 @@ inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T
 }
 template <typename T>
 inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
+  if (dim == kTriKernels) return TriApi<T>::bwd(n, Q, E, tab, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::bwd(n, Q, E, tab, in, out, s) : ElemApi<T, 3>::bwd(n, Q, E, tab, in, out, s);
 }
 template <typename T>
 inline bool launch_iproduct(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in,
                             T* out, cudaStream_t s) {
+  if (dim == kTriKernels) return TriApi<T>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::ipr(n, Q, E, deformed, tab, jg, in, out, s)
                   : ElemApi<T, 3>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
 }
 template <typename T>
 inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in,
                              T* d0, T* d1, T* d2, cudaStream_t s) {
+  if (dim == kTriKernels) return TriApi<T>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, s);
   return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
                   : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
 }
 template <typename T>
 inline bool launch_iproduct_deriv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df,
                                   const T* in0, const T* in1, const T* in2, T* out, cudaStream_t s) {
+  if (dim == kTriKernels) return TriApi<T>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, out, s);
   return dim == 2 ? ElemApi<T, 2>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s)
                   : ElemApi<T, 3>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s);
 }
 template <typename T>
 inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              T* out, cudaStream_t s) {
+  if (dim == kTriKernels) return TriApi<T>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
   return dim == 2 ? ElemApi<T, 2>::diag(n, Q, E, deformed, tab, jg, lambda, out, s)
                   : ElemApi<T, 3>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
 }
@@ -224,5 +288,14 @@ void launch_geom_factors(int dim, int Q, int E, const double* D, const double* c
 template <typename T>
 void launch_build_jg(int dim, int Q, int E, int deformed, const double* w, const double* jac, const double* df,
                      T* jg, T* dfo, cudaStream_t s);
+// Triangles: tab = the FP64 packed tables (w0, w1, h0, h1 are read). Deformed elements get
+// per point J w and J w m^{ab} with the collapsed metric of MatrixFreeOps/Helmholtz.h:
+// 581-618 folded in; regular ones per element J and J g^{ab} (the kernels add the point
+// factors).
+template <typename T>
+void launch_build_jg_tri(int n, int E, int deformed, const double* tab, const double* jac, const double* df, T* jg,
+                         T* dfo, cudaStream_t s);
+void launch_geom_factors_tri(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                             int* bad, cudaStream_t s);
 
 }  // namespace ithaca

@@ -424,7 +424,7 @@ static void sc_build(Sc* c, double lambda) {
     const size_t nloc = (size_t)Ec * nm;
     for (int j = 0; j < nm; ++j) {
       unit_kernel<<<blocks_for(nloc), BT, 0, s>>>(nloc, nm, j, u);
-      if (!launch_helmholtz<double>(op->dim, op->n, op->Q, Ec, op->deformed, op->t64.base,
+      if (!launch_helmholtz<double>(op->kdim, op->n, op->Q, Ec, op->deformed, op->t64.base,
                                     op->jg64 + (size_t)e0 * per_elem_jg, lambda, u, col, nullptr, 0, s))
         fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
       column_kernel<<<blocks_for(nloc), BT, 0, s>>>(nloc, nm, j, col, A);
@@ -575,7 +575,16 @@ int ithaca_gpu_sc_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     sreq(nglobal > 0 && ndir >= 0 && ndir <= nglobal, "bad nglobal / ndir");
     const int dim = op->dim, n = op->n, nm = op->nm, E = op->E;
     std::vector<int> bm, im;
-    for (int m = 0; m < nm; ++m) {
+    for (int m = 0, tp = 0, tq = 0; m < nm; ++m) {
+      if (op->shape == ITHACA_GPU_SHAPE_TRI) {
+        // triangle mode m(tp, tq): vertices and edges are the rows tp <= 1 and the modes tq == 0
+        (tp <= 1 || tq == 0 ? bm : im).push_back(m);
+        if (++tq == n - tp) {
+          tq = 0;
+          ++tp;
+        }
+        continue;
+      }
       const int p = m % n, q = (m / n) % n, r = dim == 3 ? m / (n * n) : n;
       (p < 2 || q < 2 || (dim == 3 && r < 2) ? bm : im).push_back(m);
     }

@@ -9,6 +9,12 @@ so this module generates them directly:
   (their local vertex order cyclically shifted) to exercise edge-orientation signs.
   Element e = j*nx + i has vertices v0..v3 counter-clockwise (QuadGeom convention)
   and the bilinear map of SpatialDomains/QuadGeom.cpp:261-330.
+* ``TriMesh``   -- the cells of a (jittered) ``QuadMesh`` split into two triangles each
+  along the diagonal from (i+1, j) to (i, j+1); optionally curved by
+  (x, y) + amp sin(pi x) sin(pi y) (1, -1/2), which fixes the square's boundary.
+  Triangle vertices v0, v1, v2 run counter-clockwise with the affine map
+  x = v0 + (v1 - v0)(1 + xi0)/2 + (v2 - v0)(1 + xi1)/2 of SpatialDomains/TriGeom.cpp;
+  ``rotate`` shifts a triangle's local vertex order cyclically.
 * ``HexMesh``   -- nx x ny x nz hexahedra of the unit cube, optionally curved by
   x_a + amp * sin(2 pi x_b) sin(2 pi x_c) applied cyclically (a, b, c) =
   (0, 1, 2), (1, 2, 0), (2, 0, 1) to the straight positions.
@@ -39,6 +45,52 @@ def gll_points(Q):
             break
     z[1:-1] = zi
     return z
+
+
+def radau_points(Q):
+    """Gauss-Radau-Jacobi points (alpha 1, beta 0, z_0 = -1): -1 and the zeros of
+    P_{Q-1}^{(1,1)}, by Newton with deflation (same values as the library's tables)."""
+    def jac11(m, x):
+        p0, p1 = np.ones_like(x), 2.0 * x
+        if m == 0:
+            return p0
+        for k in range(2, m + 1):
+            a1 = 2.0 * k * (k + 2.0) * (2.0 * k)
+            a3 = (2.0 * k) * (2.0 * k + 1.0) * (2.0 * k + 2.0)
+            a4 = 2.0 * k * k * (2.0 * k + 2.0)
+            p0, p1 = p1, (a3 / a1 * x * p1 - a4 / a1 * p0)
+        return p1
+    m = Q - 1
+    roots = []
+    for k in range(m):
+        r = -np.cos((2.0 * k + 1.0) * np.pi / (2.0 * m))
+        if k > 0:
+            r = 0.5 * (r + roots[-1])
+        for _ in range(200):
+            p = jac11(m, np.array(r))
+            dp = 0.5 * (m + 3.0) * _jacobi_ab(m - 1, 2.0, 2.0, r)
+            step = float(p / (dp - p * sum(1.0 / (r - x) for x in roots)))
+            r -= step
+            if abs(step) < 1e-16:
+                break
+        roots.append(r)
+    return np.concatenate([[-1.0], roots])
+
+
+def _jacobi_ab(m, a, b, x):
+    x = np.asarray(x, dtype=np.float64)
+    p0 = np.ones_like(x)
+    if m == 0:
+        return p0
+    p1 = 0.5 * (a - b + (a + b + 2.0) * x)
+    for k in range(2, m + 1):
+        apb = a + b
+        a1 = 2.0 * k * (k + apb) * (2.0 * k + apb - 2.0)
+        a2 = (2.0 * k + apb - 1.0) * (a * a - b * b)
+        a3 = (2.0 * k + apb - 2.0) * (2.0 * k + apb - 1.0) * (2.0 * k + apb)
+        a4 = 2.0 * (k + a - 1.0) * (k + b - 1.0) * (2.0 * k + apb)
+        p0, p1 = p1, ((a2 / a1 + a3 / a1 * x) * p1 - a4 / a1 * p0)
+    return p1
 
 
 class AssemblyMap:
@@ -160,6 +212,90 @@ class QuadMesh:
             base = nv + ne * ni + np.arange(E)[:, None, None] * ni * ni
             qq, pp = np.meshgrid(np.arange(ni), np.arange(ni), indexing="ij")
             l2g[:, 2:, 2:] = base + (qq * ni + pp)[None]
+        l2g = newid[l2g]
+        return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
+
+
+class TriMesh:
+    def __init__(self, nx, ny, jitter=0.0, seed=0, rotate=None, curve_amp=0.0):
+        q = QuadMesh(nx, ny, jitter=jitter, seed=seed)
+        self.nx, self.ny = nx, ny
+        self.V = q.V
+        self.E = 2 * nx * ny
+        self.curve_amp = curve_amp
+        c = q.EV  # cell corners c0..c3 counter-clockwise
+        # (c0, c1, c3) and (c2, c3, c1): both counter-clockwise, sharing the diagonal c1-c3
+        tris = np.empty((self.E, 3), dtype=np.int64)
+        tris[0::2] = c[:, [0, 1, 3]]
+        tris[1::2] = c[:, [2, 3, 1]]
+        self.rot = np.zeros(self.E, dtype=np.int64) if rotate is None else np.asarray(rotate, dtype=np.int64) % 3
+        k = (np.arange(3)[None, :] + self.rot[:, None]) % 3
+        self.EV = np.take_along_axis(tris, k, axis=1)
+
+    def _map(self, x, y):
+        if self.curve_amp == 0.0:
+            return x, y
+        b = self.curve_amp * np.sin(np.pi * x) * np.sin(np.pi * y)
+        return x + b, y - 0.5 * b
+
+    def coords(self, n):
+        """Coordinates at the (n + 1) x n collapsed points (GLL x Gauss-Radau), shape
+        (2, E, n (n + 1)), point j*(n + 1) + i."""
+        z0, z1 = gll_points(n + 1), radau_points(n)
+        e0, e1 = np.meshgrid(z0, z1, indexing="xy")   # [j, i]
+        xi0 = 0.5 * (1.0 + e0) * (1.0 - e1) - 1.0
+        xi1 = e1
+        W = np.stack([-0.5 * (xi0 + xi1), 0.5 * (1.0 + xi0), 0.5 * (1.0 + xi1)])  # [v, j, i]
+        X = np.einsum("vji,evc->ceji", W, self.V[self.EV]).reshape(2, self.E, -1)
+        x, y = self._map(X[0], X[1])
+        return np.stack([x, y]).copy()
+
+    def assembly(self, n):
+        """C0 numbering for the triangle expansion with n modes per direction; all boundary
+        dofs Dirichlet. Local modes m(p, q) (q fastest): vertices m(0,0) = v0, m(1,0) = v1,
+        m(0,1) = v2 (the collapsed top vertex); edge 0 (v0 -> v1) the modes (p >= 2, 0) of
+        degree p, edge 1 (v1 -> v2) the modes (1, q >= 1) of degree q + 1, edge 2
+        (v0 -> v2) the modes (0, q >= 2) of degree q; the rest interior. An edge mode of
+        degree k flips sign, (-1)^k, where the local edge runs from the higher global
+        vertex id to the lower (StdTriExp edge maps with AssemblyMapCG orientation signs)."""
+        E, EV = self.E, self.EV
+        nv = self.V.shape[0]
+        ni = max(n - 2, 0)
+        nint = max((n - 2) * (n - 3) // 2, 0)
+        le = np.stack([EV[:, [0, 1]], EV[:, [1, 2]], EV[:, [0, 2]]], axis=1)  # [e, edge, (start, end)]
+        key = np.sort(le, axis=2).reshape(-1, 2)
+        uniq, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+        inv = inv.reshape(E, 3)
+        ne = uniq.shape[0]
+        ebnd = cnt == 1
+        vbnd = np.zeros(nv, dtype=bool)
+        vbnd[uniq[ebnd].ravel()] = True
+        nglob = nv + ne * ni + E * nint
+        is_dir = np.zeros(nglob, dtype=bool)
+        is_dir[:nv] = vbnd
+        is_dir[nv:nv + ne * ni] = np.repeat(ebnd, ni)
+        newid, ndir = _renumber_dirichlet_first(np.arange(nglob), is_dir)
+        nc = n * (n + 1) // 2
+        rows = [(p, q) for p in range(n) for q in range(n - p)]
+        l2g = np.zeros((E, nc), dtype=np.int64)
+        sgn = np.ones((E, nc))
+        forward = le[:, :, 0] < le[:, :, 1]
+        icount = 0
+        for m, (p, q) in enumerate(rows):
+            if (p, q) == (0, 0):
+                l2g[:, m] = EV[:, 0]
+            elif (p, q) == (1, 0):
+                l2g[:, m] = EV[:, 1]
+            elif (p, q) == (0, 1):
+                l2g[:, m] = EV[:, 2]
+            elif q == 0 or p <= 1:
+                ed, k = (0, p) if q == 0 else ((1, q + 1) if p == 1 else (2, q))
+                l2g[:, m] = nv + inv[:, ed] * ni + (k - 2)
+                if k % 2 == 1:
+                    sgn[:, m] = np.where(forward[:, ed], 1.0, -1.0)
+            else:
+                l2g[:, m] = nv + ne * ni + np.arange(E) * nint + icount
+                icount += 1
         l2g = newid[l2g]
         return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
 

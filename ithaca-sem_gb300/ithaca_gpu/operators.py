@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _capi as C
 
-SHAPES = {"quad": C.SHAPE_QUAD, "hex": C.SHAPE_HEX}
+SHAPES = {"tri": C.SHAPE_TRI, "quad": C.SHAPE_QUAD, "hex": C.SHAPE_HEX}
 PRECISIONS = {"fp64": C.FP64, "fp32": C.FP32}
 SOLVE_MODES = {"fp64": C.SOLVE_FP64, "mixed": C.SOLVE_MIXED_FP32, "mixed_geo16": C.SOLVE_MIXED_FP32_GEO16}
 
@@ -109,14 +109,32 @@ def basis_modA(nmodes, npoints):
     return z, w, D, B, DB
 
 
+def basis_tri(nmodes):
+    """Triangle tables computed by the library: (z0, w0, D0, B0, DB0) of ModifiedA on
+    nmodes + 1 GLL points and (z1, w1, D1, B1, DB1) of ModifiedB on nmodes Gauss-Radau points."""
+    Q0, Q1, nc = nmodes + 1, nmodes, nmodes * (nmodes + 1) // 2
+    a = [np.zeros(Q0), np.zeros(Q0), np.zeros(Q0 * Q0), np.zeros(nmodes * Q0), np.zeros(nmodes * Q0)]
+    b = [np.zeros(Q1), np.zeros(Q1), np.zeros(Q1 * Q1), np.zeros(nc * Q1), np.zeros(nc * Q1)]
+    C.call("ithaca_gpu_basis_tri", nmodes, *[ctypes.c_void_p(x.ctypes.data) for x in a + b])
+    return tuple(a), tuple(b)
+
+
+def _npts(shape, npoints):
+    """Quadrature points per element (triangles: npoints x (npoints - 1) collapsed points)."""
+    if shape == "tri":
+        return npoints * (npoints - 1)
+    return npoints ** (2 if shape == "quad" else 3)
+
+
 def geom_factors(ctx, shape, npoints, coords):
-    """coords (d, E, Q^d) -> (jac (E*Q^d,), df (d*d, E*Q^d)) computed on the GPU.
+    """coords (d, E, nq) -> (jac (E*nq,), df (d*d, E*nq)) computed on the GPU, nq = Q^d
+    (triangles: Q (Q - 1) collapsed points, Q the direction-0 count).
     Host numpy in -> host numpy out; CUDA tensor in -> CUDA tensors out."""
-    dim = 2 if shape == "quad" else 3
+    dim = 3 if shape == "hex" else 2
     if _is_device(coords):
         import torch
         E = coords.shape[1]
-        nq = npoints ** dim
+        nq = _npts(shape, npoints)
         jac = torch.empty(E * nq, dtype=torch.float64, device=coords.device)
         df = torch.empty((dim * dim, E * nq), dtype=torch.float64, device=coords.device)
         C.call("ithaca_gpu_geom_factors", ctx.handle, SHAPES[shape], npoints, E, ctypes.c_void_p(coords.data_ptr()),
@@ -124,7 +142,7 @@ def geom_factors(ctx, shape, npoints, coords):
         return jac, df
     coords = np.ascontiguousarray(coords, dtype=np.float64)
     E = coords.shape[1]
-    nq = npoints ** dim
+    nq = _npts(shape, npoints)
     jac = np.zeros(E * nq)
     df = np.zeros((dim * dim, E * nq))
     C.call("ithaca_gpu_geom_factors", ctx.handle, SHAPES[shape], npoints, E, ctypes.c_void_p(coords.ctypes.data),
@@ -138,9 +156,12 @@ class Collection:
     def __init__(self, ctx, shape, nmodes, npoints, nelmt, jac, df, deformed=True, precision="fp64"):
         self.ctx = ctx
         self.shape = shape
-        self.dim = 2 if shape == "quad" else 3
+        self.dim = 3 if shape == "hex" else 2
         self.n, self.Q, self.E = nmodes, npoints, nelmt
-        self.nm, self.nq = nmodes ** self.dim, npoints ** self.dim
+        if shape == "tri":
+            self.nm, self.nq = nmodes * (nmodes + 1) // 2, _npts(shape, npoints)
+        else:
+            self.nm, self.nq = nmodes ** self.dim, npoints ** self.dim
         self.precision = precision
         self.dtype = np.float64 if precision == "fp64" else np.float32
         if not _is_device(jac):

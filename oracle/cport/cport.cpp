@@ -11,6 +11,8 @@
 // core over contiguous element / dof ranges, standing in for the reference's MPI ranks.
 // It exists because the reference tree is not available where the CPU baseline is timed;
 // where it is, oracle/_ref (the reference kernels compiled in place) pins this port.
+// Triangles: cport_tri_helmholtz restates HelmholtzTriImpl (MatrixFreeOps/Helmholtz.h:
+// 505-635) on tables passed in by the caller (the oracle's TriBasis).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -355,9 +357,106 @@ Geo regroup(int dim, int nq, int E, bool def, const double* jac, const double* d
   return g;
 }
 
+
+// ---- triangles: HelmholtzTriImpl (MatrixFreeOps/Helmholtz.h:505-635) with CORRECT ----
+// Tables (caller's, reference storage): B0/DB0 [p*Q0+i], D0 [k*Q0+i], w0, z0; B1/DB1
+// [m*Q1+j] (m(p,q), q fastest), D1 [l*Q1+j], w1 (as GetW(), the factor 1/2 applied here), z1.
+struct TriTab {
+  int n, Q0, Q1, nc;
+  const double *B0, *DB0, *D0, *w0, *z0, *B1, *DB1, *D1, *w1, *z1;
+};
+
+// IProductTriKernel: out[m] (+)= sum_j A1[m][j] w1[j] sum_i A0[p][i] w0[i] J f[j][i], CORRECT term to m = 1.
+static void tri_ipr(const TriTab& t, const double* A0, const double* A1, const double* f, const double* J,
+                    bool def, double scale, bool append, double* out, double* wsp) {
+  const int n = t.n, Q0 = t.Q0, Q1 = t.Q1;
+  for (int m = 0, p = 0; p < n; ++p) {
+    for (int j = 0; j < Q1; ++j) {
+      double s = 0;
+      for (int i = 0; i < Q0; ++i) s += f[j * Q0 + i] * A0[p * Q0 + i] * (def ? J[j * Q0 + i] : J[0]) * t.w0[i];
+      wsp[j] = s;
+    }
+    for (int q = 0; q < n - p; ++q, ++m) {
+      double s = 0;
+      for (int j = 0; j < Q1; ++j) s += wsp[j] * A1[m * Q1 + j] * 0.5 * t.w1[j];
+      out[m] = append ? out[m] + scale * s : scale * s;
+    }
+  }
+  double c = 0;
+  for (int j = 0; j < Q1; ++j)
+    for (int i = 0; i < Q0; ++i)
+      c += f[j * Q0 + i] * 0.5 * t.w1[j] * A1[Q1 + j] * t.w0[i] * (def ? J[j * Q0 + i] : J[0]) * A0[Q0 + i];
+  out[1] += scale * c;
+}
+
+static void tri_helm_elem(const TriTab& t, const double* J, const double* df, bool def, double lambda,
+                          const double* in, double* out, std::vector<double>& ws) {
+  const int n = t.n, Q0 = t.Q0, Q1 = t.Q1, nq = Q0 * Q1;
+  double* u = ws.data();
+  double* d0 = u + nq;
+  double* d1 = d0 + nq;
+  double* ps = d1 + nq;  // n * Q1, also IProduct scratch
+  // BwdTransTriKernel
+  for (int j = 0; j < Q1; ++j) {
+    for (int p = 0, m = 0; p < n; ++p) {
+      double s = 0;
+      for (int q = 0; q < n - p; ++q, ++m) s += t.B1[m * Q1 + j] * in[m];
+      ps[p] = s;
+    }
+    for (int i = 0; i < Q0; ++i) {
+      double s = 0;
+      for (int p = 0; p < n; ++p) s += ps[p] * t.B0[p * Q0 + i];
+      s += in[1] * t.B0[Q0 + i] * t.B1[Q1 + j];
+      u[j * Q0 + i] = s;
+    }
+  }
+  tri_ipr(t, t.B0, t.B1, u, J, def, lambda, false, out, ps);
+  // PhysDerivTensor2DKernel + the collapsed metric
+  for (int j = 0; j < Q1; ++j)
+    for (int i = 0; i < Q0; ++i) {
+      double a = 0, b = 0;
+      for (int k = 0; k < Q0; ++k) a += t.D0[k * Q0 + i] * u[j * Q0 + k];
+      for (int k = 0; k < Q1; ++k) b += t.D1[k * Q1 + j] * u[k * Q0 + i];
+      d0[j * Q0 + i] = a;
+      d1[j * Q0 + i] = b;
+    }
+  for (int j = 0, c = 0; j < Q1; ++j) {
+    const double h1 = 2.0 / (1.0 - t.z1[j]);
+    for (int i = 0; i < Q0; ++i, ++c) {
+      const double* f = def ? df + (size_t)c * 4 : df;
+      const double h0 = 0.5 * (1.0 + t.z0[i]);
+      const double a = h1 * (f[0] + h0 * f[1]), b = h1 * (f[2] + h0 * f[3]);
+      const double m00 = a * a + b * b, m01 = a * f[1] + b * f[3], m11 = f[1] * f[1] + f[3] * f[3];
+      const double x = d0[c], y = d1[c];
+      u[c] = m00 * x + m01 * y;
+      d0[c] = m01 * x + m11 * y;
+    }
+  }
+  tri_ipr(t, t.DB0, t.B1, u, J, def, 1.0, true, out, ps);
+  tri_ipr(t, t.B0, t.DB1, d0, J, def, 1.0, true, out, ps);
+}
 }  // namespace
 
 extern "C" {
+
+// Triangle Helmholtz apply (E elements, n modes, Q0 = n + 1, Q1 = n); geometry in the
+// reference layouts jac[e*nq + q] / df[dir][e*nq + q] (deformed) or per element.
+int cport_tri_helmholtz(int n, int E, const double* B0, const double* DB0, const double* D0, const double* w0,
+                        const double* z0, const double* B1, const double* DB1, const double* D1, const double* w1,
+                        const double* z1, const double* jac, const double* df, int deformed, double lambda,
+                        const double* in, double* out, int nthreads) {
+  if (n < 2) return 1;
+  TriTab t{n, n + 1, n, n * (n + 1) / 2, B0, DB0, D0, w0, z0, B1, DB1, D1, w1, z1};
+  const int nq = t.Q0 * t.Q1, npt = deformed ? nq : 1;
+  Geo g = regroup(2, nq, E, deformed != 0, jac, df);
+  parallel(E, nthreads, [&](long long a, long long b, int) {
+    std::vector<double> ws(3 * nq + n * t.Q1 + t.Q1);
+    for (long long e = a; e < b; ++e)
+      tri_helm_elem(t, &g.jac[e * npt], &g.df[e * npt * 4], deformed != 0, lambda, in + e * t.nc, out + e * t.nc,
+                    ws);
+  });
+  return 0;
+}
 
 int cport_helmholtz(int dim, int n, int Q, int E, const double* jac, const double* df, int deformed, double lambda,
                     const double* in, double* out, int nthreads) {

@@ -86,3 +86,16 @@ def cg_solve(dim, n, Q, E, jac, df, deformed, lam, l2g, sign, nglobal, ndir, din
                               nglobal, ndir, dp, rp, x.ctypes.data_as(_dp), ctypes.c_double(tol), max_iter, nthreads,
                               ctypes.byref(eps))
     return x, it, eps.value
+
+
+def tri_helmholtz(tb, E, jac, df, deformed, lam, coeffs, nthreads=1, out=None):
+    """Triangle Helmholtz apply through the compiled port; tb: oracle.tri.TriBasis."""
+    out = np.zeros(E * tb.nc) if out is None else out
+    held = [_d(a) for a in (tb.B0, tb.DB0, tb.D0, tb.w0, tb.z0, tb.B1, tb.DB1, tb.D1, tb.w1, tb.z1,
+                            jac, df, coeffs)]
+    ptr = [p for _, p in held]
+    rc = lib().cport_tri_helmholtz(int(tb.n), E, *ptr[:10], ptr[10], ptr[11], int(deformed), ctypes.c_double(lam),
+                                   ptr[12], out.ctypes.data_as(_dp), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"cport_tri_helmholtz returned {rc}")
+    return out

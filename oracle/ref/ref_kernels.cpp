@@ -280,6 +280,243 @@ void deriv_op(int dim, const Tables& t, const Geo& g, const double* in, double* 
   }
 }
 
+// ---- triangles: eModified_A on Q0 = n + 1 GLL points in direction 0, eModified_B on
+//      Q1 = n Gauss-Radau-Jacobi (alpha 1, beta 0) points in direction 1, the default
+//      keys of SpatialDomains/MeshGraph.cpp:1665-1681 ----
+// GaussPoints::CalculatePoints / CalculateDerivMatrix for eGaussRadauMAlpha1Beta0
+// (LibUtilities/Foundations/GaussPoints.cpp:119-121, 206-208, 235).
+void radau_tables(int Q, double* z, double* w, double* D) {
+  Polylib::zwgrjm(z, w, Q, 1.0, 0.0);
+  Polylib::Dgrjm(D, z, Q, 1.0, 0.0);
+}
+
+// Basis::GenBasis eModified_B (LibUtilities/Foundations/Basis.cpp:423-507): the
+// triangular mode index m(p, q), q fastest, 0 <= p < n, 0 <= q < n - p.
+void modB_tables(int n, int Q, const double* z, const double* D, double* B, double* DB) {
+  for (int i = 0; i < Q; ++i) {
+    B[i] = 0.5 * (1 - z[i]);
+    B[Q + i] = 0.5 * (1 + z[i]);
+  }
+  double* mode = B + 2 * Q;
+  for (int q = 2; q < n; ++q, mode += Q) {  // p = 0, q >= 2
+    Polylib::jacobfd(Q, z, mode, nullptr, q - 2, 1.0, 1.0);
+    for (int i = 0; i < Q; ++i) mode[i] *= B[i] * B[Q + i];
+  }
+  for (int i = 0; i < Q; ++i) mode[i] = 0.5 * (1 - z[i]);  // p = 1, q = 0
+  mode += Q;
+  for (int q = 2; q < n; ++q, mode += Q) {  // p = 1, q >= 1
+    Polylib::jacobfd(Q, z, mode, nullptr, q - 2, 1.0, 1.0);
+    for (int i = 0; i < Q; ++i) mode[i] *= B[i] * B[Q + i];
+  }
+  const double* one_m_z_pow = B;
+  const double* one_p_z = B + Q;
+  for (int p = 2; p < n; ++p) {
+    for (int i = 0; i < Q; ++i) mode[i] = B[i] * one_m_z_pow[i];
+    one_m_z_pow = mode;
+    mode += Q;
+    for (int q = 1; q < n - p; ++q, mode += Q) {
+      Polylib::jacobfd(Q, z, mode, nullptr, q - 1, 2 * p - 1, 1.0);
+      for (int i = 0; i < Q; ++i) mode[i] *= one_m_z_pow[i] * one_p_z[i];
+    }
+  }
+  const int nc = n * (n + 1) / 2;
+  for (int m = 0; m < nc; ++m)
+    for (int i = 0; i < Q; ++i) {
+      double s = 0;
+      for (int k = 0; k < Q; ++k) s += D[k * Q + i] * B[m * Q + k];
+      DB[m * Q + i] = s;
+    }
+}
+
+struct TriTables {
+  vvec b0, db0, D0, w0, z0, b1, db1, D1, w1, z1;
+};
+
+// The tables the MatrixFree Helper holds (MatrixFreeOps/Operator.hpp:206-275): the
+// Gauss-Radau weights carry the factor 0.5 of the collapsed map (:245-248).
+TriTables make_tri_tables(int n) {
+  const int Q0 = n + 1, Q1 = n, nc = n * (n + 1) / 2;
+  std::vector<double> z0(Q0), w0(Q0), D0(Q0 * Q0), B0(n * Q0), DB0(n * Q0);
+  std::vector<double> z1(Q1), w1(Q1), D1(Q1 * Q1), B1(nc * Q1), DB1(nc * Q1);
+  gll_tables(Q0, z0.data(), w0.data(), D0.data());
+  modA_tables(n, Q0, z0.data(), D0.data(), B0.data(), DB0.data());
+  radau_tables(Q1, z1.data(), w1.data(), D1.data());
+  modB_tables(n, Q1, z1.data(), D1.data(), B1.data(), DB1.data());
+  TriTables t;
+  t.b0.assign(B0.begin(), B0.end());
+  t.db0.assign(DB0.begin(), DB0.end());
+  t.D0.assign(D0.begin(), D0.end());
+  t.w0.assign(w0.begin(), w0.end());
+  t.z0.assign(z0.begin(), z0.end());
+  t.b1.assign(B1.begin(), B1.end());
+  t.db1.assign(DB1.begin(), DB1.end());
+  t.D1.assign(D1.begin(), D1.end());
+  for (double& v : w1) v *= 0.5;
+  t.w1.assign(w1.begin(), w1.end());
+  t.z1.assign(z1.begin(), z1.end());
+  return t;
+}
+
+// BwdTrans / IProduct / PhysDeriv for triangles (MatrixFreeOps/BwdTrans.h:540-570,
+// IProduct.h:560-590, PhysDeriv.h:470-500), CORRECT = true (eModified_A).
+template <int N>
+void tri_bwd(const TriTables& t, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) / 2, nq = (N + 1) * N;
+  vvec tin(nc), tout(nq);
+  vec_t wsp[N];
+  for (int e = b0; e < b1; ++e) {
+    load_interleave(in + (size_t)e * nc * W, nc, tin);
+    BwdTransTriKernel<N, N, N + 1, N, true>(tin, t.b0, t.b1, wsp, tout);
+    deinterleave_store(tout, nq, out + (size_t)e * nq * W);
+  }
+}
+
+template <int N, bool DEF>
+void tri_iprod(const TriTables& t, const Geo& g, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) / 2, nq = (N + 1) * N;
+  vvec tin(nq), tout(nc);
+  vec_t wsp[N];
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    IProductTriKernel<N, N, N + 1, N, true, false, false, DEF>(tin, t.b0, t.b1, t.w0, t.w1, jac_ptr, wsp, tout);
+    deinterleave_store(tout, nc, out + (size_t)e * nc * W);
+  }
+}
+
+template <int N, bool DEF>
+void tri_deriv(const TriTables& t, const Geo& g, const double* in, double* o0, double* o1, int b0, int b1) {
+  constexpr int nq = (N + 1) * N, ndf = 4;
+  vvec tin(nq), a(nq), b(nq);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nq : ndf)];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    PhysDerivTriKernel<N + 1, N, DEF>(tin, t.z0, t.z1, t.D0, t.D1, df_ptr, a, b);
+    deinterleave_store(a, nq, o0 + (size_t)e * nq * W);
+    deinterleave_store(b, nq, o1 + (size_t)e * nq * W);
+  }
+}
+
+// ---- Helmholtz: HelmholtzTriImpl (MatrixFreeOps/Helmholtz.h:290-330, 505-635) ----
+template <int N, bool DEF>
+void helm_tri(const TriTables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N, nc = N * (N + 1) / 2, nqTot = NQ0 * NQ1, ndf = 4;
+  std::vector<double> h0(NQ0), h1(NQ1);
+  for (int i = 0; i < NQ0; ++i) h0[i] = 0.5 * (1 + t.z0[i][0]);
+  for (int j = 0; j < NQ1; ++j) h1[j] = 2.0 / (1 - t.z1[j][0]);
+  vec_t wsp[NQ1 > N ? NQ1 : N];
+  vvec tmpIn(nc), tmpOut(nc), bwd(nqTot), deriv0(nqTot), deriv1(nqTot);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in + (size_t)e * nc * W, nc, tmpIn);
+    vec_t df0, df1, df2, df3, metric00, metric01, metric11;
+    if (!DEF) {
+      df0 = df_ptr[0];
+      df1 = df_ptr[1];
+      df2 = df_ptr[2];
+      df3 = df_ptr[3];
+    }
+    BwdTransTriKernel<N, N, NQ0, NQ1, true>(tmpIn, t.b0, t.b1, wsp, bwd);
+    IProductTriKernel<N, N, NQ0, NQ1, true, true, false, DEF>(bwd, t.b0, t.b1, t.w0, t.w1, jac_ptr, wsp, tmpOut,
+                                                              lambda);
+    PhysDerivTensor2DKernel<NQ0, NQ1>(bwd, t.D0, t.D1, deriv0, deriv1);
+    for (int j = 0, cnt = 0; j < NQ1; ++j) {
+      vec_t h1j = h1[j];
+      for (int i = 0; i < NQ0; ++i, ++cnt) {
+        if (DEF) {
+          df0 = df_ptr[cnt * ndf];
+          df1 = df_ptr[cnt * ndf + 1];
+          df2 = df_ptr[cnt * ndf + 2];
+          df3 = df_ptr[cnt * ndf + 3];
+        }
+        vec_t h0i = h0[i];
+        metric00 = h1j * (df0 + h0i * df1);
+        metric01 = metric00 * df1;
+        metric00 = metric00 * metric00;
+        vec_t tmp = h1j * (df2 + h0i * df3);
+        metric01.fma(tmp, df3);
+        metric00.fma(tmp, tmp);
+        metric11 = df1 * df1;
+        metric11.fma(df3, df3);
+        vec_t d0 = deriv0[cnt];
+        vec_t d1 = deriv1[cnt];
+        tmp = metric00 * d0;
+        tmp.fma(metric01, d1);
+        bwd[cnt] = tmp;
+        tmp = metric01 * d0;
+        tmp.fma(metric11, d1);
+        deriv0[cnt] = tmp;
+      }
+    }
+    IProductTriKernel<N, N, NQ0, NQ1, true, false, true, DEF>(bwd, t.db0, t.b1, t.w0, t.w1, jac_ptr, wsp, tmpOut);
+    IProductTriKernel<N, N, NQ0, NQ1, true, false, true, DEF>(deriv0, t.b0, t.db1, t.w0, t.w1, jac_ptr, wsp, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
+// ---- IProductWRTDerivBaseTriImpl (MatrixFreeOps/IProductWRTDerivBase.h:671-1060), 2-D input ----
+template <int N, bool DEF>
+void iprd_tri(const TriTables& t, const Geo& g, const double* in0, const double* in1, double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N, nc = N * (N + 1) / 2, nqTot = NQ0 * NQ1, ndf = 4;
+  vec_t sums_j[NQ1];
+  vvec tmpIn0(nqTot), tmpIn1(nqTot), tmp0(nqTot), tmp1(nqTot), tmpOut(nc);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in0 + (size_t)e * nqTot * W, nqTot, tmpIn0);
+    load_interleave(in1 + (size_t)e * nqTot * W, nqTot, tmpIn1);
+    vec_t df0, df1, df2, df3;
+    if (!DEF) {
+      df0 = df_ptr[0];
+      df1 = df_ptr[1];
+      df2 = df_ptr[2];
+      df3 = df_ptr[3];
+    }
+    for (int j = 0, cnt = 0; j < NQ1; ++j) {
+      vec_t f0 = 2.0 / (1.0 - t.z1[j]);
+      for (int i = 0; i < NQ0; ++i, ++cnt) {
+        if (DEF) {
+          df0 = df_ptr[cnt * ndf];
+          df1 = df_ptr[cnt * ndf + 1];
+          df2 = df_ptr[cnt * ndf + 2];
+          df3 = df_ptr[cnt * ndf + 3];
+        }
+        vec_t tI0 = tmpIn0[cnt], tI1 = tmpIn1[cnt];
+        vec_t t0 = df0 * tI0 + df2 * tI1;
+        vec_t t1 = df1 * tI0 + df3 * tI1;
+        vec_t hf1 = 0.5 * (1.0 + t.z0[i]);
+        t0 *= f0;
+        vec_t c1 = hf1 * t1;
+        t0.fma(c1, f0);
+        tmp0[cnt] = t0;
+        tmp1[cnt] = t1;
+      }
+    }
+    IProductTriKernel<N, N, NQ0, NQ1, true, false, false, DEF>(tmp0, t.db0, t.b1, t.w0, t.w1, jac_ptr, sums_j,
+                                                               tmpOut);
+    IProductTriKernel<N, N, NQ0, NQ1, true, false, true, DEF>(tmp1, t.b0, t.db1, t.w0, t.w1, jac_ptr, sums_j,
+                                                              tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
+// Runs CALL(N) for N in 2..10 (triangles: Q0 = N + 1, Q1 = N).
+#define TRI_DISPATCH(n, CALL)   \
+  switch (n) {                  \
+    case 2: CALL(2); return 0;  \
+    case 3: CALL(3); return 0;  \
+    case 4: CALL(4); return 0;  \
+    case 5: CALL(5); return 0;  \
+    case 6: CALL(6); return 0;  \
+    case 7: CALL(7); return 0;  \
+    case 8: CALL(8); return 0;  \
+    case 9: CALL(9); return 0;  \
+    case 10: CALL(10); return 0; \
+    default: break;             \
+  }                             \
+  return 1;
+
 // Runs fn<N, Q=N+1>(args...) for N in 2..10 (P = 1..9, Q = P + 2).
 #define ORACLE_DISPATCH(n, Q, CALL)                                    \
   switch (n) {                                                         \
@@ -465,6 +702,94 @@ int ref_cg_solve(int dim, int n, int Q, int E, const double* jac, const double* 
   }
   if (final_eps) *final_eps = eps;
   return iters;
+}
+
+// ---- triangles ----
+// Tables as the reference's Basis objects hold them (GetZ/GetW/GetD/GetBdata/GetDbdata):
+// direction 0 GLL + eModified_A (n modes, Q0 = n + 1), direction 1 Gauss-Radau (alpha 1,
+// beta 0) + eModified_B (n (n + 1) / 2 modes, Q1 = n); w1 without the factor 0.5.
+int ref_tri_tables(int n, double* z0, double* w0, double* D0, double* B0, double* DB0, double* z1, double* w1,
+                   double* D1, double* B1, double* DB1) {
+  const int Q0 = n + 1, Q1 = n;
+  gll_tables(Q0, z0, w0, D0);
+  modA_tables(n, Q0, z0, D0, B0, DB0);
+  radau_tables(Q1, z1, w1, D1);
+  modB_tables(n, Q1, z1, D1, B1, DB1);
+  return 0;
+}
+
+int ref_tri_bwdtrans(int n, int E, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  TriTables t = make_tri_tables(n);
+  const int nb = E / W;
+#define TB(NN) parallel_blocks(nb, nthreads, [&](int b0, int b1) { tri_bwd<NN>(t, in, out, b0, b1); })
+  TRI_DISPATCH(n, TB)
+#undef TB
+}
+
+int ref_tri_iproduct(int n, int E, const double* jac, int deformed, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n;
+  TriTables t = make_tri_tables(n);
+  std::vector<double> dfz((size_t)4 * E * (deformed ? nq : 1), 0.0);
+  Geo g = interleave(2, nq, E, E, jac, dfz.data(), deformed != 0);
+  const int nb = E / W;
+#define TI(NN)                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {            \
+    if (deformed) tri_iprod<NN, true>(t, g, in, out, b0, b1);    \
+    else tri_iprod<NN, false>(t, g, in, out, b0, b1);            \
+  })
+  TRI_DISPATCH(n, TI)
+#undef TI
+}
+
+int ref_tri_physderiv(int n, int E, const double* df, int deformed, const double* in, double* o0, double* o1,
+                      int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n;
+  TriTables t = make_tri_tables(n);
+  std::vector<double> jz((size_t)E * (deformed ? nq : 1), 1.0);
+  Geo g = interleave(2, nq, E, E, jz.data(), df, deformed != 0);
+  const int nb = E / W;
+#define TD(NN)                                                          \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                   \
+    if (deformed) tri_deriv<NN, true>(t, g, in, o0, o1, b0, b1);        \
+    else tri_deriv<NN, false>(t, g, in, o0, o1, b0, b1);                \
+  })
+  TRI_DISPATCH(n, TD)
+#undef TD
+}
+
+int ref_tri_helmholtz(int n, int E, const double* jac, const double* df, int deformed, double lambda,
+                      const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n;
+  TriTables t = make_tri_tables(n);
+  Geo g = interleave(2, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define TH(NN)                                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
+    if (deformed) helm_tri<NN, true>(t, g, lambda, in, out, b0, b1);           \
+    else helm_tri<NN, false>(t, g, lambda, in, out, b0, b1);                   \
+  })
+  TRI_DISPATCH(n, TH)
+#undef TH
+}
+
+int ref_tri_iproduct_deriv(int n, int E, const double* jac, const double* df, int deformed, const double* in0,
+                           const double* in1, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n;
+  TriTables t = make_tri_tables(n);
+  Geo g = interleave(2, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define TP(NN)                                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
+    if (deformed) iprd_tri<NN, true>(t, g, in0, in1, out, b0, b1);             \
+    else iprd_tri<NN, false>(t, g, in0, in1, out, b0, b1);                     \
+  })
+  TRI_DISPATCH(n, TP)
+#undef TP
 }
 
 }  // extern "C"

@@ -104,3 +104,55 @@ def cg_solve(dim, n, Q, E, jac, df, deformed, lam, l2g, sign, nglobal, ndir, din
                             _p(np.ascontiguousarray(rhs, dtype=np.float64)), _p(x), ctypes.c_double(tol),
                             max_iter, nthreads, ctypes.byref(eps))
     return x, it, eps.value
+
+
+# ---- triangles (ref_tri_* drivers) ----
+def tri_tables(n):
+    """Reference tables: (z0, w0, D0, B0, DB0), (z1, w1, D1, B1, DB1); w1 as GetW() holds it."""
+    Q0, Q1, nc = n + 1, n, n * (n + 1) // 2
+    a = [np.zeros(Q0), np.zeros(Q0), np.zeros(Q0 * Q0), np.zeros(n * Q0), np.zeros(n * Q0)]
+    b = [np.zeros(Q1), np.zeros(Q1), np.zeros(Q1 * Q1), np.zeros(nc * Q1), np.zeros(nc * Q1)]
+    _check(lib().ref_tri_tables(n, *[_p(x) for x in a], *[_p(x) for x in b]), "ref_tri_tables")
+    return a, b
+
+
+def tri_bwdtrans(n, E, coeffs, nthreads=1):
+    out = np.zeros(E * (n + 1) * n)
+    _check(lib().ref_tri_bwdtrans(n, E, _p(np.ascontiguousarray(coeffs, dtype=np.float64)), _p(out), nthreads),
+           "ref_tri_bwdtrans")
+    return out
+
+
+def tri_iproduct(n, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n * (n + 1) // 2)
+    _check(lib().ref_tri_iproduct(n, E, _p(np.ascontiguousarray(jac, dtype=np.float64)), int(deformed),
+                                  _p(np.ascontiguousarray(phys, dtype=np.float64)), _p(out), nthreads),
+           "ref_tri_iproduct")
+    return out
+
+
+def tri_physderiv(n, E, df, deformed, phys, nthreads=1):
+    nq = (n + 1) * n
+    o0, o1 = np.zeros(E * nq), np.zeros(E * nq)
+    _check(lib().ref_tri_physderiv(n, E, _p(np.ascontiguousarray(df, dtype=np.float64)), int(deformed),
+                                   _p(np.ascontiguousarray(phys, dtype=np.float64)), _p(o0), _p(o1), nthreads),
+           "ref_tri_physderiv")
+    return o0, o1
+
+
+def tri_helmholtz(n, E, jac, df, deformed, lam, coeffs, nthreads=1):
+    out = np.zeros(E * n * (n + 1) // 2)
+    _check(lib().ref_tri_helmholtz(n, E, _p(np.ascontiguousarray(jac, dtype=np.float64)),
+                                   _p(np.ascontiguousarray(df, dtype=np.float64)), int(deformed),
+                                   ctypes.c_double(lam), _p(np.ascontiguousarray(coeffs, dtype=np.float64)),
+                                   _p(out), nthreads),
+           "ref_tri_helmholtz")
+    return out
+
+
+def tri_iproduct_deriv(n, E, jac, df, deformed, in0, in1, nthreads=1):
+    out = np.zeros(E * n * (n + 1) // 2)
+    f = lambda a: _p(np.ascontiguousarray(a, dtype=np.float64))
+    _check(lib().ref_tri_iproduct_deriv(n, E, f(jac), f(df), int(deformed), f(in0), f(in1), _p(out), nthreads),
+           "ref_tri_iproduct_deriv")
+    return out

@@ -13,9 +13,20 @@ std::vector<StdRegions::StdExpansionSharedPtr> Expansions(int shape, int n, int 
   auto e = std::make_shared<StdRegions::StdExpansion>((LibUtilities::ShapeType)shape, n, Q);
   return std::vector<StdRegions::StdExpansionSharedPtr>(E, e);
 }
-std::shared_ptr<Collections::CoalescedGeomData> Geometry(int dim, int Q, int E, const double* jac, const double* df) {
+// per element: coefficients and quadrature points of the shape (triangles: n (n+1)/2 modes
+// on Q x (Q - 1) collapsed points)
+size_t ModesPerElement(int shape, int n) {
+  if (shape == LibUtilities::eTriangle) return (size_t)n * (n + 1) / 2;
+  return shape == LibUtilities::eQuadrilateral ? (size_t)n * n : (size_t)n * n * n;
+}
+size_t PointsPerElement(int shape, int Q) {
+  if (shape == LibUtilities::eTriangle) return (size_t)Q * (Q - 1);
+  return shape == LibUtilities::eQuadrilateral ? (size_t)Q * Q : (size_t)Q * Q * Q;
+}
+std::shared_ptr<Collections::CoalescedGeomData> Geometry(int shape, int Q, int E, const double* jac, const double* df) {
   auto g = std::make_shared<Collections::CoalescedGeomData>();
-  const size_t npts = (size_t)E * (dim == 2 ? Q * Q : Q * Q * Q);
+  const int dim = shape == LibUtilities::eHexahedron ? 3 : 2;
+  const size_t npts = (size_t)E * PointsPerElement(shape, Q);
   Array<OneD, NekDouble> j(npts);
   Array<TwoD, NekDouble> d(dim * dim, npts);
   std::copy(jac, jac + npts, j.get());
@@ -41,12 +52,11 @@ int probe_registry(int* nops, int* nsys, int* has_gpu_full, int* has_gpu_sc) {
 int probe_helmholtz(int shape, int n, int Q, int E, const double* jac, const double* df, double lambda,
                     const double* in, double* out, char* msg, int msglen) {
   try {
-    const int dim = shape == LibUtilities::eQuadrilateral ? 2 : 3;
     auto exps = Expansions(shape, n, Q, E);
     auto op = Collections::GetOperatorFactory().CreateInstance(
         Collections::OperatorKey((LibUtilities::ShapeType)shape, Collections::eHelmholtz, Collections::eGPU, false),
-        exps, Geometry(dim, Q, E, jac, df));
-    const size_t nloc = (size_t)E * (dim == 2 ? n * n : n * n * n);
+        exps, Geometry(shape, Q, E, jac, df));
+    const size_t nloc = (size_t)E * ModesPerElement(shape, n);
     Array<OneD, NekDouble> a(nloc), b(nloc), w;
     std::copy(in, in + nloc, a.get());
     StdRegions::ConstFactorMap f{{StdRegions::eFactorLambda, lambda}};
@@ -65,15 +75,14 @@ int probe_solve(const char* name, int shape, int n, int Q, int E, const double* 
                 const int* l2g, const double* sign, int nglobal, int ndir, double tol, const double* in, double* out,
                 char* msg, int msglen) {
   try {
-    const int dim = shape == LibUtilities::eQuadrilateral ? 2 : 3;
     auto exps = Expansions(shape, n, Q, E);
     auto op = Collections::GetOperatorFactory().CreateInstance(
         Collections::OperatorKey((LibUtilities::ShapeType)shape, Collections::eHelmholtz, Collections::eGPU, false),
-        exps, Geometry(dim, Q, E, jac, df));
+        exps, Geometry(shape, Q, E, jac, df));
     auto expList = std::make_shared<MultiRegions::ExpList>();
     expList->m_exp = exps;
     auto map = std::make_shared<MultiRegions::AssemblyMap>();
-    const size_t nloc = (size_t)E * (dim == 2 ? n * n : n * n * n);
+    const size_t nloc = (size_t)E * ModesPerElement(shape, n);
     Array<OneD, int> m(nloc);
     Array<OneD, NekDouble> s(nloc);
     std::copy(l2g, l2g + nloc, m.get());

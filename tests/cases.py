@@ -1,9 +1,10 @@
 """Seeded test cases shared by the CPU and GPU tests (small sizes the oracle runs in seconds)."""
 import numpy as np
 
-from ithaca_gpu.mesh import HexMesh, QuadMesh
+from ithaca_gpu.mesh import HexMesh, QuadMesh, TriMesh
 from oracle import basis as obasis
 from oracle import geom as ogeom
+from oracle import tri as otri
 
 
 class Case:
@@ -45,6 +46,27 @@ def hex_case(nx, ny, nz, n, amp=0.05, deformed=True):
         c.jac = jac[:, 0].copy()
         c.df = df.reshape(9, c.E, nq)[:, :, 0].copy()
     c.nm, c.nq = n ** 3, c.Q ** 3
+    return c
+
+
+def tri_case(nx, ny, n, jitter=0.15, seed=3, curve=0.05, deformed=True):
+    """TriMesh of 2 nx ny triangles (local vertex orders rotated), n modes; deformed: curved
+    and per-point geometry from the oracle's GeomFactors, else straight and per element."""
+    c = Case()
+    c.dim, c.shape, c.n, c.Q = 2, "tri", n, n + 1
+    E = 2 * nx * ny
+    c.mesh = TriMesh(nx, ny, jitter=jitter, seed=seed, rotate=np.arange(E) % 3,
+                     curve_amp=curve if deformed else 0.0)
+    c.E = E
+    c.X = c.mesh.coords(n)
+    c.basis = otri.TriBasis(n)
+    c.deformed = deformed
+    if deformed:
+        jac, df = otri.geom_factors(c.basis, c.X)
+        c.jac, c.df = jac.reshape(-1).copy(), df.copy()
+    else:
+        c.jac, c.df = otri.straight_tri_geometry(c.mesh.V[c.mesh.EV])
+    c.nm, c.nq = c.basis.nc, c.basis.nq
     return c
 
 

@@ -5,8 +5,8 @@ linked here against stand-in headers with the reference's signatures
 AssemblyMap.h:80-308), and driven through the reference's factories.
 
 CPU: the adapter compiles with -Wall -Wextra, links with every library symbol resolved
-(-Wl,--no-undefined against libithaca_gpu.so), registers 10 operator keys (5 operators x
-quad/hex) and the two systems, and turns a library error into NekError. GPU: a Helmholtz
+(-Wl,--no-undefined against libithaca_gpu.so), registers 15 operator keys (5 operators x
+tri/quad/hex) and the two systems, and turns a library error into NekError. GPU: a Helmholtz
 apply and HelmSolves through the factory-made objects match the oracle.
 """
 import ctypes
@@ -56,17 +56,17 @@ def test_adapter_registers_operators_and_systems(adapter):
     v = [ctypes.c_int() for _ in range(4)]
     adapter.probe_registry(*[ctypes.byref(x) for x in v])
     nops, nsys, full, sc = (x.value for x in v)
-    assert nops == 10 and nsys == 2 and full == 1 and sc == 1
+    assert nops == 15 and nsys == 2 and full == 1 and sc == 1
 
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def _helmholtz(adapter, c, lam, u):
+def _helmholtz(adapter, c, lam, u, shape=4):
     out = np.zeros(c.E * c.nm)
     msg = ctypes.create_string_buffer(512)
-    rc = adapter.probe_helmholtz(4, c.n, c.Q, c.E, _dp(np.ascontiguousarray(c.jac)), _dp(np.ascontiguousarray(c.df)),
+    rc = adapter.probe_helmholtz(shape, c.n, c.Q, c.E, _dp(np.ascontiguousarray(c.jac)), _dp(np.ascontiguousarray(c.df)),
                                  ctypes.c_double(lam), _dp(u), _dp(out), msg, 512)
     return rc, out, msg.value.decode()
 
@@ -88,6 +88,18 @@ def test_adapter_helmholtz_matches_oracle(adapter):
     assert rc == 0, msg
     ref = oops.helmholtz(c.basis, 2, c.jac.reshape(c.E, -1), c.df, 1.5, u).reshape(-1)
     assert rel_err(out, ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_adapter_triangle_helmholtz_matches_oracle(adapter):
+    """A triangle collection (eTriangle = 3) through the same adapter class."""
+    from cases import tri_case
+    from oracle import tri as otri
+    c = tri_case(4, 3, 6)
+    u = np.random.default_rng(4).uniform(-1, 1, c.E * c.nm)
+    rc, out, msg = _helmholtz(adapter, c, 0.8, u, shape=3)
+    assert rc == 0, msg
+    assert rel_err(out, otri.helmholtz(c.basis, c.jac.reshape(c.E, -1), c.df, 0.8, u)) < 1e-12
 
 
 @pytest.mark.gpu

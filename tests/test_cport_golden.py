@@ -76,3 +76,16 @@ def test_cport_cg_matches_reference_recurrence(cport, nthreads):
     assert it == int(g["iterations"])
     nd = int(g["ndir"])
     assert rel_err(x[nd:], g["x"][nd:]) < 1e-12
+
+
+@pytest.mark.parametrize("tag,deformed", [("mesh", True), ("reg", False)])
+def test_cport_triangle_helmholtz(cport, tag, deformed):
+    """The port's triangle Helmholtz (HelmholtzTriImpl restated) against the reference kernels."""
+    from oracle import tri as otri
+    g = load("tri.npz")
+    n = int(g[f"{tag}_n"])
+    tb = otri.TriBasis(n)
+    u = g[f"{tag}_u"]
+    E = u.size // tb.nc
+    out = cport.tri_helmholtz(tb, E, g[f"{tag}_jac"], g[f"{tag}_df"], deformed, 1.3, u, nthreads=2)
+    assert rel_err(out, g[f"{tag}_helm"]) < TOL

@@ -96,3 +96,33 @@ def test_gpu_tensor_coefficient_matches_oracle(case):
     x2, r2 = GlobalLinSysIterativeFullGPU(coll, amap).solve(1.0, rhs, tol=1e-12)
     assert r1.iterations == r2.iterations and np.array_equal(x1, x2)
     ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_gpu_coefficient_set_after_a_solve(mode):
+    """A coefficient set after a solve (its graph already captured with the old geometry
+    buffer) must reach the next solve: same result as a system that had it from the start."""
+    from ithaca_gpu.operators import Collection, Context, GlobalLinSysIterativeFullGPU
+    c = quad_case(6, 5, 6)
+    amap = c.mesh.assembly(c.n)
+    ctx = Context(0)
+    coll = Collection(ctx, c.shape, c.n, c.Q, c.E, c.jac, c.df)
+    rhs = np.random.default_rng(5).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    kappa = (1.0 + 0.5 * np.sin(3 * c.X[0]) * np.cos(2 * c.X[1])).reshape(-1)
+    a = GlobalLinSysIterativeFullGPU(coll, amap)
+    a.solve(1.0, rhs, tol=1e-10, mode=mode)
+    a.set_varcoeff(kappa)
+    xa, ra = a.solve(1.0, rhs, tol=1e-10, mode=mode)
+    b = GlobalLinSysIterativeFullGPU(coll, amap)
+    b.set_varcoeff(kappa)
+    xb, rb = b.solve(1.0, rhs, tol=1e-10, mode=mode)
+    assert ra.iterations == rb.iterations and np.array_equal(xa, xb)
+    a.set_varcoeff_tensor(_tensor(c, 3))
+    a.solve(1.0, rhs, tol=1e-10, mode=mode)
+    a.set_varcoeff(None)
+    xa, ra = a.solve(1.0, rhs, tol=1e-10, mode=mode)
+    xc, rc = GlobalLinSysIterativeFullGPU(coll, amap).solve(1.0, rhs, tol=1e-10, mode=mode)
+    assert ra.iterations == rc.iterations and np.array_equal(xa, xc)
+    ctx.close()
