@@ -42,7 +42,7 @@ enum {
 };
 
 /* LibUtilities::ShapeType values of the supported shapes (LibUtilities/BasicUtils/ShapeType.hpp). */
-enum { ITHACA_GPU_SHAPE_TRI = 3, ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_HEX = 8 };
+enum { ITHACA_GPU_SHAPE_TRI = 3, ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_TET = 5, ITHACA_GPU_SHAPE_HEX = 8 };
 
 /* Arithmetic of an element operator. */
 enum { ITHACA_GPU_FP64 = 0, ITHACA_GPU_FP32 = 1 };
@@ -92,6 +92,14 @@ int ithaca_gpu_basis_modA(int nmodes, int npoints, double* z, double* w, double*
 int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double* B0, double* DB0, double* z1,
                          double* w1, double* D1, double* B1, double* DB1);
 
+/* ---- tetrahedron basis, direction 2: eModified_C on Q2 = nmodes Gauss-Radau-Jacobi
+ *      (alpha 2, beta 0) points (MeshGraph.cpp:1683-1716; Basis.cpp:512-566: the row of mode
+ *      m(p, q, r), r fastest, is the eModified_B row (p + q, r)) ----
+ * Directions 0 and 1 are those of ithaca_gpu_basis_tri(nmodes, ...). z2, w2 (Q2, weights as
+ * Basis::GetW holds them, without the collapsed map's factor 1/4), D2 (Q2*Q2), B2 and DB2
+ * (nc*Q2, nc = nmodes (nmodes+1) (nmodes+2) / 6). Host arrays; any pointer may be NULL. */
+int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double* B2, double* DB2);
+
 /* ---- geometry (SpatialDomains/GeomFactors.cpp:168-475 ComputeDeriv/ComputeJac/
  *      ComputeDerivFactors) ----
  * coords: d arrays of E*Q^d physical coordinates at the GLL quadrature points,
@@ -100,7 +108,9 @@ int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double*
  * if any Jacobian is not positive. Triangles (shape 3): npoints = Q0, the coordinates
  * at the Q0 x Q1 collapsed points (point j*Q0 + i, Q1 = Q0 - 1), 2 arrays of E*Q0*Q1;
  * the derivatives are taken in collapsed coordinates and mapped by the chain rule of
- * StdTriExp::v_PhysDeriv. */
+ * StdTriExp::v_PhysDeriv. Tetrahedra (shape 5): npoints = Q0, coordinates at the
+ * Q0 x (Q0-1) x (Q0-1) collapsed points (point (k Q1 + j) Q0 + i), 3 arrays; chain rule of
+ * StdTetExp::v_PhysDeriv. */
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device);
 
@@ -115,12 +125,16 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
  * per element nmodes (nmodes + 1) / 2 coefficients and Q0 (Q0 - 1) points, geometry
  * (jac, df with d = 2) per point on those points or per element (MatrixFreeOps/
  * Helmholtz.h:290-330, 505-635; BwdTrans.h:540-570; IProduct.h:560-590;
- * PhysDeriv.h:470-500; IProductWRTDerivBase.h:671-1060). */
+ * PhysDeriv.h:470-500; IProductWRTDerivBase.h:671-1060). Tetrahedra (shape 5): the basis of
+ * ithaca_gpu_basis_tet, nmodes (nmodes+1) (nmodes+2) / 6 coefficients and Q0 (Q0-1)^2 points
+ * per element, geometry (d = 3) per point or per element (MatrixFreeOps/Helmholtz.h:
+ * 1970-2010, 2266-2448; BwdTrans.h:1010-1045; IProduct.h:1730-1770; PhysDeriv.h:990-1030;
+ * IProductWRTDerivBase.h:2212-2630); the library keeps their metric per point either way. */
 int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
                          const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op);
 int ithaca_gpu_op_destroy(ithaca_gpu_op* op);
 /* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282); nelmt * nmodes (nmodes+1)/2
- * for triangles. */
+ * for triangles, nelmt * nmodes (nmodes+1) (nmodes+2)/6 for tetrahedra. */
 int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof);
 
 /* BwdTrans (Collections/BwdTrans.cpp:143-240): coefficients -> physical values. */

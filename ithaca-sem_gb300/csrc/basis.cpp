@@ -15,6 +15,8 @@
 //     Chebyshev-Gauss guesses), weights 2 (1 - z_i) / (Q (Q+1) P_{Q-1}^{(1,0)}(z_i)^2)
 //   derivative matrix by the barycentric Lagrange formula (Polylib.cpp:589-626 Dgrjm)
 //   ModifiedB modes B1 (n (n+1)/2 of them, q fastest), DB1 = D1 B1 (Basis.cpp:423-507)
+// Tetrahedra add direction 2: Gauss-Radau-Jacobi points for the weight (1 - z)^2 and the
+// ModifiedC rows phi^c_{pqr} = phi^b_{p+q,r} (Basis.cpp:512-566).
 #include "ithaca_internal.h"
 
 #include <cmath>
@@ -126,13 +128,15 @@ static void jacobi_zeros(int m, double a, double b, double* x) {
   }
 }
 
-static void radau_points(int Q, double* z, double* w) {
+// Gauss-Radau-Jacobi points with z_0 = -1 for the weight (1 - z)^alpha: -1 and the zeros
+// of P_{Q-1}^{(alpha,1)}; weights 2^alpha (1 - z_i) / (Q (Q + alpha) P_{Q-1}^{(alpha,0)}(z_i)^2).
+static void radau_points(int Q, double* z, double* w, double alpha = 1.0) {
   if (Q == 1) { z[0] = 0.0; w[0] = 2.0; return; }
   z[0] = -1.0;
-  jacobi_zeros(Q - 1, 1.0, 1.0, z + 1);
+  jacobi_zeros(Q - 1, alpha, 1.0, z + 1);
   for (int i = 0; i < Q; ++i) {
-    const double p = jacobi(Q - 1, 1.0, 0.0, z[i]);
-    w[i] = 2.0 * (1.0 - z[i]) / (Q * (Q + 1.0) * p * p);
+    const double p = jacobi(Q - 1, alpha, 0.0, z[i]);
+    w[i] = std::pow(2.0, alpha) * (1.0 - z[i]) / (Q * (Q + alpha) * p * p);
   }
 }
 
@@ -191,6 +195,36 @@ TriBasisTables make_tri_basis(int n) {
   radau_points(t.Q1, t.z1.data(), t.w1.data());
   lagrange_derivative(t.Q1, t.z1.data(), t.D1.data());
   modB_tables(n, t.Q1, t.z1.data(), t.D1.data(), t.B1.data(), t.DB1.data());
+  return t;
+}
+
+TetBasisTables make_tet_basis(int n) {
+  TetBasisTables t;
+  t.n = n;
+  t.nc = n * (n + 1) * (n + 2) / 6;
+  t.t = make_tri_basis(n);
+  const int Q = n, npq = n * (n + 1) / 2;
+  t.z2.resize(Q);
+  t.w2.resize(Q);
+  t.D2.resize(Q * Q);
+  radau_points(Q, t.z2.data(), t.w2.data(), 2.0);
+  lagrange_derivative(Q, t.z2.data(), t.D2.data());
+  // ModifiedC: row (p, q, r) is the ModifiedB row (p + q, r) on the alpha-2 points
+  std::vector<double> Bb((size_t)npq * Q), DBb((size_t)npq * Q);
+  modB_tables(n, Q, t.z2.data(), t.D2.data(), Bb.data(), DBb.data());
+  t.B2.resize((size_t)t.nc * Q);
+  t.DB2.resize((size_t)t.nc * Q);
+  int m = 0;
+  for (int p = 0; p < n; ++p)
+    for (int q = 0; q < n - p; ++q)
+      for (int r = 0; r < n - p - q; ++r, ++m) {
+        int row = r;  // ModifiedB index of (p + q, r)
+        for (int pp = 0; pp < p + q; ++pp) row += n - pp;
+        for (int k = 0; k < Q; ++k) {
+          t.B2[(size_t)m * Q + k] = Bb[(size_t)row * Q + k];
+          t.DB2[(size_t)m * Q + k] = DBb[(size_t)row * Q + k];
+        }
+      }
   return t;
 }
 

@@ -99,8 +99,55 @@ static int guarded(F f) {
 
 static int shape_dim(int shape) {
   if (shape == ITHACA_GPU_SHAPE_QUAD || shape == ITHACA_GPU_SHAPE_TRI) return 2;
-  if (shape == ITHACA_GPU_SHAPE_HEX) return 3;
-  fail(ITHACA_GPU_ERR_UNSUPPORTED, "shape must be triangle (3), quadrilateral (4) or hexahedron (8)");
+  if (shape == ITHACA_GPU_SHAPE_HEX || shape == ITHACA_GPU_SHAPE_TET) return 3;
+  fail(ITHACA_GPU_ERR_UNSUPPORTED,
+       "shape must be triangle (3), quadrilateral (4), tetrahedron (5) or hexahedron (8)");
+}
+
+// Packed tetrahedron tables (layout tet_off in ithaca_internal.h), host FP64.
+static std::vector<double> pack_tet_tables(const TetBasisTables& b) {
+  const TetOff o = tet_off(b.n);
+  const int n = b.n, Q0 = n + 1, Q = n, npq = n * (n + 1) / 2, nc = b.nc;
+  const TriBasisTables& t = b.t;
+  std::vector<double> h(o.size);
+  for (int i = 0; i < n * Q0; ++i) {
+    h[o.B0 + i] = t.a.B[i];
+    h[o.DB0 + i] = t.a.DB[i];
+  }
+  for (int i = 0; i < Q0 * Q0; ++i) h[o.D0 + i] = t.a.D[i];
+  for (int i = 0; i < Q0; ++i) {
+    h[o.w0 + i] = t.a.w[i];
+    h[o.h0 + i] = 0.5 * (1.0 + t.a.z[i]);
+  }
+  for (int i = 0; i < npq * Q; ++i) {
+    h[o.B1 + i] = t.B1[i];
+    h[o.DB1 + i] = t.DB1[i];
+  }
+  for (int i = 0; i < nc * Q; ++i) {
+    h[o.B2 + i] = b.B2[i];
+    h[o.DB2 + i] = b.DB2[i];
+  }
+  for (int i = 0; i < Q * Q; ++i) {
+    h[o.D1 + i] = t.D1[i];
+    h[o.D2 + i] = b.D2[i];
+  }
+  for (int j = 0; j < Q; ++j) {
+    h[o.w1 + j] = 0.5 * t.w1[j];  // MatrixFreeOps/Operator.hpp:245-251
+    h[o.h1 + j] = 0.5 * (1.0 + t.z1[j]);
+    h[o.h2 + j] = 2.0 / (1.0 - t.z1[j]);
+    h[o.w2 + j] = 0.25 * b.w2[j];
+    h[o.h3 + j] = 2.0 / (1.0 - b.z2[j]);
+  }
+  return h;
+}
+
+template <typename T>
+static void upload_packed(DevTables<T>& dt, const std::vector<double>& h, int n, int Q) {
+  std::vector<T> ht(h.begin(), h.end());
+  dt.n = n;
+  dt.Q = Q;
+  ITHACA_CUDA(cudaMalloc(&dt.base, ht.size() * sizeof(T)));
+  ITHACA_CUDA(cudaMemcpy(dt.base, ht.data(), ht.size() * sizeof(T), cudaMemcpyHostToDevice));
 }
 
 // Packed triangle tables (layout tri_off in ithaca_internal.h), host FP64.
@@ -299,6 +346,19 @@ int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double*
   });
 }
 
+int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double* B2, double* DB2) {
+  return guarded([&] {
+    require(nmodes >= 2 && nmodes <= 16, "need 2 <= nmodes <= 16");
+    const TetBasisTables t = make_tet_basis(nmodes);
+    const int Q = nmodes, nc = t.nc;
+    if (z2) std::memcpy(z2, t.z2.data(), sizeof(double) * Q);
+    if (w2) std::memcpy(w2, t.w2.data(), sizeof(double) * Q);
+    if (D2) std::memcpy(D2, t.D2.data(), sizeof(double) * Q * Q);
+    if (B2) std::memcpy(B2, t.B2.data(), sizeof(double) * nc * Q);
+    if (DB2) std::memcpy(DB2, t.DB2.data(), sizeof(double) * nc * Q);
+  });
+}
+
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device) {
   return guarded([&] {
@@ -306,6 +366,31 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
     StreamOrder order_(ctx);
     require(nelmt > 0 && npoints >= 2 && npoints <= 16, "bad sizes");
     const int dim = shape_dim(shape);
+    if (shape == ITHACA_GPU_SHAPE_TET) {  // npoints = Q0 = n + 1; Q1 = Q2 = n Gauss-Radau
+      const int n = npoints - 1;
+      const size_t tot = (size_t)nelmt * npoints * n * n;
+      const std::vector<double> h = pack_tet_tables(make_tet_basis(n));
+      double* dtab = nullptr;
+      int* dbad = nullptr;
+      ITHACA_CUDA(cudaMalloc(&dtab, sizeof(double) * h.size()));
+      std::unique_ptr<double, decltype(&cudaFree)> g1(dtab, cudaFree);
+      ITHACA_CUDA(cudaMalloc(&dbad, sizeof(int)));
+      std::unique_ptr<int, decltype(&cudaFree)> g2(dbad, cudaFree);
+      ITHACA_CUDA(cudaMemcpyAsync(dtab, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+      ITHACA_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+      const double* X = (const double*)to_device(ctx, 0, coords, sizeof(double) * 3 * tot, on_device);
+      double* J = (double*)out_buffer(ctx, 1, jac, sizeof(double) * tot, on_device);
+      double* F = (double*)out_buffer(ctx, 2, df, sizeof(double) * 9 * tot, on_device);
+      launch_geom_factors_tet(n, nelmt, dtab, X, J, F, dbad, ctx->stream);
+      ctx->launches++;
+      from_device(ctx, jac, J, sizeof(double) * tot, on_device);
+      from_device(ctx, df, F, sizeof(double) * 9 * tot, on_device);
+      int hbad = 0;
+      ITHACA_CUDA(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (hbad) fail(ITHACA_GPU_ERR_GEOMETRY, "non-positive Jacobian at a quadrature point");
+      return;
+    }
     if (shape == ITHACA_GPU_SHAPE_TRI) {  // npoints = Q0 = n + 1 GLL points; Q1 = n Gauss-Radau
       const int n = npoints - 1;
       const size_t tot = (size_t)nelmt * npoints * n;
@@ -380,7 +465,32 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     o->deformed = deformed ? 1 : 0;
     o->precision = precision;
     const size_t npt = o->deformed ? (size_t)(dim == 2 ? npoints * npoints : npoints * npoints * npoints) : 1;
-    if (shape == ITHACA_GPU_SHAPE_TRI) {
+    if (shape == ITHACA_GPU_SHAPE_TET) {
+      // ModifiedA x ModifiedB x ModifiedC: n (n+1) (n+2) / 6 modes on (n + 1) n n collapsed
+      // points; the geometry is expanded to per-point metric terms whatever the input kind
+      o->kdim = kTetKernels;
+      o->nm = tet_nc(nmodes);
+      o->nq = npoints * nmodes * nmodes;
+      const std::vector<double> h = pack_tet_tables(make_tet_basis(nmodes));
+      upload_packed(o->t64, h, nmodes, npoints);
+      upload_packed(o->t32, h, nmodes, npoints);
+      const size_t tp = o->deformed ? (size_t)o->nq : 1;
+      const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * tp, on_device);
+      const double* F = (const double*)to_device(ctx, 1, df, sizeof(double) * 9 * nelmt * tp, on_device);
+      const int in_deformed = o->deformed;
+      o->deformed = 1;
+      const size_t njg = (size_t)nelmt * 7 * o->nq, ndf = (size_t)nelmt * 9 * o->nq;
+      ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * ndf));
+      launch_build_jg_tet<double>(nmodes, nelmt, in_deformed, o->t64.base, J, F, o->jg64, o->df64, ctx->stream);
+      ctx->launches++;
+      if (precision == ITHACA_GPU_FP32) {
+        ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
+        ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
+        launch_build_jg_tet<float>(nmodes, nelmt, in_deformed, o->t64.base, J, F, o->jg32, o->df32, ctx->stream);
+        ctx->launches++;
+      }
+    } else if (shape == ITHACA_GPU_SHAPE_TRI) {
       // ModifiedA x ModifiedB: n (n + 1) / 2 modes on (n + 1) x n collapsed points
       o->nm = tri_nc(nmodes);
       o->nq = npoints * nmodes;
@@ -561,7 +671,7 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
     if (op->precision == ITHACA_GPU_FP64)
       ok = launch_helmholtz<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
                                     (const double*)din, (double*)dout, nullptr, 0, c->stream);
-    else if (op->dim == 3 && op->deformed && op->variant32 > 0)
+    else if (op->kdim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), op->jg32,
                                      (float)lambda, (const float*)din, (float*)dout, nullptr, 0, nullptr, nullptr,
                                      c->derr, c->stream);
@@ -626,7 +736,7 @@ int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* tim
     for (int vi = 0; vi < 9; ++vi) {
       const int v = variants[vi];
       double ms_avg = -1;
-      if (v == 0 || (op->dim == 3 && op->deformed)) {
+      if (v == 0 || (op->kdim == 3 && op->deformed)) {
         auto run = [&] {
           bool ok = v == 0 ? launch_helmholtz<float>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t32.base, jg,
                                                      1.0f, x, y, nullptr, 0, s)

@@ -747,7 +747,7 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
     if (cg->geo16)
       ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
                                   v.yloc, map, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
-    else if (op->dim == 3 && op->deformed && op->variant32 > 0)
+    else if (op->kdim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,
                                      xin, v.yloc, map,
                                      zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
@@ -946,7 +946,7 @@ static void build_geo16(Cg* cg) {
 static void ensure_geo16(Cg* cg) {
   if (cg->have16) return;
   Op* op = cg->op;
-  if (!(op->dim == 3 && op->deformed))
+  if (!(op->kdim == 3 && op->deformed))
     fail(ITHACA_GPU_ERR_UNSUPPORTED, "16-bit geometry is built for curved (deformed) hexahedra");
   const size_t njg = (size_t)op->E * 7 * op->nq;
   ITHACA_CUDA(cudaMalloc(&cg->jg16, sizeof(__half) * njg + kGeoPad));
@@ -1855,7 +1855,7 @@ int ithaca_gpu_cg_set_varcoeff_tensor(ithaca_gpu_cg* cg, const double* K, int on
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
     req(op->deformed != 0, "a quadrature-point coefficient needs a deformed (per-point) collection");
-    if (op->shape == ITHACA_GPU_SHAPE_TRI)
+    if (op->kdim != op->dim)
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "the coefficient tensor is built for quadrilaterals and hexahedra");
     cudaStream_t s = op->ctx->stream;
     const int dim = op->dim, nk = dim * (dim + 1) / 2;
@@ -1886,7 +1886,7 @@ int ithaca_gpu_misfit(ithaca_gpu_cg* cg, const double* x, const double* u_target
                       int on_device) {
   return cg_guarded([&] {
     req(cg && x && u_target && J, "null argument");
-    if (cg->op->shape == ITHACA_GPU_SHAPE_TRI)
+    if (cg->op->kdim != cg->op->dim)
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "the adjoint misfit is built for quadrilaterals and hexahedra");
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;
@@ -1933,7 +1933,7 @@ int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* 
   return cg_guarded([&] {
     req(cg && x && psi && grad, "null argument");
     if (cg->aniso) fail(ITHACA_GPU_ERR_UNSUPPORTED, "the kappa gradient is for an isotropic coefficient");
-    if (cg->op->shape == ITHACA_GPU_SHAPE_TRI)
+    if (cg->op->kdim != cg->op->dim)
       fail(ITHACA_GPU_ERR_UNSUPPORTED, "the kappa gradient is built for quadrilaterals and hexahedra");
     StreamOrder order_(cg->op->ctx);
     Op* op = cg->op;

@@ -72,9 +72,55 @@ inline __host__ __device__ constexpr TriOff tri_off(int n) {
   return o;
 }
 
-// Kernel family passed where the launchers below take `dim`: 2 (quads), 3 (hexes) or
-// kTriKernels (triangles; their geometry has the 2-D layout).
+// Tetrahedron tables (host, FP64), basis.cpp: direction 0 make_basis(n, n + 1); direction 1
+// the triangle's Gauss-Radau (alpha 1) points and ModifiedB rows (n (n+1)/2 pairs (p, q));
+// direction 2 Gauss-Radau (alpha 2) points z2, weights w2, D2 and the ModifiedC rows B2,
+// DB2 of the nc = n (n+1) (n+2) / 6 modes m(p, q, r) (r fastest), each n values long.
+struct TetBasisTables {
+  int n = 0, nc = 0;
+  TriBasisTables t;
+  std::vector<double> z2, w2, D2, B2, DB2;
+};
+TetBasisTables make_tet_basis(int n);
+
+// Packed device tables of a tetrahedron expansion (Q0 = n + 1, Q = n; offsets in elements):
+//   B0 [p*Q0+i] D0 [k*Q0+i] w0 [i] h0 [i] = (1+z0_i)/2
+//   B1 [pq*Q+j] D1 [l*Q+j] w1 [j] = w1_j/2 h1 [j] = (1+z1_j)/2 h2 [j] = 2/(1-z1_j)
+//   B2 [m*Q+k]  D2 [l*Q+k] w2 [k] = w2_k/4 h3 [k] = 2/(1-z2_k)
+//   then DB0, DB1, DB2 (read by the diagonal kernel only; `core` ends before them)
+struct TetOff {
+  int B0, D0, w0, h0, B1, D1, w1, h1, h2, B2, D2, w2, h3, DB0, DB1, DB2, core, size;
+};
+inline __host__ __device__ constexpr int tet_nc(int n) { return n * (n + 1) * (n + 2) / 6; }
+inline __host__ __device__ constexpr TetOff tet_off(int n) {
+  const int Q0 = n + 1, Q = n, npq = n * (n + 1) / 2, nc = n * (n + 1) * (n + 2) / 6;
+  TetOff o{};
+  o.B0 = 0;
+  o.D0 = o.B0 + n * Q0;
+  o.w0 = o.D0 + Q0 * Q0;
+  o.h0 = o.w0 + Q0;
+  o.B1 = o.h0 + Q0;
+  o.D1 = o.B1 + npq * Q;
+  o.w1 = o.D1 + Q * Q;
+  o.h1 = o.w1 + Q;
+  o.h2 = o.h1 + Q;
+  o.B2 = o.h2 + Q;
+  o.D2 = o.B2 + nc * Q;
+  o.w2 = o.D2 + Q * Q;
+  o.h3 = o.w2 + Q;
+  o.core = o.h3 + Q;
+  o.DB0 = o.core;
+  o.DB1 = o.DB0 + n * Q0;
+  o.DB2 = o.DB1 + npq * Q;
+  o.size = o.DB2 + nc * Q;
+  return o;
+}
+
+// Kernel family passed where the launchers below take `dim`: 2 (quads), 3 (hexes),
+// kTriKernels (triangles; their geometry has the 2-D layout) or kTetKernels
+// (tetrahedra; per-point geometry with the 3-D layout, 7 fields).
 constexpr int kTriKernels = 23;
+constexpr int kTetKernels = 33;
 
 // Device copy of the 1-D tables for one (n, Q), packed for the kernels:
 //   B  [p*Q + i]   Bt  [i*n + p]   DB [p*Q + i]   DBt [i*n + p]
@@ -235,6 +281,20 @@ struct TriApi {
                    const T* in1, T* out, cudaStream_t s);
 };
 
+// Tetrahedra (elem_tet.cuh); geometry always per point.
+template <typename T>
+struct TetApi {
+  static bool helm(int n, int Q, int E, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g,
+                   int ndir, const int* skip, const T* lam_ptr, cudaStream_t s);
+  static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
+  static bool ipr(int n, int Q, int E, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
+  static bool deriv(int n, int Q, int E, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
+                    cudaStream_t s);
+  static bool diag(int n, int Q, int E, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+  static bool iprd(int n, int Q, int E, const T* tab, const T* jg, const T* df, const T* in0, const T* in1,
+                   const T* in2, T* out, cudaStream_t s);
+};
+
 template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
@@ -243,6 +303,8 @@ inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T
   if (dim == kTriKernels)
     return TriApi<T>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, esolve,
                            skip_stride, s);
+  if (dim == kTetKernels) return esolve == nullptr && TetApi<T>::helm(n, Q, E, tab, jg, lambda, in, out, l2g, ndir,
+                                                                      skip, lam_ptr, s);
   return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
                                         esolve, skip_stride, s, variant)
                   : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
@@ -251,12 +313,14 @@ inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T
 template <typename T>
 inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::bwd(n, Q, E, tab, in, out, s);
+  if (dim == kTetKernels) return TetApi<T>::bwd(n, Q, E, tab, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::bwd(n, Q, E, tab, in, out, s) : ElemApi<T, 3>::bwd(n, Q, E, tab, in, out, s);
 }
 template <typename T>
 inline bool launch_iproduct(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* in,
                             T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
+  if (dim == kTetKernels) return TetApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::ipr(n, Q, E, deformed, tab, jg, in, out, s)
                   : ElemApi<T, 3>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
 }
@@ -264,6 +328,7 @@ template <typename T>
 inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* df, const T* in,
                              T* d0, T* d1, T* d2, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, s);
+  if (dim == kTetKernels) return TetApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
   return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
                   : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
 }
@@ -271,6 +336,7 @@ template <typename T>
 inline bool launch_iproduct_deriv(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, const T* df,
                                   const T* in0, const T* in1, const T* in2, T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, out, s);
+  if (dim == kTetKernels) return TetApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
   return dim == 2 ? ElemApi<T, 2>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s)
                   : ElemApi<T, 3>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s);
 }
@@ -278,6 +344,7 @@ template <typename T>
 inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
+  if (dim == kTetKernels) return TetApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
   return dim == 2 ? ElemApi<T, 2>::diag(n, Q, E, deformed, tab, jg, lambda, out, s)
                   : ElemApi<T, 3>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
 }
@@ -296,6 +363,14 @@ template <typename T>
 void launch_build_jg_tri(int n, int E, int deformed, const double* tab, const double* jac, const double* df, T* jg,
                          T* dfo, cudaStream_t s);
 void launch_geom_factors_tri(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                             int* bad, cudaStream_t s);
+// Tetrahedra: per point J w0 w1/2 w2/4 and J w m^{ab} with the collapsed metric of
+// HelmholtzTetImpl (MatrixFreeOps/Helmholtz.h:2336-2420) folded in, from per-point
+// (deformed) or per-element geometry; dfo gets the 9 factors per point.
+template <typename T>
+void launch_build_jg_tet(int n, int E, int deformed, const double* tab, const double* jac, const double* df, T* jg,
+                         T* dfo, cudaStream_t s);
+void launch_geom_factors_tet(int n, int E, const double* tab, const double* coords, double* jac, double* df,
                              int* bad, cudaStream_t s);
 
 }  // namespace ithaca

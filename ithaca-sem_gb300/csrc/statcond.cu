@@ -576,6 +576,21 @@ int ithaca_gpu_sc_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     const int dim = op->dim, n = op->n, nm = op->nm, E = op->E;
     std::vector<int> bm, im;
     for (int m = 0, tp = 0, tq = 0; m < nm; ++m) {
+      if (op->shape == ITHACA_GPU_SHAPE_TET) {
+        // tetrahedron mode m(p, q, r): interior when p >= 2, q >= 1 and r >= 1
+        int tp_ = 0, rest = m;
+        while (rest >= (n - tp_) * (n - tp_ + 1) / 2) {
+          rest -= (n - tp_) * (n - tp_ + 1) / 2;
+          ++tp_;
+        }
+        int tq_ = 0;
+        while (rest >= n - tp_ - tq_) {
+          rest -= n - tp_ - tq_;
+          ++tq_;
+        }
+        (tp_ >= 2 && tq_ >= 1 && rest >= 1 ? im : bm).push_back(m);
+        continue;
+      }
       if (op->shape == ITHACA_GPU_SHAPE_TRI) {
         // triangle mode m(tp, tq): vertices and edges are the rows tp <= 1 and the modes tq == 0
         (tp <= 1 || tq == 0 ? bm : im).push_back(m);

@@ -15,6 +15,14 @@ so this module generates them directly:
   Triangle vertices v0, v1, v2 run counter-clockwise with the affine map
   x = v0 + (v1 - v0)(1 + xi0)/2 + (v2 - v0)(1 + xi1)/2 of SpatialDomains/TriGeom.cpp;
   ``rotate`` shifts a triangle's local vertex order cyclically.
+* ``TetMesh``   -- nx x ny x nz cubes of the unit cube, each split into the six Kuhn
+  tetrahedra v, v + e_a, v + e_a + e_b, v + e_a + e_b + e_c along the permutations (a, b, c)
+  of the axes (a conforming triangulation); interior vertices optionally jittered, the map
+  optionally curved as HexMesh's. Local vertices are sorted by global id and, where that
+  order is negatively oriented, v0 and v1 are exchanged, so that the collapsed vertex of
+  every triangular face is its highest-id vertex in both elements sharing it (the
+  orientation rule for collapsed simplex faces); x = v0 + (v1 - v0)(1 + xi0)/2 +
+  (v2 - v0)(1 + xi1)/2 + (v3 - v0)(1 + xi2)/2 (SpatialDomains/TetGeom.cpp).
 * ``HexMesh``   -- nx x ny x nz hexahedra of the unit cube, optionally curved by
   x_a + amp * sin(2 pi x_b) sin(2 pi x_c) applied cyclically (a, b, c) =
   (0, 1, 2), (1, 2, 0), (2, 0, 1) to the straight positions.
@@ -47,19 +55,9 @@ def gll_points(Q):
     return z
 
 
-def radau_points(Q):
-    """Gauss-Radau-Jacobi points (alpha 1, beta 0, z_0 = -1): -1 and the zeros of
-    P_{Q-1}^{(1,1)}, by Newton with deflation (same values as the library's tables)."""
-    def jac11(m, x):
-        p0, p1 = np.ones_like(x), 2.0 * x
-        if m == 0:
-            return p0
-        for k in range(2, m + 1):
-            a1 = 2.0 * k * (k + 2.0) * (2.0 * k)
-            a3 = (2.0 * k) * (2.0 * k + 1.0) * (2.0 * k + 2.0)
-            a4 = 2.0 * k * k * (2.0 * k + 2.0)
-            p0, p1 = p1, (a3 / a1 * x * p1 - a4 / a1 * p0)
-        return p1
+def radau_points(Q, alpha=1.0):
+    """Gauss-Radau-Jacobi points (weight (1 - z)^alpha, z_0 = -1): -1 and the zeros of
+    P_{Q-1}^{(alpha,1)}, by Newton with deflation (same values as the library's tables)."""
     m = Q - 1
     roots = []
     for k in range(m):
@@ -67,8 +65,8 @@ def radau_points(Q):
         if k > 0:
             r = 0.5 * (r + roots[-1])
         for _ in range(200):
-            p = jac11(m, np.array(r))
-            dp = 0.5 * (m + 3.0) * _jacobi_ab(m - 1, 2.0, 2.0, r)
+            p = _jacobi_ab(m, alpha, 1.0, r)
+            dp = 0.5 * (m + alpha + 2.0) * _jacobi_ab(m - 1, alpha + 1.0, 2.0, r)
             step = float(p / (dp - p * sum(1.0 / (r - x) for x in roots)))
             r -= step
             if abs(step) < 1e-16:
@@ -296,6 +294,261 @@ class TriMesh:
             else:
                 l2g[:, m] = nv + ne * ni + np.arange(E) * nint + icount
                 icount += 1
+        l2g = newid[l2g]
+        return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
+
+
+def _modA(p, x):
+    if p == 0:
+        return 0.5 * (1 - x)
+    if p == 1:
+        return 0.5 * (1 + x)
+    return 0.25 * (1 - x) * (1 + x) * _jacobi_ab(p - 2, 1.0, 1.0, x)
+
+
+def _modB(p, q, x):
+    lo, hi = 0.5 * (1 - x), 0.5 * (1 + x)
+    if p == 0:
+        return lo if q == 0 else (hi if q == 1 else lo * hi * _jacobi_ab(q - 2, 1.0, 1.0, x))
+    if q == 0:
+        return lo ** p
+    return lo ** p * hi * _jacobi_ab(q - 1, 2.0 * p - 1.0, 1.0, x)
+
+
+def tet_modal(n, xi0, xi1, xi2):
+    """Values of the tetrahedron's modes m(p, q, r) at reference points strictly inside or
+    on the faces away from the collapsed edge (xi1 + xi2 < 0, xi2 < 1): (npts, nc), with
+    the singular-vertex and singular-edge terms (mode (0,0,1) = (1 + eta2)/2, modes
+    (0,1,r) without the eta0 factor)."""
+    xi0, xi1, xi2 = (np.asarray(a, dtype=np.float64) for a in (xi0, xi1, xi2))
+    e2 = xi2
+    e1 = 2 * (1 + xi1) / (1 - xi2) - 1
+    e0 = 2 * (1 + xi0) / (-xi1 - xi2) - 1
+    cols = []
+    for p in range(n):
+        for q in range(n - p):
+            for r in range(n - p - q):
+                if (p, q, r) == (0, 0, 1):
+                    cols.append(0.5 * (1 + e2))
+                    continue
+                a = 1.0 if (p == 0 and q == 1) else _modA(p, e0)
+                cols.append(a * _modB(p, q, e1) * _modB(p + q, r, e2))
+    return np.stack(np.broadcast_arrays(*cols), axis=-1)
+
+
+_TET_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
+_TET_FACES = ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))
+_TET_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
+
+
+def _bary_to_xi(lam, verts):
+    """Reference coordinates of the point sum_v lam_v xi(v) for local vertex indices."""
+    return sum(l[..., None] * _TET_XI[v] for l, v in zip(lam, verts))
+
+
+def _tet_local_topology(n):
+    """Per local mode: ('v', vertex), ('e', edge, degree, sign along the local edge) or
+    ('f', face, restriction samples) or ('i',), found by evaluating the modes (a mode
+    belongs to the lowest-dimensional entity on which it does not vanish)."""
+    eps = 1e-9
+    cen = _TET_XI.mean(axis=0)
+    pull = lambda x: (1 - eps) * x + eps * cen
+
+    def vals(xi):
+        xi = pull(np.asarray(xi, dtype=np.float64))
+        return tet_modal(n, xi[..., 0], xi[..., 1], xi[..., 2])
+    nc = n * (n + 1) * (n + 2) // 6
+    s = np.linspace(-0.8, 0.8, n + 3)
+    vv = vals(_TET_XI)                                   # (4, nc)
+    ev = [vals(_bary_to_xi(((1 - s) / 2, (1 + s) / 2), e)) for e in _TET_EDGES]   # (ns, nc) each
+    g = np.array([(a, b) for a in np.linspace(0.1, 0.8, 5) for b in np.linspace(0.1, 0.8, 5) if a + b < 0.95])
+    fpts = (1 - g[:, 0] - g[:, 1], g[:, 0], g[:, 1])
+    fv = [vals(_bary_to_xi(fpts, f)) for f in _TET_FACES]
+    tol = 1e-6
+    one_d = np.stack([_modA(k, s) for k in range(2, n)]) if n > 2 else np.zeros((0, s.size))
+    topo = []
+    for m in range(nc):
+        on_v = np.flatnonzero(np.abs(vv[:, m]) > tol)
+        if on_v.size:
+            assert on_v.size == 1
+            topo.append(("v", int(on_v[0])))
+            continue
+        on_e = [k for k in range(6) if np.max(np.abs(ev[k][:, m])) > tol]
+        if on_e:
+            assert len(on_e) == 1
+            f = ev[on_e[0]][:, m]
+            coef = one_d @ f / np.sum(one_d * one_d, axis=1)
+            k = int(np.argmax(np.abs(coef)))
+            assert np.max(np.abs(f - coef[k] * one_d[k])) < 1e-6 and abs(abs(coef[k]) - 1) < 1e-6
+            topo.append(("e", on_e[0], k + 2, float(np.sign(coef[k]))))
+            continue
+        on_f = [k for k in range(4) if np.max(np.abs(fv[k][:, m])) > tol]
+        if on_f:
+            assert len(on_f) == 1
+            topo.append(("f", on_f[0]))
+            continue
+        topo.append(("i",))
+    return topo, fpts, fv
+
+
+def _face_match(n, fpts, fv, topo, f1, perm1, f2, perm2):
+    """Face modes of local face f2 (vertices seen in order perm2) against those of f1
+    (order perm1) on the same physical face: list of (index into f1's face modes, sign)."""
+    def face_vals(f, perm):
+        # canonical points: barycentric in the face's global order; local order = perm
+        lam = [None] * 3
+        for c, l in zip(perm, fpts):
+            lam[c] = l
+        xi = _bary_to_xi(lam, _TET_FACES[f])
+        xi = (1 - 1e-9) * xi + 1e-9 * _TET_XI.mean(axis=0)
+        v = tet_modal(n, xi[..., 0], xi[..., 1], xi[..., 2])
+        ms = [m for m, t in enumerate(topo) if t[0] == "f" and t[1] == f]
+        return v[:, ms]
+    A, B = face_vals(f1, perm1), face_vals(f2, perm2)
+    out = []
+    for b in range(B.shape[1]):
+        hit = None
+        for a in range(A.shape[1]):
+            for sg in (1.0, -1.0):
+                if np.max(np.abs(B[:, b] - sg * A[:, a])) < 1e-8:
+                    hit = (a, sg)
+        assert hit is not None, "face modes do not match across the shared face"
+        out.append(hit)
+    return out
+
+
+class TetMesh:
+    def __init__(self, nx, ny, nz, jitter=0.0, seed=0, curve_amp=0.0):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.curve_amp = curve_amp
+        gx, gy, gz = np.meshgrid(np.arange(nx + 1) / nx, np.arange(ny + 1) / ny, np.arange(nz + 1) / nz,
+                                 indexing="ij")
+        # vertex id = (k (ny + 1) + j) (nx + 1) + i
+        V = np.stack([gx.transpose(2, 1, 0).ravel(), gy.transpose(2, 1, 0).ravel(), gz.transpose(2, 1, 0).ravel()],
+                     axis=1)
+        if jitter > 0:
+            rng = np.random.default_rng(seed)
+            i = np.tile(np.arange(nx + 1), (ny + 1) * (nz + 1))
+            j = np.tile(np.repeat(np.arange(ny + 1), nx + 1), nz + 1)
+            k = np.repeat(np.arange(nz + 1), (nx + 1) * (ny + 1))
+            inner = (i > 0) & (i < nx) & (j > 0) & (j < ny) & (k > 0) & (k < nz)
+            d = rng.uniform(-jitter, jitter, size=V.shape) / np.array([nx, ny, nz])
+            V[inner] += d[inner]
+        self.V = V
+        step = np.array([1, nx + 1, (nx + 1) * (ny + 1)])
+        ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        base = ((ck * (ny + 1) + cj) * (nx + 1) + ci).transpose(2, 1, 0).ravel()
+        tets = []
+        for perm in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+            v1 = base + step[perm[0]]
+            v2 = v1 + step[perm[1]]
+            v3 = v2 + step[perm[2]]
+            tets.append(np.stack([base, v1, v2, v3], axis=1))
+        EV = np.stack(tets, axis=1).reshape(-1, 4)  # already ascending by id along each path
+        P = V[EV]
+        det = np.einsum("ei,ei->e", P[:, 1] - P[:, 0], np.cross(P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]))
+        swap = det < 0
+        EV[swap] = EV[swap][:, [1, 0, 2, 3]]
+        self.EV = EV
+        self.swapped = swap
+        self.E = EV.shape[0]
+
+    def _map(self, x, y, z):
+        if self.curve_amp == 0.0:
+            return x, y, z
+        a = self.curve_amp
+        return (x + a * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z),
+                y + a * np.sin(2 * np.pi * z) * np.sin(2 * np.pi * x),
+                z + a * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y))
+
+    def coords(self, n):
+        """Coordinates at the (n + 1) x n x n collapsed points (GLL x Gauss-Radau alpha 1 x
+        Gauss-Radau alpha 2), shape (3, E, (n + 1) n^2), point (k n + j) (n + 1) + i."""
+        z0, z1, z2 = gll_points(n + 1), radau_points(n), radau_points(n, alpha=2.0)
+        e2, e1, e0 = np.meshgrid(z2, z1, z0, indexing="ij")
+        xi2 = e2
+        xi1 = 0.5 * (1 + e1) * (1 - e2) - 1
+        xi0 = 0.25 * (1 + e0) * (1 - e1) * (1 - e2) - 1
+        W = np.stack([-0.5 * (1 + xi0 + xi1 + xi2), 0.5 * (1 + xi0), 0.5 * (1 + xi1), 0.5 * (1 + xi2)])
+        X = np.einsum("vkji,evc->cekji", W, self.V[self.EV]).reshape(3, self.E, -1)
+        return np.stack(self._map(X[0], X[1], X[2])).copy()
+
+    def assembly(self, n):
+        """C0 numbering of the tetrahedron expansion with n modes per direction; all
+        boundary dofs Dirichlet. Vertex modes take their vertex's id; an edge mode of degree
+        k flips sign, (-1)^k, where the local edge runs against the global one (low to high
+        id); face modes are matched between the two elements of a face by their restriction
+        to it (a permutation with signs: with the sorted local vertex order both sides see
+        the same collapsed vertex); interior modes are the element's own."""
+        E, EV = self.E, self.EV
+        nv = self.V.shape[0]
+        topo, fpts, fv = _tet_local_topology(n)
+        nc = len(topo)
+        ni = max(n - 2, 0)
+        nfm = max((n - 2) * (n - 3) // 2, 0)
+        nint = max((n - 2) * (n - 3) * (n - 4) // 6, 0)
+        # global edges and faces
+        le = np.stack([np.sort(EV[:, list(e)], axis=1) for e in _TET_EDGES], axis=1).reshape(-1, 2)
+        ue, einv = np.unique(le, axis=0, return_inverse=True)
+        einv = einv.reshape(E, 6)
+        lf = np.stack([np.sort(EV[:, list(f)], axis=1) for f in _TET_FACES], axis=1).reshape(-1, 3)
+        uf, finv, fcnt = np.unique(lf, axis=0, return_inverse=True, return_counts=True)
+        finv = finv.reshape(E, 4)
+        nE, nF = ue.shape[0], uf.shape[0]
+        fbnd = fcnt == 1
+        vbnd = np.zeros(nv, dtype=bool)
+        vbnd[uf[fbnd].ravel()] = True
+        ebnd = np.zeros(nE, dtype=bool)
+        for a, b in ((0, 1), (0, 2), (1, 2)):
+            pairs = np.sort(uf[fbnd][:, [a, b]], axis=1)
+            idx = np.searchsorted(ue[:, 0] * (nv + 1) + ue[:, 1], pairs[:, 0] * (nv + 1) + pairs[:, 1])
+            ebnd[idx] = True
+        nglob = nv + nE * ni + nF * nfm + E * nint
+        is_dir = np.zeros(nglob, dtype=bool)
+        is_dir[:nv] = vbnd
+        is_dir[nv:nv + nE * ni] = np.repeat(ebnd, ni)
+        is_dir[nv + nE * ni:nv + nE * ni + nF * nfm] = np.repeat(fbnd, nfm)
+        newid, ndir = _renumber_dirichlet_first(np.arange(nglob), is_dir)
+        l2g = np.zeros((E, nc), dtype=np.int64)
+        sgn = np.ones((E, nc))
+        face_modes = {f: [m for m, t in enumerate(topo) if t[0] == "f" and t[1] == f] for f in range(4)}
+        # local face vertex order against the global (sorted) one
+        perms = np.zeros((E, 4, 3), dtype=np.int64)
+        for f, fvtx in enumerate(_TET_FACES):
+            g = EV[:, list(fvtx)]
+            perms[:, f] = np.argsort(np.argsort(g, axis=1), axis=1)
+        owner = {}
+        match_cache = {}
+        icount = np.zeros(E, dtype=np.int64)
+        for m, t in enumerate(topo):
+            if t[0] == "v":
+                l2g[:, m] = EV[:, t[1]]
+            elif t[0] == "e":
+                _, ed, k, s_loc = t
+                a, b = _TET_EDGES[ed]
+                fwd = EV[:, a] < EV[:, b]
+                l2g[:, m] = nv + einv[:, ed] * ni + (k - 2)
+                sgn[:, m] = s_loc * np.where(fwd, 1.0, (-1.0) ** k)
+            elif t[0] == "i":
+                pass
+        for e in range(E):
+            for f in range(4):
+                gf = finv[e, f]
+                key = (f, tuple(perms[e, f]))
+                if gf not in owner:
+                    owner[gf] = key
+                ref = owner[gf]
+                pair = (ref, key)
+                if pair not in match_cache:
+                    match_cache[pair] = _face_match(n, fpts, fv, topo, ref[0], ref[1], f, key[1])
+                for j, m in enumerate(face_modes[f]):
+                    a, sg = match_cache[pair][j]
+                    l2g[e, m] = nv + nE * ni + gf * nfm + a
+                    sgn[e, m] = sg
+        base = nv + nE * ni + nF * nfm
+        ints = [m for m, t in enumerate(topo) if t[0] == "i"]
+        for j, m in enumerate(ints):
+            l2g[:, m] = base + np.arange(E) * nint + j
         l2g = newid[l2g]
         return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
 

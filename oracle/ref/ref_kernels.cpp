@@ -501,6 +501,253 @@ void iprd_tri(const TriTables& t, const Geo& g, const double* in0, const double*
   }
 }
 
+// ---- tetrahedra: eModified_A (Q0 = n + 1 GLL), eModified_B (Q1 = n Gauss-Radau alpha 1),
+//      eModified_C (Q2 = n Gauss-Radau alpha 2): the default keys of
+//      SpatialDomains/MeshGraph.cpp:1683-1716 ----
+// Basis::GenBasis eModified_C (Basis.cpp:512-566): phi^c_{pqr} = phi^b_{p+q,r}, i.e. for
+// each p the ModifiedB rows from (p, 0) on, (n - p)(n - p + 1)/2 of them.
+void modC_tables(int n, int Q, const double* z, const double* D, double* C, double* DC) {
+  const int ncb = n * (n + 1) / 2;
+  std::vector<double> B((size_t)ncb * Q), DB((size_t)ncb * Q);
+  modB_tables(n, Q, z, D, B.data(), DB.data());
+  int boff = 0, off = 0;
+  for (int p = 0; p < n; ++p) {
+    const int rows = (n - p) * (n - p + 1) / 2;
+    std::copy(B.begin() + (size_t)boff * Q, B.begin() + (size_t)(boff + rows) * Q, C + (size_t)off * Q);
+    boff += n - p;
+    off += rows;
+  }
+  const int nct = n * (n + 1) * (n + 2) / 6;
+  for (int m = 0; m < nct; ++m)
+    for (int i = 0; i < Q; ++i) {
+      double s = 0;
+      for (int k = 0; k < Q; ++k) s += D[k * Q + i] * C[m * Q + k];
+      DC[m * Q + i] = s;
+    }
+}
+
+struct TetTables {
+  vvec b0, db0, D0, w0, z0, b1, db1, D1, w1, z1, b2, db2, D2, w2, z2;
+};
+
+// The MatrixFree Helper's tables (Operator.hpp:206-275): Gauss-Radau weights times 0.5
+// (alpha 1) and 0.25 (alpha 2).
+TetTables make_tet_tables(int n) {
+  const int Q0 = n + 1, Q = n, ncb = n * (n + 1) / 2, nct = n * (n + 1) * (n + 2) / 6;
+  std::vector<double> z0(Q0), w0(Q0), D0(Q0 * Q0), B0(n * Q0), DB0(n * Q0);
+  std::vector<double> z1(Q), w1(Q), D1(Q * Q), B1(ncb * Q), DB1(ncb * Q);
+  std::vector<double> z2(Q), w2(Q), D2(Q * Q), B2((size_t)nct * Q), DB2((size_t)nct * Q);
+  gll_tables(Q0, z0.data(), w0.data(), D0.data());
+  modA_tables(n, Q0, z0.data(), D0.data(), B0.data(), DB0.data());
+  radau_tables(Q, z1.data(), w1.data(), D1.data());
+  modB_tables(n, Q, z1.data(), D1.data(), B1.data(), DB1.data());
+  Polylib::zwgrjm(z2.data(), w2.data(), Q, 2.0, 0.0);  // GaussPoints.cpp eGaussRadauMAlpha2Beta0
+  Polylib::Dgrjm(D2.data(), z2.data(), Q, 2.0, 0.0);
+  modC_tables(n, Q, z2.data(), D2.data(), B2.data(), DB2.data());
+  for (double& v : w1) v *= 0.5;
+  for (double& v : w2) v *= 0.25;
+  TetTables t;
+  auto put = [](vvec& dst, const std::vector<double>& src) { dst.assign(src.begin(), src.end()); };
+  put(t.b0, B0); put(t.db0, DB0); put(t.D0, D0); put(t.w0, w0); put(t.z0, z0);
+  put(t.b1, B1); put(t.db1, DB1); put(t.D1, D1); put(t.w1, w1); put(t.z1, z1);
+  put(t.b2, B2); put(t.db2, DB2); put(t.D2, D2); put(t.w2, w2); put(t.z2, z2);
+  return t;
+}
+
+// BwdTrans / IProduct / PhysDeriv for tetrahedra (MatrixFreeOps/BwdTrans.h:1010-1045,
+// IProduct.h:1730-1770, PhysDeriv.h:990-1030), CORRECT = true.
+template <int N>
+void tet_bwd(const TetTables& t, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) * (N + 2) / 6, nq = (N + 1) * N * N;
+  vvec tin(nc), tout(nq);
+  vec_t fpq[N * N], fp[N];
+  for (int e = b0; e < b1; ++e) {
+    load_interleave(in + (size_t)e * nc * W, nc, tin);
+    BwdTransTetKernel<N, N, N, N + 1, N, N, true>(tin, t.b0, t.b1, t.b2, fpq, fp, tout);
+    deinterleave_store(tout, nq, out + (size_t)e * nq * W);
+  }
+}
+
+template <int N, bool DEF>
+void tet_iprod(const TetTables& t, const Geo& g, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) * (N + 2) / 6, nq = (N + 1) * N * N;
+  vvec tin(nq), tout(nc);
+  vec_t wsp[N * N + N];
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    IProductTetKernel<N, N, N, N + 1, N, N, true, false, false, DEF>(tin, t.b0, t.b1, t.b2, t.w0, t.w1, t.w2, jac_ptr,
+                                                                     wsp, tout);
+    deinterleave_store(tout, nc, out + (size_t)e * nc * W);
+  }
+}
+
+template <int N, bool DEF>
+void tet_deriv(const TetTables& t, const Geo& g, const double* in, double* o0, double* o1, double* o2, int b0,
+               int b1) {
+  constexpr int nq = (N + 1) * N * N, ndf = 9;
+  vvec tin(nq), d0(nq), d1(nq), d2(nq), a(nq), b(nq), c(nq);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nq : ndf)];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    PhysDerivTetKernel<N + 1, N, N, DEF>(tin, t.z0, t.z1, t.z2, t.D0, t.D1, t.D2, df_ptr, d0, d1, d2, a, b, c);
+    deinterleave_store(a, nq, o0 + (size_t)e * nq * W);
+    deinterleave_store(b, nq, o1 + (size_t)e * nq * W);
+    deinterleave_store(c, nq, o2 + (size_t)e * nq * W);
+  }
+}
+
+// ---- Helmholtz: HelmholtzTetImpl (MatrixFreeOps/Helmholtz.h:1970-2010, 2266-2448) ----
+template <int N, bool DEF>
+void helm_tet(const TetTables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N, NQ2 = N, nc = N * (N + 1) * (N + 2) / 6, nqTot = NQ0 * NQ1 * NQ2, ndf = 9;
+  std::vector<double> h0(NQ0), h1(NQ1), h2(NQ1), h3(NQ2);
+  for (int i = 0; i < NQ0; ++i) h0[i] = 0.5 * (1 + t.z0[i][0]);
+  for (int j = 0; j < NQ1; ++j) {
+    h1[j] = 0.5 * (1 + t.z1[j][0]);
+    h2[j] = 2.0 / (1 - t.z1[j][0]);
+  }
+  for (int k = 0; k < NQ2; ++k) h3[k] = 2.0 / (1 - t.z2[k][0]);
+  vec_t wsp1[NQ1 * NQ2 + NQ2], wsp2[N];
+  vvec tmpIn(nc), tmpOut(nc), bwd(nqTot), deriv0(nqTot), deriv1(nqTot), deriv2(nqTot);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in + (size_t)e * nc * W, nc, tmpIn);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    BwdTransTetKernel<N, N, N, NQ0, NQ1, NQ2, true>(tmpIn, t.b0, t.b1, t.b2, wsp1, wsp2, bwd);
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, true, false, DEF>(bwd, t.b0, t.b1, t.b2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp1, tmpOut, lambda);
+    PhysDerivTensor3DKernel<NQ0, NQ1, NQ2>(bwd, t.D0, t.D1, t.D2, deriv0, deriv1, deriv2);
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t vh3 = h3[k];
+      for (int j = 0; j < NQ1; ++j) {
+        vec_t vh1 = h1[j], vh2 = h2[j];
+        vec_t h2h3 = vh2 * vh3, h1h3 = vh1 * vh3;
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t h0h2h3 = vec_t(h0[i]) * h2h3;
+          vec_t tmp1 = h0h2h3 * (df1 + df2);
+          tmp1.fma(df0, h2h3);
+          vec_t tmp2 = h0h2h3 * (df4 + df5);
+          tmp2.fma(df3, h2h3);
+          vec_t tmp3 = h0h2h3 * (df7 + df8);
+          tmp3.fma(df6, h2h3);
+          vec_t g0 = tmp1 * tmp1;
+          g0.fma(tmp2, tmp2);
+          g0.fma(tmp3, tmp3);
+          vec_t g4 = df2 * tmp1;
+          g4.fma(df5, tmp2);
+          g4.fma(df8, tmp3);
+          vec_t tmp4 = df1 * vh3;
+          tmp4.fma(df2, h1h3);
+          vec_t tmp5 = df4 * vh3;
+          tmp5.fma(df5, h1h3);
+          vec_t tmp6 = df7 * vh3;
+          tmp6.fma(df8, h1h3);
+          vec_t g3 = tmp1 * tmp4;
+          g3.fma(tmp2, tmp5);
+          g3.fma(tmp3, tmp6);
+          vec_t g1 = tmp4 * tmp4;
+          g1.fma(tmp5, tmp5);
+          g1.fma(tmp6, tmp6);
+          vec_t g5 = df2 * tmp4;
+          g5.fma(df5, tmp5);
+          g5.fma(df8, tmp6);
+          vec_t g2 = df2 * df2;
+          g2.fma(df5, df5);
+          g2.fma(df8, df8);
+          vec_t d0 = deriv0[cnt], d1 = deriv1[cnt], d2 = deriv2[cnt];
+          tmp1 = g0 * d0;
+          tmp1.fma(g3, d1);
+          tmp1.fma(g4, d2);
+          deriv0[cnt] = tmp1;
+          tmp2 = g3 * d0;
+          tmp2.fma(g1, d1);
+          tmp2.fma(g5, d2);
+          deriv1[cnt] = tmp2;
+          tmp3 = g4 * d0;
+          tmp3.fma(g5, d1);
+          tmp3.fma(g2, d2);
+          deriv2[cnt] = tmp3;
+        }
+      }
+    }
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv0, t.db0, t.b1, t.b2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp1, tmpOut);
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv1, t.b0, t.db1, t.b2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp1, tmpOut);
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv2, t.b0, t.b1, t.db2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp1, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
+// ---- IProductWRTDerivBaseTetImpl (MatrixFreeOps/IProductWRTDerivBase.h:2212-2630) ----
+template <int N, bool DEF>
+void iprd_tet(const TetTables& t, const Geo& g, const double* in0, const double* in1, const double* in2, double* out,
+              int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N, NQ2 = N, nc = N * (N + 1) * (N + 2) / 6, nqTot = NQ0 * NQ1 * NQ2, ndf = 9;
+  vec_t wsp[NQ1 * NQ2 + NQ2];
+  vvec tI0v(nqTot), tI1v(nqTot), tI2v(nqTot), tmp0(nqTot), tmp1(nqTot), tmp2(nqTot), tmpOut(nc);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in0 + (size_t)e * nqTot * W, nqTot, tI0v);
+    load_interleave(in1 + (size_t)e * nqTot * W, nqTot, tI1v);
+    load_interleave(in2 + (size_t)e * nqTot * W, nqTot, tI2v);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t f2 = 2.0 / (1.0 - t.z2[k]);
+      for (int j = 0; j < NQ1; ++j) {
+        vec_t z1l = t.z1[j];
+        vec_t f3 = 0.5 * (1.0 + z1l);
+        vec_t f0 = 2.0 * f2 / (1.0 - z1l);
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t a = tI0v[cnt], b = tI1v[cnt], c = tI2v[cnt];
+          vec_t t0 = df0 * a + df3 * b + df6 * c;
+          vec_t t1 = df1 * a + df4 * b + df7 * c;
+          vec_t t2 = df2 * a + df5 * b + df8 * c;
+          vec_t f1 = 0.5 * (1.0 + t.z0[i]);
+          t0.fma(t1 + t2, f1);
+          t0 *= f0;
+          t1.fma(t2, f3);
+          t1 *= f2;
+          tmp0[cnt] = t0;
+          tmp1[cnt] = t1;
+          tmp2[cnt] = t2;
+        }
+      }
+    }
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, false, DEF>(tmp0, t.db0, t.b1, t.b2, t.w0, t.w1, t.w2,
+                                                                      jac_ptr, wsp, tmpOut);
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp1, t.b0, t.db1, t.b2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp, tmpOut);
+    IProductTetKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp2, t.b0, t.b1, t.db2, t.w0, t.w1, t.w2,
+                                                                     jac_ptr, wsp, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
 // Runs CALL(N) for N in 2..10 (triangles: Q0 = N + 1, Q1 = N).
 #define TRI_DISPATCH(n, CALL)   \
   switch (n) {                  \
@@ -787,6 +1034,95 @@ int ref_tri_iproduct_deriv(int n, int E, const double* jac, const double* df, in
   parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
     if (deformed) iprd_tri<NN, true>(t, g, in0, in1, out, b0, b1);             \
     else iprd_tri<NN, false>(t, g, in0, in1, out, b0, b1);                     \
+  })
+  TRI_DISPATCH(n, TP)
+#undef TP
+}
+
+// ---- tetrahedra ----
+// Tables as the reference's Basis objects hold them (weights without the collapsed factors).
+int ref_tet_tables(int n, double* z0, double* w0, double* D0, double* B0, double* DB0, double* z1, double* w1,
+                   double* D1, double* B1, double* DB1, double* z2, double* w2, double* D2, double* B2, double* DB2) {
+  const int Q0 = n + 1, Q = n;
+  gll_tables(Q0, z0, w0, D0);
+  modA_tables(n, Q0, z0, D0, B0, DB0);
+  radau_tables(Q, z1, w1, D1);
+  modB_tables(n, Q, z1, D1, B1, DB1);
+  Polylib::zwgrjm(z2, w2, Q, 2.0, 0.0);
+  Polylib::Dgrjm(D2, z2, Q, 2.0, 0.0);
+  modC_tables(n, Q, z2, D2, B2, DB2);
+  return 0;
+}
+
+int ref_tet_bwdtrans(int n, int E, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  TetTables t = make_tet_tables(n);
+  const int nb = E / W;
+#define TB(NN) parallel_blocks(nb, nthreads, [&](int b0, int b1) { tet_bwd<NN>(t, in, out, b0, b1); })
+  TRI_DISPATCH(n, TB)
+#undef TB
+}
+
+int ref_tet_iproduct(int n, int E, const double* jac, int deformed, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n * n;
+  TetTables t = make_tet_tables(n);
+  std::vector<double> dfz((size_t)9 * E * (deformed ? nq : 1), 0.0);
+  Geo g = interleave(3, nq, E, E, jac, dfz.data(), deformed != 0);
+  const int nb = E / W;
+#define TI(NN)                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {            \
+    if (deformed) tet_iprod<NN, true>(t, g, in, out, b0, b1);    \
+    else tet_iprod<NN, false>(t, g, in, out, b0, b1);            \
+  })
+  TRI_DISPATCH(n, TI)
+#undef TI
+}
+
+int ref_tet_physderiv(int n, int E, const double* df, int deformed, const double* in, double* o0, double* o1,
+                      double* o2, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n * n;
+  TetTables t = make_tet_tables(n);
+  std::vector<double> jz((size_t)E * (deformed ? nq : 1), 1.0);
+  Geo g = interleave(3, nq, E, E, jz.data(), df, deformed != 0);
+  const int nb = E / W;
+#define TD(NN)                                                            \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                     \
+    if (deformed) tet_deriv<NN, true>(t, g, in, o0, o1, o2, b0, b1);      \
+    else tet_deriv<NN, false>(t, g, in, o0, o1, o2, b0, b1);              \
+  })
+  TRI_DISPATCH(n, TD)
+#undef TD
+}
+
+int ref_tet_helmholtz(int n, int E, const double* jac, const double* df, int deformed, double lambda,
+                      const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n * n;
+  TetTables t = make_tet_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define TH(NN)                                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
+    if (deformed) helm_tet<NN, true>(t, g, lambda, in, out, b0, b1);           \
+    else helm_tet<NN, false>(t, g, lambda, in, out, b0, b1);                   \
+  })
+  TRI_DISPATCH(n, TH)
+#undef TH
+}
+
+int ref_tet_iproduct_deriv(int n, int E, const double* jac, const double* df, int deformed, const double* in0,
+                           const double* in1, const double* in2, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * n * n;
+  TetTables t = make_tet_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define TP(NN)                                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                            \
+    if (deformed) iprd_tet<NN, true>(t, g, in0, in1, in2, out, b0, b1);          \
+    else iprd_tet<NN, false>(t, g, in0, in1, in2, out, b0, b1);                  \
   })
   TRI_DISPATCH(n, TP)
 #undef TP

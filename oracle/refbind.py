@@ -156,3 +156,51 @@ def tri_iproduct_deriv(n, E, jac, df, deformed, in0, in1, nthreads=1):
     _check(lib().ref_tri_iproduct_deriv(n, E, f(jac), f(df), int(deformed), f(in0), f(in1), _p(out), nthreads),
            "ref_tri_iproduct_deriv")
     return out
+
+
+# ---- tetrahedra (ref_tet_* drivers) ----
+def tet_tables(n):
+    Q0, Q, ncb, nct = n + 1, n, n * (n + 1) // 2, n * (n + 1) * (n + 2) // 6
+    a = [np.zeros(Q0), np.zeros(Q0), np.zeros(Q0 * Q0), np.zeros(n * Q0), np.zeros(n * Q0)]
+    b = [np.zeros(Q), np.zeros(Q), np.zeros(Q * Q), np.zeros(ncb * Q), np.zeros(ncb * Q)]
+    c = [np.zeros(Q), np.zeros(Q), np.zeros(Q * Q), np.zeros(nct * Q), np.zeros(nct * Q)]
+    _check(lib().ref_tet_tables(n, *[_p(x) for x in a + b + c]), "ref_tet_tables")
+    return a, b, c
+
+
+def _f(a):
+    return _p(np.ascontiguousarray(a, dtype=np.float64))
+
+
+def tet_bwdtrans(n, E, coeffs, nthreads=1):
+    out = np.zeros(E * (n + 1) * n * n)
+    _check(lib().ref_tet_bwdtrans(n, E, _f(coeffs), _p(out), nthreads), "ref_tet_bwdtrans")
+    return out
+
+
+def tet_iproduct(n, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (n + 2) // 6)
+    _check(lib().ref_tet_iproduct(n, E, _f(jac), int(deformed), _f(phys), _p(out), nthreads), "ref_tet_iproduct")
+    return out
+
+
+def tet_physderiv(n, E, df, deformed, phys, nthreads=1):
+    nq = (n + 1) * n * n
+    o = [np.zeros(E * nq) for _ in range(3)]
+    _check(lib().ref_tet_physderiv(n, E, _f(df), int(deformed), _f(phys), *[_p(x) for x in o], nthreads),
+           "ref_tet_physderiv")
+    return o
+
+
+def tet_helmholtz(n, E, jac, df, deformed, lam, coeffs, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (n + 2) // 6)
+    _check(lib().ref_tet_helmholtz(n, E, _f(jac), _f(df), int(deformed), ctypes.c_double(lam), _f(coeffs),
+                                   _p(out), nthreads), "ref_tet_helmholtz")
+    return out
+
+
+def tet_iproduct_deriv(n, E, jac, df, deformed, in0, in1, in2, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (n + 2) // 6)
+    _check(lib().ref_tet_iproduct_deriv(n, E, _f(jac), _f(df), int(deformed), _f(in0), _f(in1), _f(in2), _p(out),
+                                        nthreads), "ref_tet_iproduct_deriv")
+    return out

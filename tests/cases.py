@@ -1,9 +1,10 @@
 """Seeded test cases shared by the CPU and GPU tests (small sizes the oracle runs in seconds)."""
 import numpy as np
 
-from ithaca_gpu.mesh import HexMesh, QuadMesh, TriMesh
+from ithaca_gpu.mesh import HexMesh, QuadMesh, TetMesh, TriMesh
 from oracle import basis as obasis
 from oracle import geom as ogeom
+from oracle import tet as otet
 from oracle import tri as otri
 
 
@@ -66,6 +67,25 @@ def tri_case(nx, ny, n, jitter=0.15, seed=3, curve=0.05, deformed=True):
         c.jac, c.df = jac.reshape(-1).copy(), df.copy()
     else:
         c.jac, c.df = otri.straight_tri_geometry(c.mesh.V[c.mesh.EV])
+    c.nm, c.nq = c.basis.nc, c.basis.nq
+    return c
+
+
+def tet_case(nx, ny, nz, n, jitter=0.2, seed=3, curve=0.03, deformed=True):
+    """TetMesh of 6 nx ny nz tetrahedra, n modes; deformed: curved with per-point geometry
+    from the oracle's GeomFactors, else straight and per element."""
+    c = Case()
+    c.dim, c.shape, c.n, c.Q = 3, "tet", n, n + 1
+    c.mesh = TetMesh(nx, ny, nz, jitter=jitter, seed=seed, curve_amp=curve if deformed else 0.0)
+    c.E = c.mesh.E
+    c.X = c.mesh.coords(n)
+    c.basis = otet.TetBasis(n)
+    c.deformed = deformed
+    if deformed:
+        jac, df = otet.geom_factors(c.basis, c.X)
+        c.jac, c.df = jac.reshape(-1).copy(), df.copy()
+    else:
+        c.jac, c.df = otet.straight_tet_geometry(c.mesh.V[c.mesh.EV])
     c.nm, c.nq = c.basis.nc, c.basis.nq
     return c
 
