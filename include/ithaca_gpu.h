@@ -42,7 +42,13 @@ enum {
 };
 
 /* LibUtilities::ShapeType values of the supported shapes (LibUtilities/BasicUtils/ShapeType.hpp). */
-enum { ITHACA_GPU_SHAPE_TRI = 3, ITHACA_GPU_SHAPE_QUAD = 4, ITHACA_GPU_SHAPE_TET = 5, ITHACA_GPU_SHAPE_HEX = 8 };
+enum {
+  ITHACA_GPU_SHAPE_TRI = 3,
+  ITHACA_GPU_SHAPE_QUAD = 4,
+  ITHACA_GPU_SHAPE_TET = 5,
+  ITHACA_GPU_SHAPE_PRISM = 7,
+  ITHACA_GPU_SHAPE_HEX = 8
+};
 
 /* Arithmetic of an element operator. */
 enum { ITHACA_GPU_FP64 = 0, ITHACA_GPU_FP32 = 1 };
@@ -110,7 +116,8 @@ int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double*
  * the derivatives are taken in collapsed coordinates and mapped by the chain rule of
  * StdTriExp::v_PhysDeriv. Tetrahedra (shape 5): npoints = Q0, coordinates at the
  * Q0 x (Q0-1) x (Q0-1) collapsed points (point (k Q1 + j) Q0 + i), 3 arrays; chain rule of
- * StdTetExp::v_PhysDeriv. */
+ * StdTetExp::v_PhysDeriv. Prisms (shape 7): npoints = Q0, coordinates at the Q0 x Q0 x
+ * (Q0-1) points (point (k Q0 + j) Q0 + i), chain rule of StdPrismExp::v_PhysDeriv. */
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device);
 
@@ -129,12 +136,18 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
  * ithaca_gpu_basis_tet, nmodes (nmodes+1) (nmodes+2) / 6 coefficients and Q0 (Q0-1)^2 points
  * per element, geometry (d = 3) per point or per element (MatrixFreeOps/Helmholtz.h:
  * 1970-2010, 2266-2448; BwdTrans.h:1010-1045; IProduct.h:1730-1770; PhysDeriv.h:990-1030;
- * IProductWRTDerivBase.h:2212-2630); the library keeps their metric per point either way. */
+ * IProductWRTDerivBase.h:2212-2630); the library keeps their metric per point either way.
+ * Prisms (shape 7): eModified_A on Q0 = nmodes + 1 GLL points in directions 0 and 1,
+ * eModified_B (rows (p, r), the triangle's direction 1 of ithaca_gpu_basis_tri) on nmodes
+ * Gauss-Radau points in direction 2; nmodes^2 (nmodes+1) / 2 coefficients and Q0^2 (Q0-1)
+ * points per element, modes m(p, q, r) with r fastest and r < nmodes - p
+ * (MatrixFreeOps/Helmholtz.h:1003-1030, 1291-1440; IProductWRTDerivBase.h:1660-1760). */
 int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
                          const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op);
 int ithaca_gpu_op_destroy(ithaca_gpu_op* op);
 /* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282); nelmt * nmodes (nmodes+1)/2
- * for triangles, nelmt * nmodes (nmodes+1) (nmodes+2)/6 for tetrahedra. */
+ * for triangles, nelmt * nmodes (nmodes+1) (nmodes+2)/6 for tetrahedra, nelmt * nmodes^2 (nmodes+1)/2
+ * for prisms. */
 int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof);
 
 /* BwdTrans (Collections/BwdTrans.cpp:143-240): coefficients -> physical values. */

@@ -1,7 +1,7 @@
 // Implementation type "GPU" for the Collections operators (Collections/Operator.h:113-165,
 // registrations as Collections/Helmholtz.cpp:484-503): BwdTrans, IProductWRTBase,
-// PhysDeriv, IProductWRTDerivBase and Helmholtz of triangular, quadrilateral and
-// hexahedral collections run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
+// PhysDeriv, IProductWRTDerivBase and Helmholtz of triangular, quadrilateral,
+// tetrahedral, prismatic and hexahedral collections run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
 // keeps the reference's element-contiguous layouts and CoalescedGeomData's geometry.
 #include <Collections/Operator.h>
 
@@ -20,8 +20,9 @@ class GpuOperatorBase : public Operator {
       : Operator(pCollExp, pGeomData) {
     const auto shape = pCollExp[0]->DetShapeType();
     if (shape != LibUtilities::eTriangle && shape != LibUtilities::eQuadrilateral &&
-        shape != LibUtilities::eHexahedron)
-      NEKERROR(ErrorUtil::efatal, "GPU operators are built for triangles, quadrilaterals and hexahedra");
+        shape != LibUtilities::eTetrahedron && shape != LibUtilities::ePrism && shape != LibUtilities::eHexahedron)
+      NEKERROR(ErrorUtil::efatal, "GPU operators are built for triangles, quadrilaterals, tetrahedra, prisms and "
+                                  "hexahedra");
     const int nm = pCollExp[0]->GetBasis(0)->GetNumModes();
     const int nq = pCollExp[0]->GetBasis(0)->GetNumPoints();
     const Array<OneD, const NekDouble>& jac = pGeomData->GetJac(pCollExp);
@@ -29,7 +30,7 @@ class GpuOperatorBase : public Operator {
     Check(ithaca_gpu_op_create(GpuAdapter::GpuContext(), (int)shape, nm, nq, (int)m_numElmt, jac.get(), df.get(),
                                m_isDeformed ? 1 : 0, ITHACA_GPU_FP64, 0, &m_op));
     GpuAdapter::OperatorRegistry()[pCollExp[0].get()] = m_op;
-    m_dim = shape == LibUtilities::eHexahedron ? 3 : 2;
+    m_dim = shape == LibUtilities::eTriangle || shape == LibUtilities::eQuadrilateral ? 2 : 3;
   }
   ~GpuOperatorBase() override {
     if (m_op) ithaca_gpu_op_destroy(m_op);
@@ -116,6 +117,10 @@ class Helmholtz_GPU final : public GpuOperatorBase {
                                                    cls::create, name "_Tri"),                                  \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eQuadrilateral, op, eGPU, false), \
                                                    cls::create, name "_Quad"),                                 \
+      GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eTetrahedron, op, eGPU, false),   \
+                                                   cls::create, name "_Tet"),                                  \
+      GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::ePrism, op, eGPU, false),         \
+                                                   cls::create, name "_Prism"),                                \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eHexahedron, op, eGPU, false),    \
                                                    cls::create, name "_Hex")};
 

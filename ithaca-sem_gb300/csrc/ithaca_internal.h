@@ -116,11 +116,38 @@ inline __host__ __device__ constexpr TetOff tet_off(int n) {
   return o;
 }
 
+// Packed device tables of a prism expansion (Q0 = n + 1 for directions 0 and 1, Q2 = n):
+//   B0 [p*Q0+i] D0 [k*Q0+i] w0 [i] h0 [i] = (1+z0_i)/2 (directions 0 and 1 share them)
+//   B2 [pr*Q2+k] (ModifiedB rows (p, r)) D2 [l*Q2+k] w2 [k] = w2_k/2 h1 [k] = 2/(1-z2_k)
+//   then DB0, DB2 (diagonal kernel only; `core` ends before them)
+struct PrismOff {
+  int B0, D0, w0, h0, B2, D2, w2, h1, DB0, DB2, core, size;
+};
+inline __host__ __device__ constexpr int prism_nc(int n) { return n * n * (n + 1) / 2; }
+inline __host__ __device__ constexpr PrismOff prism_off(int n) {
+  const int Q0 = n + 1, Q2 = n, npr = n * (n + 1) / 2;
+  PrismOff o{};
+  o.B0 = 0;
+  o.D0 = o.B0 + n * Q0;
+  o.w0 = o.D0 + Q0 * Q0;
+  o.h0 = o.w0 + Q0;
+  o.B2 = o.h0 + Q0;
+  o.D2 = o.B2 + npr * Q2;
+  o.w2 = o.D2 + Q2 * Q2;
+  o.h1 = o.w2 + Q2;
+  o.core = o.h1 + Q2;
+  o.DB0 = o.core;
+  o.DB2 = o.DB0 + n * Q0;
+  o.size = o.DB2 + npr * Q2;
+  return o;
+}
+
 // Kernel family passed where the launchers below take `dim`: 2 (quads), 3 (hexes),
-// kTriKernels (triangles; their geometry has the 2-D layout) or kTetKernels
-// (tetrahedra; per-point geometry with the 3-D layout, 7 fields).
+// kTriKernels (triangles; their geometry has the 2-D layout), kTetKernels and
+// kPrismKernels (tetrahedra and prisms; per-point geometry with the 3-D layout, 7 fields).
 constexpr int kTriKernels = 23;
 constexpr int kTetKernels = 33;
+constexpr int kPrismKernels = 34;
 
 // Device copy of the 1-D tables for one (n, Q), packed for the kernels:
 //   B  [p*Q + i]   Bt  [i*n + p]   DB [p*Q + i]   DBt [i*n + p]
@@ -295,6 +322,20 @@ struct TetApi {
                    const T* in2, T* out, cudaStream_t s);
 };
 
+// Prisms (elem_prism.cuh); geometry always per point. The same entry points as TetApi.
+template <typename T>
+struct PrismApi {
+  static bool helm(int n, int Q, int E, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g,
+                   int ndir, const int* skip, const T* lam_ptr, cudaStream_t s);
+  static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
+  static bool ipr(int n, int Q, int E, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
+  static bool deriv(int n, int Q, int E, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
+                    cudaStream_t s);
+  static bool diag(int n, int Q, int E, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+  static bool iprd(int n, int Q, int E, const T* tab, const T* jg, const T* df, const T* in0, const T* in1,
+                   const T* in2, T* out, cudaStream_t s);
+};
+
 template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
@@ -305,6 +346,8 @@ inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T
                            skip_stride, s);
   if (dim == kTetKernels) return esolve == nullptr && TetApi<T>::helm(n, Q, E, tab, jg, lambda, in, out, l2g, ndir,
                                                                       skip, lam_ptr, s);
+  if (dim == kPrismKernels)
+    return esolve == nullptr && PrismApi<T>::helm(n, Q, E, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);
   return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
                                         esolve, skip_stride, s, variant)
                   : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
@@ -314,6 +357,7 @@ template <typename T>
 inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::bwd(n, Q, E, tab, in, out, s);
   if (dim == kTetKernels) return TetApi<T>::bwd(n, Q, E, tab, in, out, s);
+  if (dim == kPrismKernels) return PrismApi<T>::bwd(n, Q, E, tab, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::bwd(n, Q, E, tab, in, out, s) : ElemApi<T, 3>::bwd(n, Q, E, tab, in, out, s);
 }
 template <typename T>
@@ -321,6 +365,7 @@ inline bool launch_iproduct(int dim, int n, int Q, int E, int deformed, const T*
                             T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
   if (dim == kTetKernels) return TetApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
+  if (dim == kPrismKernels) return PrismApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::ipr(n, Q, E, deformed, tab, jg, in, out, s)
                   : ElemApi<T, 3>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
 }
@@ -329,6 +374,7 @@ inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T
                              T* d0, T* d1, T* d2, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, s);
   if (dim == kTetKernels) return TetApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
+  if (dim == kPrismKernels) return PrismApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
   return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
                   : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
 }
@@ -337,6 +383,7 @@ inline bool launch_iproduct_deriv(int dim, int n, int Q, int E, int deformed, co
                                   const T* in0, const T* in1, const T* in2, T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, out, s);
   if (dim == kTetKernels) return TetApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
+  if (dim == kPrismKernels) return PrismApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
   return dim == 2 ? ElemApi<T, 2>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s)
                   : ElemApi<T, 3>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s);
 }
@@ -345,6 +392,7 @@ inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T
                              T* out, cudaStream_t s) {
   if (dim == kTriKernels) return TriApi<T>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
   if (dim == kTetKernels) return TetApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
+  if (dim == kPrismKernels) return PrismApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
   return dim == 2 ? ElemApi<T, 2>::diag(n, Q, E, deformed, tab, jg, lambda, out, s)
                   : ElemApi<T, 3>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
 }
@@ -372,5 +420,12 @@ void launch_build_jg_tet(int n, int E, int deformed, const double* tab, const do
                          T* dfo, cudaStream_t s);
 void launch_geom_factors_tet(int n, int E, const double* tab, const double* coords, double* jac, double* df,
                              int* bad, cudaStream_t s);
+// Prisms: per point J w0 w0 w2/2 and J w m^{ab} with the collapsed metric of
+// HelmholtzPrismImpl (MatrixFreeOps/Helmholtz.h:1340-1400).
+template <typename T>
+void launch_build_jg_prism(int n, int E, int deformed, const double* tab, const double* jac, const double* df,
+                           T* jg, T* dfo, cudaStream_t s);
+void launch_geom_factors_prism(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                               int* bad, cudaStream_t s);
 
 }  // namespace ithaca

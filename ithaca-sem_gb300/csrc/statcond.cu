@@ -576,6 +576,17 @@ int ithaca_gpu_sc_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     const int dim = op->dim, n = op->n, nm = op->nm, E = op->E;
     std::vector<int> bm, im;
     for (int m = 0, tp = 0, tq = 0; m < nm; ++m) {
+      if (op->shape == ITHACA_GPU_SHAPE_PRISM) {
+        // prism mode m(p, q, r): interior when p >= 2, q >= 2 and r >= 1
+        int pp = 0, rest = m;
+        while (rest >= n * (n - pp)) {
+          rest -= n * (n - pp);
+          ++pp;
+        }
+        const int qq = rest / (n - pp), rr = rest % (n - pp);
+        (pp >= 2 && qq >= 2 && rr >= 1 ? im : bm).push_back(m);
+        continue;
+      }
       if (op->shape == ITHACA_GPU_SHAPE_TET) {
         // tetrahedron mode m(p, q, r): interior when p >= 2, q >= 1 and r >= 1
         int tp_ = 0, rest = m;

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(ROOT, "lib", "libithaca_gpu.so")
 OK = 0
 ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM = 1, 2, 3, 4
 ERR_NOT_CONVERGED, ERR_GEOMETRY, ERR_TIMEOUT, ERR_NUMERIC = 5, 6, 7, 8
-SHAPE_TRI, SHAPE_QUAD, SHAPE_TET, SHAPE_HEX = 3, 4, 5, 8
+SHAPE_TRI, SHAPE_QUAD, SHAPE_TET, SHAPE_PRISM, SHAPE_HEX = 3, 4, 5, 7, 8
 FP64, FP32 = 0, 1
 SOLVE_FP64, SOLVE_MIXED_FP32, SOLVE_MIXED_FP32_GEO16 = 0, 1, 2
 

@@ -18,11 +18,16 @@ so this module generates them directly:
 * ``TetMesh``   -- nx x ny x nz cubes of the unit cube, each split into the six Kuhn
   tetrahedra v, v + e_a, v + e_a + e_b, v + e_a + e_b + e_c along the permutations (a, b, c)
   of the axes (a conforming triangulation); interior vertices optionally jittered, the map
-  optionally curved as HexMesh's. Local vertices are sorted by global id and, where that
+  optionally curved by (x, y, z) + amp sin(pi x) sin(pi y) sin(pi z) (1, -1/2, 1/4), which
+  fixes the cube's boundary. Local vertices are sorted by global id and, where that
   order is negatively oriented, v0 and v1 are exchanged, so that the collapsed vertex of
   every triangular face is its highest-id vertex in both elements sharing it (the
   orientation rule for collapsed simplex faces); x = v0 + (v1 - v0)(1 + xi0)/2 +
   (v2 - v0)(1 + xi1)/2 + (v3 - v0)(1 + xi2)/2 (SpatialDomains/TetGeom.cpp).
+* ``PrismMesh`` -- nx x ny x nz cubes of the unit cube, each split into two prisms
+  extruded along y over the triangles (c000, c100, c001) and (c101, c001, c100) of its
+  xz-face (StdPrismExp vertex order: v0 v1 v4 at the lower y, v3 v2 v5 above them, the
+  singular edge v4-v5 along y); jitter and curvature as TetMesh.
 * ``HexMesh``   -- nx x ny x nz hexahedra of the unit cube, optionally curved by
   x_a + amp * sin(2 pi x_b) sin(2 pi x_c) applied cyclically (a, b, c) =
   (0, 1, 2), (1, 2, 0), (2, 0, 1) to the straight positions.
@@ -339,82 +344,210 @@ def tet_modal(n, xi0, xi1, xi2):
 _TET_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
 _TET_FACES = ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))
 _TET_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
+# prism (StdPrismExp): vertices, edges, faces (quads in cyclic order); the singular edge is 4-5
+_PRISM_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [-1, 1, 1]])
+_PRISM_EDGES = ((0, 1), (1, 2), (3, 2), (0, 3), (0, 4), (1, 4), (2, 5), (3, 5), (4, 5))
+_PRISM_FACES = ((0, 1, 2, 3), (0, 1, 4), (1, 2, 5, 4), (3, 2, 5), (0, 3, 5, 4))
 
 
-def _bary_to_xi(lam, verts):
-    """Reference coordinates of the point sum_v lam_v xi(v) for local vertex indices."""
-    return sum(l[..., None] * _TET_XI[v] for l, v in zip(lam, verts))
+def prism_modal(n, xi0, xi1, xi2):
+    """Values of the prism's modes m(p, q, r) (r fastest, r < n - p) at reference points
+    with xi2 < 1: (npts, nc); the singular-edge modes (0, q, 1) carry no eta0 factor."""
+    xi0, xi1, xi2 = (np.asarray(a, dtype=np.float64) for a in (xi0, xi1, xi2))
+    e0 = 2 * (1 + xi0) / (1 - xi2) - 1
+    cols = []
+    for p in range(n):
+        for q in range(n):
+            for r in range(n - p):
+                a = 1.0 if (p == 0 and r == 1) else _modA(p, e0)
+                cols.append(a * _modA(q, xi1) * _modB(p, r, xi2))
+    return np.stack(np.broadcast_arrays(*cols), axis=-1)
 
 
-def _tet_local_topology(n):
-    """Per local mode: ('v', vertex), ('e', edge, degree, sign along the local edge) or
-    ('f', face, restriction samples) or ('i',), found by evaluating the modes (a mode
-    belongs to the lowest-dimensional entity on which it does not vanish)."""
-    eps = 1e-9
-    cen = _TET_XI.mean(axis=0)
-    pull = lambda x: (1 - eps) * x + eps * cen
+def _face_points(nv):
+    """Sample parameters on a face: barycentric (3 rows) for triangles, (s, t) for quads."""
+    if nv == 3:
+        g = np.array([(a, b) for a in np.linspace(0.1, 0.8, 5) for b in np.linspace(0.1, 0.8, 5) if a + b < 0.95])
+        return np.stack([1 - g[:, 0] - g[:, 1], g[:, 0], g[:, 1]])
+    s = np.linspace(0.1, 0.9, 5)
+    S, T = np.meshgrid(s, s, indexing="ij")
+    return np.stack([S.ravel(), T.ravel()])
+
+
+def _face_xi(ref_xi, fverts, frame, pts):
+    """Reference coordinates of the sample points of a face seen in `frame` (local vertex
+    indices: the triangle's vertices, or the quad's origin, first-axis and second-axis
+    neighbours and opposite vertex)."""
+    if len(fverts) == 3:
+        return sum(pts[c][..., None] * ref_xi[frame[c]] for c in range(3))
+    o, a, b, d = (ref_xi[v] for v in frame)
+    s, t = pts[0][..., None], pts[1][..., None]
+    return (1 - s) * (1 - t) * o + s * (1 - t) * a + (1 - s) * t * b + s * t * d
+
+
+def _local_topology(n, modal, ref_xi, edges, faces):
+    """Per local mode: ('v', vertex), ('e', edge, degree, sign along the local edge),
+    ('f', face) or ('i',), found by evaluating the modes: a mode belongs to the
+    lowest-dimensional entity on which it does not vanish (points are pulled 1e-9 towards
+    the centroid to stay off the collapsed vertices and edges)."""
+    cen = ref_xi.mean(axis=0)
 
     def vals(xi):
-        xi = pull(np.asarray(xi, dtype=np.float64))
-        return tet_modal(n, xi[..., 0], xi[..., 1], xi[..., 2])
-    nc = n * (n + 1) * (n + 2) // 6
+        xi = (1 - 1e-9) * np.asarray(xi, dtype=np.float64) + 1e-9 * cen
+        return modal(n, xi[..., 0], xi[..., 1], xi[..., 2])
     s = np.linspace(-0.8, 0.8, n + 3)
-    vv = vals(_TET_XI)                                   # (4, nc)
-    ev = [vals(_bary_to_xi(((1 - s) / 2, (1 + s) / 2), e)) for e in _TET_EDGES]   # (ns, nc) each
-    g = np.array([(a, b) for a in np.linspace(0.1, 0.8, 5) for b in np.linspace(0.1, 0.8, 5) if a + b < 0.95])
-    fpts = (1 - g[:, 0] - g[:, 1], g[:, 0], g[:, 1])
-    fv = [vals(_bary_to_xi(fpts, f)) for f in _TET_FACES]
+    vv = vals(ref_xi)
+    ev = [vals(((1 - s) / 2)[:, None] * ref_xi[a] + ((1 + s) / 2)[:, None] * ref_xi[b]) for a, b in edges]
+    fv = []
+    for f in faces:
+        frame = f if len(f) == 3 else (f[0], f[1], f[3], f[2])
+        fv.append(vals(_face_xi(ref_xi, f, frame, _face_points(len(f)))))
     tol = 1e-6
     one_d = np.stack([_modA(k, s) for k in range(2, n)]) if n > 2 else np.zeros((0, s.size))
     topo = []
-    for m in range(nc):
+    for m in range(vv.shape[1]):
         on_v = np.flatnonzero(np.abs(vv[:, m]) > tol)
         if on_v.size:
-            assert on_v.size == 1
+            assert on_v.size == 1, "a vertex mode is non-zero at one vertex"
             topo.append(("v", int(on_v[0])))
             continue
-        on_e = [k for k in range(6) if np.max(np.abs(ev[k][:, m])) > tol]
+        on_e = [k for k in range(len(edges)) if np.max(np.abs(ev[k][:, m])) > tol]
         if on_e:
-            assert len(on_e) == 1
+            assert len(on_e) == 1, "an edge mode lives on one edge"
             f = ev[on_e[0]][:, m]
             coef = one_d @ f / np.sum(one_d * one_d, axis=1)
             k = int(np.argmax(np.abs(coef)))
             assert np.max(np.abs(f - coef[k] * one_d[k])) < 1e-6 and abs(abs(coef[k]) - 1) < 1e-6
             topo.append(("e", on_e[0], k + 2, float(np.sign(coef[k]))))
             continue
-        on_f = [k for k in range(4) if np.max(np.abs(fv[k][:, m])) > tol]
+        on_f = [k for k in range(len(faces)) if np.max(np.abs(fv[k][:, m])) > tol]
         if on_f:
-            assert len(on_f) == 1
+            assert len(on_f) == 1, "a face mode lives on one face"
             topo.append(("f", on_f[0]))
             continue
         topo.append(("i",))
-    return topo, fpts, fv
+    return topo
 
 
-def _face_match(n, fpts, fv, topo, f1, perm1, f2, perm2):
-    """Face modes of local face f2 (vertices seen in order perm2) against those of f1
-    (order perm1) on the same physical face: list of (index into f1's face modes, sign)."""
-    def face_vals(f, perm):
-        # canonical points: barycentric in the face's global order; local order = perm
-        lam = [None] * 3
-        for c, l in zip(perm, fpts):
-            lam[c] = l
-        xi = _bary_to_xi(lam, _TET_FACES[f])
-        xi = (1 - 1e-9) * xi + 1e-9 * _TET_XI.mean(axis=0)
-        v = tet_modal(n, xi[..., 0], xi[..., 1], xi[..., 2])
-        ms = [m for m, t in enumerate(topo) if t[0] == "f" and t[1] == f]
-        return v[:, ms]
-    A, B = face_vals(f1, perm1), face_vals(f2, perm2)
-    out = []
-    for b in range(B.shape[1]):
-        hit = None
-        for a in range(A.shape[1]):
-            for sg in (1.0, -1.0):
-                if np.max(np.abs(B[:, b] - sg * A[:, a])) < 1e-8:
-                    hit = (a, sg)
-        assert hit is not None, "face modes do not match across the shared face"
-        out.append(hit)
-    return out
+def _canonical_frame(fverts, gids):
+    """Local vertex indices of a face in the global frame: triangles by increasing global
+    id; quads from the lowest-id vertex towards its lower-id neighbour first."""
+    if len(fverts) == 3:
+        return tuple(fverts[i] for i in np.argsort(gids))
+    o = int(np.argmin(gids))
+    nb1, nb2 = (o + 1) % 4, (o + 3) % 4
+    if gids[nb2] < gids[nb1]:
+        nb1, nb2 = nb2, nb1
+    return (fverts[o], fverts[nb1], fverts[nb2], fverts[(o + 2) % 4])
+
+
+def _c0_assembly(n, modal, ref_xi, edges, faces, EV, nv):
+    """C0 numbering of a conforming mesh of one collapsed element type (vertex ids EV):
+    vertices, then edge modes (sign (-1)^k where the local edge runs against the global
+    low-to-high direction), face modes matched between the elements of a face by their
+    restriction to it in the face's global frame (a permutation with signs), then interior
+    modes; every boundary dof Dirichlet, numbered first."""
+    E = EV.shape[0]
+    topo = _local_topology(n, modal, ref_xi, edges, faces)
+    nc = len(topo)
+    ni = max(n - 2, 0)
+    ekeys = np.stack([np.sort(EV[:, list(e)], axis=1) for e in edges], axis=1).reshape(-1, 2)
+    ue, einv = np.unique(ekeys, axis=0, return_inverse=True)
+    einv = einv.reshape(E, len(edges))
+    fkeys = [tuple(sorted(EV[e, list(f)])) for e in range(E) for f in faces]
+    fid, fcount = {}, {}
+    for k in fkeys:
+        if k not in fid:
+            fid[k] = len(fid)
+        fcount[k] = fcount.get(k, 0) + 1
+    finv = np.array([fid[k] for k in fkeys]).reshape(E, len(faces))
+    nF = len(fid)
+    fmodes = {f: [m for m, t in enumerate(topo) if t[0] == "f" and t[1] == f] for f in range(len(faces))}
+    nfm = {f: len(fmodes[f]) for f in fmodes}
+    # per global face: its size in modes (the first element's count) and offset
+    fsize = np.zeros(nF, dtype=np.int64)
+    for e in range(E):
+        for f in range(len(faces)):
+            fsize[finv[e, f]] = nfm[f]
+    foff = np.concatenate([[0], np.cumsum(fsize)])
+    nint = sum(1 for t in topo if t[0] == "i")
+    nE = ue.shape[0]
+    nglob = nv + nE * ni + int(foff[-1]) + E * nint
+    fbnd = np.zeros(nF, dtype=bool)
+    for k, c in fcount.items():
+        fbnd[fid[k]] = c == 1
+    is_dir = np.zeros(nglob, dtype=bool)
+    bverts = {v for k, c in fcount.items() if c == 1 for v in k}
+    is_dir[list(bverts)] = True
+    bedges = set()
+    for k, c in fcount.items():
+        if c == 1:
+            kk = list(k)
+            for a in range(len(kk)):
+                for b in range(a + 1, len(kk)):
+                    bedges.add((kk[a], kk[b]))
+    eid = {tuple(x): i for i, x in enumerate(ue.tolist())}
+    for be in bedges:
+        if be in eid:   # quad diagonals are not edges
+            i = eid[be]
+            is_dir[nv + i * ni:nv + (i + 1) * ni] = True
+    for g in np.flatnonzero(fbnd):
+        is_dir[nv + nE * ni + foff[g]:nv + nE * ni + foff[g + 1]] = True
+    newid, ndir = _renumber_dirichlet_first(np.arange(nglob), is_dir)
+    l2g = np.zeros((E, nc), dtype=np.int64)
+    sgn = np.ones((E, nc))
+    for m, t in enumerate(topo):
+        if t[0] == "v":
+            l2g[:, m] = EV[:, t[1]]
+        elif t[0] == "e":
+            _, ed, k, s_loc = t
+            a, b = edges[ed]
+            fwd = EV[:, a] < EV[:, b]
+            l2g[:, m] = nv + einv[:, ed] * ni + (k - 2)
+            sgn[:, m] = s_loc * np.where(fwd, 1.0, (-1.0) ** k)
+    cen = ref_xi.mean(axis=0)
+    cache, owner = {}, {}
+
+    def face_vals(f, frame):
+        key = (f, frame)
+        if key not in cache:
+            xi = _face_xi(ref_xi, faces[f], frame, _face_points(len(faces[f])))
+            xi = (1 - 1e-9) * xi + 1e-9 * cen
+            cache[key] = modal(n, xi[..., 0], xi[..., 1], xi[..., 2])[:, fmodes[f]]
+        return cache[key]
+    match = {}
+    for e in range(E):
+        for f, fv in enumerate(faces):
+            if not fmodes[f]:
+                continue
+            g = finv[e, f]
+            frame = _canonical_frame(fv, EV[e, list(fv)])
+            key = (f, frame)
+            if g not in owner:
+                owner[g] = key
+            pair = (owner[g], key)
+            if pair not in match:
+                A, B = face_vals(*owner[g]), face_vals(*key)
+                hits = []
+                for b in range(B.shape[1]):
+                    hit = None
+                    for a in range(A.shape[1]):
+                        for sg in (1.0, -1.0):
+                            if np.max(np.abs(B[:, b] - sg * A[:, a])) < 1e-8:
+                                hit = (a, sg)
+                    assert hit is not None, "face modes do not match across a shared face"
+                    hits.append(hit)
+                match[pair] = hits
+            for j, m in enumerate(fmodes[f]):
+                a, sg = match[pair][j]
+                l2g[e, m] = nv + nE * ni + foff[g] + a
+                sgn[e, m] = sg
+    base = nv + nE * ni + int(foff[-1])
+    ints = [m for m, t in enumerate(topo) if t[0] == "i"]
+    for j, m in enumerate(ints):
+        l2g[:, m] = base + np.arange(E) * nint + j
+    l2g = newid[l2g]
+    return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
 
 
 class TetMesh:
@@ -456,10 +589,8 @@ class TetMesh:
     def _map(self, x, y, z):
         if self.curve_amp == 0.0:
             return x, y, z
-        a = self.curve_amp
-        return (x + a * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z),
-                y + a * np.sin(2 * np.pi * z) * np.sin(2 * np.pi * x),
-                z + a * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y))
+        b = self.curve_amp * np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)
+        return x + b, y - 0.5 * b, z + 0.25 * b
 
     def coords(self, n):
         """Coordinates at the (n + 1) x n x n collapsed points (GLL x Gauss-Radau alpha 1 x
@@ -475,82 +606,45 @@ class TetMesh:
 
     def assembly(self, n):
         """C0 numbering of the tetrahedron expansion with n modes per direction; all
-        boundary dofs Dirichlet. Vertex modes take their vertex's id; an edge mode of degree
-        k flips sign, (-1)^k, where the local edge runs against the global one (low to high
-        id); face modes are matched between the two elements of a face by their restriction
-        to it (a permutation with signs: with the sorted local vertex order both sides see
-        the same collapsed vertex); interior modes are the element's own."""
-        E, EV = self.E, self.EV
-        nv = self.V.shape[0]
-        topo, fpts, fv = _tet_local_topology(n)
-        nc = len(topo)
-        ni = max(n - 2, 0)
-        nfm = max((n - 2) * (n - 3) // 2, 0)
-        nint = max((n - 2) * (n - 3) * (n - 4) // 6, 0)
-        # global edges and faces
-        le = np.stack([np.sort(EV[:, list(e)], axis=1) for e in _TET_EDGES], axis=1).reshape(-1, 2)
-        ue, einv = np.unique(le, axis=0, return_inverse=True)
-        einv = einv.reshape(E, 6)
-        lf = np.stack([np.sort(EV[:, list(f)], axis=1) for f in _TET_FACES], axis=1).reshape(-1, 3)
-        uf, finv, fcnt = np.unique(lf, axis=0, return_inverse=True, return_counts=True)
-        finv = finv.reshape(E, 4)
-        nE, nF = ue.shape[0], uf.shape[0]
-        fbnd = fcnt == 1
-        vbnd = np.zeros(nv, dtype=bool)
-        vbnd[uf[fbnd].ravel()] = True
-        ebnd = np.zeros(nE, dtype=bool)
-        for a, b in ((0, 1), (0, 2), (1, 2)):
-            pairs = np.sort(uf[fbnd][:, [a, b]], axis=1)
-            idx = np.searchsorted(ue[:, 0] * (nv + 1) + ue[:, 1], pairs[:, 0] * (nv + 1) + pairs[:, 1])
-            ebnd[idx] = True
-        nglob = nv + nE * ni + nF * nfm + E * nint
-        is_dir = np.zeros(nglob, dtype=bool)
-        is_dir[:nv] = vbnd
-        is_dir[nv:nv + nE * ni] = np.repeat(ebnd, ni)
-        is_dir[nv + nE * ni:nv + nE * ni + nF * nfm] = np.repeat(fbnd, nfm)
-        newid, ndir = _renumber_dirichlet_first(np.arange(nglob), is_dir)
-        l2g = np.zeros((E, nc), dtype=np.int64)
-        sgn = np.ones((E, nc))
-        face_modes = {f: [m for m, t in enumerate(topo) if t[0] == "f" and t[1] == f] for f in range(4)}
-        # local face vertex order against the global (sorted) one
-        perms = np.zeros((E, 4, 3), dtype=np.int64)
-        for f, fvtx in enumerate(_TET_FACES):
-            g = EV[:, list(fvtx)]
-            perms[:, f] = np.argsort(np.argsort(g, axis=1), axis=1)
-        owner = {}
-        match_cache = {}
-        icount = np.zeros(E, dtype=np.int64)
-        for m, t in enumerate(topo):
-            if t[0] == "v":
-                l2g[:, m] = EV[:, t[1]]
-            elif t[0] == "e":
-                _, ed, k, s_loc = t
-                a, b = _TET_EDGES[ed]
-                fwd = EV[:, a] < EV[:, b]
-                l2g[:, m] = nv + einv[:, ed] * ni + (k - 2)
-                sgn[:, m] = s_loc * np.where(fwd, 1.0, (-1.0) ** k)
-            elif t[0] == "i":
-                pass
-        for e in range(E):
-            for f in range(4):
-                gf = finv[e, f]
-                key = (f, tuple(perms[e, f]))
-                if gf not in owner:
-                    owner[gf] = key
-                ref = owner[gf]
-                pair = (ref, key)
-                if pair not in match_cache:
-                    match_cache[pair] = _face_match(n, fpts, fv, topo, ref[0], ref[1], f, key[1])
-                for j, m in enumerate(face_modes[f]):
-                    a, sg = match_cache[pair][j]
-                    l2g[e, m] = nv + nE * ni + gf * nfm + a
-                    sgn[e, m] = sg
-        base = nv + nE * ni + nF * nfm
-        ints = [m for m, t in enumerate(topo) if t[0] == "i"]
-        for j, m in enumerate(ints):
-            l2g[:, m] = base + np.arange(E) * nint + j
-        l2g = newid[l2g]
-        return AssemblyMap(l2g.reshape(-1), sgn.reshape(-1), nglob, ndir)
+        boundary dofs Dirichlet (``_c0_assembly``: with the sorted local vertex order both
+        elements of a face see the same collapsed vertex, so its modes match up to sign)."""
+        return _c0_assembly(n, tet_modal, _TET_XI, _TET_EDGES, _TET_FACES, self.EV, self.V.shape[0])
+
+
+class PrismMesh:
+    def __init__(self, nx, ny, nz, jitter=0.0, seed=0, curve_amp=0.0):
+        t = TetMesh(nx, ny, nz, jitter=jitter, seed=seed)
+        self.V = t.V
+        self.curve_amp = curve_amp
+        step = np.array([1, nx + 1, (nx + 1) * (ny + 1)])
+        ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        c000 = ((ck * (ny + 1) + cj) * (nx + 1) + ci).transpose(2, 1, 0).ravel()
+        c = lambda a, b, d: c000 + a * step[0] + b * step[1] + d * step[2]
+        pa = np.stack([c(0, 0, 0), c(1, 0, 0), c(1, 1, 0), c(0, 1, 0), c(0, 0, 1), c(0, 1, 1)], axis=1)
+        pb = np.stack([c(1, 0, 1), c(0, 0, 1), c(0, 1, 1), c(1, 1, 1), c(1, 0, 0), c(1, 1, 0)], axis=1)
+        self.EV = np.stack([pa, pb], axis=1).reshape(-1, 6)
+        self.E = self.EV.shape[0]
+
+    _map = TetMesh._map
+
+    def coords(self, n):
+        """Coordinates at the (n + 1) x (n + 1) x n points (GLL x GLL x Gauss-Radau alpha 1),
+        shape (3, E, (n + 1)^2 n), point (k (n + 1) + j) (n + 1) + i."""
+        z0, z2 = gll_points(n + 1), radau_points(n)
+        e2, e1, e0 = np.meshgrid(z2, z0, z0, indexing="ij")
+        xi0 = 0.5 * (1 + e0) * (1 - e2) - 1
+        xi1, xi2 = e1, e2
+        tri = lambda: (-0.5 * (xi0 + xi2), 0.5 * (1 + xi0), 0.5 * (1 + xi2))
+        lo, hi = 0.5 * (1 - xi1), 0.5 * (1 + xi1)
+        a, b, d = tri()
+        # v0 v1 v4 below, v3 v2 v5 above
+        W = np.stack([lo * a, lo * b, hi * b, hi * a, lo * d, hi * d])
+        X = np.einsum("vkji,evc->cekji", W, self.V[self.EV]).reshape(3, self.E, -1)
+        return np.stack(self._map(X[0], X[1], X[2])).copy()
+
+    def assembly(self, n):
+        """C0 numbering of the prism expansion with n modes; all boundary dofs Dirichlet."""
+        return _c0_assembly(n, prism_modal, _PRISM_XI, _PRISM_EDGES, _PRISM_FACES, self.EV, self.V.shape[0])
 
 
 class HexMesh:

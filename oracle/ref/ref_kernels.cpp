@@ -748,6 +748,204 @@ void iprd_tet(const TetTables& t, const Geo& g, const double* in0, const double*
   }
 }
 
+// ---- prisms: eModified_A on Q0 = Q1 = n + 1 GLL points (directions 0, 1), eModified_B on
+//      Q2 = n Gauss-Radau (alpha 1) points (direction 2, rows (p, r)): the default keys of
+//      SpatialDomains/MeshGraph.cpp:1011-1045; modes (p, q, r), r fastest, r < n - p ----
+struct PrismTables {
+  vvec b0, db0, D0, w0, z0, b2, db2, D2, w2, z2;
+};
+
+PrismTables make_prism_tables(int n) {
+  const int Q0 = n + 1, Q = n, npr = n * (n + 1) / 2;
+  std::vector<double> z0(Q0), w0(Q0), D0(Q0 * Q0), B0(n * Q0), DB0(n * Q0);
+  std::vector<double> z2(Q), w2(Q), D2(Q * Q), B2(npr * Q), DB2(npr * Q);
+  gll_tables(Q0, z0.data(), w0.data(), D0.data());
+  modA_tables(n, Q0, z0.data(), D0.data(), B0.data(), DB0.data());
+  radau_tables(Q, z2.data(), w2.data(), D2.data());
+  modB_tables(n, Q, z2.data(), D2.data(), B2.data(), DB2.data());
+  for (double& v : w2) v *= 0.5;  // MatrixFreeOps/Operator.hpp:245-248
+  PrismTables t;
+  auto put = [](vvec& dst, const std::vector<double>& src) { dst.assign(src.begin(), src.end()); };
+  put(t.b0, B0); put(t.db0, DB0); put(t.D0, D0); put(t.w0, w0); put(t.z0, z0);
+  put(t.b2, B2); put(t.db2, DB2); put(t.D2, D2); put(t.w2, w2); put(t.z2, z2);
+  return t;
+}
+
+// BwdTrans / IProduct / PhysDeriv for prisms (MatrixFreeOps/BwdTrans.h, IProduct.h:1070-1110,
+// PhysDeriv.h), CORRECT = true; direction 1 uses the direction-0 tables.
+template <int N>
+void prism_bwd(const PrismTables& t, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * N * (N + 1) / 2, nq = (N + 1) * (N + 1) * N;
+  vvec tin(nc), tout(nq);
+  vec_t fpq[N * N], fp[N];
+  for (int e = b0; e < b1; ++e) {
+    load_interleave(in + (size_t)e * nc * W, nc, tin);
+    BwdTransPrismKernel<N, N, N, N + 1, N + 1, N, true>(tin, t.b0, t.b0, t.b2, fpq, fp, tout);
+    deinterleave_store(tout, nq, out + (size_t)e * nq * W);
+  }
+}
+
+template <int N, bool DEF>
+void prism_iprod(const PrismTables& t, const Geo& g, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * N * (N + 1) / 2, nq = (N + 1) * (N + 1) * N;
+  vvec tin(nq), tout(nc);
+  vec_t skj[(N + 1) * N], sk[N], cq[N];
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    IProductPrismKernel<N, N, N, N + 1, N + 1, N, true, false, false, DEF>(tin, t.b0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                           jac_ptr, skj, sk, cq, tout);
+    deinterleave_store(tout, nc, out + (size_t)e * nc * W);
+  }
+}
+
+template <int N, bool DEF>
+void prism_deriv(const PrismTables& t, const Geo& g, const double* in, double* o0, double* o1, double* o2, int b0,
+                 int b1) {
+  constexpr int nq = (N + 1) * (N + 1) * N, ndf = 9;
+  vvec tin(nq), a(nq), b(nq), c(nq);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nq : ndf)];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    PhysDerivPrismKernel<N + 1, N + 1, N, DEF>(tin, t.z0, t.z0, t.z2, t.D0, t.D0, t.D2, df_ptr, a, b, c);
+    deinterleave_store(a, nq, o0 + (size_t)e * nq * W);
+    deinterleave_store(b, nq, o1 + (size_t)e * nq * W);
+    deinterleave_store(c, nq, o2 + (size_t)e * nq * W);
+  }
+}
+
+// ---- Helmholtz: HelmholtzPrismImpl (MatrixFreeOps/Helmholtz.h:1003-1030, 1291-1440) ----
+template <int N, bool DEF>
+void helm_prism(const PrismTables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N + 1, NQ2 = N, nc = N * N * (N + 1) / 2, nqTot = NQ0 * NQ1 * NQ2, ndf = 9;
+  std::vector<double> h0(NQ0), h1(NQ2);
+  for (int i = 0; i < NQ0; ++i) h0[i] = 0.5 * (1 + t.z0[i][0]);
+  for (int k = 0; k < NQ2; ++k) h1[k] = 2.0 / (1 - t.z2[k][0]);
+  vec_t wsp1[NQ1 * NQ2], wsp2[NQ2], wsp3[N];
+  vvec tmpIn(nc), tmpOut(nc), bwd(nqTot), deriv0(nqTot), deriv1(nqTot), deriv2(nqTot);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in + (size_t)e * nc * W, nc, tmpIn);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    BwdTransPrismKernel<N, N, N, NQ0, NQ1, NQ2, true>(tmpIn, t.b0, t.b0, t.b2, wsp1, wsp2, bwd);
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, true, false, DEF>(bwd, t.b0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, wsp1, wsp2, wsp3, tmpOut, lambda);
+    PhysDerivTensor3DKernel<NQ0, NQ1, NQ2>(bwd, t.D0, t.D0, t.D2, deriv0, deriv1, deriv2);
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t vh1 = h1[k];
+      for (int j = 0; j < NQ1; ++j) {
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          vec_t vh0 = h0[i];
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t tmp1 = vh1 * (vh0 * df2 + df0);
+          vec_t tmp2 = vh1 * (vh0 * df5 + df3);
+          vec_t tmp3 = vh1 * (vh0 * df8 + df6);
+          vec_t g0 = tmp1 * tmp1;
+          g0.fma(tmp2, tmp2);
+          g0.fma(tmp3, tmp3);
+          vec_t g3 = df1 * tmp1;
+          g3.fma(df4, tmp2);
+          g3.fma(df7, tmp3);
+          vec_t g4 = df2 * tmp1;
+          g4.fma(df5, tmp2);
+          g4.fma(df8, tmp3);
+          vec_t g1 = df1 * df1;
+          g1.fma(df4, df4);
+          g1.fma(df7, df7);
+          vec_t g2 = df2 * df2;
+          g2.fma(df5, df5);
+          g2.fma(df8, df8);
+          vec_t g5 = df1 * df2;
+          g5.fma(df4, df5);
+          g5.fma(df7, df8);
+          vec_t d0 = deriv0[cnt], d1 = deriv1[cnt], d2 = deriv2[cnt];
+          tmp1 = g0 * d0;
+          tmp1.fma(g3, d1);
+          tmp1.fma(g4, d2);
+          deriv0[cnt] = tmp1;
+          tmp2 = g3 * d0;
+          tmp2.fma(g1, d1);
+          tmp2.fma(g5, d2);
+          deriv1[cnt] = tmp2;
+          tmp3 = g4 * d0;
+          tmp3.fma(g5, d1);
+          tmp3.fma(g2, d2);
+          deriv2[cnt] = tmp3;
+        }
+      }
+    }
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv0, t.db0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, wsp1, wsp2, wsp3, tmpOut);
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv1, t.b0, t.db0, t.b2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, wsp1, wsp2, wsp3, tmpOut);
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv2, t.b0, t.b0, t.db2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, wsp1, wsp2, wsp3, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
+// ---- IProductWRTDerivBasePrismImpl (MatrixFreeOps/IProductWRTDerivBase.h:1660-1760) ----
+template <int N, bool DEF>
+void iprd_prism(const PrismTables& t, const Geo& g, const double* in0, const double* in1, const double* in2,
+                double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N + 1, NQ2 = N, nc = N * N * (N + 1) / 2, nqTot = NQ0 * NQ1 * NQ2, ndf = 9;
+  vec_t skj[NQ1 * NQ2], sk[NQ2], cq[N];
+  vvec a0(nqTot), a1(nqTot), a2(nqTot), tmp0(nqTot), tmp1(nqTot), tmp2(nqTot), tmpOut(nc);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in0 + (size_t)e * nqTot * W, nqTot, a0);
+    load_interleave(in1 + (size_t)e * nqTot * W, nqTot, a1);
+    load_interleave(in2 + (size_t)e * nqTot * W, nqTot, a2);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t f0 = 2.0 / (1.0 - t.z2[k]);
+      for (int j = 0; j < NQ1; ++j) {
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t tI0 = a0[cnt], tI1 = a1[cnt], tI2 = a2[cnt];
+          vec_t t0 = df0 * tI0 + df3 * tI1 + df6 * tI2;
+          vec_t t1 = df1 * tI0 + df4 * tI1 + df7 * tI2;
+          vec_t t2 = df2 * tI0 + df5 * tI1 + df8 * tI2;
+          vec_t hf1 = 0.5 * (1.0 + t.z0[i]);
+          t0 *= f0;
+          vec_t f1t2 = hf1 * t2;
+          t0.fma(f1t2, f0);
+          tmp0[cnt] = t0;
+          tmp1[cnt] = t1;
+          tmp2[cnt] = t2;
+        }
+      }
+    }
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, false, DEF>(tmp0, t.db0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                        jac_ptr, skj, sk, cq, tmpOut);
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp1, t.b0, t.db0, t.b2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, skj, sk, cq, tmpOut);
+    IProductPrismKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp2, t.b0, t.b0, t.db2, t.w0, t.w0, t.w2,
+                                                                       jac_ptr, skj, sk, cq, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
 // Runs CALL(N) for N in 2..10 (triangles: Q0 = N + 1, Q1 = N).
 #define TRI_DISPATCH(n, CALL)   \
   switch (n) {                  \
@@ -1126,6 +1324,81 @@ int ref_tet_iproduct_deriv(int n, int E, const double* jac, const double* df, in
   })
   TRI_DISPATCH(n, TP)
 #undef TP
+}
+
+// ---- prisms ----
+int ref_prism_bwdtrans(int n, int E, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  PrismTables t = make_prism_tables(n);
+  const int nb = E / W;
+#define PB(NN) parallel_blocks(nb, nthreads, [&](int b0, int b1) { prism_bwd<NN>(t, in, out, b0, b1); })
+  TRI_DISPATCH(n, PB)
+#undef PB
+}
+
+int ref_prism_iproduct(int n, int E, const double* jac, int deformed, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PrismTables t = make_prism_tables(n);
+  std::vector<double> dfz((size_t)9 * E * (deformed ? nq : 1), 0.0);
+  Geo g = interleave(3, nq, E, E, jac, dfz.data(), deformed != 0);
+  const int nb = E / W;
+#define PI(NN)                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {            \
+    if (deformed) prism_iprod<NN, true>(t, g, in, out, b0, b1);  \
+    else prism_iprod<NN, false>(t, g, in, out, b0, b1);          \
+  })
+  TRI_DISPATCH(n, PI)
+#undef PI
+}
+
+int ref_prism_physderiv(int n, int E, const double* df, int deformed, const double* in, double* o0, double* o1,
+                        double* o2, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PrismTables t = make_prism_tables(n);
+  std::vector<double> jz((size_t)E * (deformed ? nq : 1), 1.0);
+  Geo g = interleave(3, nq, E, E, jz.data(), df, deformed != 0);
+  const int nb = E / W;
+#define PD(NN)                                                            \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                     \
+    if (deformed) prism_deriv<NN, true>(t, g, in, o0, o1, o2, b0, b1);    \
+    else prism_deriv<NN, false>(t, g, in, o0, o1, o2, b0, b1);            \
+  })
+  TRI_DISPATCH(n, PD)
+#undef PD
+}
+
+int ref_prism_helmholtz(int n, int E, const double* jac, const double* df, int deformed, double lambda,
+                        const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PrismTables t = make_prism_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define PH(NN)                                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
+    if (deformed) helm_prism<NN, true>(t, g, lambda, in, out, b0, b1);         \
+    else helm_prism<NN, false>(t, g, lambda, in, out, b0, b1);                 \
+  })
+  TRI_DISPATCH(n, PH)
+#undef PH
+}
+
+int ref_prism_iproduct_deriv(int n, int E, const double* jac, const double* df, int deformed, const double* in0,
+                             const double* in1, const double* in2, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PrismTables t = make_prism_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define PP(NN)                                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                            \
+    if (deformed) iprd_prism<NN, true>(t, g, in0, in1, in2, out, b0, b1);        \
+    else iprd_prism<NN, false>(t, g, in0, in1, in2, out, b0, b1);                \
+  })
+  TRI_DISPATCH(n, PP)
+#undef PP
 }
 
 }  // extern "C"

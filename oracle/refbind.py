@@ -204,3 +204,39 @@ def tet_iproduct_deriv(n, E, jac, df, deformed, in0, in1, in2, nthreads=1):
     _check(lib().ref_tet_iproduct_deriv(n, E, _f(jac), _f(df), int(deformed), _f(in0), _f(in1), _f(in2), _p(out),
                                         nthreads), "ref_tet_iproduct_deriv")
     return out
+
+
+# ---- prisms (ref_prism_* drivers); tables: directions 0 and 1 as ref_gll/ref_modA(n, n+1),
+# direction 2 as tri_tables(n)[1] ----
+def prism_bwdtrans(n, E, coeffs, nthreads=1):
+    out = np.zeros(E * (n + 1) * (n + 1) * n)
+    _check(lib().ref_prism_bwdtrans(n, E, _f(coeffs), _p(out), nthreads), "ref_prism_bwdtrans")
+    return out
+
+
+def prism_iproduct(n, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n * n * (n + 1) // 2)
+    _check(lib().ref_prism_iproduct(n, E, _f(jac), int(deformed), _f(phys), _p(out), nthreads), "ref_prism_iproduct")
+    return out
+
+
+def prism_physderiv(n, E, df, deformed, phys, nthreads=1):
+    nq = (n + 1) * (n + 1) * n
+    o = [np.zeros(E * nq) for _ in range(3)]
+    _check(lib().ref_prism_physderiv(n, E, _f(df), int(deformed), _f(phys), *[_p(x) for x in o], nthreads),
+           "ref_prism_physderiv")
+    return o
+
+
+def prism_helmholtz(n, E, jac, df, deformed, lam, coeffs, nthreads=1):
+    out = np.zeros(E * n * n * (n + 1) // 2)
+    _check(lib().ref_prism_helmholtz(n, E, _f(jac), _f(df), int(deformed), ctypes.c_double(lam), _f(coeffs),
+                                     _p(out), nthreads), "ref_prism_helmholtz")
+    return out
+
+
+def prism_iproduct_deriv(n, E, jac, df, deformed, in0, in1, in2, nthreads=1):
+    out = np.zeros(E * n * n * (n + 1) // 2)
+    _check(lib().ref_prism_iproduct_deriv(n, E, _f(jac), _f(df), int(deformed), _f(in0), _f(in1), _f(in2),
+                                          _p(out), nthreads), "ref_prism_iproduct_deriv")
+    return out

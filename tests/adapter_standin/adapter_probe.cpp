@@ -17,15 +17,19 @@ std::vector<StdRegions::StdExpansionSharedPtr> Expansions(int shape, int n, int 
 // on Q x (Q - 1) collapsed points)
 size_t ModesPerElement(int shape, int n) {
   if (shape == LibUtilities::eTriangle) return (size_t)n * (n + 1) / 2;
+  if (shape == LibUtilities::eTetrahedron) return (size_t)n * (n + 1) * (n + 2) / 6;
+  if (shape == LibUtilities::ePrism) return (size_t)n * n * (n + 1) / 2;
   return shape == LibUtilities::eQuadrilateral ? (size_t)n * n : (size_t)n * n * n;
 }
 size_t PointsPerElement(int shape, int Q) {
   if (shape == LibUtilities::eTriangle) return (size_t)Q * (Q - 1);
+  if (shape == LibUtilities::eTetrahedron) return (size_t)Q * (Q - 1) * (Q - 1);
+  if (shape == LibUtilities::ePrism) return (size_t)Q * Q * (Q - 1);
   return shape == LibUtilities::eQuadrilateral ? (size_t)Q * Q : (size_t)Q * Q * Q;
 }
 std::shared_ptr<Collections::CoalescedGeomData> Geometry(int shape, int Q, int E, const double* jac, const double* df) {
   auto g = std::make_shared<Collections::CoalescedGeomData>();
-  const int dim = shape == LibUtilities::eHexahedron ? 3 : 2;
+  const int dim = shape == LibUtilities::eTriangle || shape == LibUtilities::eQuadrilateral ? 2 : 3;
   const size_t npts = (size_t)E * PointsPerElement(shape, Q);
   Array<OneD, NekDouble> j(npts);
   Array<TwoD, NekDouble> d(dim * dim, npts);

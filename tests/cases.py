@@ -1,9 +1,10 @@
 """Seeded test cases shared by the CPU and GPU tests (small sizes the oracle runs in seconds)."""
 import numpy as np
 
-from ithaca_gpu.mesh import HexMesh, QuadMesh, TetMesh, TriMesh
+from ithaca_gpu.mesh import HexMesh, PrismMesh, QuadMesh, TetMesh, TriMesh
 from oracle import basis as obasis
 from oracle import geom as ogeom
+from oracle import prism as oprism
 from oracle import tet as otet
 from oracle import tri as otri
 
@@ -86,6 +87,26 @@ def tet_case(nx, ny, nz, n, jitter=0.2, seed=3, curve=0.03, deformed=True):
         c.jac, c.df = jac.reshape(-1).copy(), df.copy()
     else:
         c.jac, c.df = otet.straight_tet_geometry(c.mesh.V[c.mesh.EV])
+    c.nm, c.nq = c.basis.nc, c.basis.nq
+    return c
+
+
+def prism_case(nx, ny, nz, n, jitter=0.2, seed=3, curve=0.05, deformed=True):
+    """PrismMesh of 2 nx ny nz prisms, n modes; deformed: curved and jittered with per-point
+    geometry, else straight and unjittered with per-element geometry."""
+    c = Case()
+    c.dim, c.shape, c.n, c.Q = 3, "prism", n, n + 1
+    c.mesh = PrismMesh(nx, ny, nz, jitter=jitter if deformed else 0.0, seed=seed,
+                       curve_amp=curve if deformed else 0.0)
+    c.E = c.mesh.E
+    c.X = c.mesh.coords(n)
+    c.basis = oprism.PrismBasis(n)
+    c.deformed = deformed
+    jac, df = oprism.geom_factors(c.basis, c.X)
+    if deformed:
+        c.jac, c.df = jac.reshape(-1).copy(), df.copy()
+    else:
+        c.jac, c.df = jac[:, 0].copy(), df.reshape(9, c.E, -1)[:, :, 0].copy()
     c.nm, c.nq = c.basis.nc, c.basis.nq
     return c
 
