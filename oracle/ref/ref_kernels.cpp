@@ -946,6 +946,264 @@ void iprd_prism(const PrismTables& t, const Geo& g, const double* in0, const dou
   }
 }
 
+// ---- pyramids: eModified_A on Q0 = Q1 = n + 1 GLL points (directions 0, 1),
+//      eModifiedPyr_C on Q2 = n Gauss-Radau (alpha 2) points (direction 2): the default keys
+//      of SpatialDomains/MeshGraph.cpp:1719-1745; modes (p, q, r), r fastest,
+//      r < n - max(p, q) ----
+// Basis::GenBasis eModifiedPyr_C (LibUtilities/Foundations/Basis.cpp:568-672): rows of the
+// ModifiedB table for p <= 1 and for q <= 1, the face-0 rows ((1-z)/2)^(p+q-2) and the
+// interior rows ((1-z)/2)^(p+q-2) (1+z)/2 P_{r-1}^{(2p+2q-3,1)} for p, q >= 2.
+void modPyrC_tables(int n, int Q, const double* z, const double* D, double* C, double* DC) {
+  const int ncb = n * (n + 1) / 2, ncp = n * (n + 1) * (2 * n + 1) / 6;
+  std::vector<double> B((size_t)ncb * Q), DB((size_t)ncb * Q);
+  modB_tables(n, Q, z, D, B.data(), DB.data());
+  size_t off = 0, boff = 0;
+  auto copy_rows = [&](size_t rows) {
+    std::copy(B.begin() + boff * Q, B.begin() + (boff + rows) * Q, C + off * Q);
+    off += rows;
+  };
+  copy_rows((size_t)n * (n + 1) / 2);  // p = 0: all (q, r)
+  boff += n;
+  copy_rows(n - 1);                    // p = 1, q = 0
+  copy_rows((size_t)(n - 1) * n / 2);  // p = 1, q >= 1
+  boff += n - 1;
+  for (int p = 2; p < n; ++p) {
+    copy_rows(n - p);  // q = 0
+    boff -= 0;
+    std::copy(B.begin() + boff * Q, B.begin() + (boff + n - p) * Q, C + off * Q);  // q = 1: same rows
+    off += n - p;
+    boff += n - p;
+    for (int q = 2; q < n; ++q) {
+      double* mode = C + off * Q;
+      for (int i = 0; i < Q; ++i) mode[i] = std::pow(B[i], p + q - 2);
+      const double* one_m_z_pow = mode;
+      ++off;
+      for (int r = 1; r < n - std::max(p, q); ++r, ++off) {
+        double* md = C + off * Q;
+        Polylib::jacobfd(Q, z, md, nullptr, r - 1, 2 * p + 2 * q - 3, 1.0);
+        for (int i = 0; i < Q; ++i) md[i] *= one_m_z_pow[i] * B[Q + i];
+      }
+    }
+  }
+  for (int m = 0; m < ncp; ++m)
+    for (int i = 0; i < Q; ++i) {
+      double s = 0;
+      for (int k = 0; k < Q; ++k) s += D[k * Q + i] * C[m * Q + k];
+      DC[m * Q + i] = s;
+    }
+}
+
+struct PyrTables {
+  vvec b0, db0, D0, w0, z0, b2, db2, D2, w2, z2;
+};
+
+PyrTables make_pyr_tables(int n) {
+  const int Q0 = n + 1, Q = n, ncp = n * (n + 1) * (2 * n + 1) / 6;
+  std::vector<double> z0(Q0), w0(Q0), D0(Q0 * Q0), B0(n * Q0), DB0(n * Q0);
+  std::vector<double> z2(Q), w2(Q), D2(Q * Q), B2((size_t)ncp * Q), DB2((size_t)ncp * Q);
+  gll_tables(Q0, z0.data(), w0.data(), D0.data());
+  modA_tables(n, Q0, z0.data(), D0.data(), B0.data(), DB0.data());
+  Polylib::zwgrjm(z2.data(), w2.data(), Q, 2.0, 0.0);
+  Polylib::Dgrjm(D2.data(), z2.data(), Q, 2.0, 0.0);
+  modPyrC_tables(n, Q, z2.data(), D2.data(), B2.data(), DB2.data());
+  for (double& v : w2) v *= 0.25;  // MatrixFreeOps/Operator.hpp:249-251
+  PyrTables t;
+  auto put = [](vvec& dst, const std::vector<double>& src) { dst.assign(src.begin(), src.end()); };
+  put(t.b0, B0); put(t.db0, DB0); put(t.D0, D0); put(t.w0, w0); put(t.z0, z0);
+  put(t.b2, B2); put(t.db2, DB2); put(t.D2, D2); put(t.w2, w2); put(t.z2, z2);
+  return t;
+}
+
+template <int N>
+void pyr_bwd(const PyrTables& t, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) * (2 * N + 1) / 6, nq = (N + 1) * (N + 1) * N;
+  vvec tin(nc), tout(nq);
+  vec_t fpq[(N + 1) * N], fp[N];
+  for (int e = b0; e < b1; ++e) {
+    load_interleave(in + (size_t)e * nc * W, nc, tin);
+    BwdTransPyrKernel<N, N, N, N + 1, N + 1, N, true>(tin, t.b0, t.b0, t.b2, fpq, fp, tout);
+    deinterleave_store(tout, nq, out + (size_t)e * nq * W);
+  }
+}
+
+template <int N, bool DEF>
+void pyr_iprod(const PyrTables& t, const Geo& g, const double* in, double* out, int b0, int b1) {
+  constexpr int nc = N * (N + 1) * (2 * N + 1) / 6, nq = (N + 1) * (N + 1) * N;
+  vvec tin(nq), tout(nc);
+  vec_t skj[(N + 1) * N], sk[N];
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nq] : &g.jac[e];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    IProductPyrKernel<N, N, N, N + 1, N + 1, N, true, false, false, DEF>(tin, t.b0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                         jac_ptr, skj, sk, tout);
+    deinterleave_store(tout, nc, out + (size_t)e * nc * W);
+  }
+}
+
+template <int N, bool DEF>
+void pyr_deriv(const PyrTables& t, const Geo& g, const double* in, double* o0, double* o1, double* o2, int b0,
+               int b1) {
+  constexpr int nq = (N + 1) * (N + 1) * N, ndf = 9;
+  vvec tin(nq), a(nq), b(nq), c(nq);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nq : ndf)];
+    load_interleave(in + (size_t)e * nq * W, nq, tin);
+    PhysDerivPyrKernel<N + 1, N + 1, N, DEF>(tin, t.z0, t.z0, t.z2, t.D0, t.D0, t.D2, df_ptr, a, b, c);
+    deinterleave_store(a, nq, o0 + (size_t)e * nq * W);
+    deinterleave_store(b, nq, o1 + (size_t)e * nq * W);
+    deinterleave_store(c, nq, o2 + (size_t)e * nq * W);
+  }
+}
+
+// ---- Helmholtz: HelmholtzPyrImpl (MatrixFreeOps/Helmholtz.h:1480-1510, 1770-1960) ----
+template <int N, bool DEF>
+void helm_pyr(const PyrTables& t, const Geo& g, double lambda, const double* in, double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N + 1, NQ2 = N, nc = N * (N + 1) * (2 * N + 1) / 6, nqTot = NQ0 * NQ1 * NQ2,
+                ndf = 9;
+  std::vector<double> h0(NQ0), h2(NQ2);
+  for (int i = 0; i < NQ0; ++i) h0[i] = 0.5 * (1 + t.z0[i][0]);
+  for (int k = 0; k < NQ2; ++k) h2[k] = 2.0 / (1 - t.z2[k][0]);
+  vec_t wsp1[NQ1 * NQ2], wsp2[NQ2];
+  vvec tmpIn(nc), tmpOut(nc), bwd(nqTot), deriv0(nqTot), deriv1(nqTot), deriv2(nqTot);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in + (size_t)e * nc * W, nc, tmpIn);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    BwdTransPyrKernel<N, N, N, NQ0, NQ1, NQ2, true>(tmpIn, t.b0, t.b0, t.b2, wsp1, wsp2, bwd);
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, true, false, DEF>(bwd, t.b0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, wsp1, wsp2, tmpOut, lambda);
+    PhysDerivTensor3DKernel<NQ0, NQ1, NQ2>(bwd, t.D0, t.D0, t.D2, deriv0, deriv1, deriv2);
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t vh2 = h2[k];
+      for (int j = 0; j < NQ1; ++j) {
+        vec_t vh1 = 0.5 * (1 + t.z0[j][0]);
+        vec_t h1h2 = vh1 * vh2;
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          vec_t h0h2 = vec_t(h0[i]) * vh2;
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t tmp0 = vh2 * df0;
+          tmp0.fma(h0h2, df2);
+          vec_t tmp1 = vh2 * df3;
+          tmp1.fma(h0h2, df5);
+          vec_t tmp2 = vh2 * df6;
+          tmp2.fma(h0h2, df8);
+          vec_t tmp3 = vh2 * df1;
+          tmp3.fma(h1h2, df2);
+          vec_t tmp4 = vh2 * df4;
+          tmp4.fma(h1h2, df5);
+          vec_t tmp5 = vh2 * df7;
+          tmp5.fma(h1h2, df8);
+          vec_t g0 = tmp0 * tmp0;
+          g0.fma(tmp1, tmp1);
+          g0.fma(tmp2, tmp2);
+          vec_t g1 = tmp3 * tmp3;
+          g1.fma(tmp4, tmp4);
+          g1.fma(tmp5, tmp5);
+          vec_t g2 = df2 * df2;
+          g2.fma(df5, df5);
+          g2.fma(df8, df8);
+          vec_t g3 = tmp0 * tmp3;
+          g3.fma(tmp1, tmp4);
+          g3.fma(tmp2, tmp5);
+          vec_t g4 = df2 * tmp0;
+          g4.fma(df5, tmp1);
+          g4.fma(df8, tmp2);
+          vec_t g5 = df2 * tmp3;
+          g5.fma(df5, tmp4);
+          g5.fma(df8, tmp5);
+          vec_t d0 = deriv0[cnt], d1 = deriv1[cnt], d2 = deriv2[cnt];
+          tmp1 = g0 * d0;
+          tmp1.fma(g3, d1);
+          tmp1.fma(g4, d2);
+          deriv0[cnt] = tmp1;
+          tmp2 = g3 * d0;
+          tmp2.fma(g1, d1);
+          tmp2.fma(g5, d2);
+          deriv1[cnt] = tmp2;
+          tmp3 = g4 * d0;
+          tmp3.fma(g5, d1);
+          tmp3.fma(g2, d2);
+          deriv2[cnt] = tmp3;
+        }
+      }
+    }
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv0, t.db0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, wsp1, wsp2, tmpOut);
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv1, t.b0, t.db0, t.b2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, wsp1, wsp2, tmpOut);
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(deriv2, t.b0, t.b0, t.db2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, wsp1, wsp2, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
+// ---- IProductWRTDerivBasePyrImpl (MatrixFreeOps/IProductWRTDerivBase.h:2070-2200) ----
+template <int N, bool DEF>
+void iprd_pyr(const PyrTables& t, const Geo& g, const double* in0, const double* in1, const double* in2,
+              double* out, int b0, int b1) {
+  constexpr int NQ0 = N + 1, NQ1 = N + 1, NQ2 = N, nc = N * (N + 1) * (2 * N + 1) / 6, nqTot = NQ0 * NQ1 * NQ2,
+                ndf = 9;
+  vec_t skj[NQ1 * NQ2], sk[NQ2];
+  vvec a0(nqTot), a1(nqTot), a2(nqTot), tmp0(nqTot), tmp1(nqTot), tmp2(nqTot), tmpOut(nc);
+  for (int e = b0; e < b1; ++e) {
+    const vec_t* df_ptr = &g.df[(size_t)e * (DEF ? ndf * nqTot : ndf)];
+    const vec_t* jac_ptr = DEF ? &g.jac[(size_t)e * nqTot] : &g.jac[e];
+    load_interleave(in0 + (size_t)e * nqTot * W, nqTot, a0);
+    load_interleave(in1 + (size_t)e * nqTot * W, nqTot, a1);
+    load_interleave(in2 + (size_t)e * nqTot * W, nqTot, a2);
+    vec_t df0, df1, df2, df3, df4, df5, df6, df7, df8;
+    if (!DEF) {
+      df0 = df_ptr[0]; df1 = df_ptr[1]; df2 = df_ptr[2];
+      df3 = df_ptr[3]; df4 = df_ptr[4]; df5 = df_ptr[5];
+      df6 = df_ptr[6]; df7 = df_ptr[7]; df8 = df_ptr[8];
+    }
+    for (int k = 0, cnt = 0; k < NQ2; ++k) {
+      vec_t f0 = 2.0 / (1.0 - t.z2[k]);
+      for (int j = 0; j < NQ1; ++j) {
+        vec_t hf2 = 0.5 * (1.0 + t.z0[j]);
+        for (int i = 0; i < NQ0; ++i, ++cnt) {
+          if (DEF) {
+            df0 = df_ptr[cnt * ndf]; df1 = df_ptr[cnt * ndf + 1]; df2 = df_ptr[cnt * ndf + 2];
+            df3 = df_ptr[cnt * ndf + 3]; df4 = df_ptr[cnt * ndf + 4]; df5 = df_ptr[cnt * ndf + 5];
+            df6 = df_ptr[cnt * ndf + 6]; df7 = df_ptr[cnt * ndf + 7]; df8 = df_ptr[cnt * ndf + 8];
+          }
+          vec_t tI0 = a0[cnt], tI1 = a1[cnt], tI2 = a2[cnt];
+          vec_t t0 = df0 * tI0 + df3 * tI1 + df6 * tI2;
+          vec_t t1 = df1 * tI0 + df4 * tI1 + df7 * tI2;
+          vec_t t2 = df2 * tI0 + df5 * tI1 + df8 * tI2;
+          t0 *= f0;
+          vec_t hf1 = 0.5 * (1.0 + t.z0[i]);
+          vec_t f1t2 = hf1 * t2;
+          t0.fma(f1t2, f0);
+          t1 *= f0;
+          f1t2 = hf2 * t2;
+          t1.fma(f1t2, f0);
+          tmp0[cnt] = t0;
+          tmp1[cnt] = t1;
+          tmp2[cnt] = t2;
+        }
+      }
+    }
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, false, DEF>(tmp0, t.db0, t.b0, t.b2, t.w0, t.w0, t.w2,
+                                                                      jac_ptr, skj, sk, tmpOut);
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp1, t.b0, t.db0, t.b2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, skj, sk, tmpOut);
+    IProductPyrKernel<N, N, N, NQ0, NQ1, NQ2, true, false, true, DEF>(tmp2, t.b0, t.b0, t.db2, t.w0, t.w0, t.w2,
+                                                                     jac_ptr, skj, sk, tmpOut);
+    deinterleave_store(tmpOut, nc, out + (size_t)e * nc * W);
+  }
+}
+
 // Runs CALL(N) for N in 2..10 (triangles: Q0 = N + 1, Q1 = N).
 #define TRI_DISPATCH(n, CALL)   \
   switch (n) {                  \
@@ -1399,6 +1657,88 @@ int ref_prism_iproduct_deriv(int n, int E, const double* jac, const double* df, 
   })
   TRI_DISPATCH(n, PP)
 #undef PP
+}
+
+// ---- pyramids ----
+int ref_pyr_tables(int n, double* z2, double* w2, double* D2, double* B2, double* DB2) {
+  Polylib::zwgrjm(z2, w2, n, 2.0, 0.0);
+  Polylib::Dgrjm(D2, z2, n, 2.0, 0.0);
+  modPyrC_tables(n, n, z2, D2, B2, DB2);
+  return 0;
+}
+
+int ref_pyr_bwdtrans(int n, int E, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  PyrTables t = make_pyr_tables(n);
+  const int nb = E / W;
+#define YB(NN) parallel_blocks(nb, nthreads, [&](int b0, int b1) { pyr_bwd<NN>(t, in, out, b0, b1); })
+  TRI_DISPATCH(n, YB)
+#undef YB
+}
+
+int ref_pyr_iproduct(int n, int E, const double* jac, int deformed, const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PyrTables t = make_pyr_tables(n);
+  std::vector<double> dfz((size_t)9 * E * (deformed ? nq : 1), 0.0);
+  Geo g = interleave(3, nq, E, E, jac, dfz.data(), deformed != 0);
+  const int nb = E / W;
+#define YI(NN)                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {            \
+    if (deformed) pyr_iprod<NN, true>(t, g, in, out, b0, b1);    \
+    else pyr_iprod<NN, false>(t, g, in, out, b0, b1);            \
+  })
+  TRI_DISPATCH(n, YI)
+#undef YI
+}
+
+int ref_pyr_physderiv(int n, int E, const double* df, int deformed, const double* in, double* o0, double* o1,
+                      double* o2, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PyrTables t = make_pyr_tables(n);
+  std::vector<double> jz((size_t)E * (deformed ? nq : 1), 1.0);
+  Geo g = interleave(3, nq, E, E, jz.data(), df, deformed != 0);
+  const int nb = E / W;
+#define YD(NN)                                                            \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                     \
+    if (deformed) pyr_deriv<NN, true>(t, g, in, o0, o1, o2, b0, b1);      \
+    else pyr_deriv<NN, false>(t, g, in, o0, o1, o2, b0, b1);              \
+  })
+  TRI_DISPATCH(n, YD)
+#undef YD
+}
+
+int ref_pyr_helmholtz(int n, int E, const double* jac, const double* df, int deformed, double lambda,
+                      const double* in, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PyrTables t = make_pyr_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define YH(NN)                                                                 \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                          \
+    if (deformed) helm_pyr<NN, true>(t, g, lambda, in, out, b0, b1);           \
+    else helm_pyr<NN, false>(t, g, lambda, in, out, b0, b1);                   \
+  })
+  TRI_DISPATCH(n, YH)
+#undef YH
+}
+
+int ref_pyr_iproduct_deriv(int n, int E, const double* jac, const double* df, int deformed, const double* in0,
+                           const double* in1, const double* in2, double* out, int nthreads) {
+  if (E % W) return 2;
+  const int nq = (n + 1) * (n + 1) * n;
+  PyrTables t = make_pyr_tables(n);
+  Geo g = interleave(3, nq, E, E, jac, df, deformed != 0);
+  const int nb = E / W;
+#define YP(NN)                                                                   \
+  parallel_blocks(nb, nthreads, [&](int b0, int b1) {                            \
+    if (deformed) iprd_pyr<NN, true>(t, g, in0, in1, in2, out, b0, b1);          \
+    else iprd_pyr<NN, false>(t, g, in0, in1, in2, out, b0, b1);                  \
+  })
+  TRI_DISPATCH(n, YP)
+#undef YP
 }
 
 }  // extern "C"
