@@ -519,6 +519,84 @@ def prism_fields(torch, cuda, mesh=12, P=6):
     return out
 
 
+def pyr_helm_flops(n):
+    """FP64 operations of one pyramid Helmholtz apply (collocation form): BwdTrans and
+    IProduct (4 NC Q2 + 4 N^2 Q0 Q2 + 4 N NQ), the collapsed derivatives and their
+    transposes (4 NQ (2 Q0 + Q2)) and 17 per point."""
+    Q0, Q2, nc = n + 1, n, n * (n + 1) * (2 * n + 1) // 6
+    nq = Q0 * Q0 * Q2
+    return 4 * nc * Q2 + 4 * n * n * Q0 * Q2 + 4 * n * nq + 4 * nq * (2 * Q0 + Q2) + 17 * nq
+
+
+def pyr_fields(torch, cuda, mesh=10, P=6):
+    """Curved, jittered pyramids (mesh^3 cubes, six pyramids each) at order P: operators,
+    FP64 apply against the FP64 pipe, FP32 apply, PCG to 1e-10 (FP64 and mixed)."""
+    from ithaca_gpu.mesh import PyrMesh
+    from ithaca_gpu.operators import Collection, Context, GlobalLinSysIterativeFullGPU, geom_factors
+    n = P + 1
+    Q = n + 1
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
+    m = PyrMesh(mesh, mesh, mesh, jitter=0.15, seed=7, curve_amp=0.03)
+    E = m.E
+    X = m.coords(n)
+    jac, df = geom_factors(ctx, "pyr", Q, X)
+    coll = Collection(ctx, "pyr", n, Q, E, jac, df)
+    coll32 = Collection(ctx, "pyr", n, Q, E, jac, df, precision="fp32")
+    nc, nq = coll.nm, coll.nq
+    rng = np.random.default_rng(14)
+    u = torch.from_numpy(rng.uniform(-1, 1, E * nc)).to(cuda)
+    u32 = u.float()
+    phys = torch.empty(E * nq, dtype=torch.float64, device=cuda)
+    coef, coef32 = torch.empty_like(u), torch.empty_like(u32)
+    d = [torch.empty_like(phys) for _ in range(3)]
+    coll.bwdtrans(u, phys)
+    reps = 20
+    ms = {"bwdtrans": _time_device(torch, stream, lambda: coll.bwdtrans(u, phys), reps),
+          "iproduct": _time_device(torch, stream, lambda: coll.iproduct(phys, coef), reps),
+          "physderiv": _time_device(torch, stream, lambda: coll.physderiv(phys, d), reps),
+          "helmholtz": _time_device(torch, stream, lambda: coll.helmholtz(1.0, u, coef), reps)}
+    ms32 = _time_device(torch, stream, lambda: coll32.helmholtz(1.0, u32, coef32), reps)
+    fl = pyr_helm_flops(n)
+    tflops = E * fl / (ms["helmholtz"] / 1e3) / 1e12
+    t0 = time.perf_counter()
+    amap = m.assembly(n)
+    asm_s = time.perf_counter() - t0
+    sysg = GlobalLinSysIterativeFullGPU(coll, amap)
+    ex = (np.sin(np.pi * X[0]) * np.sin(np.pi * X[1]) * np.sin(np.pi * X[2])).reshape(-1)
+    f = -(1.0 + 3 * np.pi ** 2) * ex
+    b_h = -amap.assemble(coll.iproduct(f))
+    b_h[:amap.ndir] = 0.0
+    b = torch.from_numpy(b_h).to(cuda)
+    x = torch.zeros_like(b)
+    out = {"workload": f"{mesh}^3 cubes as {E} curved jittered pyramids, P={P} (n={n}: {nc} modes, "
+                       f"{Q}x{Q}x{n} points), lambda=1, per-point geometry",
+           "elements": E, "local_dofs": E * nc, "solve_dofs": amap.nglobal - amap.ndir, "assembly_map_s": asm_s,
+           "fp64_gdofs": {k: E * nc / (v / 1e3) / 1e9 for k, v in ms.items()},
+           "fp32_helmholtz_gdofs": E * nc / (ms32 / 1e3) / 1e9,
+           "helmholtz_fp64": {"ms": ms["helmholtz"], "flop_per_element": fl, "tflops": tflops,
+                              "bound": "fp64 pipe", "peak_tflops": FP64_FMA_PEAK_TF,
+                              "frac": tflops / FP64_FMA_PEAK_TF,
+                              "peak_source": "measured FP64 FMA issue rate (bench.py --config peaks)"}}
+    for mode in ("fp64", "mixed"):
+        sysg.solve(1.0, b, x, tol=TOL, mode=mode)
+        rate, (_, res) = _solve_rate(torch, stream, lambda: sysg.solve(1.0, b, x, tol=TOL, mode=mode), 2)
+        out[mode] = {"solves_per_s": rate, "iterations": res.iterations, "outer": res.outer_iterations,
+                     "rel_residual": res.rel_residual}
+        if mode == "fp64":
+            x64 = x.clone()
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["max_rel_diff_mixed_vs_fp64"] = float((x - x64).abs().max() / x64.abs().max())
+    uh = coll.bwdtrans(sysg.global_to_local(x64.cpu().numpy()))
+    out["max_error_vs_exact_sin_sin_sin"] = float(np.max(np.abs(uh - ex)))
+    sysg.close()
+    coll.close()
+    coll32.close()
+    ctx.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def quad_sweep_batched_fields():
     """The 32 x 32 jittered-quad mesh's lambda sweep (P = 6 and 8, lambda in {0.1, 1, 10}:
     six systems) solved as one batch to 1e-10: mixed vs FP64 solves/s, each batch solve one
@@ -719,7 +797,8 @@ def run_gpu(args, rank, world):
                         ("batched_256", batched_fields),
                         ("tri_128x128_p6", lambda: tri_fields(torch, cuda)),
                         ("tet_12x12x12_p6", lambda: tet_fields(torch, cuda)),
-                        ("prism_12x12x12_p6", lambda: prism_fields(torch, cuda))):
+                        ("prism_12x12x12_p6", lambda: prism_fields(torch, cuda)),
+                        ("pyr_10x10x10_p6", lambda: pyr_fields(torch, cuda))):
             try:
                 line[key] = fn()
             except Exception as ex:  # one failing secondary field does not void the headline
@@ -1145,7 +1224,15 @@ def suite_prism(args):
           out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", prism=out)
 
 
-SUITES = {"quad2d": suite_quad2d, "tri": suite_tri, "tet": suite_tet, "prism": suite_prism, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
+def suite_pyr(args):
+    """Pyramids: 10^3 cubes (6000 curved pyramids) at P = 6."""
+    import torch
+    out = pyr_fields(torch, "cuda:0")
+    _line("3-D Helmholtz on curved pyramids, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
+          out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", pyr=out)
+
+
+SUITES = {"quad2d": suite_quad2d, "tri": suite_tri, "tet": suite_tet, "prism": suite_prism, "pyr": suite_pyr, "mixed2d": suite_mixed2d, "hex_orders": suite_hex_orders, "batched": suite_batched,
           "pod": suite_pod, "adjoint": suite_adjoint, "inner_apply": suite_inner_apply,
           "peaks": suite_peaks}
 

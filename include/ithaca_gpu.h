@@ -46,6 +46,7 @@ enum {
   ITHACA_GPU_SHAPE_TRI = 3,
   ITHACA_GPU_SHAPE_QUAD = 4,
   ITHACA_GPU_SHAPE_TET = 5,
+  ITHACA_GPU_SHAPE_PYR = 6,
   ITHACA_GPU_SHAPE_PRISM = 7,
   ITHACA_GPU_SHAPE_HEX = 8
 };
@@ -106,6 +107,13 @@ int ithaca_gpu_basis_tri(int nmodes, double* z0, double* w0, double* D0, double*
  * (nc*Q2, nc = nmodes (nmodes+1) (nmodes+2) / 6). Host arrays; any pointer may be NULL. */
 int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double* B2, double* DB2);
 
+/* ---- pyramid basis, direction 2: eModifiedPyr_C on Q2 = nmodes Gauss-Radau-Jacobi
+ *      (alpha 2, beta 0) points (MeshGraph.cpp:1719-1745; Basis.cpp:568-672) ----
+ * Directions 0 and 1 are ithaca_gpu_basis_modA(nmodes, nmodes + 1). z2, w2 (Q2, without
+ * the collapsed map's factor 1/4), D2 (Q2*Q2), B2 and DB2 (nc*Q2, nc = nmodes (nmodes+1)
+ * (2 nmodes+1) / 6, modes m(p, q, r) with r fastest and r < nmodes - max(p, q)). */
+int ithaca_gpu_basis_pyr(int nmodes, double* z2, double* w2, double* D2, double* B2, double* DB2);
+
 /* ---- geometry (SpatialDomains/GeomFactors.cpp:168-475 ComputeDeriv/ComputeJac/
  *      ComputeDerivFactors) ----
  * coords: d arrays of E*Q^d physical coordinates at the GLL quadrature points,
@@ -117,7 +125,8 @@ int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double*
  * StdTriExp::v_PhysDeriv. Tetrahedra (shape 5): npoints = Q0, coordinates at the
  * Q0 x (Q0-1) x (Q0-1) collapsed points (point (k Q1 + j) Q0 + i), 3 arrays; chain rule of
  * StdTetExp::v_PhysDeriv. Prisms (shape 7): npoints = Q0, coordinates at the Q0 x Q0 x
- * (Q0-1) points (point (k Q0 + j) Q0 + i), chain rule of StdPrismExp::v_PhysDeriv. */
+ * (Q0-1) points (point (k Q0 + j) Q0 + i), chain rule of StdPrismExp::v_PhysDeriv; pyramids
+ * (shape 6) the same point set with the chain rule of StdPyrExp::v_PhysDeriv. */
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device);
 
@@ -141,13 +150,17 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
  * eModified_B (rows (p, r), the triangle's direction 1 of ithaca_gpu_basis_tri) on nmodes
  * Gauss-Radau points in direction 2; nmodes^2 (nmodes+1) / 2 coefficients and Q0^2 (Q0-1)
  * points per element, modes m(p, q, r) with r fastest and r < nmodes - p
- * (MatrixFreeOps/Helmholtz.h:1003-1030, 1291-1440; IProductWRTDerivBase.h:1660-1760). */
+ * (MatrixFreeOps/Helmholtz.h:1003-1030, 1291-1440; IProductWRTDerivBase.h:1660-1760).
+ * Pyramids (shape 6): eModified_A in directions 0 and 1, eModifiedPyr_C of
+ * ithaca_gpu_basis_pyr in direction 2; nmodes (nmodes+1) (2 nmodes+1) / 6 coefficients and
+ * Q0^2 (Q0-1) points per element (MatrixFreeOps/Helmholtz.h:1480-1510, 1770-1960;
+ * IProductWRTDerivBase.h:2070-2200). */
 int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints, int nelmt, const double* jac,
                          const double* df, int deformed, int precision, int on_device, ithaca_gpu_op** op);
 int ithaca_gpu_op_destroy(ithaca_gpu_op* op);
 /* Ndof() = nelmt * nmodes^d (MatrixFreeOps/Helmholtz.h:279-282); nelmt * nmodes (nmodes+1)/2
  * for triangles, nelmt * nmodes (nmodes+1) (nmodes+2)/6 for tetrahedra, nelmt * nmodes^2 (nmodes+1)/2
- * for prisms. */
+ * for prisms, nelmt * nmodes (nmodes+1) (2 nmodes+1)/6 for pyramids. */
 int ithaca_gpu_op_ndof(ithaca_gpu_op* op, long long* ndof);
 
 /* BwdTrans (Collections/BwdTrans.cpp:143-240): coefficients -> physical values. */

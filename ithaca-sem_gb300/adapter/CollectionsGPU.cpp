@@ -1,7 +1,7 @@
 // Implementation type "GPU" for the Collections operators (Collections/Operator.h:113-165,
 // registrations as Collections/Helmholtz.cpp:484-503): BwdTrans, IProductWRTBase,
-// PhysDeriv, IProductWRTDerivBase and Helmholtz of triangular, quadrilateral,
-// tetrahedral, prismatic and hexahedral collections run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
+// PhysDeriv, IProductWRTDerivBase and Helmholtz of collections of every shape
+// (triangles, quadrilaterals, tetrahedra, pyramids, prisms, hexahedra) run in the GB300 library. Nektar's arrays are passed unchanged: the C ABI
 // keeps the reference's element-contiguous layouts and CoalescedGeomData's geometry.
 #include <Collections/Operator.h>
 
@@ -19,10 +19,8 @@ class GpuOperatorBase : public Operator {
   GpuOperatorBase(std::vector<StdRegions::StdExpansionSharedPtr> pCollExp, CoalescedGeomDataSharedPtr pGeomData)
       : Operator(pCollExp, pGeomData) {
     const auto shape = pCollExp[0]->DetShapeType();
-    if (shape != LibUtilities::eTriangle && shape != LibUtilities::eQuadrilateral &&
-        shape != LibUtilities::eTetrahedron && shape != LibUtilities::ePrism && shape != LibUtilities::eHexahedron)
-      NEKERROR(ErrorUtil::efatal, "GPU operators are built for triangles, quadrilaterals, tetrahedra, prisms and "
-                                  "hexahedra");
+    if (shape < LibUtilities::eTriangle || shape > LibUtilities::eHexahedron)
+      NEKERROR(ErrorUtil::efatal, "GPU operators are built for two- and three-dimensional elements");
     const int nm = pCollExp[0]->GetBasis(0)->GetNumModes();
     const int nq = pCollExp[0]->GetBasis(0)->GetNumPoints();
     const Array<OneD, const NekDouble>& jac = pGeomData->GetJac(pCollExp);
@@ -119,6 +117,8 @@ class Helmholtz_GPU final : public GpuOperatorBase {
                                                    cls::create, name "_Quad"),                                 \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eTetrahedron, op, eGPU, false),   \
                                                    cls::create, name "_Tet"),                                  \
+      GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::ePyramid, op, eGPU, false),       \
+                                                   cls::create, name "_Pyr"),                                  \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::ePrism, op, eGPU, false),         \
                                                    cls::create, name "_Prism"),                                \
       GetOperatorFactory().RegisterCreatorFunction(OperatorKey(LibUtilities::eHexahedron, op, eGPU, false),    \

@@ -16,9 +16,11 @@
 //   derivative matrix by the barycentric Lagrange formula (Polylib.cpp:589-626 Dgrjm)
 //   ModifiedB modes B1 (n (n+1)/2 of them, q fastest), DB1 = D1 B1 (Basis.cpp:423-507)
 // Tetrahedra add direction 2: Gauss-Radau-Jacobi points for the weight (1 - z)^2 and the
-// ModifiedC rows phi^c_{pqr} = phi^b_{p+q,r} (Basis.cpp:512-566).
+// ModifiedC rows phi^c_{pqr} = phi^b_{p+q,r} (Basis.cpp:512-566); pyramids the
+// ModifiedPyr_C rows on the same points (Basis.cpp:568-672).
 #include "ithaca_internal.h"
 
+#include <algorithm>
 #include <cmath>
 
 namespace ithaca {
@@ -225,6 +227,46 @@ TetBasisTables make_tet_basis(int n) {
           t.DB2[(size_t)m * Q + k] = DBb[(size_t)row * Q + k];
         }
       }
+  return t;
+}
+
+PyrBasisTables make_pyr_basis(int n) {
+  PyrBasisTables t;
+  t.n = n;
+  t.nc = n * (n + 1) * (2 * n + 1) / 6;
+  t.a = make_basis(n, n + 1);
+  const int Q = n, npq = n * (n + 1) / 2;
+  t.z2.resize(Q);
+  t.w2.resize(Q);
+  t.D2.resize(Q * Q);
+  radau_points(Q, t.z2.data(), t.w2.data(), 2.0);
+  lagrange_derivative(Q, t.z2.data(), t.D2.data());
+  std::vector<double> Bb((size_t)npq * Q), DBb((size_t)npq * Q);
+  modB_tables(n, Q, t.z2.data(), t.D2.data(), Bb.data(), DBb.data());
+  t.B2.resize((size_t)t.nc * Q);
+  int m = 0;
+  for (int p = 0; p < n; ++p)
+    for (int q = 0; q < n; ++q)
+      for (int r = 0; r < n - std::max(p, q); ++r, ++m) {
+        double* row = &t.B2[(size_t)m * Q];
+        if (std::min(p, q) <= 1) {  // the ModifiedB row (max(p, q), r)
+          int b = r;
+          for (int pp = 0; pp < std::max(p, q); ++pp) b += n - pp;
+          for (int k = 0; k < Q; ++k) row[k] = Bb[(size_t)b * Q + k];
+        } else {  // ((1-z)/2)^(p+q-2) [(1+z)/2 P_{r-1}^{(2p+2q-3,1)}]
+          for (int k = 0; k < Q; ++k) {
+            const double z = t.z2[k], lo = 0.5 * (1.0 - z), hi = 0.5 * (1.0 + z);
+            row[k] = std::pow(lo, p + q - 2) * (r == 0 ? 1.0 : hi * jacobi(r - 1, 2.0 * p + 2.0 * q - 3.0, 1.0, z));
+          }
+        }
+      }
+  t.DB2.resize((size_t)t.nc * Q);
+  for (int mm = 0; mm < t.nc; ++mm)
+    for (int i = 0; i < Q; ++i) {
+      double acc = 0.0;
+      for (int k = 0; k < Q; ++k) acc += t.D2[k * Q + i] * t.B2[(size_t)mm * Q + k];
+      t.DB2[(size_t)mm * Q + i] = acc;
+    }
   return t;
 }
 

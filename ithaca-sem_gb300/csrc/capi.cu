@@ -99,9 +99,37 @@ static int guarded(F f) {
 
 static int shape_dim(int shape) {
   if (shape == ITHACA_GPU_SHAPE_QUAD || shape == ITHACA_GPU_SHAPE_TRI) return 2;
-  if (shape == ITHACA_GPU_SHAPE_HEX || shape == ITHACA_GPU_SHAPE_TET || shape == ITHACA_GPU_SHAPE_PRISM) return 3;
+  if (shape == ITHACA_GPU_SHAPE_HEX || shape == ITHACA_GPU_SHAPE_TET || shape == ITHACA_GPU_SHAPE_PRISM ||
+      shape == ITHACA_GPU_SHAPE_PYR)
+    return 3;
   fail(ITHACA_GPU_ERR_UNSUPPORTED,
-       "shape must be triangle (3), quadrilateral (4), tetrahedron (5), prism (7) or hexahedron (8)");
+       "shape must be triangle (3), quadrilateral (4), tetrahedron (5), pyramid (6), prism (7) or hexahedron (8)");
+}
+
+// Packed pyramid tables (layout pyr_off in ithaca_internal.h), host FP64.
+static std::vector<double> pack_pyr_tables(const PyrBasisTables& t) {
+  const PyrOff o = pyr_off(t.n);
+  const int n = t.n, Q0 = n + 1, Q2 = n, nc = t.nc;
+  std::vector<double> h(o.size);
+  for (int i = 0; i < n * Q0; ++i) {
+    h[o.B0 + i] = t.a.B[i];
+    h[o.DB0 + i] = t.a.DB[i];
+  }
+  for (int i = 0; i < Q0 * Q0; ++i) h[o.D0 + i] = t.a.D[i];
+  for (int i = 0; i < Q0; ++i) {
+    h[o.w0 + i] = t.a.w[i];
+    h[o.h0 + i] = 0.5 * (1.0 + t.a.z[i]);
+  }
+  for (int i = 0; i < nc * Q2; ++i) {
+    h[o.B2 + i] = t.B2[i];
+    h[o.DB2 + i] = t.DB2[i];
+  }
+  for (int i = 0; i < Q2 * Q2; ++i) h[o.D2 + i] = t.D2[i];
+  for (int k = 0; k < Q2; ++k) {
+    h[o.w2 + k] = 0.25 * t.w2[k];  // MatrixFreeOps/Operator.hpp:249-251
+    h[o.h2 + k] = 2.0 / (1.0 - t.z2[k]);
+  }
+  return h;
 }
 
 // Packed prism tables (layout prism_off in ithaca_internal.h), host FP64.
@@ -385,6 +413,19 @@ int ithaca_gpu_basis_tet(int nmodes, double* z2, double* w2, double* D2, double*
   });
 }
 
+int ithaca_gpu_basis_pyr(int nmodes, double* z2, double* w2, double* D2, double* B2, double* DB2) {
+  return guarded([&] {
+    require(nmodes >= 2 && nmodes <= 16, "need 2 <= nmodes <= 16");
+    const PyrBasisTables t = make_pyr_basis(nmodes);
+    const int Q = nmodes, nc = t.nc;
+    if (z2) std::memcpy(z2, t.z2.data(), sizeof(double) * Q);
+    if (w2) std::memcpy(w2, t.w2.data(), sizeof(double) * Q);
+    if (D2) std::memcpy(D2, t.D2.data(), sizeof(double) * Q * Q);
+    if (B2) std::memcpy(B2, t.B2.data(), sizeof(double) * nc * Q);
+    if (DB2) std::memcpy(DB2, t.DB2.data(), sizeof(double) * nc * Q);
+  });
+}
+
 int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nelmt, const double* coords,
                             double* jac, double* df, int on_device) {
   return guarded([&] {
@@ -392,6 +433,31 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
     StreamOrder order_(ctx);
     require(nelmt > 0 && npoints >= 2 && npoints <= 16, "bad sizes");
     const int dim = shape_dim(shape);
+    if (shape == ITHACA_GPU_SHAPE_PYR) {  // npoints = Q0 = Q1 = n + 1; Q2 = n Gauss-Radau (alpha 2)
+      const int n = npoints - 1;
+      const size_t tot = (size_t)nelmt * npoints * npoints * n;
+      const std::vector<double> h = pack_pyr_tables(make_pyr_basis(n));
+      double* dtab = nullptr;
+      int* dbad = nullptr;
+      ITHACA_CUDA(cudaMalloc(&dtab, sizeof(double) * h.size()));
+      std::unique_ptr<double, decltype(&cudaFree)> g1(dtab, cudaFree);
+      ITHACA_CUDA(cudaMalloc(&dbad, sizeof(int)));
+      std::unique_ptr<int, decltype(&cudaFree)> g2(dbad, cudaFree);
+      ITHACA_CUDA(cudaMemcpyAsync(dtab, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+      ITHACA_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+      const double* X = (const double*)to_device(ctx, 0, coords, sizeof(double) * 3 * tot, on_device);
+      double* J = (double*)out_buffer(ctx, 1, jac, sizeof(double) * tot, on_device);
+      double* F = (double*)out_buffer(ctx, 2, df, sizeof(double) * 9 * tot, on_device);
+      launch_geom_factors_pyr(n, nelmt, dtab, X, J, F, dbad, ctx->stream);
+      ctx->launches++;
+      from_device(ctx, jac, J, sizeof(double) * tot, on_device);
+      from_device(ctx, df, F, sizeof(double) * 9 * tot, on_device);
+      int hbad = 0;
+      ITHACA_CUDA(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      ITHACA_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (hbad) fail(ITHACA_GPU_ERR_GEOMETRY, "non-positive Jacobian at a quadrature point");
+      return;
+    }
     if (shape == ITHACA_GPU_SHAPE_PRISM) {  // npoints = Q0 = Q1 = n + 1; Q2 = n Gauss-Radau
       const int n = npoints - 1;
       const size_t tot = (size_t)nelmt * npoints * npoints * n;
@@ -516,7 +582,33 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     o->deformed = deformed ? 1 : 0;
     o->precision = precision;
     const size_t npt = o->deformed ? (size_t)(dim == 2 ? npoints * npoints : npoints * npoints * npoints) : 1;
-    if (shape == ITHACA_GPU_SHAPE_PRISM) {
+    if (shape == ITHACA_GPU_SHAPE_PYR) {
+      // ModifiedA x ModifiedA x ModifiedPyr_C: n (n+1) (2n+1) / 6 modes on (n + 1)^2 n points; the
+      // geometry is expanded to per-point metric terms whatever the input kind
+      o->kdim = kPyrKernels;
+      o->nm = pyr_nc(nmodes);
+      o->nq = npoints * npoints * nmodes;
+      const std::vector<double> h = pack_pyr_tables(make_pyr_basis(nmodes));
+      upload_packed(o->t64, h, nmodes, npoints);
+      upload_packed(o->t32, h, nmodes, npoints);
+      const size_t tp = o->deformed ? (size_t)o->nq : 1;
+      const double* J = (const double*)to_device(ctx, 0, jac, sizeof(double) * nelmt * tp, on_device);
+      const double* F = (const double*)to_device(ctx, 1, df, sizeof(double) * 9 * nelmt * tp, on_device);
+      const int in_deformed = o->deformed;
+      o->deformed = 1;
+      const size_t njg = (size_t)nelmt * 7 * o->nq, ndf = (size_t)nelmt * 9 * o->nq;
+      ITHACA_CUDA(cudaMalloc(&o->jg64, sizeof(double) * njg));
+      ITHACA_CUDA(cudaMalloc(&o->df64, sizeof(double) * ndf));
+      launch_build_jg_pyr<double>(nmodes, nelmt, in_deformed, o->t64.base, J, F, o->jg64, o->df64, ctx->stream);
+      ctx->launches++;
+      if (precision == ITHACA_GPU_FP32) {
+        ITHACA_CUDA(cudaMalloc(&o->jg32, sizeof(float) * njg + kGeoPad));
+        ITHACA_CUDA(cudaMalloc(&o->df32, sizeof(float) * ndf));
+        launch_build_jg_pyr<float>(nmodes, nelmt, in_deformed, o->t64.base, J, F, o->jg32, o->df32,
+                                     ctx->stream);
+        ctx->launches++;
+      }
+    } else if (shape == ITHACA_GPU_SHAPE_PRISM) {
       // ModifiedA x ModifiedA x ModifiedB: n^2 (n+1) / 2 modes on (n + 1)^2 n points; the
       // geometry is expanded to per-point metric terms whatever the input kind
       o->kdim = kPrismKernels;

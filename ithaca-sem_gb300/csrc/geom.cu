@@ -447,4 +447,110 @@ template void launch_build_jg_prism<double>(int, int, int, const double*, const 
 template void launch_build_jg_prism<float>(int, int, int, const double*, const double*, const double*, float*,
                                            float*, cudaStream_t);
 
+// ---- pyramids ----
+// xi derivatives: d/dxi0 = h2 d0, d/dxi1 = h2 d1, d/dxi2 = h0 d/dxi0 + h1 d/dxi1 + d2
+// (StdPyrExp; h1 = (1 + z0_j)/2).
+__global__ void geom_factors_pyr_kernel(int n, int E, const double* __restrict__ tab,
+                                          const double* __restrict__ X, double* __restrict__ jac,
+                                          double* __restrict__ df, int* bad) {
+  const PyrOff o = pyr_off(n);
+  const int Q0 = n + 1, Q2 = n, nq = Q0 * Q0 * Q2;
+  const size_t total = (size_t)E * nq;
+  for (size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (size_t)gridDim.x * blockDim.x) {
+    const int e = (int)(gid / nq), p = (int)(gid % nq);
+    const int i = p % Q0, j = (p / Q0) % Q0, k = p / (Q0 * Q0);
+    double M[3][3];
+    for (int c = 0; c < 3; ++c) {
+      const double* x = X + (size_t)c * total + (size_t)e * nq;
+      double d0 = 0, d1 = 0, d2 = 0;
+      for (int a = 0; a < Q0; ++a) d0 += tab[o.D0 + a * Q0 + i] * x[(k * Q0 + j) * Q0 + a];
+      for (int a = 0; a < Q0; ++a) d1 += tab[o.D0 + a * Q0 + j] * x[(k * Q0 + a) * Q0 + i];
+      for (int a = 0; a < Q2; ++a) d2 += tab[o.D2 + a * Q2 + k] * x[(a * Q0 + j) * Q0 + i];
+      M[c][0] = tab[o.h2 + k] * d0;
+      M[c][1] = tab[o.h2 + k] * d1;
+      M[c][2] = tab[o.h0 + i] * M[c][0] + tab[o.h0 + j] * M[c][1] + d2;
+    }
+    const double c00 = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+    const double c01 = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+    const double c02 = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+    const double det = M[0][0] * c00 + M[0][1] * c01 + M[0][2] * c02;
+    if (!(det > 0.0)) atomicOr(bad, 1);
+    jac[gid] = det;
+    double inv[3][3];
+    inv[0][0] = c00 / det;
+    inv[1][0] = c01 / det;
+    inv[2][0] = c02 / det;
+    inv[0][1] = (M[0][2] * M[2][1] - M[0][1] * M[2][2]) / det;
+    inv[1][1] = (M[0][0] * M[2][2] - M[0][2] * M[2][0]) / det;
+    inv[2][1] = (M[0][1] * M[2][0] - M[0][0] * M[2][1]) / det;
+    inv[0][2] = (M[0][1] * M[1][2] - M[0][2] * M[1][1]) / det;
+    inv[1][2] = (M[0][2] * M[1][0] - M[0][0] * M[1][2]) / det;
+    inv[2][2] = (M[0][0] * M[1][1] - M[0][1] * M[1][0]) / det;
+    for (int c = 0; c < 3; ++c)
+      for (int a = 0; a < 3; ++a) df[(size_t)(c * 3 + a) * total + gid] = inv[a][c];
+  }
+}
+
+void launch_geom_factors_pyr(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                               int* bad, cudaStream_t s) {
+  const size_t total = (size_t)E * (n + 1) * (n + 1) * n;
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
+  geom_factors_pyr_kernel<<<blocks, threads, 0, s>>>(n, E, tab, coords, jac, df, bad);
+}
+
+// Per point Jw = J w0_i w0_j w2_k/2 and Jw m^{ab} with the collapsed metric of
+// HelmholtzPrismImpl (MatrixFreeOps/Helmholtz.h:1340-1400): a_c = h1 (df_c0 + h0 df_c2),
+// b_c = df_c1, e_c = df_c2.
+template <typename T>
+__global__ void build_jg_pyr_kernel(int n, int E, int deformed, const double* __restrict__ tab,
+                                      const double* __restrict__ jac, const double* __restrict__ df,
+                                      T* __restrict__ jg, T* __restrict__ dfo) {
+  const PyrOff o = pyr_off(n);
+  const int Q0 = n + 1, Q2 = n, nq = Q0 * Q0 * Q2;
+  const size_t total = (size_t)E * nq, tin = (size_t)E * (deformed ? nq : 1);
+  for (size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gid < total;
+       gid += (size_t)gridDim.x * blockDim.x) {
+    const int e = (int)(gid / nq), p = (int)(gid % nq);
+    const int i = p % Q0, j = (p / Q0) % Q0, k = p / (Q0 * Q0);
+    const size_t src = deformed ? gid : (size_t)e;
+    double f[9];
+    for (int c = 0; c < 9; ++c) f[c] = df[(size_t)c * tin + src];
+    const double h0 = tab[o.h0 + i], h1 = tab[o.h0 + j], h2 = tab[o.h2 + k];
+    const double jw = jac[src] * tab[o.w0 + i] * tab[o.w0 + j] * tab[o.w2 + k];
+    double a[3], b[3], c3[3];
+    for (int c = 0; c < 3; ++c) {
+      a[c] = h2 * (f[3 * c] + h0 * f[3 * c + 2]);
+      b[c] = h2 * (f[3 * c + 1] + h1 * f[3 * c + 2]);
+      c3[c] = f[3 * c + 2];
+    }
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    T* out = jg + (size_t)e * 7 * nq + p;
+    out[0] = (T)jw;
+    out[(size_t)1 * nq] = (T)(jw * dot(a, a));
+    out[(size_t)2 * nq] = (T)(jw * dot(a, b));
+    out[(size_t)3 * nq] = (T)(jw * dot(a, c3));
+    out[(size_t)4 * nq] = (T)(jw * dot(b, b));
+    out[(size_t)5 * nq] = (T)(jw * dot(b, c3));
+    out[(size_t)6 * nq] = (T)(jw * dot(c3, c3));
+    T* o2 = dfo + (size_t)e * 9 * nq + p;
+    for (int c = 0; c < 9; ++c) o2[(size_t)c * nq] = (T)f[c];
+  }
+}
+
+template <typename T>
+void launch_build_jg_pyr(int n, int E, int deformed, const double* tab, const double* jac, const double* df,
+                           T* jg, T* dfo, cudaStream_t s) {
+  const size_t total = (size_t)E * (n + 1) * (n + 1) * n;
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)device_sm_count() * 32);
+  build_jg_pyr_kernel<T><<<blocks, threads, 0, s>>>(n, E, deformed, tab, jac, df, jg, dfo);
+}
+
+template void launch_build_jg_pyr<double>(int, int, int, const double*, const double*, const double*, double*,
+                                            double*, cudaStream_t);
+template void launch_build_jg_pyr<float>(int, int, int, const double*, const double*, const double*, float*,
+                                           float*, cudaStream_t);
+
 }  // namespace ithaca

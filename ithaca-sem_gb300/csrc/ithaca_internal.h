@@ -142,12 +142,49 @@ inline __host__ __device__ constexpr PrismOff prism_off(int n) {
   return o;
 }
 
+// Pyramid direction 2 (host, FP64), basis.cpp: Gauss-Radau (alpha 2) points and the
+// ModifiedPyr_C rows of the nc = n (n+1) (2n+1) / 6 modes m(p, q, r) (r fastest,
+// r < n - max(p, q)); directions 0 and 1 are make_basis(n, n + 1).
+struct PyrBasisTables {
+  int n = 0, nc = 0;
+  BasisTables a;
+  std::vector<double> z2, w2, D2, B2, DB2;
+};
+PyrBasisTables make_pyr_basis(int n);
+
+// Packed device tables of a pyramid expansion (Q0 = n + 1 for directions 0 and 1, Q2 = n):
+//   B0 [p*Q0+i] D0 [k*Q0+i] w0 [i] h0 [i] = (1+z0_i)/2 (directions 0 and 1 share them)
+//   B2 [m*Q2+k] D2 [l*Q2+k] w2 [k] = w2_k/4 h2 [k] = 2/(1-z2_k)
+//   then DB0, DB2 (diagonal kernel only)
+struct PyrOff {
+  int B0, D0, w0, h0, B2, D2, w2, h2, DB0, DB2, core, size;
+};
+inline __host__ __device__ constexpr int pyr_nc(int n) { return n * (n + 1) * (2 * n + 1) / 6; }
+inline __host__ __device__ constexpr PyrOff pyr_off(int n) {
+  const int Q0 = n + 1, Q2 = n, nc = n * (n + 1) * (2 * n + 1) / 6;
+  PyrOff o{};
+  o.B0 = 0;
+  o.D0 = o.B0 + n * Q0;
+  o.w0 = o.D0 + Q0 * Q0;
+  o.h0 = o.w0 + Q0;
+  o.B2 = o.h0 + Q0;
+  o.D2 = o.B2 + nc * Q2;
+  o.w2 = o.D2 + Q2 * Q2;
+  o.h2 = o.w2 + Q2;
+  o.core = o.h2 + Q2;
+  o.DB0 = o.core;
+  o.DB2 = o.DB0 + n * Q0;
+  o.size = o.DB2 + nc * Q2;
+  return o;
+}
+
 // Kernel family passed where the launchers below take `dim`: 2 (quads), 3 (hexes),
-// kTriKernels (triangles; their geometry has the 2-D layout), kTetKernels and
-// kPrismKernels (tetrahedra and prisms; per-point geometry with the 3-D layout, 7 fields).
+// kTriKernels (triangles; their geometry has the 2-D layout), kTetKernels, kPrismKernels
+// and kPyrKernels (per-point geometry with the 3-D layout, 7 fields).
 constexpr int kTriKernels = 23;
 constexpr int kTetKernels = 33;
 constexpr int kPrismKernels = 34;
+constexpr int kPyrKernels = 35;
 
 // Device copy of the 1-D tables for one (n, Q), packed for the kernels:
 //   B  [p*Q + i]   Bt  [i*n + p]   DB [p*Q + i]   DBt [i*n + p]
@@ -336,6 +373,20 @@ struct PrismApi {
                    const T* in2, T* out, cudaStream_t s);
 };
 
+// Pyramids (elem_pyr.cuh); geometry always per point. The same entry points as TetApi.
+template <typename T>
+struct PyrApi {
+  static bool helm(int n, int Q, int E, const T* tab, const T* jg, T lambda, const T* in, T* out, const int* l2g,
+                   int ndir, const int* skip, const T* lam_ptr, cudaStream_t s);
+  static bool bwd(int n, int Q, int E, const T* tab, const T* in, T* out, cudaStream_t s);
+  static bool ipr(int n, int Q, int E, const T* tab, const T* jg, const T* in, T* out, cudaStream_t s);
+  static bool deriv(int n, int Q, int E, const T* tab, const T* df, const T* in, T* d0, T* d1, T* d2,
+                    cudaStream_t s);
+  static bool diag(int n, int Q, int E, const T* tab, const T* jg, T lambda, T* out, cudaStream_t s);
+  static bool iprd(int n, int Q, int E, const T* tab, const T* jg, const T* df, const T* in0, const T* in1,
+                   const T* in2, T* out, cudaStream_t s);
+};
+
 template <typename T>
 inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T* tab, const T* jg, T lambda,
                              const T* in, T* out, const int* l2g, int ndir, cudaStream_t s,
@@ -348,6 +399,8 @@ inline bool launch_helmholtz(int dim, int n, int Q, int E, int deformed, const T
                                                                       skip, lam_ptr, s);
   if (dim == kPrismKernels)
     return esolve == nullptr && PrismApi<T>::helm(n, Q, E, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);
+  if (dim == kPyrKernels)
+    return esolve == nullptr && PyrApi<T>::helm(n, Q, E, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, s);
   return dim == 2 ? ElemApi<T, 2>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
                                         esolve, skip_stride, s, variant)
                   : ElemApi<T, 3>::helm(n, Q, E, deformed, tab, jg, lambda, in, out, l2g, ndir, skip, lam_ptr,
@@ -358,6 +411,7 @@ inline bool launch_bwdtrans(int dim, int n, int Q, int E, const T* tab, const T*
   if (dim == kTriKernels) return TriApi<T>::bwd(n, Q, E, tab, in, out, s);
   if (dim == kTetKernels) return TetApi<T>::bwd(n, Q, E, tab, in, out, s);
   if (dim == kPrismKernels) return PrismApi<T>::bwd(n, Q, E, tab, in, out, s);
+  if (dim == kPyrKernels) return PyrApi<T>::bwd(n, Q, E, tab, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::bwd(n, Q, E, tab, in, out, s) : ElemApi<T, 3>::bwd(n, Q, E, tab, in, out, s);
 }
 template <typename T>
@@ -366,6 +420,7 @@ inline bool launch_iproduct(int dim, int n, int Q, int E, int deformed, const T*
   if (dim == kTriKernels) return TriApi<T>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
   if (dim == kTetKernels) return TetApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
   if (dim == kPrismKernels) return PrismApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
+  if (dim == kPyrKernels) return PyrApi<T>::ipr(n, Q, E, tab, jg, in, out, s);
   return dim == 2 ? ElemApi<T, 2>::ipr(n, Q, E, deformed, tab, jg, in, out, s)
                   : ElemApi<T, 3>::ipr(n, Q, E, deformed, tab, jg, in, out, s);
 }
@@ -375,6 +430,7 @@ inline bool launch_physderiv(int dim, int n, int Q, int E, int deformed, const T
   if (dim == kTriKernels) return TriApi<T>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, s);
   if (dim == kTetKernels) return TetApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
   if (dim == kPrismKernels) return PrismApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
+  if (dim == kPyrKernels) return PyrApi<T>::deriv(n, Q, E, tab, df, in, d0, d1, d2, s);
   return dim == 2 ? ElemApi<T, 2>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s)
                   : ElemApi<T, 3>::deriv(n, Q, E, deformed, tab, df, in, d0, d1, d2, s);
 }
@@ -384,6 +440,7 @@ inline bool launch_iproduct_deriv(int dim, int n, int Q, int E, int deformed, co
   if (dim == kTriKernels) return TriApi<T>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, out, s);
   if (dim == kTetKernels) return TetApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
   if (dim == kPrismKernels) return PrismApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
+  if (dim == kPyrKernels) return PyrApi<T>::iprd(n, Q, E, tab, jg, df, in0, in1, in2, out, s);
   return dim == 2 ? ElemApi<T, 2>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s)
                   : ElemApi<T, 3>::iprd(n, Q, E, deformed, tab, jg, df, in0, in1, in2, out, s);
 }
@@ -393,6 +450,7 @@ inline bool launch_helm_diag(int dim, int n, int Q, int E, int deformed, const T
   if (dim == kTriKernels) return TriApi<T>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
   if (dim == kTetKernels) return TetApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
   if (dim == kPrismKernels) return PrismApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
+  if (dim == kPyrKernels) return PyrApi<T>::diag(n, Q, E, tab, jg, lambda, out, s);
   return dim == 2 ? ElemApi<T, 2>::diag(n, Q, E, deformed, tab, jg, lambda, out, s)
                   : ElemApi<T, 3>::diag(n, Q, E, deformed, tab, jg, lambda, out, s);
 }
@@ -427,5 +485,12 @@ void launch_build_jg_prism(int n, int E, int deformed, const double* tab, const 
                            T* jg, T* dfo, cudaStream_t s);
 void launch_geom_factors_prism(int n, int E, const double* tab, const double* coords, double* jac, double* df,
                                int* bad, cudaStream_t s);
+// Pyramids: per point J w0 w0 w2/4 and J w m^{ab} with the collapsed metric of
+// HelmholtzPyrImpl (MatrixFreeOps/Helmholtz.h:1841-1905).
+template <typename T>
+void launch_build_jg_pyr(int n, int E, int deformed, const double* tab, const double* jac, const double* df, T* jg,
+                         T* dfo, cudaStream_t s);
+void launch_geom_factors_pyr(int n, int E, const double* tab, const double* coords, double* jac, double* df,
+                             int* bad, cudaStream_t s);
 
 }  // namespace ithaca

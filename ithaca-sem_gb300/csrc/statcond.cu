@@ -26,6 +26,8 @@
 #include <string>
 #include <vector>
 
+#include <algorithm>
+
 #include "ithaca_internal.h"
 
 namespace ithaca {
@@ -576,6 +578,19 @@ int ithaca_gpu_sc_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
     const int dim = op->dim, n = op->n, nm = op->nm, E = op->E;
     std::vector<int> bm, im;
     for (int m = 0, tp = 0, tq = 0; m < nm; ++m) {
+      if (op->shape == ITHACA_GPU_SHAPE_PYR) {
+        // pyramid mode m(p, q, r): interior when p >= 2, q >= 2 and r >= 1
+        int pp = 0, qq = 0, rest = m;
+        while (rest >= n - std::max(pp, qq)) {
+          rest -= n - std::max(pp, qq);
+          if (++qq == n) {
+            qq = 0;
+            ++pp;
+          }
+        }
+        (pp >= 2 && qq >= 2 && rest >= 1 ? im : bm).push_back(m);
+        continue;
+      }
       if (op->shape == ITHACA_GPU_SHAPE_PRISM) {
         // prism mode m(p, q, r): interior when p >= 2, q >= 2 and r >= 1
         int pp = 0, rest = m;

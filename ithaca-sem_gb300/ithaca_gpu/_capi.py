@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(ROOT, "lib", "libithaca_gpu.so")
 OK = 0
 ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM = 1, 2, 3, 4
 ERR_NOT_CONVERGED, ERR_GEOMETRY, ERR_TIMEOUT, ERR_NUMERIC = 5, 6, 7, 8
-SHAPE_TRI, SHAPE_QUAD, SHAPE_TET, SHAPE_PRISM, SHAPE_HEX = 3, 4, 5, 7, 8
+SHAPE_TRI, SHAPE_QUAD, SHAPE_TET, SHAPE_PYR, SHAPE_PRISM, SHAPE_HEX = 3, 4, 5, 6, 7, 8
 FP64, FP32 = 0, 1
 SOLVE_FP64, SOLVE_MIXED_FP32, SOLVE_MIXED_FP32_GEO16 = 0, 1, 2
 
@@ -64,6 +64,7 @@ SIGNATURES = {
     "ithaca_gpu_basis_modA": [_i, _i, _vp, _vp, _vp, _vp, _vp],
     "ithaca_gpu_basis_tri": [_i] + [_vp] * 10,
     "ithaca_gpu_basis_tet": [_i] + [_vp] * 5,
+    "ithaca_gpu_basis_pyr": [_i] + [_vp] * 5,
     "ithaca_gpu_geom_factors": [_vp, _i, _i, _i, _vp, _vp, _vp, _i],
     "ithaca_gpu_op_create": [_vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _i, _pp],
     "ithaca_gpu_op_destroy": [_vp],

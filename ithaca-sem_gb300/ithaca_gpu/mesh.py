@@ -28,6 +28,9 @@ so this module generates them directly:
   extruded along y over the triangles (c000, c100, c001) and (c101, c001, c100) of its
   xz-face (StdPrismExp vertex order: v0 v1 v4 at the lower y, v3 v2 v5 above them, the
   singular edge v4-v5 along y); jitter and curvature as TetMesh.
+* ``PyrMesh``   -- nx x ny x nz cubes of the unit cube, each split into six pyramids with
+  the cube's centre as apex and a face as base (StdPyrExp vertex order, base cycle chosen
+  so that the element is positively oriented); jitter and curvature as TetMesh.
 * ``HexMesh``   -- nx x ny x nz hexahedra of the unit cube, optionally curved by
   x_a + amp * sin(2 pi x_b) sin(2 pi x_c) applied cyclically (a, b, c) =
   (0, 1, 2), (1, 2, 0), (2, 0, 1) to the straight positions.
@@ -348,6 +351,32 @@ _TET_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
 _PRISM_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [-1, 1, 1]])
 _PRISM_EDGES = ((0, 1), (1, 2), (3, 2), (0, 3), (0, 4), (1, 4), (2, 5), (3, 5), (4, 5))
 _PRISM_FACES = ((0, 1, 2, 3), (0, 1, 4), (1, 2, 5, 4), (3, 2, 5), (0, 3, 5, 4))
+# pyramid (StdPyrExp): the apex is vertex 4
+_PYR_XI = np.array([[-1.0, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1]])
+_PYR_EDGES = ((0, 1), (1, 2), (3, 2), (0, 3), (0, 4), (1, 4), (2, 4), (3, 4))
+_PYR_FACES = ((0, 1, 2, 3), (0, 1, 4), (1, 2, 4), (3, 2, 4), (0, 3, 4))
+
+
+def pyr_modal(n, xi0, xi1, xi2):
+    """Values of the pyramid's modes m(p, q, r) (r fastest, r < n - max(p, q)) at reference
+    points with xi2 < 1: (npts, nc); mode 1, the apex, is (1 + eta2)/2."""
+    xi0, xi1, xi2 = (np.asarray(a, dtype=np.float64) for a in (xi0, xi1, xi2))
+    e0 = 2 * (1 + xi0) / (1 - xi2) - 1
+    e1 = 2 * (1 + xi1) / (1 - xi2) - 1
+    lo, hi = 0.5 * (1 - xi2), 0.5 * (1 + xi2)
+    cols = []
+    for p in range(n):
+        for q in range(n):
+            for r in range(n - max(p, q)):
+                if (p, q, r) == (0, 0, 1):
+                    cols.append(hi)
+                    continue
+                if min(p, q) <= 1:
+                    c = _modB(max(p, q), r, xi2)
+                else:
+                    c = lo ** (p + q - 2) * (1.0 if r == 0 else hi * _jacobi_ab(r - 1, 2.0 * p + 2.0 * q - 3.0, 1.0, xi2))
+                cols.append(_modA(p, e0) * _modA(q, e1) * c)
+    return np.stack(np.broadcast_arrays(*cols), axis=-1)
 
 
 def prism_modal(n, xi0, xi1, xi2):
@@ -645,6 +674,53 @@ class PrismMesh:
     def assembly(self, n):
         """C0 numbering of the prism expansion with n modes; all boundary dofs Dirichlet."""
         return _c0_assembly(n, prism_modal, _PRISM_XI, _PRISM_EDGES, _PRISM_FACES, self.EV, self.V.shape[0])
+
+
+class PyrMesh:
+    def __init__(self, nx, ny, nz, jitter=0.0, seed=0, curve_amp=0.0):
+        t = TetMesh(nx, ny, nz, jitter=jitter, seed=seed)
+        nv = t.V.shape[0]
+        self.curve_amp = curve_amp
+        step = np.array([1, nx + 1, (nx + 1) * (ny + 1)])
+        ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        c000 = ((ck * (ny + 1) + cj) * (nx + 1) + ci).transpose(2, 1, 0).ravel()
+        ncell = c000.size
+        c = lambda a, b, d: c000 + a * step[0] + b * step[1] + d * step[2]
+        corners = {(a, b, d): c(a, b, d) for a in (0, 1) for b in (0, 1) for d in (0, 1)}
+        centres = nv + np.arange(ncell)
+        cen_xyz = np.mean([t.V[corners[k]] for k in corners], axis=0)
+        self.V = np.concatenate([t.V, cen_xyz])
+        faces = (((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)), ((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1)),
+                 ((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)), ((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)),
+                 ((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), ((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)))
+        pyrs = []
+        for f in faces:
+            base = np.stack([corners[k] for k in f], axis=1)
+            pyrs.append(np.concatenate([base, centres[:, None]], axis=1))
+        EV = np.stack(pyrs, axis=1).reshape(-1, 5)
+        P = self.V[EV]
+        det = np.einsum("ei,ei->e", P[:, 1] - P[:, 0], np.cross(P[:, 3] - P[:, 0], P[:, 4] - P[:, 0]))
+        flip = det < 0
+        EV[flip] = EV[flip][:, [0, 3, 2, 1, 4]]
+        self.EV = EV
+        self.E = EV.shape[0]
+
+    _map = TetMesh._map
+
+    def coords(self, n):
+        """Coordinates at the (n + 1) x (n + 1) x n points (GLL x GLL x Gauss-Radau alpha 2),
+        shape (3, E, (n + 1)^2 n): x = (1 - eta2)/2 (bilinear base map) + (1 + eta2)/2 apex."""
+        z0, z2 = gll_points(n + 1), radau_points(n, alpha=2.0)
+        e2, e1, e0 = np.meshgrid(z2, z0, z0, indexing="ij")
+        lo, hi = 0.5 * (1 - e2), 0.5 * (1 + e2)
+        a0, b0, a1, b1 = 0.5 * (1 - e0), 0.5 * (1 + e0), 0.5 * (1 - e1), 0.5 * (1 + e1)
+        W = np.stack([lo * a0 * a1, lo * b0 * a1, lo * b0 * b1, lo * a0 * b1, hi])
+        X = np.einsum("vkji,evc->cekji", W, self.V[self.EV]).reshape(3, self.E, -1)
+        return np.stack(self._map(X[0], X[1], X[2])).copy()
+
+    def assembly(self, n):
+        """C0 numbering of the pyramid expansion with n modes; all boundary dofs Dirichlet."""
+        return _c0_assembly(n, pyr_modal, _PYR_XI, _PYR_EDGES, _PYR_FACES, self.EV, self.V.shape[0])
 
 
 class HexMesh:

@@ -19,8 +19,8 @@ import numpy as np
 
 from . import _capi as C
 
-SHAPES = {"tri": C.SHAPE_TRI, "quad": C.SHAPE_QUAD, "tet": C.SHAPE_TET, "prism": C.SHAPE_PRISM,
-          "hex": C.SHAPE_HEX}
+SHAPES = {"tri": C.SHAPE_TRI, "quad": C.SHAPE_QUAD, "tet": C.SHAPE_TET, "pyr": C.SHAPE_PYR,
+          "prism": C.SHAPE_PRISM, "hex": C.SHAPE_HEX}
 PRECISIONS = {"fp64": C.FP64, "fp32": C.FP32}
 SOLVE_MODES = {"fp64": C.SOLVE_FP64, "mixed": C.SOLVE_MIXED_FP32, "mixed_geo16": C.SOLVE_MIXED_FP32_GEO16}
 
@@ -129,6 +129,15 @@ def basis_tet(nmodes):
     return tuple(c)
 
 
+def basis_pyr(nmodes):
+    """Direction 2 of the pyramid tables computed by the library: (z2, w2, D2, B2, DB2) of
+    ModifiedPyr_C on nmodes Gauss-Radau (alpha 2) points."""
+    Q, nc = nmodes, nmodes * (nmodes + 1) * (2 * nmodes + 1) // 6
+    c = [np.zeros(Q), np.zeros(Q), np.zeros(Q * Q), np.zeros(nc * Q), np.zeros(nc * Q)]
+    C.call("ithaca_gpu_basis_pyr", nmodes, *[ctypes.c_void_p(x.ctypes.data) for x in c])
+    return tuple(c)
+
+
 def _npts(shape, npoints):
     """Quadrature points per element (triangles: npoints x (npoints - 1) collapsed points,
     tetrahedra npoints x (npoints - 1)^2)."""
@@ -136,7 +145,7 @@ def _npts(shape, npoints):
         return npoints * (npoints - 1)
     if shape == "tet":
         return npoints * (npoints - 1) ** 2
-    if shape == "prism":
+    if shape in ("prism", "pyr"):
         return npoints * npoints * (npoints - 1)
     return npoints ** (2 if shape == "quad" else 3)
 
@@ -145,7 +154,7 @@ def geom_factors(ctx, shape, npoints, coords):
     """coords (d, E, nq) -> (jac (E*nq,), df (d*d, E*nq)) computed on the GPU, nq = Q^d
     (triangles: Q (Q - 1) collapsed points, Q the direction-0 count).
     Host numpy in -> host numpy out; CUDA tensor in -> CUDA tensors out."""
-    dim = 3 if shape in ("hex", "tet", "prism") else 2
+    dim = 3 if shape in ("hex", "tet", "prism", "pyr") else 2
     if _is_device(coords):
         import torch
         E = coords.shape[1]
@@ -171,7 +180,7 @@ class Collection:
     def __init__(self, ctx, shape, nmodes, npoints, nelmt, jac, df, deformed=True, precision="fp64"):
         self.ctx = ctx
         self.shape = shape
-        self.dim = 3 if shape in ("hex", "tet", "prism") else 2
+        self.dim = 3 if shape in ("hex", "tet", "prism", "pyr") else 2
         self.n, self.Q, self.E = nmodes, npoints, nelmt
         if shape == "tri":
             self.nm, self.nq = nmodes * (nmodes + 1) // 2, _npts(shape, npoints)
@@ -179,6 +188,8 @@ class Collection:
             self.nm, self.nq = nmodes * (nmodes + 1) * (nmodes + 2) // 6, _npts(shape, npoints)
         elif shape == "prism":
             self.nm, self.nq = nmodes * nmodes * (nmodes + 1) // 2, _npts(shape, npoints)
+        elif shape == "pyr":
+            self.nm, self.nq = nmodes * (nmodes + 1) * (2 * nmodes + 1) // 6, _npts(shape, npoints)
         else:
             self.nm, self.nq = nmodes ** self.dim, npoints ** self.dim
         self.precision = precision

@@ -240,3 +240,45 @@ def prism_iproduct_deriv(n, E, jac, df, deformed, in0, in1, in2, nthreads=1):
     _check(lib().ref_prism_iproduct_deriv(n, E, _f(jac), _f(df), int(deformed), _f(in0), _f(in1), _f(in2),
                                           _p(out), nthreads), "ref_prism_iproduct_deriv")
     return out
+
+
+# ---- pyramids (ref_pyr_* drivers); directions 0 and 1 as ref_gll/ref_modA(n, n+1) ----
+def pyr_tables(n):
+    ncp = n * (n + 1) * (2 * n + 1) // 6
+    c = [np.zeros(n), np.zeros(n), np.zeros(n * n), np.zeros(ncp * n), np.zeros(ncp * n)]
+    _check(lib().ref_pyr_tables(n, *[_p(x) for x in c]), "ref_pyr_tables")
+    return c
+
+
+def pyr_bwdtrans(n, E, coeffs, nthreads=1):
+    out = np.zeros(E * (n + 1) * (n + 1) * n)
+    _check(lib().ref_pyr_bwdtrans(n, E, _f(coeffs), _p(out), nthreads), "ref_pyr_bwdtrans")
+    return out
+
+
+def pyr_iproduct(n, E, jac, deformed, phys, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (2 * n + 1) // 6)
+    _check(lib().ref_pyr_iproduct(n, E, _f(jac), int(deformed), _f(phys), _p(out), nthreads), "ref_pyr_iproduct")
+    return out
+
+
+def pyr_physderiv(n, E, df, deformed, phys, nthreads=1):
+    nq = (n + 1) * (n + 1) * n
+    o = [np.zeros(E * nq) for _ in range(3)]
+    _check(lib().ref_pyr_physderiv(n, E, _f(df), int(deformed), _f(phys), *[_p(x) for x in o], nthreads),
+           "ref_pyr_physderiv")
+    return o
+
+
+def pyr_helmholtz(n, E, jac, df, deformed, lam, coeffs, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (2 * n + 1) // 6)
+    _check(lib().ref_pyr_helmholtz(n, E, _f(jac), _f(df), int(deformed), ctypes.c_double(lam), _f(coeffs),
+                                   _p(out), nthreads), "ref_pyr_helmholtz")
+    return out
+
+
+def pyr_iproduct_deriv(n, E, jac, df, deformed, in0, in1, in2, nthreads=1):
+    out = np.zeros(E * n * (n + 1) * (2 * n + 1) // 6)
+    _check(lib().ref_pyr_iproduct_deriv(n, E, _f(jac), _f(df), int(deformed), _f(in0), _f(in1), _f(in2),
+                                        _p(out), nthreads), "ref_pyr_iproduct_deriv")
+    return out

@@ -19,12 +19,13 @@ size_t ModesPerElement(int shape, int n) {
   if (shape == LibUtilities::eTriangle) return (size_t)n * (n + 1) / 2;
   if (shape == LibUtilities::eTetrahedron) return (size_t)n * (n + 1) * (n + 2) / 6;
   if (shape == LibUtilities::ePrism) return (size_t)n * n * (n + 1) / 2;
+  if (shape == LibUtilities::ePyramid) return (size_t)n * (n + 1) * (2 * n + 1) / 6;
   return shape == LibUtilities::eQuadrilateral ? (size_t)n * n : (size_t)n * n * n;
 }
 size_t PointsPerElement(int shape, int Q) {
   if (shape == LibUtilities::eTriangle) return (size_t)Q * (Q - 1);
   if (shape == LibUtilities::eTetrahedron) return (size_t)Q * (Q - 1) * (Q - 1);
-  if (shape == LibUtilities::ePrism) return (size_t)Q * Q * (Q - 1);
+  if (shape == LibUtilities::ePrism || shape == LibUtilities::ePyramid) return (size_t)Q * Q * (Q - 1);
   return shape == LibUtilities::eQuadrilateral ? (size_t)Q * Q : (size_t)Q * Q * Q;
 }
 std::shared_ptr<Collections::CoalescedGeomData> Geometry(int shape, int Q, int E, const double* jac, const double* df) {

@@ -1,10 +1,11 @@
 """Seeded test cases shared by the CPU and GPU tests (small sizes the oracle runs in seconds)."""
 import numpy as np
 
-from ithaca_gpu.mesh import HexMesh, PrismMesh, QuadMesh, TetMesh, TriMesh
+from ithaca_gpu.mesh import HexMesh, PrismMesh, PyrMesh, QuadMesh, TetMesh, TriMesh
 from oracle import basis as obasis
 from oracle import geom as ogeom
 from oracle import prism as oprism
+from oracle import pyr as opyr
 from oracle import tet as otet
 from oracle import tri as otri
 
@@ -103,6 +104,27 @@ def prism_case(nx, ny, nz, n, jitter=0.2, seed=3, curve=0.05, deformed=True):
     c.basis = oprism.PrismBasis(n)
     c.deformed = deformed
     jac, df = oprism.geom_factors(c.basis, c.X)
+    if deformed:
+        c.jac, c.df = jac.reshape(-1).copy(), df.copy()
+    else:
+        c.jac, c.df = jac[:, 0].copy(), df.reshape(9, c.E, -1)[:, :, 0].copy()
+    c.nm, c.nq = c.basis.nc, c.basis.nq
+    return c
+
+
+def pyr_case(nx, ny, nz, n, jitter=0.2, seed=3, curve=0.05, deformed=True):
+    """PyrMesh of 6 nx ny nz pyramids, n modes; deformed: curved and jittered with per-point
+    geometry, else straight with per-element geometry (the straight pyramid maps of this mesh
+    are affine)."""
+    c = Case()
+    c.dim, c.shape, c.n, c.Q = 3, "pyr", n, n + 1
+    c.mesh = PyrMesh(nx, ny, nz, jitter=jitter if deformed else 0.0, seed=seed,
+                     curve_amp=curve if deformed else 0.0)
+    c.E = c.mesh.E
+    c.X = c.mesh.coords(n)
+    c.basis = opyr.PyrBasis(n)
+    c.deformed = deformed
+    jac, df = opyr.geom_factors(c.basis, c.X)
     if deformed:
         c.jac, c.df = jac.reshape(-1).copy(), df.copy()
     else:

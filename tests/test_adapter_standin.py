@@ -5,8 +5,8 @@ linked here against stand-in headers with the reference's signatures
 AssemblyMap.h:80-308), and driven through the reference's factories.
 
 CPU: the adapter compiles with -Wall -Wextra, links with every library symbol resolved
-(-Wl,--no-undefined against libithaca_gpu.so), registers 25 operator keys (5 operators x
-tri/quad/tet/prism/hex) and the two systems, and turns a library error into NekError. GPU: a Helmholtz
+(-Wl,--no-undefined against libithaca_gpu.so), registers 30 operator keys (5 operators x
+the six shapes) and the two systems, and turns a library error into NekError. GPU: a Helmholtz
 apply and HelmSolves through the factory-made objects match the oracle.
 """
 import ctypes
@@ -56,7 +56,7 @@ def test_adapter_registers_operators_and_systems(adapter):
     v = [ctypes.c_int() for _ in range(4)]
     adapter.probe_registry(*[ctypes.byref(x) for x in v])
     nops, nsys, full, sc = (x.value for x in v)
-    assert nops == 25 and nsys == 2 and full == 1 and sc == 1
+    assert nops == 30 and nsys == 2 and full == 1 and sc == 1
 
 
 def _dp(a):
@@ -103,12 +103,14 @@ def test_adapter_triangle_helmholtz_matches_oracle(adapter):
 
 
 @pytest.mark.gpu
-def test_adapter_tetrahedron_and_prism_helmholtz_match_oracle(adapter):
-    """Tetrahedron (eTetrahedron = 5) and prism (ePrism = 7) collections through the adapter."""
-    from cases import prism_case, tet_case
+def test_adapter_3d_collapsed_helmholtz_match_oracle(adapter):
+    """Tetrahedron (5), pyramid (6) and prism (7) collections through the adapter."""
+    from cases import prism_case, pyr_case, tet_case
     from oracle import prism as oprism
+    from oracle import pyr as opyr
     from oracle import tet as otet
-    for c, shape, mod in ((tet_case(1, 1, 1, 5), 5, otet), (prism_case(1, 1, 1, 5), 7, oprism)):
+    for c, shape, mod in ((tet_case(1, 1, 1, 5), 5, otet), (pyr_case(1, 1, 1, 5), 6, opyr),
+                          (prism_case(1, 1, 1, 5), 7, oprism)):
         u = np.random.default_rng(shape).uniform(-1, 1, c.E * c.nm)
         rc, out, msg = _helmholtz(adapter, c, 0.6, u, shape=shape)
         assert rc == 0, msg
