@@ -136,8 +136,8 @@ int ithaca_gpu_geom_factors(ithaca_gpu_ctx* ctx, int shape, int npoints, int nel
  * MatrixFree::Operator (MatrixFreeOps/Operator.hpp:21-201) with its SetJac/SetDF.
  * Basis: ModifiedA with `nmodes` modes on `npoints` GLL points in every direction
  * (the homogeneous case MatrixFreeOps/Helmholtz.h:42-44 requires). Supported:
- * npoints == nmodes + 1, 2 <= nmodes <= 10. `precision` selects the arithmetic.
- * Triangles (shape 3): the basis of ithaca_gpu_basis_tri with npoints = Q0 = nmodes + 1;
+ * npoints == nmodes + 1, 2 <= nmodes <= 10 (triangles: <= 12). `precision` selects the
+ * arithmetic. Triangles (shape 3): the basis of ithaca_gpu_basis_tri with npoints = Q0 = nmodes + 1;
  * per element nmodes (nmodes + 1) / 2 coefficients and Q0 (Q0 - 1) points, geometry
  * (jac, df with d = 2) per point on those points or per element (MatrixFreeOps/
  * Helmholtz.h:290-330, 505-635; BwdTrans.h:540-570; IProduct.h:560-590;
@@ -391,7 +391,8 @@ int ithaca_gpu_kappa_gradient(ithaca_gpu_cg* cg, const double* x, const double* 
 /* Gram matrix C = S^T S (ns x ns) of the snapshot matrix S (N x ns). */
 int ithaca_gpu_pod_gram(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, double* C, int on_device);
 /* ROM_offline_phase (:3916-4001) by the method of snapshots: the leading `nmodes`
- * orthonormal POD modes V (N x nmodes) and all ns singular values sigma (descending).
+ * orthonormal POD modes V (N x nmodes) and all ns singular values sigma (descending;
+ * sigma is a host array whatever on_device says, S and V follow on_device).
  * *nmodes_out < nmodes when trailing modes are not resolved in FP64. */
 int ithaca_gpu_pod_offline(ithaca_gpu_ctx* ctx, int N, int ns, const double* S, int nmodes, double* V,
                            double* sigma, int* nmodes_out, int on_device);

@@ -567,10 +567,12 @@ int ithaca_gpu_op_create(ithaca_gpu_ctx* ctx, int shape, int nmodes, int npoints
     require(nelmt > 0, "nelmt must be positive");
     require(precision == ITHACA_GPU_FP64 || precision == ITHACA_GPU_FP32, "unknown precision");
     const int dim = shape_dim(shape);
-    if (!(npoints == nmodes + 1 && nmodes >= 2 && nmodes <= 10))
+    // triangles are built to 12 modes (P = 11, the order of 2-D snapshot sets), the rest to 10
+    const int nmax = shape == ITHACA_GPU_SHAPE_TRI ? 12 : 10;
+    if (!(npoints == nmodes + 1 && nmodes >= 2 && nmodes <= nmax))
       fail(ITHACA_GPU_ERR_UNSUPPORTED,
-           "GPU operators are built for npoints == nmodes + 1, 2 <= nmodes <= 10 (got nmodes=" +
-               std::to_string(nmodes) + ", npoints=" + std::to_string(npoints) + ")");
+           "GPU operators are built for npoints == nmodes + 1, 2 <= nmodes <= " + std::to_string(nmax) +
+               " (got nmodes=" + std::to_string(nmodes) + ", npoints=" + std::to_string(npoints) + ")");
     auto o = std::make_unique<ithaca_gpu_op>();
     o->ctx = ctx;
     o->shape = shape;

@@ -472,7 +472,7 @@ void tri_diag_n(int E, int deformed, const T* tab, const T* jg, T lambda, T* out
 
 }  // namespace dev
 
-// Runs CALL(N) for 2 <= n <= 10 with Q == n + 1; false otherwise.
+// Runs CALL(N) for 2 <= n <= 12 with Q == n + 1; false otherwise.
 #define ITHACA_TRI_DISPATCH(n, Q, CALL)        \
   if ((Q) != (n) + 1) return false;            \
   switch (n) {                                 \
@@ -485,6 +485,8 @@ void tri_diag_n(int E, int deformed, const T* tab, const T* jg, T lambda, T* out
     case 8: CALL(8); return true;              \
     case 9: CALL(9); return true;              \
     case 10: CALL(10); return true;            \
+    case 11: CALL(11); return true;            \
+    case 12: CALL(12); return true;            \
     default: return false;                     \
   }
 

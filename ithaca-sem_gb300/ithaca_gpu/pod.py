@@ -2,6 +2,9 @@
 
 * ``offline(ctx, S, nmodes)``      -- method-of-snapshots POD of the snapshot matrix
   S (N x ns, one snapshot per column): V (N x r orthonormal), singular values, r.
+* ``offline_device(ctx, St, nmodes)`` -- the same for a snapshot matrix already on the
+  device: a CUDA tensor St (ns, N) whose row k is snapshot k (fieldio.load_snapshots);
+  V comes back on the device as (r, N), one mode per row.
 * ``rb_size(sigma, tol)``          -- reduced-basis size from POD_tolerance (:3935-3944).
 * ``project(system, V)``           -- A_L = V^T L V, A_M = V^T M V on the free dofs.
 * ``online(ctx, A_L, A_M, f_r, lambdas)`` -- batched FP64 LU solves of
@@ -39,6 +42,19 @@ def offline(ctx, S, nmodes):
     r = ctypes.c_int()
     C.call("ithaca_gpu_pod_offline", ctx.handle, N, ns, _p(S), nmodes, _p(V), _p(sigma), ctypes.byref(r), 0)
     return np.asfortranarray(V[:, :r.value]), sigma, r.value
+
+
+def offline_device(ctx, St, nmodes):
+    import torch
+    if not getattr(St, "is_cuda", False) or St.dtype != torch.float64 or St.dim() != 2 or not St.is_contiguous():
+        raise ValueError("St must be a contiguous FP64 CUDA tensor (nsnapshots, N)")
+    ns, N = St.shape
+    V = torch.zeros((nmodes, N), dtype=torch.float64, device=St.device)
+    sigma = np.zeros(ns)
+    r = ctypes.c_int()
+    C.call("ithaca_gpu_pod_offline", ctx.handle, N, ns, ctypes.c_void_p(St.data_ptr()), nmodes,
+           ctypes.c_void_p(V.data_ptr()), _p(sigma), ctypes.byref(r), 1)
+    return V[:r.value], sigma, r.value
 
 
 def rb_size(sigma, pod_tolerance):

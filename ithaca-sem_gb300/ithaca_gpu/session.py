@@ -1,11 +1,12 @@
 """Session and mesh input: the subset of the reference's XML session format that the
-Helmholtz path needs, for quadrilateral meshes.
+Helmholtz path needs, for quadrilateral meshes (with boundary conditions) and triangle
+meshes (geometry and expansions, the meshes of 2-D snapshot sets).
 
 Reads what LibUtilities::SessionReader (LibUtilities/BasicUtils/SessionReader.cpp) and
 SpatialDomains::MeshGraphXml (SpatialDomains/MeshGraphXml.cpp) read from an uncompressed
 session file:
-  GEOMETRY      VERTEX <V ID>x y z</V>, EDGE <E ID>v0 v1</E>, ELEMENT <Q ID>e0 e1 e2 e3</Q>,
-                COMPOSITE <C ID>Q[0-15]</C> / E[0,13,22,31], DOMAIN
+  GEOMETRY      VERTEX <V ID>x y z</V>, EDGE <E ID>v0 v1</E>, ELEMENT <Q ID>e0 e1 e2 e3</Q>
+                and <T ID>e0 e1 e2</T>, COMPOSITE <C ID>Q[0-15]</C> / T[..] / E[0,13,22,31], DOMAIN
   EXPANSIONS    <E COMPOSITE NUMMODES TYPE FIELDS> (TYPE MODIFIED: ModifiedA on Q = n + 1 GLL points)
   CONDITIONS    PARAMETERS <P>name = value</P>, SOLVERINFO <I PROPERTY VALUE>, VARIABLES,
                 BOUNDARYREGIONS <B ID>C[..]</B>, BOUNDARYCONDITIONS (D, N, R, P per region),
@@ -30,7 +31,7 @@ import xml.etree.ElementTree as ET
 
 import numpy as np
 
-from .mesh import AssemblyMap, gll_points
+from .mesh import AssemblyMap, gll_points, radau_points
 
 _FUNCS = {"sin": np.sin, "cos": np.cos, "tan": np.tan, "exp": np.exp, "log": np.log, "log10": np.log10,
           "sqrt": np.sqrt, "abs": np.abs, "fabs": np.abs, "sinh": np.sinh, "cosh": np.cosh, "tanh": np.tanh,
@@ -394,3 +395,51 @@ class QuadSessionMesh:
         if np.any(np.isnan(out)):
             raise ValueError("some Dirichlet dofs lie on no Dirichlet edge")
         return out
+
+
+class TriSessionMesh:
+    """A straight-sided triangle mesh from a session, each element in the reference's own
+    frame: vertex j is the vertex of edge j that edge j + 1 does not share (TriGeom.cpp:55-80,
+    the edge cycle's start of edge j), so v0 = e0 ^ e2, v1 = e0 ^ e1, v2 = e1 ^ e2. Field
+    files store each triangle's coefficients in that frame, so it is kept as it is; a
+    clockwise triangle (negative Jacobian) is rejected, as the reference rejects it. Elements
+    are numbered by sorted global id (``elem_ids``)."""
+
+    def __init__(self, session):
+        s = session
+        if s.dim != 2:
+            raise ValueError("TriSessionMesh takes a 2-D session")
+        elems = []
+        for cid in s.domain:
+            kind, ids = s.composites[cid]
+            if kind != "T":
+                raise ValueError("only triangular elements are supported")
+            elems.extend(ids)
+        self.session = s
+        self.elem_ids = sorted(elems)
+        self.vid = sorted(s.vertices)
+        vindex = {v: i for i, v in enumerate(self.vid)}
+        self.V = np.stack([s.vertices[v][:2] for v in self.vid])
+        EV = []
+        for t in self.elem_ids:
+            tag, ed = s.elements[t]
+            if tag != "T":
+                raise ValueError("only triangular elements are supported")
+            e3 = [set(s.edges[e]) for e in ed]
+            cyc = [(e3[0] & e3[2]).pop(), (e3[0] & e3[1]).pop(), (e3[1] & e3[2]).pop()]
+            P = self.V[[vindex[v] for v in cyc]]
+            area = 0.5 * ((P[1, 0] - P[0, 0]) * (P[2, 1] - P[0, 1]) - (P[2, 0] - P[0, 0]) * (P[1, 1] - P[0, 1]))
+            if area <= 0:
+                raise ValueError(f"triangle {t} is clockwise or degenerate in its edge order")
+            EV.append([vindex[v] for v in cyc])
+        self.EV = np.array(EV)
+        self.E = len(self.EV)
+
+    def coords(self, n):
+        """Coordinates at the (n + 1) x n collapsed points of n-mode triangles (GLL x
+        Gauss-Radau), shape (2, E, n (n + 1)), point j (n + 1) + i."""
+        z0, z1 = gll_points(n + 1), radau_points(n)
+        e0, e1 = np.meshgrid(z0, z1, indexing="xy")
+        xi0 = 0.5 * (1.0 + e0) * (1.0 - e1) - 1.0
+        W = np.stack([-0.5 * (xi0 + e1), 0.5 * (1.0 + xi0), 0.5 * (1.0 + e1)])
+        return np.einsum("vji,evc->ceji", W, self.V[self.EV]).reshape(2, self.E, -1).copy()

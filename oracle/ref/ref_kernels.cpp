@@ -1204,7 +1204,25 @@ void iprd_pyr(const PyrTables& t, const Geo& g, const double* in0, const double*
   }
 }
 
-// Runs CALL(N) for N in 2..10 (triangles: Q0 = N + 1, Q1 = N).
+// Runs CALL(N) for N in 2..12 (triangles: Q0 = N + 1, Q1 = N).
+#define TRI12_DISPATCH(n, CALL) \
+  switch (n) {                  \
+    case 2: CALL(2); return 0;  \
+    case 3: CALL(3); return 0;  \
+    case 4: CALL(4); return 0;  \
+    case 5: CALL(5); return 0;  \
+    case 6: CALL(6); return 0;  \
+    case 7: CALL(7); return 0;  \
+    case 8: CALL(8); return 0;  \
+    case 9: CALL(9); return 0;  \
+    case 10: CALL(10); return 0; \
+    case 11: CALL(11); return 0; \
+    case 12: CALL(12); return 0; \
+    default: break;             \
+  }                             \
+  return 1;
+
+// Runs CALL(N) for N in 2..10 (tetrahedra, prisms, pyramids).
 #define TRI_DISPATCH(n, CALL)   \
   switch (n) {                  \
     case 2: CALL(2); return 0;  \
@@ -1426,7 +1444,7 @@ int ref_tri_bwdtrans(int n, int E, const double* in, double* out, int nthreads) 
   TriTables t = make_tri_tables(n);
   const int nb = E / W;
 #define TB(NN) parallel_blocks(nb, nthreads, [&](int b0, int b1) { tri_bwd<NN>(t, in, out, b0, b1); })
-  TRI_DISPATCH(n, TB)
+  TRI12_DISPATCH(n, TB)
 #undef TB
 }
 
@@ -1442,7 +1460,7 @@ int ref_tri_iproduct(int n, int E, const double* jac, int deformed, const double
     if (deformed) tri_iprod<NN, true>(t, g, in, out, b0, b1);    \
     else tri_iprod<NN, false>(t, g, in, out, b0, b1);            \
   })
-  TRI_DISPATCH(n, TI)
+  TRI12_DISPATCH(n, TI)
 #undef TI
 }
 
@@ -1459,7 +1477,7 @@ int ref_tri_physderiv(int n, int E, const double* df, int deformed, const double
     if (deformed) tri_deriv<NN, true>(t, g, in, o0, o1, b0, b1);        \
     else tri_deriv<NN, false>(t, g, in, o0, o1, b0, b1);                \
   })
-  TRI_DISPATCH(n, TD)
+  TRI12_DISPATCH(n, TD)
 #undef TD
 }
 
@@ -1475,7 +1493,7 @@ int ref_tri_helmholtz(int n, int E, const double* jac, const double* df, int def
     if (deformed) helm_tri<NN, true>(t, g, lambda, in, out, b0, b1);           \
     else helm_tri<NN, false>(t, g, lambda, in, out, b0, b1);                   \
   })
-  TRI_DISPATCH(n, TH)
+  TRI12_DISPATCH(n, TH)
 #undef TH
 }
 
@@ -1491,7 +1509,7 @@ int ref_tri_iproduct_deriv(int n, int E, const double* jac, const double* df, in
     if (deformed) iprd_tri<NN, true>(t, g, in0, in1, out, b0, b1);             \
     else iprd_tri<NN, false>(t, g, in0, in1, out, b0, b1);                     \
   })
-  TRI_DISPATCH(n, TP)
+  TRI12_DISPATCH(n, TP)
 #undef TP
 }
 

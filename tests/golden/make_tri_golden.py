@@ -6,7 +6,7 @@ Outputs come from oracle/_ref/libithaca_ref.so: Polylib.cpp (zwglj/Dglj, zwgrjm/
 and the MatrixFree triangle kernel templates (BwdTransTriKernel, IProductTriKernel,
 PhysDerivTriKernel, PhysDerivTensor2DKernel) compiled in place and driven as the
 reference operators drive them (oracle/ref/ref_kernels.cpp). Contents:
-  * t{n}_*        tables of the n-mode triangle expansion, n = 2..10: z0 w0 D0 B0 DB0
+  * t{n}_*        tables of the n-mode triangle expansion, n = 2..12: z0 w0 D0 B0 DB0
                   (GLL, ModifiedA) and z1 w1 D1 B1 DB1 (Gauss-Radau alpha 1 beta 0, ModifiedB)
   * unit_*        the MatrixFree cases of library/UnitTests/Collections/TestTriCollection.cpp:
                   BwdTrans (:322-382, standard triangle, 4 modes, coefficients 1),
@@ -43,7 +43,7 @@ def straight_coords(tb, verts):
 
 def main():
     out = {}
-    for n in range(2, 11):
+    for n in range(2, 13):
         a, b = refbind.tri_tables(n)
         for name, v in zip(("z0", "w0", "D0", "B0", "DB0"), a):
             out[f"t{n}_{name}"] = v

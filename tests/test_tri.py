@@ -25,7 +25,7 @@ TOL32 = 2e-5
 
 
 # ---------------------------------------------------------------------------- CPU
-@pytest.mark.parametrize("n", range(2, 11))
+@pytest.mark.parametrize("n", range(2, 13))
 def test_tables_match_reference(n):
     """Library host tables and the oracle's against Polylib / Basis (eModified_B)."""
     from ithaca_gpu.operators import basis_tri
@@ -162,7 +162,7 @@ def _coll(ctx, c, precision="fp64"):
     return Collection(ctx, "tri", c.n, c.Q, c.E, c.jac, c.df, deformed=c.deformed, precision=precision)
 
 
-CASES = [(n, True) for n in range(2, 11)] + [(4, False), (7, False), (10, False)]
+CASES = [(n, True) for n in range(2, 13)] + [(4, False), (7, False), (10, False), (12, False)]
 
 
 @pytest.mark.gpu
