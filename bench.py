@@ -134,16 +134,20 @@ def fp32_kernel_name(variant, n, Q):
         return f"helm_kernel<float,3,{n},{Q}>"
     if variant in (2, 4):
         return f"helm3_pencil_kernel<float,{n},{Q},{variant}>"
+    if variant in (43, 44):
+        if Q != 8:  # vector pencils exist for Q = 8; elsewhere 42 / 41 run
+            return fp32_kernel_name(41 if variant == 44 else 42, n, Q)
+        return f"helm3_pipe_kernel<float,{n},{Q},{1 if variant == 44 else 2},gather,1,packed,vec4>"
     return (f"helm3_pipe_kernel<float,{n},{Q},{variant % 10},gather,{2 if variant // 10 == 2 else 1}"
             + (",packed>" if variant // 10 == 4 else ">"))
 
 
 # DRAM bytes (read + write) per element of one gathered FP32 apply as the inner iteration
 # launches it (scattered output: owned rows and assembly-ordered slots), from an ncu
-# capture of the kernel on 28^3 hexes (394.1 MB read + 5.4 MB written per launch over
-# 21,952 elements, variant 42); a launch's traffic grows with the number of elements, so
-# the bench scales it by E. Keys: (kernel variant, modes, points).
-TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200}
+# capture of the kernel on 28^3 hexes (variant 42: 394.1 MB read + 5.4 MB written per
+# launch over 21,952 elements; variant 43: 394.1 + 5.5 MB); a launch's traffic grows with
+# the number of elements, so the bench scales it by E. Keys: (kernel variant, modes, points).
+TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200, (43, 7, 8): 18204}
 
 
 def workload_config(args, n, Q, E, N, ndir):
@@ -652,8 +656,13 @@ def run_gpu(args, rank, world):
     sysg = GlobalLinSysIterativeFullGPU(coll, amap)
     stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
     # pick the FP32 element-kernel variant by timing the solver's own gathered inner
-    # apply (CollectionOptimisation analogue)
-    variant, variant_ms = sysg.autotune_inner(LAMBDA, reps=10)
+    # apply (CollectionOptimisation analogue), unless --variant names one (kernel captures,
+    # whose serialised timings would mislead the autotuner)
+    if args.variant >= 0:
+        variant, variant_ms = args.variant, {}
+        sysg.coll.set_variant(variant)
+    else:
+        variant, variant_ms = sysg.autotune_inner(LAMBDA, reps=10)
     coll32.set_variant(variant)
 
     # b = Assemble(-IProductWRTBase(f)) on the device (ContField::v_HelmSolve)
@@ -1168,10 +1177,12 @@ def suite_inner_apply(args):
     autotuned one) and the FP64 apply, CUDA-event time per launch against the algorithmic
     bytes. A small mesh keeps it a case the kernel captures can take."""
     from ithaca_gpu.workload import hex_workload
+    args.mesh = args.mesh or 32
     w = hex_workload(args.mesh, args.order)
     sysg, E, n, Q = w["system"], w["mesh"].E, w["n"], w["Q"]
+    tuned = {}
     if args.variant < 0:
-        variant, _ = sysg.autotune_inner(LAMBDA, reps=3)
+        variant, tuned = sysg.autotune_inner(LAMBDA, reps=max(3, args.steps))
     else:
         variant = args.variant
         w["coll"].set_variant(variant)
@@ -1179,7 +1190,8 @@ def suite_inner_apply(args):
     ms64, by64 = sysg.profile_apply(LAMBDA, mode="fp64", reps=args.steps)
     peak, kind = load_peaks()
     cfg = {"workload": f"gathered element Helmholtz applies of the solver, {args.mesh}^3 curved hexes, P={args.order}",
-           "elements": E, "fp32_kernel_variant": variant}
+           "elements": E, "fp32_kernel_variant": variant,
+           "autotune_ms": {str(v): round(t, 4) for v, t in tuned.items()}}
     _line("inner FP32 gathered apply: algorithmic GB/s", by32 / (ms32 / 1e3) / 1e9, "GB/s", args, cfg, dtype="f32",
           fp32={"kernel": fp32_kernel_name(variant, n, Q), "ms": ms32, "bytes": by32,
                 "frac_of_hbm": by32 / (ms32 / 1e3) / 1e9 / peak, "peak_source": kind},
@@ -1202,7 +1214,7 @@ def suite_peaks(args):
 def suite_tri(args):
     """Triangles: 128 x 128 cells (32768 curved triangles) at P = 6."""
     import torch
-    out = tri_fields(torch, "cuda:0")
+    out = tri_fields(torch, "cuda:0", mesh=args.mesh or 128)
     _line("2-D Helmholtz on curved triangles, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
           out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", tri=out,
           cpu_baseline=out.get("cpu_baseline"))
@@ -1211,7 +1223,7 @@ def suite_tri(args):
 def suite_tet(args):
     """Tetrahedra: 12^3 cubes (10368 curved tetrahedra) at P = 6."""
     import torch
-    out = tet_fields(torch, "cuda:0")
+    out = tet_fields(torch, "cuda:0", mesh=args.mesh or 12)
     _line("3-D Helmholtz on curved tetrahedra, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
           out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", tet=out)
 
@@ -1219,7 +1231,7 @@ def suite_tet(args):
 def suite_prism(args):
     """Prisms: 12^3 cubes (3456 curved prisms) at P = 6."""
     import torch
-    out = prism_fields(torch, "cuda:0")
+    out = prism_fields(torch, "cuda:0", mesh=args.mesh or 12)
     _line("3-D Helmholtz on curved prisms, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
           out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", prism=out)
 
@@ -1227,7 +1239,7 @@ def suite_prism(args):
 def suite_pyr(args):
     """Pyramids: 10^3 cubes (6000 curved pyramids) at P = 6."""
     import torch
-    out = pyr_fields(torch, "cuda:0")
+    out = pyr_fields(torch, "cuda:0", mesh=args.mesh or 10)
     _line("3-D Helmholtz on curved pyramids, P=6: CG solves/s (FP64, 1e-10) and operator GDOF/s",
           out["fp64"]["solves_per_s"], "solves/s", args, {"workload": out["workload"]}, dtype="f64", pyr=out)
 
@@ -1244,15 +1256,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--order", type=int, default=6)
-    ap.add_argument("--mesh", type=int, default=32)
+    ap.add_argument("--mesh", type=int, default=None,
+                    help="cells per direction (default: 32 hex, 128 tri, 12 tet / prism, 10 pyr)")
     ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed",
                     help="inner solve of the headline: FP32 on FP32 geometry, or FP32 on 16-bit geometry")
-    ap.add_argument("--variant", type=int, default=-1, help="inner_apply: FP32 hex kernel variant (-1: autotune)")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="FP32 hex kernel variant of the inner apply (-1: autotune; the headline and inner_apply)")
     ap.add_argument("--full", type=int, default=1,
                     help="1: add the P=8 hexes, the 2-D mixed sweep and the 256-solve batch to the line")
     ap.add_argument("--config", choices=["hex"] + list(SUITES) + ["all"], default="hex",
                     help="hex: the headline workload (default); the others: secondary workloads, one line each")
     args = ap.parse_args()
+    if args.config in ("hex", "inner_apply") and args.mesh is None:
+        args.mesh = 32  # the headline mesh (the other suites take their own defaults)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.config != "hex" and args.impl == "gpu":

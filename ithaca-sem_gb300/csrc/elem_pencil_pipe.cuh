@@ -83,15 +83,46 @@ __device__ __forceinline__ void contract2(Get W, const float (&c)[NI], float (&o
   }
 }
 
-template <typename T, int N, int Q, int EB, int NB, typename TG = T>
+// Vector pencils (V4, Q = 8 only): plane stride 68 (= 4 mod 32) instead of 73. The pencils
+// along the unit-stride index are then read and written as two 16-byte words each, and a
+// quarter warp (lanes (j, k) = (t / 8, t % 8), k = 0..7) hits eight different 16-byte bank
+// groups ((2 j + 17 k) mod 8 = (2 j + k) mod 8); the pencils along j run on lanes
+// (i, k) = (t % 4 + 4 (t / 32), (t / 4) % 8), whose banks i + 68 k = i + 4 k (mod 32) are
+// all different; the columns along k keep lanes (t % 8, t / 8), banks i + 8 j. No bank
+// conflicts in any stage, and a quarter of the shared-memory instructions of the
+// unit-stride stages.
+template <int Q, bool V4>
+__host__ __device__ constexpr int pipe_pk(void) {
+  return V4 ? 68 : pk_stride(Q);
+}
+
+template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool V4 = false>
 struct PipeLayout {
   static constexpr int NQ = Q * Q * Q, GEO = 7 * NQ;
-  static constexpr int PJ = Q, PK = pk_stride(Q), FS = PK * Q;
+  static constexpr int PJ = Q, PK = pipe_pk<Q, V4>(), FS = PK * Q;
   static constexpr size_t GEO_BYTES = ((size_t)EB * GEO * sizeof(TG) + 32 + 15) / 16 * 16;  // + window slack
   static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
-template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false>
+// 8 consecutive floats from / to 16-byte aligned shared memory as two 16-byte words; the
+// first M are used (M <= 8), the rest of the store is zero.
+template <int M>
+__device__ __forceinline__ void lds8(const float* p, float (&c)[M]) {
+  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
+  const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int i = 0; i < M; ++i) c[i] = v[i];
+}
+template <int M>
+__device__ __forceinline__ void sts8(float* p, const float (&o)[M]) {
+  float v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = i < M ? o[i] : 0.f;
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false, bool V4 = false>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                                const PTabs<T, N, Q> tab, const PTabs2<N, Q> tab2,
                                                                const TG* __restrict__ jg,
@@ -104,13 +135,14 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
                                                                const int* __restrict__ ocode = nullptr) {
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
+  static_assert(!V4 || (PACK && Q == 8 && N <= 8), "vector pencils: packed FP32, Q = 8");
   constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
   auto BF = [&](int i) { return tab2.BF[i]; };
   auto DF = [&](int i) { return tab2.DF[i]; };
   auto BT = [&](int i) { return tab2.BT[i]; };
   auto DT = [&](int i) { return tab2.DT[i]; };
   constexpr bool HALF = !std::is_same<TG, T>::value;
-  using L = PipeLayout<T, N, Q, EB, NB, TG>;
+  using L = PipeLayout<T, N, Q, EB, NB, TG, V4>;
   constexpr int NQ = L::NQ, NM = N * N * N, TPE = Q * Q, GEO = L::GEO;
   constexpr int PJ = L::PJ, PK = L::PK, FS = L::FS;
   constexpr int NPT = (NM + TPE - 1) / TPE;  // coefficients gathered per thread
@@ -119,6 +151,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   // a warp then hit 32 different shared-memory banks in every stage but the two
   // j-direction derivative stages (2-way); same arithmetic per pencil either way.
   constexpr bool M8 = (Q == 8);
+  // V4 lanes of the j-direction pencils: i = t % 4 + 4 (t / 32), k = (t / 4) % 8
+  const int vj_i = (threadIdx.x & 3) + 4 * (threadIdx.x >> 5), vj_k = (threadIdx.x >> 2) & 7;
   if (skip != nullptr && *skip) return;  // converged solve: the whole CTA leaves together
   if (lam_ptr != nullptr) lambda = *lam_ptr;
 
@@ -256,7 +290,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 2: BwdTrans along p: pencils (q, r) ----
-    if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
+    if constexpr (V4) {
+      const int q = t / 8, r = t % 8;
+      if (q < N && r < N) {
+        T c[N], o[Q];
+        lds8(S0 + PJ * q + PK * r, c);
+        contract2<N, Q, QP, false>(BF, c, o);
+        sts8(S1 + PJ * q + PK * r, o);
+      }
+    } else if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
       const int q = M8 ? t / 8 : t % N, r = M8 ? t % 8 : t / N;
       T c[N];
 #pragma unroll
@@ -278,7 +320,17 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 3: along q: pencils (i, r) ----
-    if (M8 ? t % 8 < N : t < Q * N) {
+    if constexpr (V4) {
+      const int i = vj_i, r = vj_k;
+      if (r < N) {
+        T c[N], o[Q];
+#pragma unroll
+        for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
+        contract2<N, Q, QP, false>(BF, c, o);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) S0[i + PJ * j + PK * r] = o[j];
+      }
+    } else if (M8 ? t % 8 < N : t < Q * N) {
       const int i = M8 ? t / 8 : t % Q, r = M8 ? t % 8 : t / Q;
       T c[N];
 #pragma unroll
@@ -330,7 +382,17 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 5: d/dxi_0 on pencils (j, k) -> S0 ; d/dxi_1 on pencils (i, k) -> S1 ----
-    {
+    if constexpr (V4) {
+      T c[Q], o[Q];
+      lds8(SU + PJ * (t / 8) + PK * (t % 8), c);
+      contract2<Q, Q, QP, false>(DF, c, o);
+      sts8(S0 + PJ * (t / 8) + PK * (t % 8), o);
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = SU[vj_i + PJ * a + PK * vj_k];
+      contract2<Q, Q, QP, false>(DF, c, o);
+#pragma unroll
+      for (int j = 0; j < Q; ++j) S1[vj_i + PJ * j + PK * vj_k] = o[j];
+    } else {
       const int pj = M8 ? t / 8 : t % Q, pk = M8 ? t % 8 : t / Q;
       T c[Q];
 #pragma unroll
@@ -418,7 +480,17 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     // single buffer: stage 6 has read it, so the next group's copy can start now
     if (NB == 1 && tid == 0 && has_next) issue_geometry(nxt, 0);
     // ---- 7: D^T along i on pencils (j, k) in S0, along j on pencils (i, k) in S1 ----
-    {
+    if constexpr (V4) {
+      T c[Q], o[Q];
+      lds8(S0 + PJ * (t / 8) + PK * (t % 8), c);
+      contract2<Q, Q, QP, false>(DT, c, o);
+      sts8(S0 + PJ * (t / 8) + PK * (t % 8), o);
+#pragma unroll
+      for (int a = 0; a < Q; ++a) c[a] = S1[vj_i + PJ * a + PK * vj_k];
+      contract2<Q, Q, QP, false>(DT, c, o);
+#pragma unroll
+      for (int j = 0; j < Q; ++j) S1[vj_i + PJ * j + PK * vj_k] = o[j];
+    } else {
       const int pj = M8 ? t / 8 : t % Q, pk = M8 ? t % 8 : t / Q;
       T c[Q], o[Q];
 #pragma unroll
@@ -478,7 +550,17 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 9: along j: pencils (i, r) -> S0 as (i, q, r) ----
-    if (M8 ? t % 8 < N : t < Q * N) {
+    if constexpr (V4) {
+      const int i = vj_i, r = vj_k;
+      if (r < N) {
+        T c[Q], o[N];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
+        contract2<Q, N, NP, false>(BT, c, o);
+#pragma unroll
+        for (int q = 0; q < N; ++q) S0[i + PJ * q + PK * r] = o[q];
+      }
+    } else if (M8 ? t % 8 < N : t < Q * N) {
       const int i = M8 ? t / 8 : t % Q, r = M8 ? t % 8 : t / Q;
       T c[Q];
 #pragma unroll
@@ -500,7 +582,15 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 10: along i: pencils (q, r) -> S1 as (p, q, r) ----
-    if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
+    if constexpr (V4) {
+      const int q = t / 8, r = t % 8;
+      if (q < N && r < N) {
+        T c[Q], o[N];
+        lds8(S0 + PJ * q + PK * r, c);
+        contract2<Q, N, NP, false>(BT, c, o);
+        sts8(S1 + PJ * q + PK * r, o);  // p = N..7 of the pencil: padding, written as zero
+      }
+    } else if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
       const int q = M8 ? t / 8 : t % N, r = M8 ? t % 8 : t / N;
       T c[Q];
 #pragma unroll

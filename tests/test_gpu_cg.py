@@ -107,7 +107,7 @@ def test_mixed_curved_hex_inner_tolerances(ctx, inner_tol):
     assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
 
 
-@pytest.mark.parametrize("variant", [4, 21, 31, 41, 42])
+@pytest.mark.parametrize("variant", [4, 21, 31, 41, 42, 43, 44])
 def test_mixed_kernel_variants_curved_hex(ctx, variant):
     """Mixed solves with each FP32 hex kernel; the pipelined ones (21-42) also assemble
     the single-entry rows inside the element kernel. All reach the FP64 residual, agree
@@ -127,6 +127,24 @@ def test_mixed_kernel_variants_curved_hex(ctx, variant):
     assert abs(res.iterations - ref.iterations) <= 4, (res.iterations, ref.iterations)
 
 
+@pytest.mark.parametrize("variant", [43, 44])
+def test_mixed_vector_pencils_q8(ctx, variant):
+    """The vector-pencil kernels (Q = 8) inside the mixed solver against their scalar-pencil
+    counterparts (42, 41), whose arithmetic they share: the same inner iterations within
+    one and the same solution."""
+    c = hex_case(3, 3, 2, 7, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(29).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    coll.set_variant(41 if variant == 44 else 42)
+    xr, ref = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    coll.set_variant(variant)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+    assert abs(res.iterations - ref.iterations) <= 1, (res.iterations, ref.iterations)
+    assert rel_err(x[amap.ndir:], xr[amap.ndir:]) < 1e-9
+
+
 def _merged_map(amap):
     """The map with a few free global dofs merged: three interior vertices into one row
     of 24 local entries (longer than the ELL classes), a face dof into an edge dof (6
@@ -143,7 +161,7 @@ def _merged_map(amap):
     return AssemblyMap(l2g, amap.sign, ids.size, amap.ndir)
 
 
-@pytest.mark.parametrize("variant", [4, 41, 42])
+@pytest.mark.parametrize("variant", [4, 41, 42, 43])
 def test_mixed_long_rows(ctx, variant):
     """Rows of 1, 2, 4, 6, 8 and 24 local entries: the FP64 solve against the oracle, and
     the mixed solve with the element-ordered (4) and the scattered (41, 42: owned rows

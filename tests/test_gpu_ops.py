@@ -156,7 +156,7 @@ def test_unsupported_order_raises(ctx):
 
 
 @pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 7, 8, 9, 10])
-@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22, 31, 32, 41, 42])
+@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44])
 def test_hex_fp32_kernel_variants(ctx, n, variant):
     """Every FP32 hex Helmholtz kernel variant (shared-memory; register-pencil with a
     TMA-staged geometry slab, one pass with 2 or 4 elements per CTA or persistent and
@@ -172,7 +172,7 @@ def test_hex_fp32_kernel_variants(ctx, n, variant):
     assert rel_err(out, ref) < TOL32
 
 
-@pytest.mark.parametrize("n", [3, 6, 9])
+@pytest.mark.parametrize("n", [3, 6, 7, 9])
 def test_hex_pencil_variants_bit_identical(ctx, n):
     """The pencil kernels share one summation order: the single-pass, pipelined
     (one or two geometry buffers) and packed-pair variants give identical bits."""
@@ -180,7 +180,7 @@ def test_hex_pencil_variants_bit_identical(ctx, n):
     coll = _coll(ctx, c, "fp32")
     u = np.random.default_rng(70 + n).uniform(-1, 1, c.E * c.nm).astype(np.float32)
     outs = {}
-    for v in (2, 4, 21, 22, 31, 32, 41, 42):
+    for v in (2, 4, 21, 22, 31, 32, 41, 42, 43, 44):
         coll.set_variant(v)
         outs[v] = coll.helmholtz(0.3, u)
     for v, o in outs.items():
@@ -191,7 +191,7 @@ def test_autotune_picks_a_working_variant(ctx):
     c = hex_case(4, 4, 2, 7)
     coll = _coll(ctx, c, "fp32")
     chosen, times = coll.autotune(reps=3)
-    assert chosen in (0, 2, 4, 21, 22, 31, 32, 41, 42) and all(t > 0 for t in times.values())
+    assert chosen in (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44) and all(t > 0 for t in times.values())
     u = np.random.default_rng(3).uniform(-1, 1, c.E * c.nm)
     out = coll.helmholtz(1.0, u.astype(np.float32))
     ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, u)
