@@ -26,7 +26,8 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 
 // Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
 // occupancy calculator), never more CTAs than element groups.
-template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool PACK = false, bool V4 = false>
+template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool PACK = false, bool V4 = false,
+          bool TC = false>
 static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T lambda, const T* in, T* out,
                     const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s,
                     const float* gscale = nullptr, OwnedRows* own = nullptr) {
@@ -46,8 +47,8 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
       tab2.DT[i * QP + k] = (float)hD[k * Q + i];
     }
   using L = PipeLayout<T, N, Q, EB, NB, TG, V4>;
-  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG, PACK, V4>
-               : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG, PACK, V4>;
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG, PACK, V4, TC>
+               : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG, PACK, V4, TC>;
   static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
   const int gi = l2g ? 1 : 0;
   if (slots[gi] == 0) {
@@ -96,17 +97,22 @@ bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double*
 // elements per CTA; 21 or 22 = the persistent pipelined kernel with 1 or 2 elements per
 // group and a double geometry buffer; 31 or 32 = the same with a single buffer; 41 or 42 =
 // the single-buffer kernel with its contractions on packed FP32 pairs (fma.rn.f32x2); 43 or
-// 44 = 42 or 41 with vector pencils in shared memory (Q = 8; other orders run 42 or 41).
+// 44 = 42 or 41 with vector pencils in shared memory, 46 = 43 with the contractions along i
+// and j on the tensor cores (TF32 MMAs in three-term split precision; Q = 8; other orders
+// run 42 or 41).
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s, OwnedRows* own) {
   if (own != nullptr) own->ctas = -1;  // set by the pipelined kernels only
-  if (variant == 43 || variant == 44) {
+  if (variant == 43 || variant == 44 || variant == 46) {
     // vector pencils are built for Q = 8; elsewhere the scalar-pencil kernel with the same
     // arithmetic (and so the same results) runs
     if (n == 7 && Q == 8 && std::is_same<T, float>::value) {
-      if (variant == 43)
+      if (variant == 46)
+        dev::pipe_nq<T, 7, 8, 2, 1, T, true, true, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err,
+                                                         s, nullptr, own);
+      else if (variant == 43)
         dev::pipe_nq<T, 7, 8, 2, 1, T, true, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err, s,
                                                    nullptr, own);
       else

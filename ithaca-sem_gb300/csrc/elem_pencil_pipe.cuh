@@ -104,6 +104,81 @@ struct PipeLayout {
   static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
+// ---- warp-level TF32 tensor-core contractions in three-term split precision (TC) ----
+// A contraction of an element's 64 pencils (rows r) with a 1-D table W (8 x 8, zero padded)
+// is a 64 x 8 x 8 product: four m16n8k8 tiles, two per warp of the element. Each FP32
+// operand x is split into hi = tf32(x) and lo = tf32(x - hi); the product is
+// hi.hi + hi.lo + lo.hi (three MMAs, smallest first, FP32 accumulation), which drops only
+// lo.lo, below 2^-21 of each product: FP32-level accuracy for the inner solve.
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+struct TfFrag {
+  uint32_t hi[2], lo[2];
+};
+// The B fragment of lane (g = lane / 4, t4 = lane % 4): W[t4][g] and W[t4 + 4][g], split.
+__device__ __forceinline__ TfFrag tf_frag(float w0, float w1) {
+  TfFrag f;
+  f.hi[0] = tf32_rna(w0);
+  f.lo[0] = tf32_rna(w0 - __uint_as_float(f.hi[0]));
+  f.hi[1] = tf32_rna(w1);
+  f.lo[1] = tf32_rna(w1 - __uint_as_float(f.hi[1]));
+  return f;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+// KIND 0: along the unit-stride index, row r = (u, v) = (r / 8, r % 8) at offset 8 u + 68 v;
+// KIND 1: along j (stride 8), row r = (i, k) = (r % 8, r / 8) at offset i + 68 k (the V4
+// layout). Lane (g, t4) of warp w loads A[r][t4], A[r][t4 + 4] for rows r = 16 m + g and
+// r + 8 of its tiles m = 2 w, 2 w + 1 (banks t4 + 4 g and 8 t4 + g: no conflicts); rows
+// failing `valid` and inputs a >= KI read as zero. All eight outputs of every row are
+// written (zero where the table column is zero). src may equal dst: a tile's loads all
+// precede its MMAs, and the tiles' rows are disjoint.
+template <int KIND, int KI, typename Valid>
+__device__ __forceinline__ void tc_contract(const float* src, float* dst, const TfFrag& w, int t, Valid valid) {
+  constexpr int SA = KIND == 0 ? 1 : 8;
+  const int lane = t & 31, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int m = 2 * (t >> 5) + h;
+    int off[2];
+    bool ok[2];
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int r = 16 * m + g + 8 * s2;
+      const int a = KIND == 0 ? r >> 3 : r & 7, b = KIND == 0 ? r & 7 : r >> 3;
+      off[s2] = KIND == 0 ? 8 * a + 68 * b : a + 68 * b;
+      ok[s2] = valid(a, b);
+    }
+    float x[4];
+    x[0] = (ok[0] && t4 < KI) ? src[t4 * SA + off[0]] : 0.f;
+    x[1] = (ok[1] && t4 < KI) ? src[t4 * SA + off[1]] : 0.f;
+    x[2] = (ok[0] && t4 + 4 < KI) ? src[(t4 + 4) * SA + off[0]] : 0.f;
+    x[3] = (ok[1] && t4 + 4 < KI) ? src[(t4 + 4) * SA + off[1]] : 0.f;
+    uint32_t ah[4], al[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      ah[i] = tf32_rna(x[i]);
+      al[i] = tf32_rna(x[i] - __uint_as_float(ah[i]));
+    }
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    mma_tf32(d, al, w.hi);
+    mma_tf32(d, ah, w.lo);
+    mma_tf32(d, ah, w.hi);
+    dst[2 * t4 * SA + off[0]] = d[0];
+    dst[(2 * t4 + 1) * SA + off[0]] = d[1];
+    dst[2 * t4 * SA + off[1]] = d[2];
+    dst[(2 * t4 + 1) * SA + off[1]] = d[3];
+  }
+}
+
 // 8 consecutive floats from / to 16-byte aligned shared memory as two 16-byte words; the
 // first M are used (M <= 8), the rest of the store is zero.
 template <int M>
@@ -122,7 +197,8 @@ __device__ __forceinline__ void sts8(float* p, const float (&o)[M]) {
   *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
 }
 
-template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false, bool V4 = false>
+template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false, bool V4 = false,
+          bool TC = false>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                                const PTabs<T, N, Q> tab, const PTabs2<N, Q> tab2,
                                                                const TG* __restrict__ jg,
@@ -136,6 +212,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   static_assert(NB == 1 || NB == 2, "one or two geometry buffers");
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
   static_assert(!V4 || (PACK && Q == 8 && N <= 8), "vector pencils: packed FP32, Q = 8");
+  static_assert(!TC || (V4 && Q * Q == 64), "tensor-core stages: the vector-pencil layout, 64 pencils");
   constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
   auto BF = [&](int i) { return tab2.BF[i]; };
   auto DF = [&](int i) { return tab2.DF[i]; };
@@ -153,6 +230,19 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   constexpr bool M8 = (Q == 8);
   // V4 lanes of the j-direction pencils: i = t % 4 + 4 (t / 32), k = (t / 4) % 8
   const int vj_i = (threadIdx.x & 3) + 4 * (threadIdx.x >> 5), vj_k = (threadIdx.x >> 2) & 7;
+  // TC: this lane's B fragments of the four 1-D tables, W[a][x] zero-padded to 8 x 8:
+  // BwdTrans (B(a, z_x), a < N), derivative (l_a'(z_x)), its transpose (l_x'(z_a)) and
+  // IProduct (B(x, z_a), x < N)
+  TfFrag wbf{}, wdf{}, wdt{}, wbt{};
+  if constexpr (TC) {
+    const int g = (threadIdx.x & 31) >> 2, t4 = threadIdx.x & 3;
+    auto bf = [&](int a, int x) { return a < N ? tab.B[a * Q + x] : T(0); };
+    auto bt = [&](int a, int x) { return x < N ? tab.B[x * Q + a] : T(0); };
+    wbf = tf_frag(bf(t4, g), bf(t4 + 4, g));
+    wdf = tf_frag(tab.D[t4 * Q + g], tab.D[(t4 + 4) * Q + g]);
+    wdt = tf_frag(tab.D[g * Q + t4], tab.D[g * Q + t4 + 4]);
+    wbt = tf_frag(bt(t4, g), bt(t4 + 4, g));
+  }
   if (skip != nullptr && *skip) return;  // converged solve: the whole CTA leaves together
   if (lam_ptr != nullptr) lambda = *lam_ptr;
 
@@ -290,7 +380,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 2: BwdTrans along p: pencils (q, r) ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<0, N>(S0, S1, wbf, t, [](int q, int r) { return q < N && r < N; });
+    } else if constexpr (V4) {
       const int q = t / 8, r = t % 8;
       if (q < N && r < N) {
         T c[N], o[Q];
@@ -320,7 +412,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 3: along q: pencils (i, r) ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<1, N>(S1, S0, wbf, t, [](int, int r) { return r < N; });
+    } else if constexpr (V4) {
       const int i = vj_i, r = vj_k;
       if (r < N) {
         T c[N], o[Q];
@@ -382,7 +476,10 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 5: d/dxi_0 on pencils (j, k) -> S0 ; d/dxi_1 on pencils (i, k) -> S1 ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<0, Q>(SU, S0, wdf, t, [](int, int) { return true; });
+      tc_contract<1, Q>(SU, S1, wdf, t, [](int, int) { return true; });
+    } else if constexpr (V4) {
       T c[Q], o[Q];
       lds8(SU + PJ * (t / 8) + PK * (t % 8), c);
       contract2<Q, Q, QP, false>(DF, c, o);
@@ -480,7 +577,10 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     // single buffer: stage 6 has read it, so the next group's copy can start now
     if (NB == 1 && tid == 0 && has_next) issue_geometry(nxt, 0);
     // ---- 7: D^T along i on pencils (j, k) in S0, along j on pencils (i, k) in S1 ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<0, Q>(S0, S0, wdt, t, [](int, int) { return true; });
+      tc_contract<1, Q>(S1, S1, wdt, t, [](int, int) { return true; });
+    } else if constexpr (V4) {
       T c[Q], o[Q];
       lds8(S0 + PJ * (t / 8) + PK * (t % 8), c);
       contract2<Q, Q, QP, false>(DT, c, o);
@@ -550,7 +650,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 9: along j: pencils (i, r) -> S0 as (i, q, r) ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<1, Q>(SU, S0, wbt, t, [](int, int r) { return r < N; });
+    } else if constexpr (V4) {
       const int i = vj_i, r = vj_k;
       if (r < N) {
         T c[Q], o[N];
@@ -582,7 +684,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     }
     __syncthreads();
     // ---- 10: along i: pencils (q, r) -> S1 as (p, q, r) ----
-    if constexpr (V4) {
+    if constexpr (TC) {
+      tc_contract<0, Q>(S0, S1, wbt, t, [](int q, int r) { return q < N && r < N; });
+    } else if constexpr (V4) {
       const int q = t / 8, r = t % 8;
       if (q < N && r < N) {
         T c[Q], o[N];

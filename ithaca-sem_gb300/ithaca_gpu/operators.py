@@ -266,13 +266,14 @@ class Collection:
         geometry (elements per CTA), 21/22 persistent pipelined pencil (1/2 elements per group,
         double geometry buffer), 31/32 the same with a single geometry buffer, 41/42 = 31/32
         with the contractions on packed FP32 pairs, 43/44 = 42/41 with vector pencils in a
-        bank-conflict-free shared-memory layout (Q = 8)."""
+        bank-conflict-free shared-memory layout (Q = 8), 46 = 43 with the i and j contractions
+        on the tensor cores (TF32 in three-term split precision)."""
         C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
 
     def autotune(self, reps=10):
         """Times each kernel variant on this collection and keeps the fastest."""
         chosen = ctypes.c_int()
-        variants = (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44)
+        variants = (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46)
         times = np.zeros(len(variants))
         C.call("ithaca_gpu_op_autotune", self.handle, int(reps), ctypes.byref(chosen),
                ctypes.c_void_p(times.ctypes.data))
@@ -416,7 +417,7 @@ class GlobalLinSysIterativeFullGPU:
                ctypes.byref(ms), ctypes.byref(nbytes))
         return ms.value, nbytes.value
 
-    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44), reps=10):
+    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46), reps=10):
         """Times the gathered FP32 apply of the mixed solver's inner iteration with each
         FP32 kernel variant of the collection and keeps the fastest (the solver-side
         counterpart of Collection.autotune, which times the ungathered apply).

@@ -127,11 +127,12 @@ def test_mixed_kernel_variants_curved_hex(ctx, variant):
     assert abs(res.iterations - ref.iterations) <= 4, (res.iterations, ref.iterations)
 
 
-@pytest.mark.parametrize("variant", [43, 44])
+@pytest.mark.parametrize("variant", [43, 44, 46])
 def test_mixed_vector_pencils_q8(ctx, variant):
     """The vector-pencil kernels (Q = 8) inside the mixed solver against their scalar-pencil
-    counterparts (42, 41), whose arithmetic they share: the same inner iterations within
-    one and the same solution."""
+    counterparts (42, 41): the same inner iterations within one and the same solution where
+    the arithmetic is shared (43, 44); within 2% of the inner iterations summed over the
+    refinement steps with the tensor-core stages (46)."""
     c = hex_case(3, 3, 2, 7, amp=0.08)
     coll, amap, sys_ = _system(ctx, c)
     rhs = np.random.default_rng(29).uniform(-1, 1, amap.nglobal)
@@ -141,7 +142,8 @@ def test_mixed_vector_pencils_q8(ctx, variant):
     coll.set_variant(variant)
     x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
     assert res.rel_residual < 1e-10
-    assert abs(res.iterations - ref.iterations) <= 1, (res.iterations, ref.iterations)
+    slack = max(4, ref.iterations // 50) if variant == 46 else 1
+    assert abs(res.iterations - ref.iterations) <= slack, (res.iterations, ref.iterations)
     assert rel_err(x[amap.ndir:], xr[amap.ndir:]) < 1e-9
 
 
