@@ -39,7 +39,7 @@ struct TetShape {
   static constexpr int TS = align_up(O.core, 4);  // tables the operators read
   static constexpr int TSD = align_up(O.size, 4);  // with DB0, DB1, DB2 (diagonal)
   static constexpr int SLAB = 4 * NQ;
-  static constexpr int TPE = NQ <= 32 ? 32 : (NQ <= 64 ? 64 : (NQ <= 128 ? 128 : 256));
+  static constexpr int TPE = NQ <= 32 ? 32 : (NQ <= 64 ? 64 : 128);  // larger elements: two per CTA
   static constexpr int EB = 256 / TPE;
   template <typename T>
   static constexpr size_t bytes() {
