@@ -134,11 +134,11 @@ def fp32_kernel_name(variant, n, Q):
         return f"helm_kernel<float,3,{n},{Q}>"
     if variant in (2, 4):
         return f"helm3_pencil_kernel<float,{n},{Q},{variant}>"
-    if variant in (43, 44, 46):
+    if variant in (43, 44, 46, 47):
         if Q != 8:  # vector pencils exist for Q = 8; elsewhere 42 / 41 run
             return fp32_kernel_name(41 if variant == 44 else 42, n, Q)
         return (f"helm3_pipe_kernel<float,{n},{Q},{1 if variant == 44 else 2},gather,1,packed,vec4"
-                + (",tf32x3>" if variant == 46 else ">"))
+                + {46: ",tf32x3>", 47: ",evenodd>"}.get(variant, ">"))
     return (f"helm3_pipe_kernel<float,{n},{Q},{variant % 10},gather,{2 if variant // 10 == 2 else 1}"
             + (",packed>" if variant // 10 == 4 else ">"))
 

@@ -189,15 +189,17 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
  * default), 43 or 44 = 42 or 41 with the unit-stride pencils moved as 16-byte words in a
  * bank-conflict-free shared-memory layout (same results), 46 = 43 with the contractions along
  * i and j as TF32 tensor-core MMAs in three-term split precision (FP32-level accuracy, not
- * bit-identical); 43, 44 and 46 are built for Q = 8, other orders run 42 or 41.
- * Inside the mixed solver the pipelined variants (21-46) also write the rows of
+ * bit-identical), 47 = 43 with every 1-D operator in its even-odd form (the symmetry of
+ * the GLL points and the parity of the modes: half the multiply-adds; FP32-level accuracy,
+ * not bit-identical); 43, 44, 46 and 47 are built for Q = 8, other orders run 42 or 41.
+ * Inside the mixed solver the pipelined variants (21-47) also write the rows of
  * the global system that have a single local entry themselves, so the assembly that
  * follows skips them. */
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
 /* Times every variant on the operator's own data and keeps the fastest, like
  * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)
- * picks an implementation type. times_ms (12 entries, may be NULL) receives the average
- * FP32 apply time of variants 0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46 (-1 where a
+ * picks an implementation type. times_ms (13 entries, may be NULL) receives the average
+ * FP32 apply time of variants 0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47 (-1 where a
  * variant does not apply). */
 int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* times_ms);
 /* Diagonals of the element Helmholtz matrices (E*n^d), the per-element input of

@@ -861,8 +861,9 @@ int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant) {
   return guarded([&] {
     require(op != nullptr, "null argument");
     require(variant == 0 || variant == 2 || variant == 4 || variant == 21 || variant == 22 || variant == 31 ||
-                variant == 32 || variant == 41 || variant == 42 || variant == 43 || variant == 44 || variant == 46,
-            "variant must be 0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44 or 46");
+                variant == 32 || variant == 41 || variant == 42 || variant == 43 || variant == 44 || variant == 46 ||
+                variant == 47,
+            "variant must be 0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46 or 47");
     op->variant32 = variant;
   });
 }
@@ -901,10 +902,10 @@ int ithaca_gpu_op_autotune(ithaca_gpu_op* op, int reps, int* chosen, double* tim
     ITHACA_CUDA(cudaMalloc(&x, sizeof(float) * nm));
     ITHACA_CUDA(cudaMalloc(&y, sizeof(float) * nm));
     ITHACA_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * nm, s));
-    const int variants[12] = {0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46};
+    const int variants[13] = {0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47};
     double best = 1e300;
     int best_v = 0;
-    for (int vi = 0; vi < 12; ++vi) {
+    for (int vi = 0; vi < 13; ++vi) {
       const int v = variants[vi];
       double ms_avg = -1;
       if (v == 0 || (op->kdim == 3 && op->deformed)) {

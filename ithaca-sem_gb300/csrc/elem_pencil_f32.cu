@@ -26,8 +26,36 @@ static void pencil_nq(int E, const double* hB, const double* hD, const T* jg, T 
 
 // Persistent pipelined kernel: one CTA per resident slot (SMs x CTAs per SM, from the
 // occupancy calculator), never more CTAs than element groups.
+template <int N, int Q>
+static PTabs3<N, Q> eo_tables(const double* hB, const double* hD) {
+  PTabs3<N, Q> t{};
+  if constexpr (Q % 2 == 0) {
+    constexpr int H = Q / 2, NE = (N + 1) / 2;
+    for (int i = 0; i < H; ++i) {
+      for (int j = 0; j < NE; ++j) {
+        double x, y;
+        if (j == 0) {
+          x = 0.5 * (hB[i] + hB[Q + i]);
+          y = 0.5 * (hB[i] - hB[Q + i]);
+        } else {
+          x = 2 * j < N ? hB[2 * j * Q + i] : 0.0;
+          y = 2 * j + 1 < N ? hB[(2 * j + 1) * Q + i] : 0.0;
+        }
+        t.bw[i][j] = make_float2((float)x, (float)y);
+      }
+      for (int k = 0; k < H; ++k) {
+        const double a = hD[k * Q + i], b = hD[(Q - 1 - k) * Q + i];            // l'_k(z_i), l'_{Q-1-k}(z_i)
+        const double c = hD[i * Q + k], d = hD[i * Q + Q - 1 - k];              // l'_i(z_k), l'_i(z_{Q-1-k})
+        t.d[i][k] = make_float2((float)(0.5 * (a + b)), (float)(0.5 * (a - b)));
+        t.dt[i][k] = make_float2((float)(0.5 * (c + d)), (float)(0.5 * (c - d)));
+      }
+    }
+  }
+  return t;
+}
+
 template <typename T, int N, int Q, int EB, int NB, typename TG = T, bool PACK = false, bool V4 = false,
-          bool TC = false>
+          bool TC = false, bool EO = false>
 static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T lambda, const T* in, T* out,
                     const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err, cudaStream_t s,
                     const float* gscale = nullptr, OwnedRows* own = nullptr) {
@@ -47,8 +75,9 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
       tab2.DT[i * QP + k] = (float)hD[k * Q + i];
     }
   using L = PipeLayout<T, N, Q, EB, NB, TG, V4>;
-  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG, PACK, V4, TC>
-               : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG, PACK, V4, TC>;
+  const PTabs3<N, Q> tab3 = eo_tables<N, Q>(hB, hD);
+  auto k = l2g ? helm3_pipe_kernel<T, N, Q, EB, true, NB, TG, PACK, V4, TC, EO>
+               : helm3_pipe_kernel<T, N, Q, EB, false, NB, TG, PACK, V4, TC, EO>;
   static int slots[2] = {0, 0};  // resident CTAs on the whole GPU
   const int gi = l2g ? 1 : 0;
   if (slots[gi] == 0) {
@@ -70,8 +99,8 @@ static void pipe_nq(int E, const double* hB, const double* hD, const TG* jg, T l
     ocode = own->ocode;
     own->ctas = (int)grid.x;
   }
-  k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale, sown,
-                                    opart, ocode);
+  k<<<grid, block, L::bytes(), s>>>(in, out, tab, tab2, tab3, jg, lambda, E, l2g, ndir, skip, lam_ptr, err, gscale,
+                                    sown, opart, ocode);
 }
 
 }  // namespace dev
@@ -98,18 +127,22 @@ bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double*
 // group and a double geometry buffer; 31 or 32 = the same with a single buffer; 41 or 42 =
 // the single-buffer kernel with its contractions on packed FP32 pairs (fma.rn.f32x2); 43 or
 // 44 = 42 or 41 with vector pencils in shared memory, 46 = 43 with the contractions along i
-// and j on the tensor cores (TF32 MMAs in three-term split precision; Q = 8; other orders
-// run 42 or 41).
+// and j on the tensor cores (TF32 MMAs in three-term split precision), 47 = 43 with every
+// 1-D operator in its even-odd form (half the multiply-adds; Q = 8; other orders run 42 or
+// 41).
 template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s, OwnedRows* own) {
   if (own != nullptr) own->ctas = -1;  // set by the pipelined kernels only
-  if (variant == 43 || variant == 44 || variant == 46) {
+  if (variant == 43 || variant == 44 || variant == 46 || variant == 47) {
     // vector pencils are built for Q = 8; elsewhere the scalar-pencil kernel with the same
     // arithmetic (and so the same results) runs
     if (n == 7 && Q == 8 && std::is_same<T, float>::value) {
-      if (variant == 46)
+      if (variant == 47)
+        dev::pipe_nq<T, 7, 8, 2, 1, T, true, true, false, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip,
+                                                                lam_ptr, err, s, nullptr, own);
+      else if (variant == 46)
         dev::pipe_nq<T, 7, 8, 2, 1, T, true, true, true>(E, hB, hD, jg, lambda, in, out, l2g, ndir, skip, lam_ptr, err,
                                                          s, nullptr, own);
       else if (variant == 43)

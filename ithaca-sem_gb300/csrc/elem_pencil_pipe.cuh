@@ -104,6 +104,87 @@ struct PipeLayout {
   static constexpr size_t bytes() { return 16 + NB * GEO_BYTES + (size_t)EB * 3 * FS * sizeof(T); }
 };
 
+// ---- even-odd contractions (EO, Q even) ----
+// The GLL points are symmetric (z_{Q-1-i} = -z_i), so the collocation derivative is
+// antisymmetric (l'_{Q-1-k}(z_{Q-1-i}) = -l'_k(z_i)) and the ModifiedA modes have parity
+// (B_0 and B_1 swap under z -> -z, B_p(-z) = (-1)^p B_p(z) for p >= 2). Each pair of
+// outputs (i, Q-1-i) then follows from half-length sums over the even and odd parts of the
+// input (e_k = u_k + u_{Q-1-k}, o_k = u_k - u_{Q-1-k}), the E and O sums riding in the two
+// halves of one packed FP32 pair: half the multiply-adds of the plain contraction.
+//   bw[i][j] = ((B_0 + B_1) / 2, (B_0 - B_1) / 2)(z_i) for j = 0, (B_2j, B_2j+1)(z_i) else
+//   d[i][k]  = (D_ki + D_(Q-1-k)i, D_ki - D_(Q-1-k)i) / 2 with D_ki = l'_k(z_i)
+//   dt[i][k] = the same for the transposed derivative T_ki = l'_i(z_k)
+template <int N, int Q>
+struct PTabs3 {
+  static constexpr int H = Q / 2, NE = (N + 1) / 2;
+  alignas(8) float2 bw[H][NE];
+  alignas(8) float2 d[H][H];
+  alignas(8) float2 dt[H][H];
+};
+__device__ __forceinline__ unsigned long long pk2f(const float2& v) {
+  return *reinterpret_cast<const unsigned long long*>(&v);
+}
+// modes -> points: o[i], i < Q, from c[p], p < N
+template <int N, int Q>
+__device__ __forceinline__ void eo_bwd(const PTabs3<N, Q>& tb, const float (&c)[N], float (&o)[Q]) {
+  constexpr int H = Q / 2, NE = (N + 1) / 2;
+  unsigned long long x[NE];
+  x[0] = pk2(c[0] + c[1], c[0] - c[1]);
+#pragma unroll
+  for (int j = 1; j < NE; ++j) x[j] = pk2(c[2 * j], 2 * j + 1 < N ? c[2 * j + 1] : 0.f);
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    unsigned long long acc = pk2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < NE; ++j) acc = ffma2(pk2f(tb.bw[i][j]), x[j], acc);
+    float E, O;
+    upk2(acc, E, O);
+    o[i] = E + O;
+    o[Q - 1 - i] = E - O;
+  }
+}
+// points -> modes (IProduct): o[p], p < N, from v[i], i < Q
+template <int N, int Q>
+__device__ __forceinline__ void eo_ipr(const PTabs3<N, Q>& tb, const float (&v)[Q], float (&o)[N]) {
+  constexpr int H = Q / 2, NE = (N + 1) / 2;
+  unsigned long long x[H];
+#pragma unroll
+  for (int k = 0; k < H; ++k) x[k] = pk2(v[k] + v[Q - 1 - k], v[k] - v[Q - 1 - k]);
+#pragma unroll
+  for (int j = 0; j < NE; ++j) {
+    unsigned long long acc = pk2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < H; ++k) acc = ffma2(pk2f(tb.bw[k][j]), x[k], acc);
+    float E, O;
+    upk2(acc, E, O);
+    if (j == 0) {
+      o[0] = E + O;
+      o[1] = E - O;
+    } else {
+      o[2 * j] = E;
+      if (2 * j + 1 < N) o[2 * j + 1] = O;
+    }
+  }
+}
+// antisymmetric Q x Q operator (derivative or its transpose); INIT adds to o
+template <int Q, bool INIT>
+__device__ __forceinline__ void eo_anti(const float2 (&t)[Q / 2][Q / 2], const float (&u)[Q], float (&o)[Q]) {
+  constexpr int H = Q / 2;
+  unsigned long long x[H];
+#pragma unroll
+  for (int k = 0; k < H; ++k) x[k] = pk2(u[k] + u[Q - 1 - k], u[k] - u[Q - 1 - k]);
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    unsigned long long acc = pk2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < H; ++k) acc = ffma2(pk2f(t[i][k]), x[k], acc);
+    float E, O;
+    upk2(acc, E, O);
+    o[i] = INIT ? o[i] + (E + O) : E + O;
+    o[Q - 1 - i] = INIT ? o[Q - 1 - i] + (O - E) : O - E;
+  }
+}
+
 // ---- warp-level TF32 tensor-core contractions in three-term split precision (TC) ----
 // A contraction of an element's 64 pencils (rows r) with a 1-D table W (8 x 8, zero padded)
 // is a 64 x 8 x 8 product: four m16n8k8 tiles, two per warp of the element. Each FP32
@@ -198,9 +279,10 @@ __device__ __forceinline__ void sts8(float* p, const float (&o)[M]) {
 }
 
 template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T, bool PACK = false, bool V4 = false,
-          bool TC = false>
+          bool TC = false, bool EO = false>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                                const PTabs<T, N, Q> tab, const PTabs2<N, Q> tab2,
+                                                               const PTabs3<N, Q> tab3,
                                                                const TG* __restrict__ jg,
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
@@ -213,6 +295,38 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
   static_assert(!V4 || (PACK && Q == 8 && N <= 8), "vector pencils: packed FP32, Q = 8");
   static_assert(!TC || (V4 && Q * Q == 64), "tensor-core stages: the vector-pencil layout, 64 pencils");
+  static_assert(!EO || (V4 && !TC && Q % 2 == 0 && N >= 2), "even-odd stages: the vector-pencil layout, Q even");
+  // the 1-D operators of the packed stages: plain contractions or their even-odd forms
+  auto op_bwd = [&](const T (&c)[N], T (&o)[Q]) {
+    if constexpr (EO)
+      eo_bwd<N, Q>(tab3, c, o);
+    else
+      contract2<N, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.BF[i]; }, c, o);
+  };
+  auto op_der = [&](const T (&c)[Q], T (&o)[Q]) {
+    if constexpr (EO)
+      eo_anti<Q, false>(tab3.d, c, o);
+    else
+      contract2<Q, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.DF[i]; }, c, o);
+  };
+  auto op_dert = [&](const T (&c)[Q], T (&o)[Q]) {
+    if constexpr (EO)
+      eo_anti<Q, false>(tab3.dt, c, o);
+    else
+      contract2<Q, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.DT[i]; }, c, o);
+  };
+  auto op_dert_add = [&](const T (&c)[Q], T (&o)[Q]) {
+    if constexpr (EO)
+      eo_anti<Q, true>(tab3.dt, c, o);
+    else
+      contract2<Q, Q, PTabs2<N, Q>::QP, true>([&](int i) { return tab2.DT[i]; }, c, o);
+  };
+  auto op_ipr = [&](const T (&c)[Q], T (&o)[N]) {
+    if constexpr (EO)
+      eo_ipr<N, Q>(tab3, c, o);
+    else
+      contract2<Q, N, PTabs2<N, Q>::NP, false>([&](int i) { return tab2.BT[i]; }, c, o);
+  };
   constexpr int QP = PTabs2<N, Q>::QP, NP = PTabs2<N, Q>::NP;
   auto BF = [&](int i) { return tab2.BF[i]; };
   auto DF = [&](int i) { return tab2.DF[i]; };
@@ -387,7 +501,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       if (q < N && r < N) {
         T c[N], o[Q];
         lds8(S0 + PJ * q + PK * r, c);
-        contract2<N, Q, QP, false>(BF, c, o);
+        op_bwd(c, o);
         sts8(S1 + PJ * q + PK * r, o);
       }
     } else if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {
@@ -420,7 +534,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         T c[N], o[Q];
 #pragma unroll
         for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
-        contract2<N, Q, QP, false>(BF, c, o);
+        op_bwd(c, o);
 #pragma unroll
         for (int j = 0; j < Q; ++j) S0[i + PJ * j + PK * r] = o[j];
       }
@@ -453,8 +567,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 #pragma unroll
       for (int r = 0; r < N; ++r) c[r] = S0[ci + PJ * cj + PK * r];
       if constexpr (PACK) {
-        contract2<N, Q, QP, false>(BF, c, u);
-        contract2<Q, Q, QP, false>(DF, u, g2);
+        op_bwd(c, u);
+        op_der(u, g2);
       } else {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
@@ -482,11 +596,11 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     } else if constexpr (V4) {
       T c[Q], o[Q];
       lds8(SU + PJ * (t / 8) + PK * (t % 8), c);
-      contract2<Q, Q, QP, false>(DF, c, o);
+      op_der(c, o);
       sts8(S0 + PJ * (t / 8) + PK * (t % 8), o);
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = SU[vj_i + PJ * a + PK * vj_k];
-      contract2<Q, Q, QP, false>(DF, c, o);
+      op_der(c, o);
 #pragma unroll
       for (int j = 0; j < Q; ++j) S1[vj_i + PJ * j + PK * vj_k] = o[j];
     } else {
@@ -562,7 +676,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         v[k] = lambda * jw * u[k];
       }
       if constexpr (PACK) {
-        contract2<Q, Q, QP, true>(DT, f2, v);
+        op_dert_add(f2, v);
       } else {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
@@ -583,11 +697,11 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
     } else if constexpr (V4) {
       T c[Q], o[Q];
       lds8(S0 + PJ * (t / 8) + PK * (t % 8), c);
-      contract2<Q, Q, QP, false>(DT, c, o);
+      op_dert(c, o);
       sts8(S0 + PJ * (t / 8) + PK * (t % 8), o);
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S1[vj_i + PJ * a + PK * vj_k];
-      contract2<Q, Q, QP, false>(DT, c, o);
+      op_dert(c, o);
 #pragma unroll
       for (int j = 0; j < Q; ++j) S1[vj_i + PJ * j + PK * vj_k] = o[j];
     } else {
@@ -635,7 +749,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       }
       if constexpr (PACK) {
         T o[N];
-        contract2<Q, N, NP, false>(BT, v, o);
+        op_ipr(v, o);
 #pragma unroll
         for (int r = 0; r < N; ++r) SU[ci + PJ * cj + PK * r] = o[r];
       } else {
@@ -658,7 +772,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         T c[Q], o[N];
 #pragma unroll
         for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
-        contract2<Q, N, NP, false>(BT, c, o);
+        op_ipr(c, o);
 #pragma unroll
         for (int q = 0; q < N; ++q) S0[i + PJ * q + PK * r] = o[q];
       }
@@ -691,7 +805,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       if (q < N && r < N) {
         T c[Q], o[N];
         lds8(S0 + PJ * q + PK * r, c);
-        contract2<Q, N, NP, false>(BT, c, o);
+        op_ipr(c, o);
         sts8(S1 + PJ * q + PK * r, o);  // p = N..7 of the pencil: padding, written as zero
       }
     } else if (M8 ? (t / 8 < N && t % 8 < N) : t < N * N) {

@@ -267,13 +267,14 @@ class Collection:
         double geometry buffer), 31/32 the same with a single geometry buffer, 41/42 = 31/32
         with the contractions on packed FP32 pairs, 43/44 = 42/41 with vector pencils in a
         bank-conflict-free shared-memory layout (Q = 8), 46 = 43 with the i and j contractions
-        on the tensor cores (TF32 in three-term split precision)."""
+        on the tensor cores (TF32 in three-term split precision), 47 = 43 with the 1-D
+        operators in even-odd form."""
         C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
 
     def autotune(self, reps=10):
         """Times each kernel variant on this collection and keeps the fastest."""
         chosen = ctypes.c_int()
-        variants = (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46)
+        variants = (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47)
         times = np.zeros(len(variants))
         C.call("ithaca_gpu_op_autotune", self.handle, int(reps), ctypes.byref(chosen),
                ctypes.c_void_p(times.ctypes.data))
@@ -417,7 +418,7 @@ class GlobalLinSysIterativeFullGPU:
                ctypes.byref(ms), ctypes.byref(nbytes))
         return ms.value, nbytes.value
 
-    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46), reps=10):
+    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47), reps=10):
         """Times the gathered FP32 apply of the mixed solver's inner iteration with each
         FP32 kernel variant of the collection and keeps the fastest (the solver-side
         counterpart of Collection.autotune, which times the ungathered apply).

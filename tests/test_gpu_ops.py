@@ -156,7 +156,7 @@ def test_unsupported_order_raises(ctx):
 
 
 @pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 7, 8, 9, 10])
-@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46])
+@pytest.mark.parametrize("variant", [0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47])
 def test_hex_fp32_kernel_variants(ctx, n, variant):
     """Every FP32 hex Helmholtz kernel variant (shared-memory; register-pencil with a
     TMA-staged geometry slab, one pass with 2 or 4 elements per CTA or persistent and
@@ -187,28 +187,30 @@ def test_hex_pencil_variants_bit_identical(ctx, n):
         assert np.array_equal(o, outs[2]), v
 
 
-def test_hex_tensor_core_stages_fp32_accuracy(ctx):
-    """Variant 46 runs the i and j contractions as TF32 MMAs in three-term split precision:
-    its apply stays within a few FP32 rounding steps of the FP32-FMA kernel (43) and of the
-    FP64 oracle, on a curved mesh with a partial last group."""
+def test_hex_tensor_core_and_even_odd_stages_fp32_accuracy(ctx):
+    """Variant 46 runs the i and j contractions as TF32 MMAs in three-term split precision,
+    variant 47 every 1-D operator in even-odd form: each apply stays within a few FP32
+    rounding steps of the FP32-FMA kernel (43) and of the FP64 oracle, on a curved mesh with
+    a partial last group."""
     c = hex_case(5, 2, 2, 7)
     coll = _coll(ctx, c, "fp32")
     u = np.random.default_rng(77).uniform(-1, 1, c.E * c.nm)
     ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 0.9, u)
     outs = {}
-    for v in (43, 46):
+    for v in (43, 46, 47):
         coll.set_variant(v)
         outs[v] = coll.helmholtz(0.9, u.astype(np.float32)).astype(np.float64)
-    e43, e46 = rel_err(outs[43], ref), rel_err(outs[46], ref)
-    assert e46 < 4 * max(e43, 1e-7), (e46, e43)
-    assert rel_err(outs[46], outs[43]) < 5e-6
+    e43 = rel_err(outs[43], ref)
+    for v in (46, 47):  # tensor-core stages; even-odd 1-D operators
+        assert rel_err(outs[v], ref) < 4 * max(e43, 1e-7), (v, rel_err(outs[v], ref), e43)
+        assert rel_err(outs[v], outs[43]) < 5e-6, v
 
 
 def test_autotune_picks_a_working_variant(ctx):
     c = hex_case(4, 4, 2, 7)
     coll = _coll(ctx, c, "fp32")
     chosen, times = coll.autotune(reps=3)
-    assert chosen in (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46) and all(t > 0 for t in times.values())
+    assert chosen in (0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47) and all(t > 0 for t in times.values())
     u = np.random.default_rng(3).uniform(-1, 1, c.E * c.nm)
     out = coll.helmholtz(1.0, u.astype(np.float32))
     ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, u)
