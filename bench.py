@@ -146,9 +146,9 @@ def fp32_kernel_name(variant, n, Q):
 # DRAM bytes (read + write) per element of one gathered FP32 apply as the inner iteration
 # launches it (scattered output: owned rows and assembly-ordered slots), from an ncu
 # capture of the kernel on 28^3 hexes (variant 42: 394.1 MB read + 5.4 MB written per
-# launch over 21,952 elements; variant 43: 394.1 + 5.5 MB); a launch's traffic grows with
-# the number of elements, so the bench scales it by E. Keys: (kernel variant, modes, points).
-TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200, (43, 7, 8): 18204}
+# launch over 21,952 elements; variants 43 and 47: 394.1 + 5.5 MB); a launch's traffic grows
+# with the number of elements, so the bench scales it by E. Keys: (kernel variant, modes, points).
+TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200, (43, 7, 8): 18204, (47, 7, 8): 18204}
 
 
 def workload_config(args, n, Q, E, N, ndir):
