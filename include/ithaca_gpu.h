@@ -196,6 +196,14 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
  * the global system that have a single local entry themselves, so the assembly that
  * follows skips them. */
 int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant);
+/* FP64 hex Helmholtz kernel of a deformed hexahedral operator (the FP64 apply, the FP64
+ * solves and the outer residuals of the mixed solve): 0 = the shared-memory kernel (default),
+ * 1 / 2 = the persistent pipelined kernel with scalar FP64 pencils and every 1-D operator in
+ * its even-odd form (the symmetry of the GLL points and the parity of the ModifiedA modes:
+ * half the multiply-adds of the contractions), one / two elements per group; built for
+ * Q = 4, 6, 8, 10, other orders keep the shared-memory kernel. FP64-level agreement with
+ * variant 0, not bit-identical. */
+int ithaca_gpu_op_set_variant64(ithaca_gpu_op* op, int variant);
 /* Times every variant on the operator's own data and keeps the fastest, like
  * CollectionOptimisation::SetWithTimings (Collections/CollectionOptimisation.cpp:321-469)
  * picks an implementation type. times_ms (13 entries, may be NULL) receives the average

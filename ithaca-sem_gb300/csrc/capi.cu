@@ -838,11 +838,16 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
     const size_t es = elt(op), nm = (size_t)op->E * op->nm;
     const void* din = to_device(c, 0, in, es * nm, on_device);
     void* dout = out_buffer(c, 1, out, es * nm, on_device);
-    bool ok;
-    if (op->precision == ITHACA_GPU_FP64)
-      ok = launch_helmholtz<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
-                                    (const double*)din, (double*)dout, nullptr, 0, c->stream);
-    else if (op->kdim == 3 && op->deformed && op->variant32 > 0)
+    bool ok = false;
+    if (op->precision == ITHACA_GPU_FP64) {
+      if (op->kdim == 3 && op->deformed && op->variant64 > 0)  // even-odd pencil kernel where it is built
+        ok = launch_helm_pencil64(op->n, op->Q, op->E, op->variant64, op->hB.data(), op->hD.data(), op->jg64, lambda,
+                                  (const double*)din, (double*)dout, nullptr, 0, nullptr, nullptr, c->derr,
+                                  c->stream);
+      if (!ok)
+        ok = launch_helmholtz<double>(op->kdim, op->n, op->Q, op->E, op->deformed, op->t64.base, op->jg64, lambda,
+                                      (const double*)din, (double*)dout, nullptr, 0, c->stream);
+    } else if (op->kdim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), op->jg32,
                                      (float)lambda, (const float*)din, (float*)dout, nullptr, 0, nullptr, nullptr,
                                      c->derr, c->stream);
@@ -865,6 +870,14 @@ int ithaca_gpu_op_set_variant(ithaca_gpu_op* op, int variant) {
                 variant == 47,
             "variant must be 0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46 or 47");
     op->variant32 = variant;
+  });
+}
+
+int ithaca_gpu_op_set_variant64(ithaca_gpu_op* op, int variant) {
+  return guarded([&] {
+    require(op != nullptr, "null argument");
+    require(variant >= 0 && variant <= 2, "variant must be 0, 1 or 2");
+    op->variant64 = variant;
   });
 }
 

@@ -695,6 +695,9 @@ struct Cg {
   // coefficient set later (a new geometry buffer) needs a new capture
   const void* graph64_geo = nullptr;
   const void* graph32_geo = nullptr;
+  // element-kernel variant each graph was captured with (a variant set later needs a new
+  // capture too: the captured launch names its kernel)
+  int graph64_variant = -1, graph32_variant = -1;
   SuccessiveRhs proj;
   ~Cg();
 };
@@ -755,8 +758,13 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
       ok = launch_helmholtz<T>(op->kdim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
                                zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
   } else {
-    ok = launch_helmholtz<T>(op->kdim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
-                             zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
+    ok = false;
+    if (op->kdim == 3 && op->deformed && op->variant64 > 0)  // even-odd pencil kernel where it is built
+      ok = launch_helm_pencil64(op->n, op->Q, op->E, op->variant64, op->hB.data(), op->hD.data(), jg, lambda, xin,
+                                v.yloc, cg->l2g, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s);
+    if (!ok)
+      ok = launch_helmholtz<T>(op->kdim, op->n, op->Q, op->E, op->deformed, tab, jg, lambda, xin, v.yloc, cg->l2g,
+                               zero_dir ? cg->ndir : 0, s, skip, lam_ptr);
   }
   if (!ok) fail(ITHACA_GPU_ERR_UNSUPPORTED, "Helmholtz: (modes, points) combination not built");
   op->ctx->launches++;
@@ -879,13 +887,16 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
   int& len = sizeof(T) == 8 ? cg->graph64_len : cg->graph32_len;
   const void*& geo = sizeof(T) == 8 ? cg->graph64_geo : cg->graph32_geo;
+  int& gvar = sizeof(T) == 8 ? cg->graph64_variant : cg->graph32_variant;
+  const int var = sizeof(T) == 8 ? cg->op->variant64 : cg->op->variant32;
   const bool geo_changed = (sizeof(T) == 4 && cg->graph32_geo16 != cg->geo16) || geo != (const void*)jg;
-  if (!ex || len != chunk || geo_changed) {
+  if (!ex || len != chunk || geo_changed || gvar != var) {
     if (ex) cudaGraphExecDestroy(ex);
     ex = nullptr;
     ex = capture_chunk<T>(cg, v, tab, jg, chunk);
     len = chunk;
     geo = jg;
+    gvar = var;
     if (sizeof(T) == 4) cg->graph32_geo16 = cg->geo16;
   }
   // Bounded host loop: at most max_iter / chunk + 2 graph launches.

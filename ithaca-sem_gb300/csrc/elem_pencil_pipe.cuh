@@ -114,19 +114,23 @@ struct PipeLayout {
 //   bw[i][j] = ((B_0 + B_1) / 2, (B_0 - B_1) / 2)(z_i) for j = 0, (B_2j, B_2j+1)(z_i) else
 //   d[i][k]  = (D_ki + D_(Q-1-k)i, D_ki - D_(Q-1-k)i) / 2 with D_ki = l'_k(z_i)
 //   dt[i][k] = the same for the transposed derivative T_ki = l'_i(z_k)
-template <int N, int Q>
+template <typename T>
+struct alignas(2 * sizeof(T)) TPair {
+  T x, y;
+};
+template <typename T, int N, int Q>
 struct PTabs3 {
   static constexpr int H = Q / 2, NE = (N + 1) / 2;
-  alignas(8) float2 bw[H][NE];
-  alignas(8) float2 d[H][H];
-  alignas(8) float2 dt[H][H];
+  TPair<T> bw[H][NE];
+  TPair<T> d[H][H];
+  TPair<T> dt[H][H];
 };
-__device__ __forceinline__ unsigned long long pk2f(const float2& v) {
+__device__ __forceinline__ unsigned long long pk2f(const TPair<float>& v) {
   return *reinterpret_cast<const unsigned long long*>(&v);
 }
 // modes -> points: o[i], i < Q, from c[p], p < N
 template <int N, int Q>
-__device__ __forceinline__ void eo_bwd(const PTabs3<N, Q>& tb, const float (&c)[N], float (&o)[Q]) {
+__device__ __forceinline__ void eo_bwd(const PTabs3<float, N, Q>& tb, const float (&c)[N], float (&o)[Q]) {
   constexpr int H = Q / 2, NE = (N + 1) / 2;
   unsigned long long x[NE];
   x[0] = pk2(c[0] + c[1], c[0] - c[1]);
@@ -145,7 +149,7 @@ __device__ __forceinline__ void eo_bwd(const PTabs3<N, Q>& tb, const float (&c)[
 }
 // points -> modes (IProduct): o[p], p < N, from v[i], i < Q
 template <int N, int Q>
-__device__ __forceinline__ void eo_ipr(const PTabs3<N, Q>& tb, const float (&v)[Q], float (&o)[N]) {
+__device__ __forceinline__ void eo_ipr(const PTabs3<float, N, Q>& tb, const float (&v)[Q], float (&o)[N]) {
   constexpr int H = Q / 2, NE = (N + 1) / 2;
   unsigned long long x[H];
 #pragma unroll
@@ -168,7 +172,7 @@ __device__ __forceinline__ void eo_ipr(const PTabs3<N, Q>& tb, const float (&v)[
 }
 // antisymmetric Q x Q operator (derivative or its transpose); INIT adds to o
 template <int Q, bool INIT>
-__device__ __forceinline__ void eo_anti(const float2 (&t)[Q / 2][Q / 2], const float (&u)[Q], float (&o)[Q]) {
+__device__ __forceinline__ void eo_anti(const TPair<float> (&t)[Q / 2][Q / 2], const float (&u)[Q], float (&o)[Q]) {
   constexpr int H = Q / 2;
   unsigned long long x[H];
 #pragma unroll
@@ -180,6 +184,78 @@ __device__ __forceinline__ void eo_anti(const float2 (&t)[Q / 2][Q / 2], const f
     for (int k = 0; k < H; ++k) acc = ffma2(pk2f(t[i][k]), x[k], acc);
     float E, O;
     upk2(acc, E, O);
+    o[i] = INIT ? o[i] + (E + O) : E + O;
+    o[Q - 1 - i] = INIT ? o[Q - 1 - i] + (O - E) : O - E;
+  }
+}
+
+// The same even-odd forms with scalar E and O sums (FP64 pencils).
+template <typename T, int N, int Q>
+__device__ __forceinline__ void eo_bwd_s(const PTabs3<T, N, Q>& tb, const T (&c)[N], T (&o)[Q]) {
+  constexpr int H = Q / 2, NE = (N + 1) / 2;
+  T xe[NE], xo[NE];
+  xe[0] = c[0] + c[1];
+  xo[0] = c[0] - c[1];
+#pragma unroll
+  for (int j = 1; j < NE; ++j) {
+    xe[j] = c[2 * j];
+    xo[j] = 2 * j + 1 < N ? c[2 * j + 1] : T(0);
+  }
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    T E = tb.bw[i][0].x * xe[0], O = tb.bw[i][0].y * xo[0];
+#pragma unroll
+    for (int j = 1; j < NE; ++j) {
+      E = fma(tb.bw[i][j].x, xe[j], E);
+      O = fma(tb.bw[i][j].y, xo[j], O);
+    }
+    o[i] = E + O;
+    o[Q - 1 - i] = E - O;
+  }
+}
+template <typename T, int N, int Q>
+__device__ __forceinline__ void eo_ipr_s(const PTabs3<T, N, Q>& tb, const T (&v)[Q], T (&o)[N]) {
+  constexpr int H = Q / 2, NE = (N + 1) / 2;
+  T xe[H], xo[H];
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    xe[k] = v[k] + v[Q - 1 - k];
+    xo[k] = v[k] - v[Q - 1 - k];
+  }
+#pragma unroll
+  for (int j = 0; j < NE; ++j) {
+    T E = tb.bw[0][j].x * xe[0], O = tb.bw[0][j].y * xo[0];
+#pragma unroll
+    for (int k = 1; k < H; ++k) {
+      E = fma(tb.bw[k][j].x, xe[k], E);
+      O = fma(tb.bw[k][j].y, xo[k], O);
+    }
+    if (j == 0) {
+      o[0] = E + O;
+      o[1] = E - O;
+    } else {
+      o[2 * j] = E;
+      if (2 * j + 1 < N) o[2 * j + 1] = O;
+    }
+  }
+}
+template <typename T, int Q, bool INIT>
+__device__ __forceinline__ void eo_anti_s(const TPair<T> (&t)[Q / 2][Q / 2], const T (&u)[Q], T (&o)[Q]) {
+  constexpr int H = Q / 2;
+  T xe[H], xo[H];
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    xe[k] = u[k] + u[Q - 1 - k];
+    xo[k] = u[k] - u[Q - 1 - k];
+  }
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    T E = t[i][0].x * xe[0], O = t[i][0].y * xo[0];
+#pragma unroll
+    for (int k = 1; k < H; ++k) {
+      E = fma(t[i][k].x, xe[k], E);
+      O = fma(t[i][k].y, xo[k], O);
+    }
     o[i] = INIT ? o[i] + (E + O) : E + O;
     o[Q - 1 - i] = INIT ? o[Q - 1 - i] + (O - E) : O - E;
   }
@@ -282,7 +358,7 @@ template <typename T, int N, int Q, int EB, bool GATHER, int NB, typename TG = T
           bool TC = false, bool EO = false>
 __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                                const PTabs<T, N, Q> tab, const PTabs2<N, Q> tab2,
-                                                               const PTabs3<N, Q> tab3,
+                                                               const PTabs3<T, N, Q> tab3,
                                                                const TG* __restrict__ jg,
                                                                T lambda, int E, const int* __restrict__ l2g,
                                                                int ndir, const int* __restrict__ skip,
@@ -295,34 +371,45 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
   static_assert(!PACK || std::is_same<T, float>::value, "packed pairs are FP32");
   static_assert(!V4 || (PACK && Q == 8 && N <= 8), "vector pencils: packed FP32, Q = 8");
   static_assert(!TC || (V4 && Q * Q == 64), "tensor-core stages: the vector-pencil layout, 64 pencils");
-  static_assert(!EO || (V4 && !TC && Q % 2 == 0 && N >= 2), "even-odd stages: the vector-pencil layout, Q even");
+  static_assert(!EO || ((V4 || !PACK) && !TC && Q % 2 == 0 && N >= 2),
+                "even-odd stages: packed in the vector-pencil layout or scalar, Q even");
   // the 1-D operators of the packed stages: plain contractions or their even-odd forms
   auto op_bwd = [&](const T (&c)[N], T (&o)[Q]) {
-    if constexpr (EO)
+    if constexpr (EO && !PACK)
+      eo_bwd_s<T, N, Q>(tab3, c, o);
+    else if constexpr (EO)
       eo_bwd<N, Q>(tab3, c, o);
     else
       contract2<N, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.BF[i]; }, c, o);
   };
   auto op_der = [&](const T (&c)[Q], T (&o)[Q]) {
-    if constexpr (EO)
+    if constexpr (EO && !PACK)
+      eo_anti_s<T, Q, false>(tab3.d, c, o);
+    else if constexpr (EO)
       eo_anti<Q, false>(tab3.d, c, o);
     else
       contract2<Q, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.DF[i]; }, c, o);
   };
   auto op_dert = [&](const T (&c)[Q], T (&o)[Q]) {
-    if constexpr (EO)
+    if constexpr (EO && !PACK)
+      eo_anti_s<T, Q, false>(tab3.dt, c, o);
+    else if constexpr (EO)
       eo_anti<Q, false>(tab3.dt, c, o);
     else
       contract2<Q, Q, PTabs2<N, Q>::QP, false>([&](int i) { return tab2.DT[i]; }, c, o);
   };
   auto op_dert_add = [&](const T (&c)[Q], T (&o)[Q]) {
-    if constexpr (EO)
+    if constexpr (EO && !PACK)
+      eo_anti_s<T, Q, true>(tab3.dt, c, o);
+    else if constexpr (EO)
       eo_anti<Q, true>(tab3.dt, c, o);
     else
       contract2<Q, Q, PTabs2<N, Q>::QP, true>([&](int i) { return tab2.DT[i]; }, c, o);
   };
   auto op_ipr = [&](const T (&c)[Q], T (&o)[N]) {
-    if constexpr (EO)
+    if constexpr (EO && !PACK)
+      eo_ipr_s<T, N, Q>(tab3, c, o);
+    else if constexpr (EO)
       eo_ipr<N, Q>(tab3, c, o);
     else
       contract2<Q, N, PTabs2<N, Q>::NP, false>([&](int i) { return tab2.BT[i]; }, c, o);
@@ -509,9 +596,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int p = 0; p < N; ++p) c[p] = S0[p + PJ * q + PK * r];
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[Q];
-        contract2<N, Q, QP, false>(BF, c, o);
+        op_bwd(c, o);
 #pragma unroll
         for (int i = 0; i < Q; ++i) S1[i + PJ * q + PK * r] = o[i];
       } else {
@@ -543,9 +630,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int q = 0; q < N; ++q) c[q] = S1[i + PJ * q + PK * r];
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[Q];
-        contract2<N, Q, QP, false>(BF, c, o);
+        op_bwd(c, o);
 #pragma unroll
         for (int j = 0; j < Q; ++j) S0[i + PJ * j + PK * r] = o[j];
       } else {
@@ -566,7 +653,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[N];
 #pragma unroll
       for (int r = 0; r < N; ++r) c[r] = S0[ci + PJ * cj + PK * r];
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         op_bwd(c, u);
         op_der(u, g2);
       } else {
@@ -609,14 +696,14 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = SU[a + PJ * pj + PK * pk];
       const int pi = t % Q, pkb = t / Q;
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[Q];
-        contract2<Q, Q, QP, false>(DF, c, o);
+        op_der(c, o);
 #pragma unroll
         for (int i = 0; i < Q; ++i) S0[i + PJ * pj + PK * pk] = o[i];
 #pragma unroll
         for (int a = 0; a < Q; ++a) c[a] = SU[pi + PJ * a + PK * pkb];
-        contract2<Q, Q, QP, false>(DF, c, o);
+        op_der(c, o);
 #pragma unroll
         for (int j = 0; j < Q; ++j) S1[pi + PJ * j + PK * pkb] = o[j];
       } else {
@@ -675,7 +762,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         f2[k] = fma(m02, g0, fma(m12, g1, m22 * g2[k]));
         v[k] = lambda * jw * u[k];
       }
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         op_dert_add(f2, v);
       } else {
 #pragma unroll
@@ -709,8 +796,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q], o[Q];
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S0[a + PJ * pj + PK * pk];
-      if constexpr (PACK) {
-        contract2<Q, Q, QP, false>(DT, c, o);
+      if constexpr (PACK || EO) {
+        op_dert(c, o);
       } else {
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
@@ -725,8 +812,8 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       const int pi = t % Q, pkb = t / Q;
 #pragma unroll
       for (int a = 0; a < Q; ++a) c[a] = S1[pi + PJ * a + PK * pkb];
-      if constexpr (PACK) {
-        contract2<Q, Q, QP, false>(DT, c, o);
+      if constexpr (PACK || EO) {
+        op_dert(c, o);
       } else {
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
@@ -747,7 +834,7 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
         const int s = ci + PJ * cj + PK * k;
         v[k] += S0[s] + S1[s];
       }
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[N];
         op_ipr(v, o);
 #pragma unroll
@@ -781,9 +868,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q];
 #pragma unroll
       for (int j = 0; j < Q; ++j) c[j] = SU[i + PJ * j + PK * r];
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[N];
-        contract2<Q, N, NP, false>(BT, c, o);
+        op_ipr(c, o);
 #pragma unroll
         for (int q = 0; q < N; ++q) S0[i + PJ * q + PK * r] = o[q];
       } else {
@@ -813,9 +900,9 @@ __global__ void __launch_bounds__(Q* Q* EB) helm3_pipe_kernel(const T* __restric
       T c[Q];
 #pragma unroll
       for (int i = 0; i < Q; ++i) c[i] = S0[i + PJ * q + PK * r];
-      if constexpr (PACK) {
+      if constexpr (PACK || EO) {
         T o[N];
-        contract2<Q, N, NP, false>(BT, c, o);
+        op_ipr(c, o);
 #pragma unroll
         for (int p = 0; p < N; ++p) S1[p + PJ * q + PK * r] = o[p];
       } else {

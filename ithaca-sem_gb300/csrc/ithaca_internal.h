@@ -269,6 +269,7 @@ struct Op {
   // TMA-staged geometry slab, 21/22 (31/32) = persistent pipelined pencil kernel with a
   // double (single) geometry buffer (elem_pencil_pipe.cuh), 41/42 = 31/32 on packed pairs.
   int variant32 = 41;
+  int variant64 = 0;  // FP64 hex apply: 0 the shared-memory kernel, 1 / 2 the even-odd pencil kernel (1 / 2 elements)
   ~Op();
 };
 
@@ -300,6 +301,11 @@ template <typename T>
 bool launch_helm_pencil(int n, int Q, int E, int variant, const double* hB, const double* hD, const T* jg, T lambda,
                         const T* in, T* out, const int* l2g, int ndir, const int* skip, const T* lam_ptr, int* err,
                         cudaStream_t s, OwnedRows* own = nullptr);
+// FP64 hexes, persistent pipelined kernel with even-odd 1-D operators (Q even); variant 1 / 2
+// = one / two elements per group. False for other (n, Q).
+bool launch_helm_pencil64(int n, int Q, int E, int variant, const double* hB, const double* hD, const double* jg,
+                          double lambda, const double* in, double* out, const int* l2g, int ndir, const int* skip,
+                          const double* lam_ptr, int* err, cudaStream_t s);
 // Half-precision geometry (E x 7 x Q^3 halves) with 8 FP32 scales per element; FP32 hexes.
 bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
                             const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,

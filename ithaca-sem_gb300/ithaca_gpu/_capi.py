@@ -76,6 +76,7 @@ SIGNATURES = {
     "ithaca_gpu_helmholtz": [_vp, _d, _vp, _vp, _i],
     "ithaca_gpu_helmholtz_diag": [_vp, _d, _vp, _i],
     "ithaca_gpu_op_set_variant": [_vp, _i],
+    "ithaca_gpu_op_set_variant64": [_vp, _i],
     "ithaca_gpu_op_autotune": [_vp, _i, ctypes.POINTER(ctypes.c_int), _vp],
     "ithaca_gpu_cg_create": [_vp, _vp, _vp, _i, _i, _pp],
     "ithaca_gpu_cg_destroy": [_vp],

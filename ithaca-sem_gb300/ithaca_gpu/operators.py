@@ -271,6 +271,11 @@ class Collection:
         operators in even-odd form."""
         C.call("ithaca_gpu_op_set_variant", self.handle, int(variant))
 
+    def set_variant64(self, variant):
+        """FP64 hex Helmholtz kernel: 0 shared-memory (default), 1 / 2 persistent pipelined
+        pencils with even-odd 1-D operators, one / two elements per group (Q even)."""
+        C.call("ithaca_gpu_op_set_variant64", self.handle, int(variant))
+
     def autotune(self, reps=10):
         """Times each kernel variant on this collection and keeps the fastest."""
         chosen = ctypes.c_int()
@@ -429,6 +434,17 @@ class GlobalLinSysIterativeFullGPU:
             times[v] = self.profile_apply(lam, mode="mixed", reps=reps)[0]
         best = min(times, key=times.get)
         self.coll.set_variant(best)
+        return best, times
+
+    def autotune_fp64(self, lam=1.0, variants=(0, 1, 2), reps=10):
+        """Times the gathered FP64 apply (the FP64 solve's and the outer residual's) with each
+        FP64 hex kernel variant and keeps the fastest. Returns (chosen variant, {variant: ms})."""
+        times = {}
+        for v in variants:
+            self.coll.set_variant64(v)
+            times[v] = self.profile_apply(lam, mode="fp64", reps=reps)[0]
+        best = min(times, key=times.get)
+        self.coll.set_variant64(best)
         return best, times
 
     def diagonal(self, lam, out=None):

@@ -148,6 +148,27 @@ def test_mixed_vector_pencils_q8(ctx, variant):
     assert rel_err(x[amap.ndir:], xr[amap.ndir:]) < 1e-9
 
 
+@pytest.mark.parametrize("variant", [1, 2])
+def test_fp64_cg_even_odd_kernel(ctx, variant):
+    """FP64 and mixed solves with the FP64 even-odd pencil kernel (P = 6) against the same
+    solves with the shared-memory kernel: the same iterations within 1%, the same solution;
+    the variant set after a solve reaches the captured iteration graphs."""
+    c = hex_case(4, 3, 3, 7, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(31).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x0, r0 = sys_.solve(1.0, rhs, tol=1e-12)
+    coll.set_variant64(variant)
+    x1, r1 = sys_.solve(1.0, rhs, tol=1e-12)
+    # about 1300 iterations to 1e-12: the count moves by a few with the rounding order
+    assert abs(r1.iterations - r0.iterations) <= max(2, r0.iterations // 100), (r1.iterations, r0.iterations)
+    assert rel_err(x1[amap.ndir:], x0[amap.ndir:]) < 1e-10
+    x2, r2 = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert r2.rel_residual < 1e-10
+    assert rel_err(x2[amap.ndir:], x0[amap.ndir:]) < 1e-8
+    coll.set_variant64(0)
+
+
 def _merged_map(amap):
     """The map with a few free global dofs merged: three interior vertices into one row
     of 24 local entries (longer than the ELL classes), a face dof into an edge dof (6

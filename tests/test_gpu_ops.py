@@ -206,6 +206,19 @@ def test_hex_tensor_core_and_even_odd_stages_fp32_accuracy(ctx):
         assert rel_err(outs[v], outs[43]) < 5e-6, v
 
 
+@pytest.mark.parametrize("n", [3, 4, 5, 7, 9])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_hex_fp64_even_odd_kernel(ctx, n, variant):
+    """The FP64 pipelined kernel with even-odd 1-D operators (Q even; Q odd keeps the
+    shared-memory kernel) against the FP64 oracle; E = 7 leaves a partial last group."""
+    c = hex_case(7, 1, 1, n)
+    coll = _coll(ctx, c, "fp64")
+    coll.set_variant64(variant)
+    u = np.random.default_rng(90 + n).uniform(-1, 1, c.E * c.nm)
+    ref = oops.helmholtz(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 0.7, u)
+    assert rel_err(coll.helmholtz(0.7, u), ref) < TOL64
+
+
 def test_autotune_picks_a_working_variant(ctx):
     c = hex_case(4, 4, 2, 7)
     coll = _coll(ctx, c, "fp32")
