@@ -5,7 +5,9 @@ cube curved by x_a + 0.05 sin(2 pi x_b) sin(2 pi x_c) (cyclic), per-quadrature-p
 Jacobians, ModifiedA P = 6 (7 modes, 8 GLL points per direction), forcing
 f = sin(pi x) sin(pi y) sin(pi z), homogeneous Dirichlet boundary. A step is one
 Jacobi-preconditioned CG solve of the assembled C0 system to an FP64 relative residual
-||b - A x||_2 / ||b||_2 < 1e-10, FP32 inner solves inside FP64 iterative refinement.
+||b - A x||_2 / ||b||_2 < 1e-10, FP32 inner solves inside FP64 iterative refinement (the
+inner operator's geometry stored as halves with per-element scales, --mixed-mode mixed_geo16;
+the FP32-geometry inner solve is measured beside it).
 Inputs are synthetic and seeded; no dataset is involved.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--order P] [--mesh M] [--full 0|1]
@@ -143,12 +145,46 @@ def fp32_kernel_name(variant, n, Q):
             + (",packed>" if variant // 10 == 4 else ">"))
 
 
+def geo16_kernel_name(variant, n, Q):
+    """Name of the FP32 hex Helmholtz kernel on 16-bit geometry for an autotuner variant."""
+    if Q == 8 and variant in (43, 47):
+        return f"helm3_pipe_kernel<float,{n},{Q},2,gather,1,half,packed,vec4" + (",evenodd>" if variant == 47 else ">")
+    return f"helm3_pipe_kernel<float,{n},{Q},1,gather,1,half,packed>"
+
+
+# FP32 kernel variants with a 16-bit-geometry form (any other variant runs the packed one, 42).
+GEO16_VARIANTS = (42, 43, 47)
+
+
 # DRAM bytes (read + write) per element of one gathered FP32 apply as the inner iteration
 # launches it (scattered output: owned rows and assembly-ordered slots), from an ncu
 # capture of the kernel on 28^3 hexes (variant 42: 394.1 MB read + 5.4 MB written per
-# launch over 21,952 elements; variants 43 and 47: 394.1 + 5.5 MB); a launch's traffic grows
-# with the number of elements, so the bench scales it by E. Keys: (kernel variant, modes, points).
-TRAFFIC_PER_ELEMENT = {(42, 7, 8): 18200, (43, 7, 8): 18204, (47, 7, 8): 18204}
+# launch over 21,952 elements; variants 43 and 47: 394.1 + 5.5 MB; variant 47 on 16-bit
+# geometry: 237.3 + 5.2 MB); a launch's traffic grows with the number of elements, so the
+# bench scales it by E. Keys: (mixed mode, kernel variant, modes, points).
+TRAFFIC_PER_ELEMENT = {("mixed", 42, 7, 8): 18200, ("mixed", 43, 7, 8): 18204, ("mixed", 47, 7, 8): 18204,
+                       ("mixed_geo16", 47, 7, 8): 11044}
+
+
+def inner_roofline(mode, variant, n, Q, E, ms, nbytes, peak, peak_kind):
+    """Roofline entry of the inner FP32 gathered apply: algorithmic bytes per launch over its
+    CUDA-event time, against the measured copy bandwidth; DRAM traffic from the ncu
+    capture of the same kernel where one exists."""
+    achieved = nbytes / (ms / 1e3) / 1e9
+    key = (mode, variant, n, Q)
+    half = mode == "mixed_geo16"
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": TRAFFIC_PER_ELEMENT[key] * E if key in TRAFFIC_PER_ELEMENT else None,
+            "kernel": (geo16_kernel_name(variant, n, Q) if half else fp32_kernel_name(variant, n, Q))
+                      + " gather (inner FP32 apply)",
+            "kernel_ms": ms, "bytes_per_launch": nbytes, "mixed_mode": mode,
+            "bytes_rule": ("per element 4 (2 n^3) + 2 (7 Q^3) + 32 + 4 n^3: FP32 coefficients in and out, J w "
+                           "and the six metric terms per point as halves with 8 FP32 scales, the signed index "
+                           "per local dof" if half else
+                           "per element 4 (2 n^3 + 7 Q^3) + 4 n^3: FP32 coefficients in and out, J w and the "
+                           "six metric terms per point, the signed index per local dof"),
+            "layout_overhead_bytes_per_launch": 4.0 * E * n ** 3,
+            "peak_source": peak_kind}
 
 
 def workload_config(args, n, Q, E, N, ndir):
@@ -665,7 +701,9 @@ def run_gpu(args, rank, world):
         variant, variant_ms = args.variant, {}
         sysg.coll.set_variant(variant)
     else:
-        variant, variant_ms = sysg.autotune_inner(LAMBDA, reps=10)
+        variant, variant_ms = sysg.autotune_inner(
+            LAMBDA, reps=10, mode=args.mixed_mode,
+            **({"variants": GEO16_VARIANTS} if args.mixed_mode == "mixed_geo16" else {}))
     coll32.set_variant(variant)
     # the FP64 apply's kernel (FP64 solves, outer residuals of the mixed solve), by timing
     variant64, variant64_ms = sysg.autotune_fp64(LAMBDA, reps=5)
@@ -716,7 +754,8 @@ def run_gpu(args, rank, world):
     # ---- dominant kernel: the FP32 gather + element Helmholtz of the inner solve ----
     k_ms, k_bytes = sysg.profile_apply(LAMBDA, mode=mode, reps=20)
     peak, peak_kind = load_peaks()
-    achieved = k_bytes / (k_ms / 1e3) / 1e9
+    # the other mode's inner apply (same variant), for its own roofline beside the headline's
+    ko_ms, ko_bytes = sysg.profile_apply(LAMBDA, mode=other, reps=20)
 
     # ---- FP64 reference recurrence on the GPU ----
     sysg.solve(LAMBDA, b, x, tol=TOL, mode="fp64")
@@ -784,16 +823,8 @@ def run_gpu(args, rank, world):
                  "apply_ms": k64_ms, "apply_fp64_tflops": None},
         "helmholtz_gdofs": {"fp64": gdofs64, "fp32": gdofs32},
         "solver_gdofs": {"mixed": value / world * (N - ndir) / 1e9, "fp64": fp64_solves * (N - ndir) / 1e9},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (TRAFFIC_PER_ELEMENT[(variant, n, Q)] * E
-                                 if mode == "mixed" and (variant, n, Q) in TRAFFIC_PER_ELEMENT else None),
-                     "kernel": (f"helm3_pipe_kernel<float,{n},{Q},1,gather,1,half,packed>" if mode == "mixed_geo16"
-                                else fp32_kernel_name(variant, n, Q)) + " gather (inner FP32 apply)",
-                     "kernel_ms": k_ms, "bytes_per_launch": k_bytes,
-                     "bytes_rule": "per element 4 (2 n^3 + 7 Q^3) + 4 n^3: FP32 coefficients in and out, J w and the "
-                                   "six metric terms per point, the signed index per local dof",
-                     "layout_overhead_bytes_per_launch": 4.0 * E * n ** 3,
-                     "peak_source": peak_kind},
+        "roofline": inner_roofline(mode, variant, n, Q, E, k_ms, k_bytes, peak, peak_kind),
+        "roofline_other_mixed_mode": inner_roofline(other, variant, n, Q, E, ko_ms, ko_bytes, peak, peak_kind),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_host.nbytes),
                 "d2h_bytes_per_step": int(out_host.nbytes), "rel_residual": rese.rel_residual},
         "gpu_launches": launches_total,
@@ -1192,19 +1223,22 @@ def suite_inner_apply(args):
     w = hex_workload(args.mesh, args.order)
     sysg, E, n, Q = w["system"], w["mesh"].E, w["n"], w["Q"]
     tuned = {}
+    mode = args.mixed_mode
     if args.variant < 0:
-        variant, tuned = sysg.autotune_inner(LAMBDA, reps=max(3, args.steps))
+        variant, tuned = sysg.autotune_inner(LAMBDA, reps=max(3, args.steps), mode=mode,
+                                             **({"variants": GEO16_VARIANTS} if mode == "mixed_geo16" else {}))
     else:
         variant = args.variant
         w["coll"].set_variant(variant)
-    ms32, by32 = sysg.profile_apply(LAMBDA, mode="mixed", reps=args.steps)
+    ms32, by32 = sysg.profile_apply(LAMBDA, mode=mode, reps=args.steps)
     ms64, by64 = sysg.profile_apply(LAMBDA, mode="fp64", reps=args.steps)
     peak, kind = load_peaks()
     cfg = {"workload": f"gathered element Helmholtz applies of the solver, {args.mesh}^3 curved hexes, P={args.order}",
-           "elements": E, "fp32_kernel_variant": variant,
+           "elements": E, "fp32_kernel_variant": variant, "mixed_mode": mode,
            "autotune_ms": {str(v): round(t, 4) for v, t in tuned.items()}}
     _line("inner FP32 gathered apply: algorithmic GB/s", by32 / (ms32 / 1e3) / 1e9, "GB/s", args, cfg, dtype="f32",
-          fp32={"kernel": fp32_kernel_name(variant, n, Q), "ms": ms32, "bytes": by32,
+          fp32={"kernel": geo16_kernel_name(variant, n, Q) if mode == "mixed_geo16" else fp32_kernel_name(variant, n, Q),
+                "ms": ms32, "bytes": by32,
                 "frac_of_hbm": by32 / (ms32 / 1e3) / 1e9 / peak, "peak_source": kind},
           fp64={"ms": ms64, "bytes": by64, "gbs": by64 / (ms64 / 1e3) / 1e9})
 
@@ -1269,8 +1303,9 @@ def main():
     ap.add_argument("--order", type=int, default=6)
     ap.add_argument("--mesh", type=int, default=None,
                     help="cells per direction (default: 32 hex, 128 tri, 12 tet / prism, 10 pyr)")
-    ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed",
-                    help="inner solve of the headline: FP32 on FP32 geometry, or FP32 on 16-bit geometry")
+    ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed_geo16",
+                    help="inner solve of the headline: FP32 arithmetic on 16-bit geometry storage (default, the "
+                         "faster), or on FP32 geometry (reported beside it in either case)")
     ap.add_argument("--variant", type=int, default=-1,
                     help="FP32 hex kernel variant of the inner apply (-1: autotune; the headline and inner_apply)")
     ap.add_argument("--full", type=int, default=1,

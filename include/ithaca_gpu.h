@@ -191,7 +191,9 @@ int ithaca_gpu_helmholtz(ithaca_gpu_op* op, double lambda, const void* in, void*
  * i and j as TF32 tensor-core MMAs in three-term split precision (FP32-level accuracy, not
  * bit-identical), 47 = 43 with every 1-D operator in its even-odd form (the symmetry of
  * the GLL points and the parity of the modes: half the multiply-adds; FP32-level accuracy,
- * not bit-identical); 43, 44, 46 and 47 are built for Q = 8, other orders run 42 or 41.
+ * not bit-identical); 43, 44, 46 and 47 are built for Q = 8, other orders run 42 or 41. On
+ * 16-bit geometry (ITHACA_GPU_SOLVE_MIXED_FP32_GEO16) 43 and 47 have their own forms at
+ * Q = 8 and every other variant runs the packed-pair kernel with one element per group.
  * Inside the mixed solver the pipelined variants (21-47) also write the rows of
  * the global system that have a single local entry themselves, so the assembly that
  * follows skips them. */

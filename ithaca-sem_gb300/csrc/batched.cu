@@ -185,12 +185,15 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
     if (sc[ch.solve].done) continue;  // converged solve: no work, no partials
     T sw = 0;  // per-thread s.w in T, CTA sum in FP64
     if (!sc[ch.solve].done) {
-      // U rows per thread step; each row's entries summed in CSR order, the first
-      // entries of the U rows (and w) loaded together
-      constexpr int U = 4;
+      // U rows per thread step (2 in FP64), each row's entries summed in CSR order. The first K
+      // entries of every row (a quad-mesh vertex has 4, an edge mode 2, an interior
+      // mode 1) are loaded without a loop: all column indices of the U rows in flight
+      // together, then all their values, so a row costs three dependent loads (rowptr,
+      // cols, yloc) rather than two per entry. Longer rows finish in a loop.
+      constexpr int U = sizeof(T) == 8 ? 2 : 4, K = 4;
       for (int g0 = ch.begin + threadIdx.x; g0 < ch.end; g0 += U * BT) {
-        int a[U], b[U];
-        T wv[U], acc[U];
+        int a[U], b[U], cc[U][K];
+        T wv[U], acc[U], val[U][K];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int g = g0 + u * BT;
@@ -200,18 +203,28 @@ __global__ void __launch_bounds__(BT) bassemble_kernel(const Chunk* __restrict__
           wv[u] = in ? w[g] : T(0);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          acc[u] = 0;
-          if (a[u] < b[u]) {
-            const int cc = cols[a[u]];
-            acc[u] = cc >= 0 ? yloc[cc] : -yloc[~cc];
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int j = 0; j < K; ++j) cc[u][j] = a[u] + j < b[u] ? cols[a[u] + j] : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int j = 0; j < K; ++j) {
+            const int c = cc[u][j];
+            val[u][j] = a[u] + j < b[u] ? (c >= 0 ? yloc[c] : -yloc[~c]) : T(0);
           }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          acc[u] = val[u][0];
+#pragma unroll
+          for (int j = 1; j < K; ++j)
+            if (a[u] + j < b[u]) acc[u] += val[u][j];
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
-          for (int j = a[u] + 1; j < b[u]; ++j) {
-            const int cc = cols[j];
-            acc[u] += cc >= 0 ? yloc[cc] : -yloc[~cc];
+          for (int j = a[u] + K; j < b[u]; ++j) {
+            const int c = cols[j];
+            acc[u] += c >= 0 ? yloc[c] : -yloc[~c];
           }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -339,10 +352,23 @@ __global__ void __launch_bounds__(BT) bresidual_kernel(const Chunk* __restrict__
     if (skip_done && sc[ch.solve].outer_done) continue;
     double v[2] = {0, 0};
     for (int g = ch.begin + threadIdx.x; g < ch.end; g += BT) {
+      // the first K entries' indices, then their values, in flight together (as in
+      // bassemble_kernel); summed in CSR order
+      constexpr int K = 4;
+      const int a0 = rowptr[g], a1 = rowptr[g + 1];
+      int cc[K];
+      double val[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) cc[j] = a0 + j < a1 ? cols[a0 + j] : 0;
+#pragma unroll
+      for (int j = 0; j < K; ++j) val[j] = a0 + j < a1 ? (cc[j] >= 0 ? yloc[cc[j]] : -yloc[~cc[j]]) : 0.0;
       double acc = 0;
-      for (int j = rowptr[g]; j < rowptr[g + 1]; ++j) {
-        const int cc = cols[j];
-        acc += cc >= 0 ? yloc[cc] : -yloc[~cc];
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+        if (a0 + j < a1) acc += val[j];
+      for (int j = a0 + K; j < a1; ++j) {
+        const int c2 = cols[j];
+        acc += c2 >= 0 ? yloc[c2] : -yloc[~c2];
       }
       const double rg = b[g] - acc;
       r[g] = rg;

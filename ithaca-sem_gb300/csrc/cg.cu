@@ -748,7 +748,7 @@ static void launch_apply(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, T lambda
     const int* map = cg->l2g;
     if (own != nullptr) own->ocode = cg->ocode;
     if (cg->geo16)
-      ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
+      ok = launch_helm_pipe_geo16(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), cg->jg16, cg->jgs, lambda, xin,
                                   v.yloc, map, zero_dir ? cg->ndir : 0, skip, lam_ptr, op->ctx->derr, s, own);
     else if (op->kdim == 3 && op->deformed && op->variant32 > 0)
       ok = launch_helm_pencil<float>(op->n, op->Q, op->E, op->variant32, op->hB.data(), op->hD.data(), jg, lambda,

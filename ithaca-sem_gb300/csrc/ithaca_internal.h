@@ -307,7 +307,9 @@ bool launch_helm_pencil64(int n, int Q, int E, int variant, const double* hB, co
                           double lambda, const double* in, double* out, const int* l2g, int ndir, const int* skip,
                           const double* lam_ptr, int* err, cudaStream_t s);
 // Half-precision geometry (E x 7 x Q^3 halves) with 8 FP32 scales per element; FP32 hexes.
-bool launch_helm_pipe_geo16(int n, int Q, int E, const double* hB, const double* hD, const void* jg16,
+// variant: the FP32 kernel variant of the operator (43 and 47 have half-geometry forms at
+// (n, Q) = (7, 8); any other value runs the packed-pair kernel).
+bool launch_helm_pipe_geo16(int n, int Q, int E, int variant, const double* hB, const double* hD, const void* jg16,
                             const float* gscale, float lambda, const float* in, float* out, const int* l2g, int ndir,
                             const int* skip, const float* lam_ptr, int* err, cudaStream_t s,
                             OwnedRows* own = nullptr);

@@ -423,15 +423,18 @@ class GlobalLinSysIterativeFullGPU:
                ctypes.byref(ms), ctypes.byref(nbytes))
         return ms.value, nbytes.value
 
-    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47), reps=10):
+    def autotune_inner(self, lam=1.0, variants=(0, 2, 4, 21, 22, 31, 32, 41, 42, 43, 44, 46, 47), reps=10,
+                       mode="mixed"):
         """Times the gathered FP32 apply of the mixed solver's inner iteration with each
         FP32 kernel variant of the collection and keeps the fastest (the solver-side
-        counterpart of Collection.autotune, which times the ungathered apply).
+        counterpart of Collection.autotune, which times the ungathered apply). mode
+        "mixed_geo16" times the applies on 16-bit geometry (variants 43 and 47 have their
+        own forms at Q = 8; the others run the packed-pair kernel).
         Returns (chosen variant, {variant: ms})."""
         times = {}
         for v in variants:
             self.coll.set_variant(v)
-            times[v] = self.profile_apply(lam, mode="mixed", reps=reps)[0]
+            times[v] = self.profile_apply(lam, mode=mode, reps=reps)[0]
         best = min(times, key=times.get)
         self.coll.set_variant(best)
         return best, times

@@ -229,6 +229,32 @@ def test_mixed_geo16_curved_hex(ctx, inner_tol):
     assert ms > 0 and nbytes > 0
 
 
+@pytest.mark.parametrize("variant", [43, 47])
+def test_mixed_geo16_vector_pencils_q8(ctx, variant):
+    """Half-precision geometry under the vector-pencil kernels (Q = 8, two elements per
+    group; 27 elements, so the last group holds one): the FP64 residual is reached, the
+    solution equals the FP64 solve's, and the inner iterations match the packed-pair
+    half-geometry kernel's (within one for 43, whose arithmetic is the same; within 10%
+    for the even-odd operators of 47, whose rounding differs)."""
+    c = hex_case(3, 3, 3, 7, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(31).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, _ = sys_.solve(1.0, rhs, tol=1e-12)
+    coll.set_variant(42)
+    xr, ref = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed_geo16")
+    coll.set_variant(variant)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed_geo16")
+    assert res.rel_residual < 1e-10
+    assert rel_err(x[amap.ndir:], x64[amap.ndir:]) < 1e-8
+    slack = max(4, ref.iterations // 10) if variant == 47 else 1
+    assert abs(res.iterations - ref.iterations) <= slack, (res.iterations, ref.iterations)
+    if variant == 43:
+        assert rel_err(x[amap.ndir:], xr[amap.ndir:]) < 1e-9
+    ms, nbytes = sys_.profile_apply(1.0, mode="mixed_geo16", reps=2)
+    assert ms > 0 and nbytes > 0
+
+
 def test_mixed_geo16_rejects_quads(ctx):
     from ithaca_gpu._capi import ERR_UNSUPPORTED, GpuError
     c = quad_case(4, 4, 5)
