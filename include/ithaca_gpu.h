@@ -305,6 +305,29 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
                                    double* out_local, const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res,
                                    int on_device);
 
+/* ---- the ROM solvers' HelmSolve callers ----
+ * VelocityCorrectionScheme_ROM::v_SolveViscous
+ * (solvers/IncNavierStokesSolver/EquationSystems/VelocityCorrectionScheme_ROM.cpp:1538-1567):
+ * for each of the nfields velocity fields (which share one expansion, so one system `cg`),
+ * lambda = 1 / aii_dt / diff_coeff[i], HelmSolve of forcing[i] (E*Q^d values at the
+ * quadrature points) with the field's Dirichlet data dirichlet[i] (ndir global coefficients,
+ * NULL for homogeneous data; dirichlet == NULL for all fields homogeneous) into coeffs[i]
+ * (E*n^d local coefficients), then BwdTrans into phys[i] (E*Q^d; phys == NULL or phys[i] ==
+ * NULL skips it). res (NULL or nfields entries) gets each solve's result. The fields are
+ * solved in order on the context stream; the first failing one stops the call and its status
+ * is returned. Spectral vanishing viscosity (AppendSVVFactors) is not supported. */
+int ithaca_gpu_vcs_solve_viscous(ithaca_gpu_cg* cg, int nfields, const double* const* forcing,
+                                 const double* const* dirichlet, double aii_dt, const double* diff_coeff,
+                                 double* const* coeffs, double* const* phys, const ithaca_gpu_cg_opts* opts,
+                                 ithaca_gpu_cg_result* res, int on_device);
+/* VelocityCorrectionScheme_ROM::v_SolvePressure (:1522-1534): the pressure Poisson equation,
+ * HelmSolve with lambda = 0, forcing at the quadrature points -> local coefficients of the
+ * pressure expansion's system. The system needs Dirichlet dofs (ITHACA_GPU_ERR_ARG
+ * otherwise: without them the Poisson operator is singular). */
+int ithaca_gpu_vcs_solve_pressure(ithaca_gpu_cg* cg, const double* forcing, const double* dirichlet,
+                                  double* coeffs, const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res,
+                                  int on_device);
+
 /* ---- batched parametric solves ----
  * Many independent C0 Helmholtz systems (own mesh, order, lambda, rhs; homogeneous
  * Dirichlet data) solved together: the parameter loop that produces the snapshots of

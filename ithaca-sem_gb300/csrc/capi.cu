@@ -12,6 +12,7 @@ namespace ithaca {
 static thread_local std::string g_last_error;
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+const std::string& last_error_text() { return g_last_error; }
 
 void fail(int code, const std::string& msg) { throw Error{code, msg}; }
 

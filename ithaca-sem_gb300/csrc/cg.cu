@@ -513,10 +513,10 @@ __global__ void __launch_bounds__(RT) axpy_f32_kernel(int N, int ndir, const dou
   for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) x[g] += sc * (double)d32[g];
 }
 
-// b[g] -= y[g] on the free dofs g >= ndir.
-__global__ void __launch_bounds__(RT) sub_free_kernel(int N, int ndir, const double* __restrict__ y,
+// b[g] -= y[g] for g in [first, N).
+__global__ void __launch_bounds__(RT) sub_rows_kernel(int N, int first, const double* __restrict__ y,
                                                       double* __restrict__ b) {
-  for (int g = ndir + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) b[g] -= y[g];
+  for (int g = first + blockIdx.x * RT + threadIdx.x; g < N; g += gridDim.x * RT) b[g] -= y[g];
 }
 
 __global__ void __launch_bounds__(RT) inv_kernel(int n, const double* __restrict__ d, double* __restrict__ dinv,
@@ -1680,7 +1680,10 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
       launch_apply<double>(cg, cg->v64, op->t64.base, geo64(cg), lambda, nullptr, xd, s, false, nullptr);
       assemble_dot_kernel<double><<<cg->rba, RT, 0, s>>>(cg->plan, false, cg->asm_rows, cg->asm_cols, cg->rowptr,
                                                     cg->cols, cg->v64.yloc, cg->v64.s, nullptr, nullptr, nullptr);
-      sub_free_kernel<<<RB, RT, 0, s>>>(cg->N, cg->ndir, cg->v64.s, cg->v64.b);
+      // every row, the Dirichlet ones included: the reference assembles the lifted local
+      // rhs (GlobalLinSysIterativeFull.cpp:182-186) and its CG takes ||b||^2 over the whole
+      // assembled vector (NekLinSysIter.cpp:128-142); the solve reads only the free rows
+      sub_rows_kernel<<<RB, RT, 0, s>>>(cg->N, 0, cg->v64.s, cg->v64.b);
       c->launches += 2;
       double* keep = (double*)c->stage_ptr(2, sizeof(double) * cg->ndir);  // the solve reuses v64.p
       ITHACA_CUDA(cudaMemcpyAsync(keep, xd, sizeof(double) * cg->ndir, cudaMemcpyDeviceToDevice, s));
@@ -1698,6 +1701,46 @@ int ithaca_gpu_helmsolve_dirichlet(ithaca_gpu_cg* cg, double lambda, const doubl
     if (!on_device) ITHACA_CUDA(cudaMemcpyAsync(out_local, dout, sizeof(double) * nloc, cudaMemcpyDeviceToHost, s));
     ITHACA_CUDA(cudaGetLastError());
     ITHACA_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+// VelocityCorrectionScheme_ROM::v_SolveViscous: per field, lambda = 1 / aii_dt / diff_coeff,
+// HelmSolve into the field's coefficients, BwdTrans into its physical values.
+int ithaca_gpu_vcs_solve_viscous(ithaca_gpu_cg* cg, int nfields, const double* const* forcing,
+                                 const double* const* dirichlet, double aii_dt, const double* diff_coeff,
+                                 double* const* coeffs, double* const* phys, const ithaca_gpu_cg_opts* opts,
+                                 ithaca_gpu_cg_result* res, int on_device) {
+  return cg_guarded([&] {
+    req(cg && forcing && coeffs && diff_coeff, "null argument");
+    req(nfields > 0, "nfields must be positive");
+    req(aii_dt > 0 && std::isfinite(aii_dt), "aii_dt must be positive and finite");
+    for (int i = 0; i < nfields; ++i) {
+      req(forcing[i] != nullptr && coeffs[i] != nullptr, "null field pointer");
+      req(diff_coeff[i] > 0 && std::isfinite(diff_coeff[i]), "diffusion coefficients must be positive and finite");
+    }
+    for (int i = 0; i < nfields; ++i) {
+      const double lambda = 1.0 / aii_dt / diff_coeff[i];
+      int rc = ithaca_gpu_helmsolve_dirichlet(cg, lambda, forcing[i], dirichlet ? dirichlet[i] : nullptr, coeffs[i],
+                                              opts, res ? res + i : nullptr, on_device);
+      if (rc != ITHACA_GPU_OK) fail(rc, "field " + std::to_string(i) + ": " + last_error_text());
+      if (phys != nullptr && phys[i] != nullptr) {
+        rc = ithaca_gpu_bwdtrans(reinterpret_cast<ithaca_gpu_op*>(cg->op), coeffs[i], phys[i], on_device);
+        if (rc != ITHACA_GPU_OK) fail(rc, "field " + std::to_string(i) + ": " + last_error_text());
+      }
+    }
+  });
+}
+
+// VelocityCorrectionScheme_ROM::v_SolvePressure: the pressure Poisson equation, HelmSolve
+// with lambda = 0.
+int ithaca_gpu_vcs_solve_pressure(ithaca_gpu_cg* cg, const double* forcing, const double* dirichlet,
+                                  double* coeffs, const ithaca_gpu_cg_opts* opts, ithaca_gpu_cg_result* res,
+                                  int on_device) {
+  return cg_guarded([&] {
+    req(cg && forcing && coeffs, "null argument");
+    req(cg->ndir > 0, "the pressure system needs Dirichlet dofs (a pure-Neumann Poisson system is singular)");
+    const int rc = ithaca_gpu_helmsolve_dirichlet(cg, 0.0, forcing, dirichlet, coeffs, opts, res, on_device);
+    if (rc != ITHACA_GPU_OK) fail(rc, last_error_text());
   });
 }
 

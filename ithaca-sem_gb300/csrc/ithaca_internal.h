@@ -20,6 +20,7 @@ struct Error {
   std::string msg;
 };
 void set_last_error(const std::string& msg);
+const std::string& last_error_text();  // this thread's last error message
 [[noreturn]] void fail(int code, const std::string& msg);
 void check_cuda(cudaError_t e, const char* what);
 #define ITHACA_CUDA(x) ::ithaca::check_cuda((x), #x)

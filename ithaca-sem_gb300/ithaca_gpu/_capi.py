@@ -91,6 +91,9 @@ SIGNATURES = {
     "ithaca_gpu_cg_global_to_local": [_vp, _vp, _vp, _i],
     "ithaca_gpu_helmsolve": [_vp, _d, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_helmsolve_dirichlet": [_vp, _d, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_vcs_solve_viscous": [_vp, _i, _pp, _pp, _d, _vp, _pp, _pp, ctypes.POINTER(CgOpts),
+                                     ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_vcs_solve_pressure": [_vp, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_sc_create": [_vp, _vp, _vp, _i, _i, _pp],
     "ithaca_gpu_sc_destroy": [_vp],
     "ithaca_gpu_sc_info": [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),

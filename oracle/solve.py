@@ -117,6 +117,29 @@ def helmsolve(basis, dim, jac, df, lam, amap, forcing, tol=1e-9, max_iter=5000, 
     return m.gather(x), it
 
 
+def solve_viscous(basis, dim, jac, df, amap, forcing, aii_dt, diff_coeff, dirichlet=None, tol=1e-9,
+                  max_iter=5000):
+    """VelocityCorrectionScheme_ROM::v_SolveViscous (solvers/IncNavierStokesSolver/
+    EquationSystems/VelocityCorrectionScheme_ROM.cpp:1538-1567): per velocity field,
+    lambda = 1 / aii_dt / diff_coeff[i], HelmSolve of forcing[i], then BwdTrans.
+    Returns ([local coefficients], [physical values], [iterations])."""
+    coeffs, phys, its = [], [], []
+    for i, f in enumerate(forcing):
+        lam = 1.0 / aii_dt / diff_coeff[i]
+        d = None if dirichlet is None else dirichlet[i]
+        c, it = helmsolve(basis, dim, jac, df, lam, amap, f, tol, max_iter, dirichlet=d)
+        coeffs.append(c)
+        phys.append(ops.bwdtrans(basis, dim, c).reshape(-1))
+        its.append(it)
+    return coeffs, phys, its
+
+
+def solve_pressure(basis, dim, jac, df, amap, forcing, dirichlet=None, tol=1e-9, max_iter=5000):
+    """VelocityCorrectionScheme_ROM::v_SolvePressure (:1522-1534): HelmSolve with
+    lambda = 0 (the pressure Poisson equation). Returns (local coefficients, iterations)."""
+    return helmsolve(basis, dim, jac, df, 0.0, amap, forcing, tol, max_iter, dirichlet=dirichlet)
+
+
 # ---------------------------------------------------------------------------------
 # Successive right-hand sides: projection onto previous solutions (Fischer 1998), as
 # GlobalLinSysIterative::DoProjection / UpdateKnownSolutions / ResetKnownSolutionsToLatestOne
