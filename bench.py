@@ -693,6 +693,7 @@ def run_gpu(args, rank, world):
     coll = Collection(ctx, "hex", n, Q, E, jac, df, deformed=True, precision="fp64")
     coll32 = Collection(ctx, "hex", n, Q, E, jac, df, deformed=True, precision="fp32")
     sysg = GlobalLinSysIterativeFullGPU(coll, amap)
+    sysg.set_fused_update(args.fused_update)
     stream = torch.cuda.ExternalStream(ctx.stream, device=cuda)
     # pick the FP32 element-kernel variant by timing the solver's own gathered inner
     # apply (CollectionOptimisation analogue), unless --variant names one (kernel captures,
@@ -804,6 +805,7 @@ def run_gpu(args, rank, world):
     x64_h = x64_gpu.cpu().numpy()
     cfg = workload_config(args, n, Q, E, N, ndir)
     cfg["fp32_kernel_variant"] = variant
+    cfg["fused_update"] = bool(args.fused_update)
     cfg["autotune_ms"] = {str(k): round(v, 4) for k, v in variant_ms.items()}
     cfg["fp64_kernel_variant"] = variant64
     cfg["autotune_fp64_ms"] = {str(k): round(v, 4) for k, v in variant64_ms.items()}
@@ -1306,6 +1308,9 @@ def main():
     ap.add_argument("--mixed-mode", choices=["mixed", "mixed_geo16"], default="mixed_geo16",
                     help="inner solve of the headline: FP32 arithmetic on 16-bit geometry storage (default, the "
                          "faster), or on FP32 geometry (reported beside it in either case)")
+    ap.add_argument("--fused-update", type=int, default=0, choices=[0, 1],
+                    help="1: the inner FP32 iterations fuse the assembly with the vector update; "
+                         "0: separate assembly and update kernels (default, measured faster)")
     ap.add_argument("--variant", type=int, default=-1,
                     help="FP32 hex kernel variant of the inner apply (-1: autotune; the headline and inner_apply)")
     ap.add_argument("--full", type=int, default=1,

@@ -232,6 +232,15 @@ int ithaca_gpu_cg_destroy(ithaca_gpu_cg* cg);
  * graph-captured kernels. 1: always the persistent solver for 2-D systems. Both paths run
  * the same recurrence (NekLinSysIterCG.cpp:104-263); 3-D systems always use the graph. */
 int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode);
+/* FP32 inner iterations of the mixed solve (no reference counterpart): 1 fuses the
+ * assembly of the element kernel's scattered output with the vector update of the same
+ * iteration (two launches per iteration: the update computes the iteration's scalars
+ * itself), 0 (default: measured faster on the 32^3 hexes) keeps the separate assembly and
+ * update (three launches). The fused form needs
+ * a pipelined FP32 element kernel (hexahedra, variants 21-47, or 16-bit geometry); with
+ * other kernels the separate form runs. Same recurrence; the partial sums are grouped
+ * differently, so iteration counts can differ by a few. */
+int ithaca_gpu_cg_set_fused_update(ithaca_gpu_cg* cg, int on);
 
 /* Successive right-hand sides: projection onto previous solutions (P. F. Fischer,
  * Comput. Methods Appl. Mech. Engrg. 163, 1998), as GlobalLinSysIterative::DoProjection /

@@ -379,13 +379,209 @@ __global__ void __launch_bounds__(RT, kAsmPerSM) assemble_dot_kernel(const AsmPl
   }
 }
 
-// Reference initial step (NekLinSysIterCG.cpp:147-190).
-__global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc, int nv, int na) {
+// ---- fused assembly + update of the FP32 inner iteration (scattered element output) ----
+// One launch does what the assembly (with its loop-tail scalars) and the next update did:
+//  * every CTA computes this iteration's scalars itself from the same partials in the same
+//    order (r.w and r.r of the previous launch, s.w of the element kernel), so all agree
+//    on alpha, beta and the stop decision (the reference loop tail,
+//    NekLinSysIterCG.cpp:219-261); right after the initial step (sc->fresh) it takes
+//    them from sc instead;
+//  * each free row g of each class gets s_g (an owned row: written by the element kernel;
+//    any other: the sum of its slots in the assembly-ordered buffer, in the assembly's
+//    order) and is updated at once, p, q, x, r, w = M^-1 r, with its r.w and r.r;
+//  * the partials alternate between two slot pairs by iteration parity (a CTA may write
+//    the next partials while a slower one still sums the current ones); the last CTA to
+//    finish (ticket) stores the scalars: every CTA has read sc before taking its ticket.
+// s is never written for the non-owned rows, and the separate assembly launch is gone.
+template <int K>
+__device__ __forceinline__ void upd_class(const AsmPlan& P, int c, int cta, int ncta, const int* __restrict__ rows,
+                                          const int* __restrict__ tail_ptr, const float* __restrict__ yslot,
+                                          const float* __restrict__ s, float* __restrict__ x, float* __restrict__ r,
+                                          float* __restrict__ w, float* __restrict__ p, float* __restrict__ q,
+                                          const float* __restrict__ dinv, float alpha, float beta, float& rw,
+                                          float& rr) {
+  constexpr int U = (K >= 4 || K == 0) ? 2 : 4;  // rows per thread step, their loads in flight together
+  const int n = P.n[c];
+  const int* R = rows + P.rows_off[c];
+  const int stride = ncta * RT;
+  for (int i0 = P.ndir[c] + cta * RT + threadIdx.x; i0 < n; i0 += U * stride) {
+    int g[U];
+    float sg[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * stride;
+      g[u] = i < n ? R[i] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * stride;
+      sg[u] = 0.f;
+      if (g[u] < 0) continue;
+      if constexpr (K == 1) {
+        sg[u] = s[g[u]];  // owned row: the element kernel wrote it
+      } else if constexpr (K > 1) {
+        const float* Y = yslot + P.col_off[c];
+        float v[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) v[j] = Y[(size_t)j * n + i];
+        float acc = v[0];
+#pragma unroll
+        for (int j = 1; j < K; ++j) acc += v[j];
+        sg[u] = acc;
+      } else {  // K == 0: the tail class (more than kAsmK entries)
+        const float* Y = yslot + P.tail_off;
+        float acc = 0.f;
+        for (int j = tail_ptr[i]; j < tail_ptr[i + 1]; ++j) acc += Y[j];
+        sg[u] = acc;
+      }
+    }
+    float pv[U], wv[U], qv[U], xv[U], rv[U], dv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int gg = g[u] >= 0 ? g[u] : 0;
+      pv[u] = p[gg];
+      wv[u] = w[gg];
+      qv[u] = q[gg];
+      xv[u] = x[gg];
+      rv[u] = r[gg];
+      dv[u] = dinv[gg];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (g[u] < 0) continue;
+      const float pg = fmaf(beta, pv[u], wv[u]);
+      const float qg = fmaf(beta, qv[u], sg[u]);
+      p[g[u]] = pg;
+      q[g[u]] = qg;
+      x[g[u]] = fmaf(alpha, pg, xv[u]);
+      const float rg = fmaf(-alpha, qg, rv[u]);
+      r[g[u]] = rg;
+      const float wg = dv[u] * rg;
+      w[g[u]] = wg;
+      rw = fmaf(rg, wg, rw);
+      rr = fmaf(rg, rg, rr);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RT, kRedPerSM) asm_update_f32_kernel(const AsmPlan P, const int* __restrict__ rows,
+                                                            const int* __restrict__ tail_ptr,
+                                                            const float* __restrict__ yslot,
+                                                            const float* __restrict__ s, float* __restrict__ x,
+                                                            float* __restrict__ r, float* __restrict__ w,
+                                                            float* __restrict__ p, float* __restrict__ q,
+                                                            const float* __restrict__ dinv, double* part_even,
+                                                            double* part_odd, CgScalars* sc, unsigned int* counter,
+                                                            const double* apart, int napart) {
+  __shared__ double shv[4][RT];
+  __shared__ CgScalars st;
+  if (threadIdx.x == 0) st = *sc;
+  __syncthreads();
+  if (st.done) return;  // every CTA reads the same flag: only this launch's last CTA sets it
+  const bool fresh = st.fresh != 0;
+  if (!fresh) {
+    // this iteration's scalars from the previous launch's r.w, r.r (the pair of parity
+    // k) and the element kernel's s.w: every CTA sums them in the same order
+    const double* pin = (st.k & 1) ? part_odd : part_even;
+    constexpr int MV = (RB + RT - 1) / RT;
+    double a[3];
+    a[0] = thread_partials<MV>(pin, gridDim.x);
+    a[1] = thread_partials<MV>(pin + RB, gridDim.x);
+    a[2] = napart > 0 ? thread_partials<MV>(apart, napart) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) shv[k][threadIdx.x] = a[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      constexpr int PER = RT / 32;
+      double red[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double t = shv[k][threadIdx.x * PER];
+#pragma unroll
+        for (int i = 1; i < PER; ++i) t += shv[k][threadIdx.x * PER + i];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+        red[k] = t;
+      }
+      if (threadIdx.x == 0) {
+        const double rho_new = red[0], eps = red[1], mu = red[2];
+        st.eps = eps;
+        st.mu = mu;
+        st.iters += 1;
+        if (!isfinite(eps) || !isfinite(rho_new) || !isfinite(mu)) {
+          st.status = ITHACA_GPU_ERR_NUMERIC;
+          st.done = 1;
+        } else if (eps < st.tol2 * st.rhs_mag) {
+          st.done = 1;
+        } else {
+          const double beta = rho_new / st.rho;
+          st.alpha = rho_new / (mu - rho_new * beta / st.alpha);
+          st.beta = beta;
+          st.rho = rho_new;
+          st.k += 1;
+          if (st.k >= st.max_iter) {
+            st.status = ITHACA_GPU_ERR_NOT_CONVERGED;
+            st.done = 1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  float rw = 0.f, rr = 0.f;
+  if (!st.done) {
+    const float alpha = (float)st.alpha, beta = (float)st.beta;
+    int c = 0;
+    while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
+    const int cta = blockIdx.x - P.cta0[c], ncta = P.cta0[c + 1] - P.cta0[c];
+    switch (c) {
+      case 0: upd_class<1>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 1: upd_class<2>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 2: upd_class<3>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 3: upd_class<4>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 4: upd_class<5>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 5: upd_class<6>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 6: upd_class<7>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      case 7: upd_class<8>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+      default: upd_class<0>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr);
+    }
+    // this launch's partials go to the pair of the next iteration's parity (k after the
+    // update above), which no CTA of this launch reads
+    float v[2] = {rw, rr};
+    const int slots[2] = {0, 1};
+    block_partials<2>(v, (st.k & 1) ? part_odd : part_even, slots);
+  }
+  __shared__ unsigned int ticket;
+  if (threadIdx.x == 0) {  // thread 0 wrote this CTA's partials: visible before its ticket
+    __threadfence();
+    ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  if (ticket == gridDim.x - 1 && threadIdx.x == 0) {
+    st.fresh = 0;
+    *sc = st;
+    *counter = 0u;  // re-armed for the next launch
+    __threadfence();
+  }
+}
+
+// Reference initial step (NekLinSysIterCG.cpp:147-190). apart (napart entries): the
+// element kernel's s.w partials, added to slot 3 where the element kernel summed s.w (the
+// fused iteration's start); the scalars are then marked fresh for the first fused launch.
+__global__ void __launch_bounds__(RT) scalars_init_kernel(const double* partials, CgScalars* sc, int nv, int na,
+                                                          const double* apart = nullptr, int napart = 0) {
   const int slots[4] = {0, 1, 2, 3};
   double red[4];
   reduce_slots<4>(partials, slots, red, nv, na);
-  const double rw = red[0], rr = red[1], bb = red[2], sw = red[3];
+  double asw = 0.0;
+  if (napart > 0) {
+    double a[1] = {thread_partials<(RB + RT - 1) / RT>(apart, napart)}, o[1];
+    block_sum<1>(a, o);
+    asw = o[0];
+  }
+  const double rw = red[0], rr = red[1], bb = red[2], sw = red[3] + asw;
   if (threadIdx.x == 0) {
+    sc->fresh = napart > 0 ? 1 : 0;
     sc->rhs_mag = sc->mag_override > 0 ? sc->mag_override : (bb > 1e-6 ? bb : 1.0);
     sc->eps = rr;
     sc->iters = 0;
@@ -686,6 +882,14 @@ struct Cg {
   double* partials = nullptr;
   double* dscal = nullptr;  // scratch doubles (norms)
   unsigned int* counter = nullptr;  // CTA ticket of the fused assembly + scalar update
+  // fused FP32 inner iteration (asm_update_f32_kernel): the full row classes with the CTAs
+  // split by the update's work, the odd-parity pair of r.w / r.r partial slots, the
+  // element kernel's grid (its s.w partials), on / off
+  AsmPlan plan_upd{};
+  double* partials_odd = nullptr;
+  int own_ctas = -1;
+  bool fuse_tail = false;
+  bool graph32_fused = false;
   CgScalars* sc = nullptr;
   CgScalars* sc_host = nullptr;  // pinned
   double diag_lambda = NAN;
@@ -723,6 +927,7 @@ Cg::~Cg() {
   cudaFree(jgk64);
   cudaFree(adj_scratch);
   cudaFree(partials);
+  cudaFree(partials_odd);
   cudaFree(dscal);
   cudaFree(counter);
   cudaFree(sc);
@@ -807,13 +1012,37 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
   cg->op->ctx->launches += 2;
 }
 
+// One fused FP32 iteration (scattered element output): the assembly and update of the
+// previous apply's output with this iteration's scalars (asm_update_f32_kernel), then the
+// gather + element apply of the new w, which writes the owned rows of s, the slots of the
+// others and its s.w partials.
+static void enqueue_iteration_fused(Cg* cg, Vecs<float>& v, const float* tab, const float* jg, cudaStream_t s) {
+  asm_update_f32_kernel<<<cg->rbv, RT, 0, s>>>(cg->plan_upd, cg->asm_rows, cg->tail_ptr, v.yloc, v.s, v.x, v.r, v.w,
+                                               v.p, v.q, v.dinv, cg->partials, cg->partials_odd, cg->sc,
+                                               cg->counter, cg->opart, cg->own_ctas);
+  OwnedRows own;
+  own.s = v.s;
+  own.part = cg->opart;
+  launch_apply<float>(cg, v, tab, jg, 0.f, lam_dev<float>(cg), v.w, s, true, skip_ptr(cg), &own);
+  if (own.ctas != cg->own_ctas) fail(ITHACA_GPU_ERR_ARG, "element kernel grid changed within a fused solve");
+  cg->op->ctx->launches += 1;  // (+1 in launch_apply)
+}
+
 template <typename T>
-static cudaGraphExec_t capture_chunk(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, int iters) {
+static cudaGraphExec_t capture_chunk(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, int iters, bool fused = false) {
   cudaStream_t s = cg->op->ctx->stream;
   cudaGraph_t g;
   ITHACA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   const long long before = cg->op->ctx->launches;
-  for (int i = 0; i < iters; ++i) enqueue_iteration<T>(cg, v, tab, jg, s);
+  for (int i = 0; i < iters; ++i) {
+    if constexpr (sizeof(T) == 4) {
+      if (fused) {
+        enqueue_iteration_fused(cg, v, tab, jg, s);
+        continue;
+      }
+    }
+    enqueue_iteration<T>(cg, v, tab, jg, s);
+  }
   cg->op->ctx->launches = before;  // captured, not launched
   ITHACA_CUDA(cudaStreamEndCapture(s, &g));
   cudaGraphExec_t ex;
@@ -878,11 +1107,33 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
     }
   }
   pcg_init_kernel<T><<<cg->rbv, RT, 0, s>>>(cg->N, cg->ndir, v.b, v.x, v.r, v.w, v.dinv, cg->partials);
-  launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
-  assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols, v.yloc, v.s, v.w, nullptr,
-                                           cg->partials);
-  scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc, cg->rbv, cg->rba);
-  c->launches += 3;
+  // fused FP32 iterations need the scattered output of a pipelined element kernel: the
+  // initial apply tries it, and the solve falls back to the separate assembly and update
+  // where the kernel cannot write it
+  bool fused = false, tried = false;
+  OwnedRows own0;
+  if constexpr (sizeof(T) == 4) {
+    if (cg->fuse_tail && cg->own_ok && cg->partials_odd != nullptr) {
+      tried = true;
+      own0.s = v.s;
+      own0.part = cg->opart;
+      launch_apply<float>(cg, v, tab, jg, 0.f, lam_dev<float>(cg), v.w, s, true, nullptr, &own0);
+      if (own0.ctas > cg->opart_cap) fail(ITHACA_GPU_ERR_ARG, "element kernel launched more CTAs than partial slots");
+      fused = own0.ctas >= 0;
+    }
+  }
+  if (fused) {
+    cg->own_ctas = own0.ctas;
+    scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc, cg->rbv, 0, cg->opart, own0.ctas);
+    c->launches += 2;
+  } else {
+    // an attempt that could not scatter wrote the element-ordered output already
+    if (!tried) launch_apply<T>(cg, v, tab, jg, T(0), lam_dev<T>(cg), v.w, s, true, nullptr);
+    assemble_dot_kernel<T><<<cg->rba, RT, 0, s>>>(cg->plan, true, cg->asm_rows, cg->asm_cols, cg->rowptr, cg->cols,
+                                             v.yloc, v.s, v.w, nullptr, cg->partials);
+    scalars_init_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc, cg->rbv, cg->rba);
+    c->launches += 3;
+  }
   ITHACA_CUDA(cudaGetLastError());
   cudaGraphExec_t& ex = sizeof(T) == 8 ? cg->graph64 : cg->graph32;
   int& len = sizeof(T) == 8 ? cg->graph64_len : cg->graph32_len;
@@ -890,14 +1141,18 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   int& gvar = sizeof(T) == 8 ? cg->graph64_variant : cg->graph32_variant;
   const int var = sizeof(T) == 8 ? cg->op->variant64 : cg->op->variant32;
   const bool geo_changed = (sizeof(T) == 4 && cg->graph32_geo16 != cg->geo16) || geo != (const void*)jg;
-  if (!ex || len != chunk || geo_changed || gvar != var) {
+  const bool fused_changed = sizeof(T) == 4 && cg->graph32_fused != fused;
+  if (!ex || len != chunk || geo_changed || gvar != var || fused_changed) {
     if (ex) cudaGraphExecDestroy(ex);
     ex = nullptr;
-    ex = capture_chunk<T>(cg, v, tab, jg, chunk);
+    ex = capture_chunk<T>(cg, v, tab, jg, chunk, fused);
     len = chunk;
     geo = jg;
     gvar = var;
-    if (sizeof(T) == 4) cg->graph32_geo16 = cg->geo16;
+    if (sizeof(T) == 4) {
+      cg->graph32_geo16 = cg->geo16;
+      cg->graph32_fused = fused;
+    }
   }
   // Bounded host loop: at most max_iter / chunk + 2 graph launches.
   const long long max_launches = (long long)max_iter / chunk + 2;
@@ -907,7 +1162,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
     if (cg->sc_host->done) break;
     if (it >= max_launches) fail(ITHACA_GPU_ERR_TIMEOUT, "CG did not flag completion within its iteration bound");
     ITHACA_CUDA(cudaGraphLaunch(ex, s));
-    c->launches += 3LL * chunk;
+    c->launches += (fused ? 2LL : 3LL) * chunk;
   }
 }
 
@@ -1445,6 +1700,35 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
       ent_own[0] = plan.ndir[0];
       split_ctas(plan_own, ent_own);
     }
+    // The fused inner iteration (asm_update_f32_kernel): every class, over a vector-kernel
+    // grid (rbv CTAs: its r.w / r.r partials fill at most RB slots), the CTAs split by the
+    // update's work per class: 11 vector accesses per free row plus the row's s or slot
+    // reads. Needs a CTA for every class that has free rows.
+    AsmPlan plan_upd = plan;
+    bool upd_ok = false;
+    if (own_ok) {
+      long long wgt[kAsmK + 1], total = 0;
+      int nonempty = 0, big = 0;
+      for (int c = 0; c <= kAsmK; ++c) {
+        const long long nfree = plan.n[c] - plan.ndir[c];
+        const long long efree = c < kAsmK ? (long long)(c + 1) * nfree : (nfree > 0 ? entries[c] * nfree / plan.n[c] : 0);
+        wgt[c] = nfree > 0 ? 11 * nfree + efree : 0;
+        total += wgt[c];
+        nonempty += nfree > 0;
+        if (wgt[c] > wgt[big]) big = c;
+      }
+      if (nonempty > 0 && rbv >= nonempty) {
+        int share[kAsmK + 1], used = 0;
+        for (int c = 0; c <= kAsmK; ++c) {
+          share[c] = wgt[c] > 0 ? std::max(1, (int)((double)(rbv - nonempty) * wgt[c] / std::max(total, 1LL))) : 0;
+          used += share[c];
+        }
+        share[big] += rbv - used;
+        plan_upd.cta0[0] = 0;
+        for (int c = 0; c <= kAsmK; ++c) plan_upd.cta0[c + 1] = plan_upd.cta0[c] + share[c];
+        upd_ok = plan_upd.cta0[kAsmK + 1] == rbv;
+      }
+    }
     auto cg = std::make_unique<ithaca_gpu_cg>();
     cg->op = op;
     cg->N = nglobal;
@@ -1469,6 +1753,10 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
                                   cudaMemcpyHostToDevice, s));
       cg->own_ok = true;
       cg->plan_own = plan_own;
+      if (upd_ok) {
+        cg->plan_upd = plan_upd;
+        ITHACA_CUDA(cudaMalloc(&cg->partials_odd, sizeof(double) * 2 * RB));
+      }
     }
     ITHACA_CUDA(cudaMalloc(&cg->asm_cols, sizeof(int) * asm_cols.size()));
     ITHACA_CUDA(cudaMemcpyAsync(cg->l2g, code.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
@@ -1497,6 +1785,14 @@ int ithaca_gpu_cg_set_persistent(ithaca_gpu_cg* cg, int mode) {
     req(cg != nullptr, "null solver");
     req(mode >= -1 && mode <= 1, "persistent mode must be -1, 0 or 1");
     cg->persist = mode;
+  });
+}
+
+int ithaca_gpu_cg_set_fused_update(ithaca_gpu_cg* cg, int on) {
+  return cg_guarded([&] {
+    req(cg != nullptr, "null solver");
+    req(on == 0 || on == 1, "on must be 0 or 1");
+    cg->fuse_tail = on != 0;
   });
 }
 

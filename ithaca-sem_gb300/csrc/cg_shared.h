@@ -11,7 +11,8 @@ struct CgScalars {
   double alpha, beta, rho, mu, eps, rhs_mag, tol2, mag_override;
   double lambda;
   float lambda32, pad0;
-  int iters, k, done, status, max_iter, pad1;
+  int iters, k, done, status, max_iter;
+  int fresh;  // alpha / beta were just set by the initial step (fused inner iteration)
 };
 
 // ---- assembly plan: rows grouped by their number of local entries ----------------

@@ -93,6 +93,7 @@ SIGNATURES = {
     "ithaca_gpu_helmsolve_dirichlet": [_vp, _d, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_vcs_solve_viscous": [_vp, _i, _pp, _pp, _d, _vp, _pp, _pp, ctypes.POINTER(CgOpts),
                                      ctypes.POINTER(CgResult), _i],
+    "ithaca_gpu_cg_set_fused_update": [_vp, _i],
     "ithaca_gpu_vcs_solve_pressure": [_vp, _vp, _vp, _vp, ctypes.POINTER(CgOpts), ctypes.POINTER(CgResult), _i],
     "ithaca_gpu_sc_create": [_vp, _vp, _vp, _i, _i, _pp],
     "ithaca_gpu_sc_destroy": [_vp],

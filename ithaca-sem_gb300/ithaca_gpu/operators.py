@@ -403,6 +403,11 @@ class GlobalLinSysIterativeFullGPU:
         graph-captured kernels, 1 the persistent single-launch solver."""
         C.call("ithaca_gpu_cg_set_persistent", self.handle, int(mode))
 
+    def set_fused_update(self, on):
+        """1: the mixed solve's FP32 iterations fuse the assembly with the vector update (two
+        launches per iteration); 0 (default): separate assembly and update."""
+        C.call("ithaca_gpu_cg_set_fused_update", self.handle, int(on))
+
     def set_successive_rhs(self, nsuccessive):
         """SuccessiveRHS projection of later solves onto up to |nsuccessive| previous
         solutions (> 0 A-conjugate, < 0 residual-minimising, 0 off); resets the buffer."""

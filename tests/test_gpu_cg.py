@@ -255,6 +255,58 @@ def test_mixed_geo16_vector_pencils_q8(ctx, variant):
     assert ms > 0 and nbytes > 0
 
 
+@pytest.mark.parametrize("variant,mode", [(42, "mixed"), (43, "mixed"), (47, "mixed"), (47, "mixed_geo16"),
+                                          (4, "mixed")])
+def test_mixed_fused_update_matches_separate(ctx, variant, mode):
+    """The inner FP32 iterations with the assembly fused into the vector update (two
+    launches per iteration, the scalars computed by every CTA of the update) against the
+    separate assembly and update: the same FP64 residual, inner iterations within a few
+    (the partial sums are grouped differently) and the same solution. Variant 4 writes no
+    scattered output, so its solve falls back to the separate kernels."""
+    c = hex_case(3, 3, 3, 7, amp=0.08)
+    coll, amap, sys_ = _system(ctx, c)
+    rhs = np.random.default_rng(37).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    x64, _ = sys_.solve(1.0, rhs, tol=1e-12)
+    coll.set_variant(variant)
+    sys_.set_fused_update(0)
+    xs, rs = sys_.solve(1.0, rhs, tol=1e-10, mode=mode)
+    sys_.set_fused_update(1)
+    xf, rf = sys_.solve(1.0, rhs, tol=1e-10, mode=mode)
+    assert rs.rel_residual < 1e-10 and rf.rel_residual < 1e-10
+    assert abs(rf.iterations - rs.iterations) <= max(3, rs.iterations // 50), (rf.iterations, rs.iterations)
+    assert rel_err(xf[amap.ndir:], x64[amap.ndir:]) < 1e-8
+    assert rel_err(xf[amap.ndir:], xs[amap.ndir:]) < 1e-8
+    # again after the graph of the other form was captured: the same solve as the first fused one
+    xf2, rf2 = sys_.solve(1.0, rhs, tol=1e-10, mode=mode)
+    assert rf2.iterations == rf.iterations and rel_err(xf2, xf) == 0.0
+
+
+def test_mixed_fused_update_long_rows_and_max_iter(ctx):
+    """Fused iterations on a mesh whose rows reach 24 local entries (the tail class read
+    through its slot ranges), and a max_iter that stops the fused recurrence: NOT_CONVERGED,
+    then a normal solve on the same system."""
+    from ithaca_gpu._capi import ERR_NOT_CONVERGED, GpuError
+    c = hex_case(3, 3, 3, 7, amp=0.08)
+    amap = _merged_map(c.mesh.assembly(c.n))
+    from ithaca_gpu.operators import Collection, GlobalLinSysIterativeFullGPU
+    coll = Collection(ctx, c.shape, c.n, c.Q, c.E, c.jac, c.df, deformed=c.deformed)
+    sys_ = GlobalLinSysIterativeFullGPU(coll, amap)
+    rhs = np.random.default_rng(41).uniform(-1, 1, amap.nglobal)
+    rhs[:amap.ndir] = 0
+    coll.set_variant(47)
+    sys_.set_fused_update(1)
+    xo, it_o, _, _ = osolve.solve(c.basis, 3, c.jac.reshape(c.E, -1), c.df, 1.0, amap, rhs, tol=1e-12)
+    x, res = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res.rel_residual < 1e-10
+    assert rel_err(x[amap.ndir:], xo[amap.ndir:]) < 1e-8
+    with pytest.raises(GpuError) as ei:
+        sys_.solve(1.0, rhs, tol=1e-10, mode="mixed", max_iter=7)
+    assert ei.value.code == ERR_NOT_CONVERGED
+    x2, res2 = sys_.solve(1.0, rhs, tol=1e-10, mode="mixed")
+    assert res2.iterations == res.iterations and rel_err(x2, x) == 0.0
+
+
 def test_mixed_geo16_rejects_quads(ctx):
     from ithaca_gpu._capi import ERR_UNSUPPORTED, GpuError
     c = quad_case(4, 4, 5)
