@@ -380,19 +380,14 @@ __global__ void __launch_bounds__(RT, kAsmPerSM) assemble_dot_kernel(const AsmPl
 }
 
 // ---- fused assembly + update of the FP32 inner iteration (scattered element output) ----
-// One launch does what the assembly (with its loop-tail scalars) and the next update did:
-//  * every CTA computes this iteration's scalars itself from the same partials in the same
-//    order (r.w and r.r of the previous launch, s.w of the element kernel), so all agree
-//    on alpha, beta and the stop decision (the reference loop tail,
-//    NekLinSysIterCG.cpp:219-261); right after the initial step (sc->fresh) it takes
-//    them from sc instead;
-//  * each free row g of each class gets s_g (an owned row: written by the element kernel;
-//    any other: the sum of its slots in the assembly-ordered buffer, in the assembly's
-//    order) and is updated at once, p, q, x, r, w = M^-1 r, with its r.w and r.r;
-//  * the partials alternate between two slot pairs by iteration parity (a CTA may write
-//    the next partials while a slower one still sums the current ones); the last CTA to
-//    finish (ticket) stores the scalars: every CTA has read sc before taking its ticket.
-// s is never written for the non-owned rows, and the separate assembly launch is gone.
+// One launch does what the assembly and the next update did: each free row g of each
+// class gets s_g (an owned row: written by the element kernel; any other: the sum of its
+// slots in the assembly-ordered buffer, in the assembly's order) and is updated at once,
+// p, q, x, r, w = M^-1 r, with its r.w and r.r. The iteration's scalars (the reference
+// loop tail, NekLinSysIterCG.cpp:219-261) come from a one-CTA kernel before it
+// (scalars_fused_kernel): computing them in every CTA of the update had all CTAs read the
+// same partials at once, and that hot spot in L2 cost more than the launch it saved.
+// s is never written for the non-owned rows.
 template <int K>
 __device__ __forceinline__ void upd_class(const AsmPlan& P, int c, int cta, int ncta, const int* __restrict__ rows,
                                           const int* __restrict__ tail_ptr, const float* __restrict__ yslot,
@@ -470,99 +465,42 @@ __global__ void __launch_bounds__(RT, kRedPerSM) asm_update_f32_kernel(const Asm
                                                             const float* __restrict__ s, float* __restrict__ x,
                                                             float* __restrict__ r, float* __restrict__ w,
                                                             float* __restrict__ p, float* __restrict__ q,
-                                                            const float* __restrict__ dinv, double* part_even,
-                                                            double* part_odd, CgScalars* sc, unsigned int* counter,
-                                                            const double* apart, int napart) {
-  __shared__ double shv[4][RT];
-  __shared__ CgScalars st;
-  if (threadIdx.x == 0) st = *sc;
-  __syncthreads();
-  if (st.done) return;  // every CTA reads the same flag: only this launch's last CTA sets it
-  const bool fresh = st.fresh != 0;
-  if (!fresh) {
-    // this iteration's scalars from the previous launch's r.w, r.r (the pair of parity
-    // k) and the element kernel's s.w: every CTA sums them in the same order
-    const double* pin = (st.k & 1) ? part_odd : part_even;
-    constexpr int MV = (RB + RT - 1) / RT;
-    double a[3];
-    a[0] = thread_partials<MV>(pin, gridDim.x);
-    a[1] = thread_partials<MV>(pin + RB, gridDim.x);
-    a[2] = napart > 0 ? thread_partials<MV>(apart, napart) : 0.0;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) shv[k][threadIdx.x] = a[k];
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      constexpr int PER = RT / 32;
-      double red[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        double t = shv[k][threadIdx.x * PER];
-#pragma unroll
-        for (int i = 1; i < PER; ++i) t += shv[k][threadIdx.x * PER + i];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-        red[k] = t;
-      }
-      if (threadIdx.x == 0) {
-        const double rho_new = red[0], eps = red[1], mu = red[2];
-        st.eps = eps;
-        st.mu = mu;
-        st.iters += 1;
-        if (!isfinite(eps) || !isfinite(rho_new) || !isfinite(mu)) {
-          st.status = ITHACA_GPU_ERR_NUMERIC;
-          st.done = 1;
-        } else if (eps < st.tol2 * st.rhs_mag) {
-          st.done = 1;
-        } else {
-          const double beta = rho_new / st.rho;
-          st.alpha = rho_new / (mu - rho_new * beta / st.alpha);
-          st.beta = beta;
-          st.rho = rho_new;
-          st.k += 1;
-          if (st.k >= st.max_iter) {
-            st.status = ITHACA_GPU_ERR_NOT_CONVERGED;
-            st.done = 1;
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
+                                                            const float* __restrict__ dinv, double* partials,
+                                                            const CgScalars* sc) {
+  if (sc->done) return;
+  const float alpha = (float)sc->alpha, beta = (float)sc->beta;
   float rw = 0.f, rr = 0.f;
-  if (!st.done) {
-    const float alpha = (float)st.alpha, beta = (float)st.beta;
-    int c = 0;
-    while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
-    const int cta = blockIdx.x - P.cta0[c], ncta = P.cta0[c + 1] - P.cta0[c];
-    switch (c) {
-      case 0: upd_class<1>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 1: upd_class<2>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 2: upd_class<3>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 3: upd_class<4>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 4: upd_class<5>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 5: upd_class<6>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 6: upd_class<7>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      case 7: upd_class<8>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
-      default: upd_class<0>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr);
-    }
-    // this launch's partials go to the pair of the next iteration's parity (k after the
-    // update above), which no CTA of this launch reads
-    float v[2] = {rw, rr};
-    const int slots[2] = {0, 1};
-    block_partials<2>(v, (st.k & 1) ? part_odd : part_even, slots);
+  int c = 0;
+  while (c < kAsmK && (int)blockIdx.x >= P.cta0[c + 1]) ++c;
+  const int cta = blockIdx.x - P.cta0[c], ncta = P.cta0[c + 1] - P.cta0[c];
+  switch (c) {
+    case 0: upd_class<1>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 1: upd_class<2>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 2: upd_class<3>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 3: upd_class<4>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 4: upd_class<5>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 5: upd_class<6>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 6: upd_class<7>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    case 7: upd_class<8>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr); break;
+    default: upd_class<0>(P, c, cta, ncta, rows, tail_ptr, yslot, s, x, r, w, p, q, dinv, alpha, beta, rw, rr);
   }
-  __shared__ unsigned int ticket;
-  if (threadIdx.x == 0) {  // thread 0 wrote this CTA's partials: visible before its ticket
-    __threadfence();
-    ticket = atomicAdd(counter, 1u);
+  float v[2] = {rw, rr};
+  const int slots[2] = {0, 1};
+  block_partials<2>(v, partials, slots);
+}
+
+// The loop tail of the fused iteration (one CTA): this iteration's scalars from the fused
+// update's r.w, r.r and the element kernel's s.w (apart); right after the initial step
+// (sc->fresh) they are already set and only the flag is cleared.
+__global__ void __launch_bounds__(RT) scalars_fused_kernel(const double* partials, CgScalars* sc, const double* apart,
+                                                           int napart, int nv) {
+  if (sc->done) return;
+  if (sc->fresh) {
+    __syncthreads();
+    if (threadIdx.x == 0) sc->fresh = 0;
+    return;
   }
-  __syncthreads();
-  if (ticket == gridDim.x - 1 && threadIdx.x == 0) {
-    st.fresh = 0;
-    *sc = st;
-    *counter = 0u;  // re-armed for the next launch
-    __threadfence();
-  }
+  scalars_iter_body(partials, sc, apart, napart, nv, 0);
 }
 
 // Reference initial step (NekLinSysIterCG.cpp:147-190). apart (napart entries): the
@@ -883,10 +821,10 @@ struct Cg {
   double* dscal = nullptr;  // scratch doubles (norms)
   unsigned int* counter = nullptr;  // CTA ticket of the fused assembly + scalar update
   // fused FP32 inner iteration (asm_update_f32_kernel): the full row classes with the CTAs
-  // split by the update's work, the odd-parity pair of r.w / r.r partial slots, the
-  // element kernel's grid (its s.w partials), on / off
+  // split by the update's work (upd_ok: every class with free rows has a CTA), the element
+  // kernel's grid (its s.w partials), on / off
   AsmPlan plan_upd{};
-  double* partials_odd = nullptr;
+  bool upd_ok = false;
   int own_ctas = -1;
   bool fuse_tail = false;
   bool graph32_fused = false;
@@ -927,7 +865,6 @@ Cg::~Cg() {
   cudaFree(jgk64);
   cudaFree(adj_scratch);
   cudaFree(partials);
-  cudaFree(partials_odd);
   cudaFree(dscal);
   cudaFree(counter);
   cudaFree(sc);
@@ -1017,15 +954,15 @@ static void enqueue_iteration(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, cud
 // gather + element apply of the new w, which writes the owned rows of s, the slots of the
 // others and its s.w partials.
 static void enqueue_iteration_fused(Cg* cg, Vecs<float>& v, const float* tab, const float* jg, cudaStream_t s) {
+  scalars_fused_kernel<<<1, RT, 0, s>>>(cg->partials, cg->sc, cg->opart, cg->own_ctas, cg->rbv);
   asm_update_f32_kernel<<<cg->rbv, RT, 0, s>>>(cg->plan_upd, cg->asm_rows, cg->tail_ptr, v.yloc, v.s, v.x, v.r, v.w,
-                                               v.p, v.q, v.dinv, cg->partials, cg->partials_odd, cg->sc,
-                                               cg->counter, cg->opart, cg->own_ctas);
+                                               v.p, v.q, v.dinv, cg->partials, cg->sc);
   OwnedRows own;
   own.s = v.s;
   own.part = cg->opart;
   launch_apply<float>(cg, v, tab, jg, 0.f, lam_dev<float>(cg), v.w, s, true, skip_ptr(cg), &own);
   if (own.ctas != cg->own_ctas) fail(ITHACA_GPU_ERR_ARG, "element kernel grid changed within a fused solve");
-  cg->op->ctx->launches += 1;  // (+1 in launch_apply)
+  cg->op->ctx->launches += 2;  // (+1 in launch_apply)
 }
 
 template <typename T>
@@ -1113,7 +1050,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
   bool fused = false, tried = false;
   OwnedRows own0;
   if constexpr (sizeof(T) == 4) {
-    if (cg->fuse_tail && cg->own_ok && cg->partials_odd != nullptr) {
+    if (cg->fuse_tail && cg->own_ok && cg->upd_ok) {
       tried = true;
       own0.s = v.s;
       own0.part = cg->opart;
@@ -1162,7 +1099,7 @@ static void run_pcg(Cg* cg, Vecs<T>& v, const T* tab, const T* jg, double lambda
     if (cg->sc_host->done) break;
     if (it >= max_launches) fail(ITHACA_GPU_ERR_TIMEOUT, "CG did not flag completion within its iteration bound");
     ITHACA_CUDA(cudaGraphLaunch(ex, s));
-    c->launches += (fused ? 2LL : 3LL) * chunk;
+    c->launches += 3LL * chunk;
   }
 }
 
@@ -1753,10 +1690,8 @@ int ithaca_gpu_cg_create(ithaca_gpu_op* opp, const int* l2g, const double* sign,
                                   cudaMemcpyHostToDevice, s));
       cg->own_ok = true;
       cg->plan_own = plan_own;
-      if (upd_ok) {
-        cg->plan_upd = plan_upd;
-        ITHACA_CUDA(cudaMalloc(&cg->partials_odd, sizeof(double) * 2 * RB));
-      }
+      cg->plan_upd = plan_upd;
+      cg->upd_ok = upd_ok;
     }
     ITHACA_CUDA(cudaMalloc(&cg->asm_cols, sizeof(int) * asm_cols.size()));
     ITHACA_CUDA(cudaMemcpyAsync(cg->l2g, code.data(), sizeof(int) * nloc, cudaMemcpyHostToDevice, s));
