@@ -825,7 +825,10 @@ def run_gpu(args, rank, world):
                  "apply_ms": k64_ms, "apply_fp64_tflops": None},
         "helmholtz_gdofs": {"fp64": gdofs64, "fp32": gdofs32},
         "solver_gdofs": {"mixed": value / world * (N - ndir) / 1e9, "fp64": fp64_solves * (N - ndir) / 1e9},
-        "roofline": inner_roofline(mode, variant, n, Q, E, k_ms, k_bytes, peak, peak_kind),
+        "roofline": dict(inner_roofline(mode, variant, n, Q, E, k_ms, k_bytes, peak, peak_kind),
+                         **({"fp32_geometry_bytes_per_launch": ko_bytes,
+                             "fp32_geometry_equivalent_frac": ko_bytes / (k_ms / 1e3) / 1e9 / peak}
+                            if mode == "mixed_geo16" else {})),
         "roofline_other_mixed_mode": inner_roofline(other, variant, n, Q, E, ko_ms, ko_bytes, peak, peak_kind),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_host.nbytes),
                 "d2h_bytes_per_step": int(out_host.nbytes), "rel_residual": rese.rel_residual},
