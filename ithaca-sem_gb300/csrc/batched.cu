@@ -130,10 +130,51 @@ __global__ void __launch_bounds__(BT, kChunkPerSM) bupdate_kernel(const Chunk* _
     // per-thread sums in T (a chunk gives each thread 16 dofs; FP32 sums keep the
     // FP32 solve off the slow FP64 pipe), CTA sums in FP64
     T rw = 0, rr = 0;
-    if (!S.done) {
+    if constexpr (sizeof(T) == 4) {
+      // FP32: the 16-byte-aligned interior of the chunk as float4 groups (one group per
+      // thread step, every vector moved with 16-byte loads and stores), the ragged ends
+      // (fewer than 4 dofs each) one dof per thread
+      const float alpha = (float)S.alpha, beta = (float)S.beta;
+      auto upd = [&](float& pv, float& qv, float& xv, float& rv, float& wv, float dv, float sv) {
+        pv = beta * pv + wv;
+        qv = beta * qv + sv;
+        xv = xv + alpha * pv;
+        rv = rv - alpha * qv;
+        wv = dv * rv;
+        rw = fma(rv, wv, rw);
+        rr = fma(rv, rv, rr);
+      };
+      const int a0 = min((ch.begin + 3) & ~3, ch.end), a1 = max(ch.end & ~3, a0);
+      const int nh = a0 - ch.begin, nt = ch.end - a1;
+      if ((int)threadIdx.x < nh + nt) {
+        const int g = (int)threadIdx.x < nh ? ch.begin + threadIdx.x : a1 + (threadIdx.x - nh);
+        float pv = p[g], qv = q[g], xv = x[g], rv = r[g], wv = w[g];
+        upd(pv, qv, xv, rv, wv, dinv[g], s[g]);
+        p[g] = pv;
+        q[g] = qv;
+        x[g] = xv;
+        r[g] = rv;
+        w[g] = wv;
+      }
+      for (int q4 = (a0 >> 2) + threadIdx.x; q4 < (a1 >> 2); q4 += BT) {
+        float4 P4 = reinterpret_cast<const float4*>(p)[q4], W4 = reinterpret_cast<const float4*>(w)[q4];
+        float4 Q4 = reinterpret_cast<const float4*>(q)[q4], X4 = reinterpret_cast<const float4*>(x)[q4];
+        float4 R4 = reinterpret_cast<const float4*>(r)[q4];
+        const float4 S4 = reinterpret_cast<const float4*>(s)[q4], D4 = reinterpret_cast<const float4*>(dinv)[q4];
+        upd(P4.x, Q4.x, X4.x, R4.x, W4.x, D4.x, S4.x);
+        upd(P4.y, Q4.y, X4.y, R4.y, W4.y, D4.y, S4.y);
+        upd(P4.z, Q4.z, X4.z, R4.z, W4.z, D4.z, S4.z);
+        upd(P4.w, Q4.w, X4.w, R4.w, W4.w, D4.w, S4.w);
+        reinterpret_cast<float4*>(p)[q4] = P4;
+        reinterpret_cast<float4*>(q)[q4] = Q4;
+        reinterpret_cast<float4*>(x)[q4] = X4;
+        reinterpret_cast<float4*>(r)[q4] = R4;
+        reinterpret_cast<float4*>(w)[q4] = W4;
+      }
+    } else {
       const T alpha = (T)S.alpha, beta = (T)S.beta;
       // U dofs per thread step with their loads issued together (memory-level parallelism)
-      constexpr int U = sizeof(T) == 8 ? 2 : 4;
+      constexpr int U = 2;
       for (int g0 = ch.begin + threadIdx.x; g0 < ch.end; g0 += U * BT) {
         T pv[U], wv[U], qv[U], sv[U], xv[U], rv[U], dv[U];
 #pragma unroll
